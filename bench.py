@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Benchmark: Mpoints/s of the plain per-pair GPU path on the 5 MP workload.
+
+Workload (one step = one stereo pair): 2448x2048 per camera, hierarchical
+1/8/64-fringe phase shift, 4 steps each (12 frames), 12-bit values in u16,
+seeded synthetic scene (Gaussian bumps over a plane at 900 mm plus box
+occluders), f = 2400 px, baseline 200 mm, k1 = -0.05, k2 = 0.01; decode ->
+rectify -> match -> 5x5 median -> Q reprojection -> SOR (k = 30) -> MLS
+(radius 2 mm, order 2) -> Gaussian (sigma 0.5 mm).  Inputs (240 MB per pair)
+exceed the 129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun: independent replicas, one pair per rank per step
+(weak scaling, no collective on the data path); the time is the max over ranks.
+--impl reference times the CPU restatement of the path (oracle/, all host
+threads) on a bounded sample of the same workload: a band of rectified rows.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpoints/s at 5 MP (plain per-pair GPU path)"
+UNIT = "Mpoints/s"
+WORKLOAD = "5MP pair: 2448x2048 x2 cams, hierarchical 1/8/64 x 4 steps, u16 12-bit; decode+rectify+match+median+reproject+SOR(k30)+MLS(r2mm,o2)+Gaussian(0.5mm)"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def config1_recon(api):
+    return api.recon_config(use_px_gaussian=0, use_ror=0, use_sor=1, sor_mean_k=30, sor_std_mul=1.0, use_mls=1,
+                            mls_window_size=7, mls_spatial_sigma=2.0 / math.sqrt(2.0), mls_polynomial_order=2,
+                            mls_max_radius=2.0, mls_iterations=1, use_metric_gaussian=1, metric_gaussian_sigma=0.5)
+
+
+def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
+    """Per-stage device time (CUDA events on the launching stream), ms per launch."""
+    import torch
+    H, W = dL.shape[1:]
+    st = torch.cuda.current_stream()
+    names = ["decode", "rectify", "match", "median_reproject", "sor", "mls", "metric_gaussian"]
+    acc = {n: 0.0 for n in names}
+    cnt = {n: 0 for n in names}
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for _ in range(steps):
+        e = [ev() for _ in range(12)]
+        e[0].record(st)
+        dl = api.decode(ctx, dcfg, dL, want_mod=False, want_valid=False)
+        e[1].record(st)
+        dr = api.decode(ctx, dcfg, dR, want_mod=False, want_valid=False)
+        e[2].record(st)
+        rl = api.rectify(ctx, 0, dl["order"], dl["residual"], True)
+        rr = api.rectify(ctx, 1, dr["order"], dr["residual"], True)
+        e[3].record(st)
+        disp, _ = api.match(ctx, rl, rr, spec.pha_f, 1.0, want_best=False)
+        e[4].record(st)
+        _, xyz, mask = api.median_reproject(ctx, rcfg, disp)
+        e[5].record(st)
+        m2, _ = api.filter_sor(ctx, xyz, mask, 30, 1.0)
+        e[6].record(st)
+        x2 = api.filter_mls(ctx, xyz, m2, 7, 2.0 / math.sqrt(2.0), 2, 2.0, 1)
+        e[7].record(st)
+        api.filter_metric_gaussian(ctx, x2, m2, 0.5)
+        e[8].record(st)
+        torch.cuda.synchronize()
+        acc["decode"] += e[0].elapsed_time(e[1]) + e[1].elapsed_time(e[2]); cnt["decode"] += 2
+        acc["rectify"] += e[2].elapsed_time(e[3]); cnt["rectify"] += 2
+        acc["match"] += e[3].elapsed_time(e[4]); cnt["match"] += 1
+        acc["median_reproject"] += e[4].elapsed_time(e[5]); cnt["median_reproject"] += 1
+        acc["sor"] += e[5].elapsed_time(e[6]); cnt["sor"] += 1
+        acc["mls"] += e[6].elapsed_time(e[7]); cnt["mls"] += 1
+        acc["metric_gaussian"] += e[7].elapsed_time(e[8]); cnt["metric_gaussian"] += 1
+    per_step = {n: acc[n] / steps for n in names}
+    per_launch = {n: acc[n] / cnt[n] for n in names}
+    return per_step, per_launch
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from zim_gb300 import api, synth
+
+    rank, local, world = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    spec = synth.config1(seed=1 + rank)
+    L, R = spec.render(0), spec.render(1)
+    F, H, W = L.shape
+    ctx = api.Context(local)
+    ctx.set_calibration(spec.rig.as_dict(), True)
+    dcfg = api.decode_config(**spec.decode_kwargs())
+    rcfg = config1_recon(api)
+    dL, dR = torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda()
+    xyz = torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32, device="cuda")
+    mask = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device="cuda")
+    out = (xyz, mask, None)
+    for _ in range(args.warmup):
+        api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
+    torch.cuda.synchronize()
+    n_pts = int(mask.sum().item())
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count()
+        e0.record(st)
+        for _ in range(args.steps):
+            api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier()
+        launches = ctx.launch_count() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    pts_total = n_pts
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        p = torch.tensor([n_pts], device="cuda", dtype=torch.float64)
+        dist.all_reduce(p, op=dist.ReduceOp.SUM)
+        pts_total = int(p.item())
+    value = pts_total / (ms * 1e-3) / 1e6
+
+    # end to end through the host entry: pinned frames in, xyz + mask out, copies timed
+    hL = torch.from_numpy(L).pin_memory()
+    hR = torch.from_numpy(R).pin_memory()
+    hx = torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32).pin_memory()
+    hm = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory()
+    for _ in range(max(1, args.warmup // 2)):
+        api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(st)
+    for _ in range(args.steps):
+        api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
+    e1.record(st)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    barrier()
+    e2e_ms = max(e0.elapsed_time(e1) / args.steps, wall * 1e3)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = pts_total / (e2e_ms * 1e-3) / 1e6
+    h2d = 2 * L.nbytes
+    d2h = hx.numel() * 4 + hm.numel()
+
+    result = None
+    if rank == 0:
+        per_step, per_launch = stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, max(3, min(args.steps, 10)))
+        dom = max(per_step, key=per_step.get)
+        peak, src = peaks()
+        npx, rpx = H * W, ctx.rect_h * ctx.rect_w
+        # algorithmic bytes per launch (measurement section)
+        alg = {"decode": npx * (F * 2 + 8), "rectify": npx * 8 + rpx * 12, "match": rpx * (12 + 12 + 4),
+               "median_reproject": rpx * (4 + 13), "sor": rpx * (13 + 13), "mls": rpx * (13 + 12),
+               "metric_gaussian": rpx * (13 + 12)}
+        stages = {n: {"ms_per_step": round(per_step[n], 4), "ms_per_launch": round(per_launch[n], 4),
+                      "gbs": round(alg[n] / (per_launch[n] * 1e-3) / 1e9, 1)} for n in per_step}
+        achieved = alg[dom] / (per_launch[dom] * 1e-3) / 1e9
+        dec_achieved = alg["decode"] / (per_launch["decode"] * 1e-3) / 1e9
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cpu = cpu_baseline(spec, L, R)
+        result = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (u16 samples; FP64 only for near-zero-disparity divides)",
+            "data": "synthetic (seeded scene renderer, zim_gb300/synth)",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "rect": [ctx.rect_w, ctx.rect_h],
+                       "frames_per_camera": F, "points_per_pair": n_pts, "parallelism": f"replicas x{world}",
+                       "l2": "inputs 240 MB per pair > 129 MB L2 (no flush)"},
+            "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": round(e2e_ms, 4)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_source": src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": None,
+                         "decode_kernel": {"achieved": round(dec_achieved, 1),
+                                           "frac": round(dec_achieved / peak, 4)}},
+            "stages": stages,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            result["cpu_baseline"] = cpu
+        print(json.dumps(result))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return result
+
+
+def cpu_band_step(spec, L, R, rect, y0, y1):
+    from oracle import pipeline as P
+    t = time.perf_counter()
+    xyz, mask = P.run_band(spec.decode_kwargs(), spec.pha_f, L, R, rect, y0, y1, P.CONFIG1_FILTERS)
+    return time.perf_counter() - t, int(mask.sum())
+
+
+def cpu_baseline(spec, L, R, band_rows=256):
+    """The CPU restatement on a bounded sample: one band of rectified rows."""
+    from oracle import pipeline as P
+    rect = P.Rectification(spec.rig.as_dict(), True)
+    y0 = rect.h // 2 - band_rows // 2
+    cpu_band_step(spec, L, R, rect, y0, y0 + 16)  # warm caches / OpenMP pool
+    dt, n = cpu_band_step(spec, L, R, rect, y0, y0 + band_rows)
+    return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"rectified rows [{y0},{y0 + band_rows}) of the same pair ({band_rows}/{rect.h} rows), "
+                      f"whole path incl. filters, {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank, local, world = env_rank()
+    if rank != 0:
+        return None
+    from oracle import pipeline as P
+    from zim_gb300 import synth
+    spec = synth.config1(seed=1)
+    L, R = spec.render(0), spec.render(1)
+    rect = P.Rectification(spec.rig.as_dict(), True)
+    band = 128
+    rows = list(range(0, rect.h - band, band))
+    for i in range(args.warmup):
+        y0 = rows[(i * 7) % len(rows)]
+        cpu_band_step(spec, L, R, rect, y0, y0 + band)
+    tot_t, tot_n = 0.0, 0
+    for i in range(args.steps):
+        y0 = rows[(i * 5 + 3) % len(rows)]
+        dt, n = cpu_band_step(spec, L, R, rect, y0, y0 + band)
+        tot_t += dt
+        tot_n += n
+    value = tot_n / tot_t / 1e6
+    res = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene renderer)",
+           "config": {"workload": WORKLOAD, "parallelism": "host threads"}, "impl": "reference",
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"each step: {band} rectified rows of the 5 MP pair, whole path incl. filters"},
+           "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(res))
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

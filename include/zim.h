@@ -1,0 +1,245 @@
+/*
+ * zim.h -- C ABI of zim_gb300, the GB300 (sm_103a) structured-light stereo
+ * reconstruction path: phase-shift decode + unwrap, rectification, order-
+ * constrained matching, Q reprojection and point-cloud filters.
+ *
+ * Reference interfaces replaced (PhaseShiftGrayCode3D/src/):
+ *   JSLAB_PhaseShiftDecoder::Config / create / setImages / startCalculate /
+ *     getOrderMap / getModulationMap        JSLAB_PhaseShiftDecoder.h:10-92
+ *   JSLAB_DecodePhase_GPU / _Warmup / _Release
+ *                                           JSLAB_PhaseShiftDecoder_V2_GPU.h:50-60
+ *   JSLAB_StereoCalibParams_V1              JSLAB_StereoCalibParams_V1.h:9-20
+ *   JSLAB_PhaseEpipolarReconstructor_V2::Config / setCalibrationParams /
+ *     setData / startCalculate / getDisparityMap
+ *                                           JSLAB_PhaseEpipolarReconstructor_V2.h:11-171
+ *   JSLAB_ReconstructPipeline_GPU           JSLAB_PhaseEpipolarReconstructor_V2_GPU.h:131-137
+ *   applyMLSFilterToPointCloud              JSLAB_MLS_Filter.h:31-57
+ *
+ * Conventions: plain pointers and sizes only.  Unless a name ends in _host,
+ * every array argument is DEVICE memory and work is enqueued on `stream`
+ * (a cudaStream_t passed as void*, NULL = legacy default stream); calls are
+ * asynchronous w.r.t. the host.  Images are row-major, tightly packed.
+ * A decoded phase is carried as (order k, residual r): phase = 2*pi*k + r,
+ * which keeps 1e-6 rad resolution at hundreds of fringe periods in FP32.
+ * Errors: every call returns a zim_status; nothing throws across the ABI;
+ * zim_last_error() describes the last failure on that context.
+ * Threading: one context per host thread; a context is not re-entrant.
+ */
+#ifndef ZIM_H
+#define ZIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define ZIM_API __declspec(dllexport)
+#else
+#define ZIM_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum zim_status {
+    ZIM_OK = 0,
+    ZIM_ERR_INVALID_ARG = 1,    /* bad pointer/size/config (reference: CV_Assert, nullptr factory) */
+    ZIM_ERR_UNSUPPORTED = 2,    /* valid but not implemented on this path */
+    ZIM_ERR_NOT_CALIBRATED = 3, /* reconstruction before zim_set_calibration */
+    ZIM_ERR_CUDA = 4,           /* a CUDA runtime call failed */
+    ZIM_ERR_OUT_OF_MEMORY = 5,  /* scratch allocation failed */
+    ZIM_ERR_TIMEOUT = 6,        /* a bounded device wait gave up */
+    ZIM_ERR_DEVICE_CHECK = 7    /* a kernel's own bounds check tripped (device error word) */
+} zim_status;
+
+typedef struct zim_ctx zim_ctx;
+
+typedef enum zim_encoding {
+    ZIM_ENC_HETERODYNE3 = 0,            /* reference: 3-frequency heterodyne, beat-to-one */
+    ZIM_ENC_HIERARCHICAL = 1,           /* temporal unwrapping, f0 = 1, integer ratios */
+    ZIM_ENC_GRAYCODE = 2,               /* N-step phase shift + Gray code */
+    ZIM_ENC_GRAYCODE_COMPLEMENTARY = 3  /* ... + one complementary (half-period) Gray bit */
+} zim_encoding;
+
+typedef enum zim_sample_type { ZIM_SAMPLE_U8 = 0, ZIM_SAMPLE_U16 = 1 } zim_sample_type;
+
+/* JSLAB_PhaseShiftDecoder::Config (JSLAB_PhaseShiftDecoder.h:22-54), plus the
+ * encoding selector.  Frames are ordered frequency 0 steps, frequency 1 steps,
+ * ... (JSLAB_PhaseShiftDecoder_V2.cpp:230-238); Gray encodings: the shift_num[0]
+ * phase frames, then gray_bits Gray frames MSB first, then the complementary frame. */
+typedef struct zim_decode_config {
+    double freq[4];              /* fringe counts across the projector (integers) */
+    int shift_num[4];            /* phase steps per frequency (3..32) */
+    double modulation_threshold; /* default 1.0 */
+    double preblur_sigma;        /* 3x3 pre-blur sigma, default 3.0 (<= 0: OpenCV default kernel) */
+    int avg_three_phase;         /* default 1 (heterodyne only) */
+    int post_smooth;             /* default 1: 3x3 Gaussian of the absolute phase */
+    int enable_hdr;              /* default 0; 1 is not implemented (ZIM_ERR_UNSUPPORTED) */
+    double hdr_saturation_gray;
+    double hdr_min_amplitude;
+    int encoding;                /* zim_encoding, default ZIM_ENC_HETERODYNE3 */
+    int n_freq;                  /* frequencies used (heterodyne 3, hierarchical 2..4, Gray 1) */
+    int gray_bits;               /* Gray encodings: bits (1..12) */
+} zim_decode_config;
+
+/* JSLAB_StereoCalibParams_V1 (JSLAB_StereoCalibParams_V1.h:9-20): row-major
+ * 3x3 K, (k1 k2 p1 p2 k3), left->right R and t, calibration image size. */
+typedef struct zim_stereo_calib {
+    double camera_matrix[2][9];
+    double dist_coeffs[2][5];
+    double R[9];
+    double t[3];
+    int width, height;
+} zim_stereo_calib;
+
+/* JSLAB_PhaseEpipolarReconstructor_V2::Config (JSLAB_PhaseEpipolarReconstructor_V2.h:18-55)
+ * plus the PCL-style filters.  Filter chain order: pixel Gaussian, radius
+ * outlier (ROR), statistical outlier (SOR), MLS, metric Gaussian. */
+typedef struct zim_recon_config {
+    double min_depth, max_depth;             /* 0, 1000 */
+    double min_phase_diff, max_phase_diff;   /* unused by V2, kept for layout parity */
+    double grad_threshold;                   /* 1.0 */
+    int use_rectified_coords;                /* 1 */
+    int use_disp_median_filter;              /* 1 */
+    int use_full_left_rectification;         /* 1 */
+    int use_px_gaussian;                     /* 1: applyGaussianFilterToPointCloudV2 */
+    int px_gaussian_updates_mask;            /* 0: CPU semantics (ROR sees the pre-filter mask); 1: GPU semantics */
+    int use_ror;                             /* 1 */
+    float radius_search;                     /* 0.7 */
+    int radius_min_neighbors;                /* 10 */
+    int radius_window_size;                  /* 10 */
+    int use_mls;                             /* 0 */
+    int mls_window_size;                     /* 30 (half size) */
+    float mls_spatial_sigma;                 /* 0.6 */
+    int mls_polynomial_order;                /* 1 */
+    float mls_max_radius;                    /* 0 = 3 sigma */
+    int mls_iterations;                      /* 3 */
+    int use_sor;                             /* 0: PCL StatisticalOutlierRemoval semantics */
+    int sor_mean_k;                          /* 50 */
+    double sor_std_mul;                      /* 1.0 */
+    int use_metric_gaussian;                 /* 0: radius-3-sigma Gaussian in millimetres */
+    double metric_gaussian_sigma;            /* 0.5 */
+} zim_recon_config;
+
+/* PCL PointXYZ memory layout: x, y, z, padding (16 bytes). */
+typedef struct zim_point_xyz { float x, y, z, pad; } zim_point_xyz;
+
+ZIM_API const char* zim_version(void);
+ZIM_API void zim_decode_config_default(zim_decode_config* cfg);
+ZIM_API void zim_recon_config_default(zim_recon_config* cfg);
+
+/* Frames a config consumes; <= 0 if the config is invalid. */
+ZIM_API int zim_decode_frame_count(const zim_decode_config* cfg);
+/* JSLAB_PhaseShiftDecoder::create's validity test (JSLAB_PhaseShiftDecoder.cpp:9-29:
+ * nullptr unless every frequency is non-zero) plus this path's own limits. */
+ZIM_API zim_status zim_decode_validate(const zim_decode_config* cfg);
+/* Highest fringe order a config produces (the reference passes freq[0] as pha_f). */
+ZIM_API int zim_decode_max_order(const zim_decode_config* cfg);
+
+/* Context (replaces the reference decoder's static device buffers,
+ * JSLAB_PhaseShiftDecoder_V2_GPU.cu:153-185).  zim_create also warms the
+ * CUDA context (JSLAB_DecodePhase_GPU_Warmup). */
+ZIM_API zim_status zim_create(int device, zim_ctx** out);
+ZIM_API void zim_destroy(zim_ctx* ctx);
+ZIM_API const char* zim_last_error(const zim_ctx* ctx);
+/* Frees the context's scratch (JSLAB_DecodePhase_GPU_Release). */
+ZIM_API zim_status zim_release_scratch(zim_ctx* ctx);
+/* Bytes of device scratch the context currently holds. */
+ZIM_API size_t zim_scratch_bytes(const zim_ctx* ctx);
+/* Number of CUDA kernels this context has launched so far (all entry points). */
+ZIM_API unsigned long long zim_launch_count(const zim_ctx* ctx);
+/* Synchronises the context's device and reads/clears the device error word. */
+ZIM_API zim_status zim_check_device(zim_ctx* ctx, uint32_t* error_word);
+
+/* ---- decoder: JSLAB_DecodePhase_GPU (JSLAB_PhaseShiftDecoder_V2_GPU.cu:192-291) ----
+ * frames: zim_decode_frame_count(cfg) planes of rows*cols samples (u8 or u16).
+ * Outputs (rows*cols each): order (getOrderMap), residual (phase - 2*pi*order,
+ * unsmoothed; 0 where invalid), mod (getModulationMap: frequency-0 normalised
+ * modulation), valid (1/0).  Any output pointer except order/residual may be NULL. */
+ZIM_API zim_status zim_decode(zim_ctx* ctx, const zim_decode_config* cfg, const void* frames,
+                              int sample_type, int rows, int cols, int32_t* order, float* residual,
+                              float* mod, uint8_t* valid, void* stream);
+
+/* startCalculate(phase) as CV_64F: phase = 2*pi*order + residual, then the
+ * optional 3x3 post-smooth (JSLAB_PhaseShiftDecoder_V2.cpp:274-295). */
+ZIM_API zim_status zim_decode_phase_f64(zim_ctx* ctx, const int32_t* order, const float* residual,
+                                        int rows, int cols, int post_smooth, double* phase,
+                                        void* stream);
+
+/* ---- reconstructor ----
+ * setCalibrationParams (JSLAB_PhaseEpipolarReconstructor_V2.cpp:292-339):
+ * stereoRectify(flags 0, alpha -1), optional full-left canvas, rectification
+ * maps (built once, on the device, in FP64). */
+ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo_calib* calib,
+                                       int use_full_left_rectification);
+ZIM_API zim_status zim_get_rectification(const zim_ctx* ctx, double R1[9], double R2[9],
+                                         double P1[12], double P2[12], double Q[16], int* rect_w,
+                                         int* rect_h);
+/* Copies the float rectification maps (rect_h*rect_w each) into device buffers. */
+ZIM_API zim_status zim_get_rectify_maps(zim_ctx* ctx, int cam, float* mapx, float* mapy,
+                                        void* stream);
+
+/* setData for one camera (JSLAB_PhaseEpipolarReconstructor_V2.cpp:368-395):
+ * post-smooth (optional) + remap INTER_LINEAR of the phase, INTER_NEAREST of
+ * the order.  Rectified phase = 2*pi*rect_base + rect_res (rect_h*rect_w). */
+ZIM_API zim_status zim_rectify(zim_ctx* ctx, int cam, const int32_t* order, const float* residual,
+                               int rows, int cols, int post_smooth, int32_t* rect_base,
+                               float* rect_res, int32_t* rect_order, void* stream);
+
+/* stereoMatch (JSLAB_PhaseEpipolarReconstructor_V2.cpp:933-1006): disparity
+ * (0 = no match) and the integer match column (-1 = none; may be NULL). */
+ZIM_API zim_status zim_match(zim_ctx* ctx, const int32_t* l_base, const float* l_res,
+                             const int32_t* l_order, const int32_t* r_base, const float* r_res,
+                             const int32_t* r_order, int rows, int cols, int pha_f,
+                             double grad_threshold, float* disp, int32_t* best_col, void* stream);
+
+/* Optional 5x5 median (reference :405-410) + Q reprojection (:414-461). */
+ZIM_API zim_status zim_median_reproject(zim_ctx* ctx, const zim_recon_config* cfg,
+                                        const float* disp, int rows, int cols, float* disp_out,
+                                        float* xyz, uint8_t* mask, void* stream);
+
+/* Point-cloud filters on an organised cloud (rows*cols points, xyz float3). */
+ZIM_API zim_status zim_filter_px_gaussian(zim_ctx* ctx, const float* xyz, const uint8_t* mask,
+                                          int rows, int cols, float* out, uint8_t* mask_out,
+                                          void* stream);
+ZIM_API zim_status zim_filter_ror(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
+                                  int cols, float radius, int min_neighbors, int window_size,
+                                  float* out, uint8_t* mask_out, void* stream);
+ZIM_API zim_status zim_filter_mls(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
+                                  int cols, int window, float sigma, int order, float max_radius,
+                                  int iterations, float* out, void* stream);
+ZIM_API zim_status zim_filter_sor(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
+                                  int cols, int mean_k, double std_mul, uint8_t* mask_out,
+                                  float* mean_dist, void* stream);
+ZIM_API zim_status zim_filter_metric_gaussian(zim_ctx* ctx, const float* xyz, const uint8_t* mask,
+                                              int rows, int cols, double sigma, float* out,
+                                              void* stream);
+
+/* Compacts valid points into PCL PointXYZ layout; *count_dev (device) gets the
+ * number written.  Row-major order is preserved. */
+ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz, const uint8_t* mask,
+                                      int rows, int cols, zim_point_xyz* points,
+                                      uint64_t* count_dev, void* stream);
+
+/* Whole plain per-pair path (decode L+R, rectify, match, median, reproject,
+ * filters) on device buffers.  xyz/mask/disp are rect_h*rect_w.  pha_f <= 0
+ * selects zim_decode_max_order(dcfg). */
+ZIM_API zim_status zim_reconstruct_pair(zim_ctx* ctx, const zim_decode_config* dcfg,
+                                        const zim_recon_config* rcfg, const void* left_frames,
+                                        const void* right_frames, int sample_type, int rows,
+                                        int cols, int pha_f, float* xyz, uint8_t* mask, float* disp,
+                                        void* stream);
+
+/* The same from HOST buffers (the reference's cv::Mat entry): uploads both frame
+ * stacks, runs the pair, downloads xyz and mask (and disp if non-NULL), and
+ * synchronises.  Host buffers may be pageable; pinned is faster. */
+ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_config* dcfg,
+                                             const zim_recon_config* rcfg, const void* left_frames,
+                                             const void* right_frames, int sample_type, int rows,
+                                             int cols, int pha_f, float* xyz, uint8_t* mask,
+                                             float* disp, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZIM_H */

@@ -1,0 +1,110 @@
+"""Decoder parity: zim_decode (FP32, sm_103a) against the FP64 oracle.
+
+Tolerances: fringe order, validity and Gray bits are bit-exact except on pixels
+the oracle flags as within EPS of a decision threshold (a wrapped phase within
+1e-5 rad of the +-pi wrap, a round() argument within 1e-5 of a half integer, a
+modulation within 1e-5 of the threshold); those pixels are counted and must
+stay below 1e-3 of the image.  Phase (as order + residual) agrees within
+PHASE_TOL = 1e-5 rad and modulation within 1e-5 relative on the other pixels.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import SMALL_SCENES, scene_data
+
+EPS = 1e-5
+PHASE_TOL = 1e-5
+MOD_TOL = 1e-5
+
+
+def oracle_decode(oracle, spec, frames):
+    cfg = oracle.make_decode_cfg(**spec.decode_kwargs())
+    return oracle.decode(cfg, frames, eps=EPS)
+
+
+def gpu_decode(ctx, spec, frames):
+    from zim_gb300 import api
+    cfg = api.decode_config(**spec.decode_kwargs())
+    d = api.decode(ctx, cfg, torch.from_numpy(frames).cuda())
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def compare_decode(o, g, report=None):
+    phase, order, mod, valid, near = o
+    near_b = near != 0
+    vmis = (g["valid"] != valid)
+    omis = (g["order"] != order) & (valid > 0) & (g["valid"] > 0)
+    stats = dict(pixels=valid.size, valid=int(valid.sum()), near=int(near_b.sum()),
+                 valid_mismatch=int(vmis.sum()), order_mismatch=int(omis.sum()),
+                 unexplained_valid=int((vmis & ~near_b).sum()), unexplained_order=int((omis & ~near_b).sum()))
+    both = (valid > 0) & (g["valid"] > 0) & ~near_b & ~omis
+    res_o = phase - 2 * math.pi * order
+    err = np.abs(g["residual"].astype(np.float64) - res_o)[both]
+    stats["phase_max_err"] = float(err.max()) if err.size else 0.0
+    stats["phase_rms_err"] = float(np.sqrt((err ** 2).mean())) if err.size else 0.0
+    m = ~near_b
+    merr = np.abs(g["mod"].astype(np.float64) - mod)[m] / np.maximum(1.0, np.abs(mod[m]))
+    stats["mod_max_err"] = float(merr.max())
+    if report is not None:
+        report.update(stats)
+    return stats
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,kw", SMALL_SCENES)
+def test_decode_parity(ctx, oracle_lib, name, kw):
+    spec, L, R, _ = scene_data(name, **kw)
+    for frames in (L, R):
+        o = oracle_decode(oracle_lib, spec, frames)
+        g = gpu_decode(ctx, spec, frames)
+        s = compare_decode(o, g)
+        print(name, s)
+        assert s["unexplained_valid"] == 0, s
+        assert s["unexplained_order"] == 0, s
+        assert s["valid_mismatch"] + s["order_mismatch"] <= 1e-3 * s["pixels"], s
+        assert s["near"] <= 1e-3 * s["pixels"], s
+        assert s["phase_max_err"] <= PHASE_TOL, s
+        assert s["mod_max_err"] <= MOD_TOL, s
+        # invalid pixels carry order 0 and residual 0, like the reference's zeroed maps
+        inv = g["valid"] == 0
+        assert (g["order"][inv] == 0).all() and (g["residual"][inv] == 0).all()
+
+
+@pytest.mark.gpu
+def test_decode_u8_vs_u16_same_values(ctx, oracle_lib):
+    """A u8 stack and the same values widened to u16 decode identically."""
+    spec, L, _, _ = scene_data("config0")
+    g8 = gpu_decode(ctx, spec, L)
+    g16 = gpu_decode(ctx, spec, L.astype(np.uint16))
+    for k in ("order", "residual", "mod", "valid"):
+        assert np.array_equal(g8[k], g16[k]), k
+
+
+@pytest.mark.gpu
+def test_decode_edge_shapes(ctx, oracle_lib):
+    """Ragged sizes (not multiples of the tile), one-row and one-column images."""
+    spec, L, _, _ = scene_data("config0")
+    for (h, w) in ((1, 640), (480, 1), (37, 53), (9, 33)):
+        fr = np.ascontiguousarray(L[:, :h, :w])
+        o = oracle_decode(oracle_lib, spec, fr)
+        g = gpu_decode(ctx, spec, fr)
+        s = compare_decode(o, g)
+        assert s["unexplained_valid"] == 0 and s["unexplained_order"] == 0, (h, w, s)
+        assert s["phase_max_err"] <= PHASE_TOL, (h, w, s)
+
+
+@pytest.mark.gpu
+def test_phase_f64_matches_post_smoothed_oracle(ctx, oracle_lib):
+    from zim_gb300 import api
+    spec, L, _, _ = scene_data("config1", width=612, height=512)
+    cfg = api.decode_config(**spec.decode_kwargs())
+    d = api.decode(ctx, cfg, torch.from_numpy(L).cuda())
+    ph = api.decode_phase_f64(ctx, d["order"], d["residual"], True).cpu().numpy()
+    # oracle post-smooth applied to the GPU's own unsmoothed phase isolates the smoothing
+    raw = 2 * math.pi * d["order"].cpu().numpy().astype(np.float64) + d["residual"].cpu().numpy().astype(np.float64)
+    ref = oracle_lib.post_smooth(raw)
+    assert np.abs(ph - ref).max() < 1e-9 * max(1.0, np.abs(ref).max())

@@ -1,0 +1,133 @@
+"""Point-cloud filter parity (pixel Gaussian, ROR, MLS, SOR, metric Gaussian).
+
+Every filter gets the same input cloud (the GPU's reprojected config-1-geometry
+cloud) on both sides.  Tolerances: masks bit-exact except decisions within 1e-5
+of their threshold (counted); smoothed points within POINT_TOL_MM plus 2 float
+ulps of the coordinate (an absolute 1e-5 mm cannot be represented at 900 mm,
+where one float ulp is 6.1e-5 mm).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import scene_data
+
+EPS = 1e-5
+POINT_TOL_MM = 1e-5
+
+
+def cloud(ctx, oracle, name="config1", width=612, height=512):
+    from zim_gb300 import api
+    spec, L, R, _ = scene_data(name, width=width, height=height)
+    rig = spec.rig.as_dict()
+    ctx.set_calibration(rig, True)
+    cfg = api.decode_config(**spec.decode_kwargs())
+    rects = []
+    for cam, fr in enumerate((L, R)):
+        d = api.decode(ctx, cfg, torch.from_numpy(fr).cuda())
+        rects.append(api.rectify(ctx, cam, d["order"], d["residual"], True))
+    disp, _ = api.match(ctx, rects[0], rects[1], spec.pha_f, 1.0, want_best=False)
+    _, xyz, mask = api.median_reproject(ctx, api.recon_config(), disp)
+    return xyz, mask
+
+
+def point_tol(ref):
+    return POINT_TOL_MM + 2 * np.spacing(np.abs(ref).astype(np.float32))
+
+
+def report(tag, got, ref, sel):
+    err = np.abs(got[sel].astype(np.float64) - ref[sel].astype(np.float64))
+    print(tag, "points", int(sel.sum()), "max err mm", float(err.max()) if err.size else 0.0,
+          "rms", float(np.sqrt((err ** 2).mean())) if err.size else 0.0)
+    return err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("update_mask", [False, True])
+def test_px_gaussian_parity(ctx, oracle_lib, update_mask):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    out, mo = api.filter_px_gaussian(ctx, xyz, mask, update_mask)
+    ox, om, near = oracle_lib.px_gaussian(xyz.cpu().numpy(), mask.cpu().numpy(), update_mask, eps=EPS)
+    g, gm = out.cpu().numpy(), mo.cpu().numpy()
+    assert ((gm != om) & (near == 0)).sum() == 0
+    sel = (near == 0)
+    err = report("px_gaussian", g, ox, sel)
+    assert (err <= point_tol(ox[sel])).all()
+
+
+@pytest.mark.gpu
+def test_ror_parity(ctx, oracle_lib):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    for (r, mn, win) in ((0.7, 10, 10), (0.5, 5, 5), (2.0, 30, 15)):
+        out, mo = api.filter_ror(ctx, xyz, mask, r, mn, win)
+        ox, om, near = oracle_lib.ror(xyz.cpu().numpy(), mask.cpu().numpy(), r, mn, win, eps=EPS)
+        gm = mo.cpu().numpy()
+        mis = gm != om
+        print("ror", r, mn, win, "kept", int(om.sum()), "mismatch", int(mis.sum()), "near", int(near.sum()))
+        assert (mis & (near == 0)).sum() == 0
+        assert np.array_equal(out.cpu().numpy()[~mis], ox[~mis])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order,window,sigma,radius,iters", [(2, 7, 1.41421356, 2.0, 1), (1, 5, 0.6, 0.0, 2),
+                                                               (0, 4, 0.5, 0.0, 1)])
+def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    out = api.filter_mls(ctx, xyz, mask, window, sigma, order, radius, iters)
+    ox, near = oracle_lib.mls(xyz.cpu().numpy(), mask.cpu().numpy(), window, sigma, order, radius, iters, eps=EPS)
+    g = out.cpu().numpy()
+    m = mask.cpu().numpy() > 0
+    sel = m & (near == 0)
+    err = report(f"mls o{order} w{window}", g, ox, sel)
+    tol = point_tol(ox[sel])
+    bad = (err > tol).any(axis=1)
+    print("  points beyond tolerance:", int(bad.sum()), "of", int(sel.sum()))
+    assert bad.mean() <= 1e-3
+    assert np.array_equal(g[~m], xyz.cpu().numpy()[~m])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("k", [30, 50])
+def test_sor_parity(ctx, oracle_lib, k):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    mo, md = api.filter_sor(ctx, xyz, mask, k, 1.0, want_mean_dist=True)
+    om, omd, thr, near = oracle_lib.sor(xyz.cpu().numpy(), mask.cpu().numpy(), k, 1.0, eps=EPS)
+    gm, gmd = mo.cpu().numpy(), md.cpu().numpy()
+    m = mask.cpu().numpy() > 0
+    rel = np.abs(gmd[m] - omd[m]) / np.maximum(omd[m], 1e-6)
+    mis = gm != om
+    print("sor k", k, "threshold", thr, "kept", int(om.sum()), "of", int(m.sum()), "mismatch", int(mis.sum()),
+          "mean-dist max rel err", float(rel.max()))
+    assert rel.max() <= 1e-5
+    assert (mis & (near == 0)).sum() == 0
+    assert ctx.check_device() == 0
+
+
+@pytest.mark.gpu
+def test_metric_gaussian_parity(ctx, oracle_lib):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    out = api.filter_metric_gaussian(ctx, xyz, mask, 0.5)
+    ox, near = oracle_lib.metric_gaussian(xyz.cpu().numpy(), mask.cpu().numpy(), 0.5, eps=EPS)
+    g = out.cpu().numpy()
+    m = mask.cpu().numpy() > 0
+    sel = m & (near == 0)
+    err = report("metric_gaussian", g, ox, sel)
+    bad = (err > point_tol(ox[sel])).any(axis=1)
+    assert bad.mean() <= 1e-3
+    assert np.array_equal(g[~m], xyz.cpu().numpy()[~m])
+
+
+@pytest.mark.gpu
+def test_compact_points_layout(ctx, oracle_lib):
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    pts = api.compact_points(ctx, xyz, mask).cpu().numpy()
+    m = mask.cpu().numpy() > 0
+    ref = xyz.cpu().numpy()[m]
+    assert pts.shape == (int(m.sum()), 4)
+    assert np.array_equal(pts[:, :3], ref)

@@ -1,0 +1,538 @@
+"""Python host API over the zim_gb300 C ABI.
+
+Two layers:
+
+* thin functions (``decode``, ``rectify``, ``match``, ...) that call one C-ABI
+  entry point on torch CUDA tensors, on the current torch stream;
+* mirrors of the reference's classes with the same names, argument meaning and
+  error behaviour (PhaseShiftGrayCode3D/src/): ``JSLAB_PhaseShiftDecoder``
+  (JSLAB_PhaseShiftDecoder.h:10-92), ``JSLAB_StereoCalibParams_V1``
+  (JSLAB_StereoCalibParams_V1.h:9-20) and ``JSLAB_PhaseEpipolarReconstructor_V2``
+  (JSLAB_PhaseEpipolarReconstructor_V2.h:11-171).
+
+Everything runs on the GPU through libzim_gb300.so; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import math
+from dataclasses import dataclass, field, fields
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import (ENC_GRAYCODE, ENC_GRAYCODE_COMPLEMENTARY, ENC_HETERODYNE3, ENC_HIERARCHICAL, SAMPLE_U8,
+                   SAMPLE_U16, ZimError, check)
+
+__all__ = ["Context", "decode_config", "recon_config", "calib_struct", "decode", "decode_phase_f64",
+           "rectify", "match", "median_reproject", "filter_px_gaussian", "filter_ror", "filter_mls", "filter_sor",
+           "filter_metric_gaussian", "compact_points", "reconstruct_pair", "reconstruct_pair_host", "DecodedPhase",
+           "JSLAB_PhaseShiftDecoder", "JSLAB_PhaseShiftDecoderV2_GPU", "JSLAB_StereoCalibParams_V1",
+           "JSLAB_PhaseEpipolarReconstructor_V2", "ZimError", "ENC_HETERODYNE3", "ENC_HIERARCHICAL",
+           "ENC_GRAYCODE", "ENC_GRAYCODE_COMPLEMENTARY"]
+
+
+def _p(t) -> Optional[C.c_void_p]:
+    if t is None:
+        return None
+    if isinstance(t, torch.Tensor):
+        if not t.is_cuda:
+            raise ValueError("device tensor expected")
+        if not t.is_contiguous():
+            raise ValueError("contiguous tensor expected")
+        return C.c_void_p(t.data_ptr())
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data_as(C.c_void_p)
+    return t
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Context:
+    """Owns a zim_ctx: calibration, rectification maps and scratch on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        st = self._L.zim_create(int(device), C.byref(h))
+        if st != _lib.OK:
+            raise ZimError(st, "zim_create failed")
+        self.h = h
+        self.device = device
+        self.rect_w = self.rect_h = 0
+        self.src_w = self.src_h = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.zim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        check(st, self.h)
+
+    def set_calibration(self, calib, full_left: bool = True):
+        cs = calib if isinstance(calib, _lib.StereoCalib) else calib_struct(**calib)
+        self.check(self._L.zim_set_calibration(self.h, C.byref(cs), int(bool(full_left))))
+        R1 = np.zeros(9); R2 = np.zeros(9); P1 = np.zeros(12); P2 = np.zeros(12); Q = np.zeros(16)
+        w = C.c_int(); h = C.c_int()
+        self.check(self._L.zim_get_rectification(self.h, _p(R1), _p(R2), _p(P1), _p(P2), _p(Q), C.byref(w),
+                                                 C.byref(h)))
+        self.R1, self.R2 = R1.reshape(3, 3), R2.reshape(3, 3)
+        self.P1, self.P2, self.Q = P1.reshape(3, 4), P2.reshape(3, 4), Q.reshape(4, 4)
+        self.rect_w, self.rect_h = w.value, h.value
+        self.src_w, self.src_h = cs.width, cs.height
+        return self
+
+    def rectify_maps(self, cam: int):
+        mx = torch.empty((self.rect_h, self.rect_w), dtype=torch.float32, device="cuda")
+        my = torch.empty_like(mx)
+        self.check(self._L.zim_get_rectify_maps(self.h, cam, _p(mx), _p(my), _stream()))
+        return mx, my
+
+    def scratch_bytes(self) -> int:
+        return int(self._L.zim_scratch_bytes(self.h))
+
+    def launch_count(self) -> int:
+        return int(self._L.zim_launch_count(self.h))
+
+    def check_device(self) -> int:
+        w = C.c_uint32()
+        self.check(self._L.zim_check_device(self.h, C.byref(w)))
+        return w.value
+
+
+def decode_config(encoding=ENC_HETERODYNE3, freq=(121, 110, 120), shift_num=(8, 8, 8), gray_bits=0,
+                  modulation_threshold=1.0, preblur_sigma=3.0, avg_three_phase=True, post_smooth=True,
+                  enable_hdr=False, hdr_saturation_gray=255.0, hdr_min_amplitude=2.0, n_freq=None):
+    c = _lib.DecodeConfig()
+    _lib.load().zim_decode_config_default(C.byref(c))
+    for i in range(4):
+        c.freq[i] = 0.0
+        c.shift_num[i] = 0
+    for i, f in enumerate(list(freq)[:4]):
+        c.freq[i] = float(f)
+    for i, s in enumerate(list(shift_num)[:4]):
+        c.shift_num[i] = int(s)
+    c.encoding = int(encoding)
+    c.n_freq = int(n_freq) if n_freq is not None else (
+        3 if encoding == ENC_HETERODYNE3 else (len(freq) if encoding == ENC_HIERARCHICAL else 1))
+    c.gray_bits = int(gray_bits)
+    c.modulation_threshold = float(modulation_threshold)
+    c.preblur_sigma = float(preblur_sigma)
+    c.avg_three_phase = int(bool(avg_three_phase))
+    c.post_smooth = int(bool(post_smooth))
+    c.enable_hdr = int(bool(enable_hdr))
+    c.hdr_saturation_gray = float(hdr_saturation_gray)
+    c.hdr_min_amplitude = float(hdr_min_amplitude)
+    return c
+
+
+def recon_config(**kw):
+    c = _lib.ReconConfig()
+    _lib.load().zim_recon_config_default(C.byref(c))
+    names = {f[0] for f in _lib.ReconConfig._fields_}
+    for k, v in kw.items():
+        if k not in names:
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+def calib_struct(K, D, R, t, width, height) -> _lib.StereoCalib:
+    c = _lib.StereoCalib()
+    for k in range(2):
+        for i, v in enumerate(np.asarray(K[k], float).reshape(9)):
+            c.camera_matrix[k][i] = v
+        for i, v in enumerate(np.asarray(D[k], float).reshape(5)):
+            c.dist_coeffs[k][i] = v
+    for i, v in enumerate(np.asarray(R, float).reshape(9)):
+        c.R[i] = v
+    for i, v in enumerate(np.asarray(t, float).reshape(3)):
+        c.t[i] = v
+    c.width, c.height = int(width), int(height)
+    return c
+
+
+def _sample_type(t: torch.Tensor) -> int:
+    if t.dtype == torch.uint8:
+        return SAMPLE_U8
+    if t.dtype in (torch.uint16, torch.int16):
+        return SAMPLE_U16
+    raise ValueError("frames must be uint8 or uint16")
+
+
+def frame_count(cfg) -> int:
+    return _lib.load().zim_decode_frame_count(C.byref(cfg))
+
+
+def decode(ctx: Context, cfg, frames: torch.Tensor, want_mod=True, want_valid=True):
+    """zim_decode: frames (F, H, W) u8/u16 on the device -> dict of maps."""
+    F, H, W = frames.shape
+    dev = frames.device
+    order = torch.empty((H, W), dtype=torch.int32, device=dev)
+    res = torch.empty((H, W), dtype=torch.float32, device=dev)
+    mod = torch.empty((H, W), dtype=torch.float32, device=dev) if want_mod else None
+    valid = torch.empty((H, W), dtype=torch.uint8, device=dev) if want_valid else None
+    ctx.check(_lib.load().zim_decode(ctx.h, C.byref(cfg), _p(frames), _sample_type(frames), H, W, _p(order), _p(res),
+                                     _p(mod), _p(valid), _stream()))
+    return dict(order=order, residual=res, mod=mod, valid=valid)
+
+
+def decode_phase_f64(ctx: Context, order, residual, post_smooth=True):
+    H, W = order.shape
+    out = torch.empty((H, W), dtype=torch.float64, device=order.device)
+    ctx.check(_lib.load().zim_decode_phase_f64(ctx.h, _p(order), _p(residual), H, W, int(bool(post_smooth)), _p(out),
+                                               _stream()))
+    return out
+
+
+def rectify(ctx: Context, cam, order, residual, post_smooth=True):
+    H, W = order.shape
+    shp = (ctx.rect_h, ctx.rect_w)
+    base = torch.empty(shp, dtype=torch.int32, device=order.device)
+    res = torch.empty(shp, dtype=torch.float32, device=order.device)
+    rord = torch.empty(shp, dtype=torch.int32, device=order.device)
+    ctx.check(_lib.load().zim_rectify(ctx.h, int(cam), _p(order), _p(residual), H, W, int(bool(post_smooth)),
+                                      _p(base), _p(res), _p(rord), _stream()))
+    return base, res, rord
+
+
+def match(ctx: Context, left, right, pha_f, grad_threshold=1.0, want_best=True):
+    """left/right: (base, res, order) rectified triples."""
+    lb, lr, lo = left
+    rb, rr, ro = right
+    H, W = lo.shape
+    disp = torch.empty((H, W), dtype=torch.float32, device=lo.device)
+    best = torch.empty((H, W), dtype=torch.int32, device=lo.device) if want_best else None
+    ctx.check(_lib.load().zim_match(ctx.h, _p(lb), _p(lr), _p(lo), _p(rb), _p(rr), _p(ro), H, W, int(pha_f),
+                                    float(grad_threshold), _p(disp), _p(best), _stream()))
+    return disp, best
+
+
+def median_reproject(ctx: Context, rcfg, disp):
+    H, W = disp.shape
+    dout = torch.empty_like(disp)
+    xyz = torch.empty((H, W, 3), dtype=torch.float32, device=disp.device)
+    mask = torch.empty((H, W), dtype=torch.uint8, device=disp.device)
+    ctx.check(_lib.load().zim_median_reproject(ctx.h, C.byref(rcfg), _p(disp), H, W, _p(dout), _p(xyz), _p(mask),
+                                               _stream()))
+    return dout, xyz, mask
+
+
+def filter_px_gaussian(ctx, xyz, mask, update_mask=False):
+    H, W = mask.shape
+    out = torch.empty_like(xyz)
+    mo = torch.empty_like(mask) if update_mask else None
+    ctx.check(_lib.load().zim_filter_px_gaussian(ctx.h, _p(xyz), _p(mask), H, W, _p(out), _p(mo), _stream()))
+    return out, (mo if update_mask else mask)
+
+
+def filter_ror(ctx, xyz, mask, radius, min_neighbors, window_size):
+    H, W = mask.shape
+    out = torch.empty_like(xyz)
+    mo = torch.empty_like(mask)
+    ctx.check(_lib.load().zim_filter_ror(ctx.h, _p(xyz), _p(mask), H, W, float(radius), int(min_neighbors),
+                                         int(window_size), _p(out), _p(mo), _stream()))
+    return out, mo
+
+
+def filter_mls(ctx, xyz, mask, window, sigma, order, max_radius=0.0, iterations=1):
+    H, W = mask.shape
+    out = torch.empty_like(xyz)
+    ctx.check(_lib.load().zim_filter_mls(ctx.h, _p(xyz), _p(mask), H, W, int(window), float(sigma), int(order),
+                                         float(max_radius), int(iterations), _p(out), _stream()))
+    return out
+
+
+def filter_sor(ctx, xyz, mask, mean_k, std_mul=1.0, want_mean_dist=False):
+    H, W = mask.shape
+    mo = torch.empty_like(mask)
+    md = torch.empty((H, W), dtype=torch.float32, device=mask.device) if want_mean_dist else None
+    ctx.check(_lib.load().zim_filter_sor(ctx.h, _p(xyz), _p(mask), H, W, int(mean_k), float(std_mul), _p(mo), _p(md),
+                                         _stream()))
+    return mo, md
+
+
+def filter_metric_gaussian(ctx, xyz, mask, sigma):
+    H, W = mask.shape
+    out = torch.empty_like(xyz)
+    ctx.check(_lib.load().zim_filter_metric_gaussian(ctx.h, _p(xyz), _p(mask), H, W, float(sigma), _p(out),
+                                                     _stream()))
+    return out
+
+
+def compact_points(ctx, xyz, mask):
+    """Valid points in PCL PointXYZ layout (N, 4) float32, row-major order."""
+    H, W = mask.shape
+    pts = torch.empty((H * W, 4), dtype=torch.float32, device=mask.device)
+    cnt = torch.zeros(1, dtype=torch.int64, device=mask.device)
+    ctx.check(_lib.load().zim_compact_points(ctx.h, _p(xyz), _p(mask), H, W, _p(pts), _p(cnt), _stream()))
+    return pts[: int(cnt.item())]
+
+
+def reconstruct_pair(ctx, dcfg, rcfg, left, right, pha_f=0, out=None, want_disp=False):
+    """Whole plain per-pair path on device frames.  Returns (xyz, mask, disp)."""
+    F, H, W = left.shape
+    if out is None:
+        xyz = torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32, device=left.device)
+        mask = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device=left.device)
+        disp = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.float32, device=left.device) if want_disp else None
+    else:
+        xyz, mask, disp = out
+    ctx.check(_lib.load().zim_reconstruct_pair(ctx.h, C.byref(dcfg), C.byref(rcfg), _p(left), _p(right),
+                                               _sample_type(left), H, W, int(pha_f), _p(xyz), _p(mask), _p(disp),
+                                               _stream()))
+    return xyz, mask, disp
+
+
+def reconstruct_pair_host(ctx, dcfg, rcfg, left: np.ndarray, right: np.ndarray, pha_f=0, xyz=None, mask=None,
+                          disp=None):
+    """The same from host arrays (numpy or pinned CPU tensors); synchronous."""
+    F, H, W = left.shape
+    st = SAMPLE_U8 if left.dtype in (np.uint8, torch.uint8) else SAMPLE_U16
+    if xyz is None:
+        xyz = np.empty((ctx.rect_h, ctx.rect_w, 3), np.float32)
+    if mask is None:
+        mask = np.empty((ctx.rect_h, ctx.rect_w), np.uint8)
+
+    def hp(a):
+        if a is None:
+            return None
+        if isinstance(a, torch.Tensor):
+            return C.c_void_p(a.data_ptr())
+        return a.ctypes.data_as(C.c_void_p)
+
+    ctx.check(_lib.load().zim_reconstruct_pair_host(ctx.h, C.byref(dcfg), C.byref(rcfg), hp(left), hp(right), st, H,
+                                                    W, int(pha_f), hp(xyz), hp(mask), hp(disp), _stream()))
+    return xyz, mask, disp
+
+
+# ---------------------------------------------------------------------------
+# Reference-shaped classes
+# ---------------------------------------------------------------------------
+@dataclass
+class DecodedPhase:
+    """A decoded camera: phase = 2*pi*order + residual (unsmoothed)."""
+    order: torch.Tensor
+    residual: torch.Tensor
+    mod: Optional[torch.Tensor]
+    valid: Optional[torch.Tensor]
+    post_smooth: bool
+
+
+class JSLAB_PhaseShiftDecoder:
+    """Mirror of the reference's abstract decoder + factory (JSLAB_PhaseShiftDecoder.h:10-92)."""
+
+    class Version(enum.Enum):
+        V1 = 0
+        V2 = 1
+
+    @dataclass
+    class Config:
+        freq: Sequence[float] = (121.0, 110.0, 120.0)
+        shift_num: Sequence[int] = (8, 8, 8)
+        modulation_threshold: float = 1.0
+        preblur_sigma: float = 3.0
+        avg_three_phase: bool = True
+        post_smooth: bool = True
+        enable_hdr: bool = False
+        hdr_saturation_gray: float = 255.0
+        hdr_min_amplitude: float = 2.0
+        encoding: int = ENC_HETERODYNE3
+        gray_bits: int = 0
+
+    @staticmethod
+    def create(config: "JSLAB_PhaseShiftDecoder.Config", version: "JSLAB_PhaseShiftDecoder.Version" = None,
+               ctx: Optional[Context] = None):
+        """Returns a GPU decoder, or None for an invalid config (JSLAB_PhaseShiftDecoder.cpp:9-29).
+
+        The reference's default version is V1 (the legacy decoder without order
+        maps); this path implements V2 only and raises ZimError(UNSUPPORTED) for V1.
+        """
+        version = JSLAB_PhaseShiftDecoder.Version.V1 if version is None else version
+        cfg = _config_struct(config)
+        st = _lib.load().zim_decode_validate(C.byref(cfg))
+        if st == _lib.ERR_INVALID_ARG:
+            return None
+        if st != _lib.OK:
+            raise ZimError(st, "unsupported decoder configuration")
+        if version != JSLAB_PhaseShiftDecoder.Version.V2:
+            raise ZimError(_lib.ERR_UNSUPPORTED, "only Version.V2 is implemented on the GPU path")
+        return JSLAB_PhaseShiftDecoderV2_GPU(config, ctx)
+
+
+def _config_struct(config: JSLAB_PhaseShiftDecoder.Config):
+    return decode_config(encoding=config.encoding, freq=config.freq, shift_num=config.shift_num,
+                         gray_bits=config.gray_bits, modulation_threshold=config.modulation_threshold,
+                         preblur_sigma=config.preblur_sigma, avg_three_phase=config.avg_three_phase,
+                         post_smooth=config.post_smooth, enable_hdr=config.enable_hdr,
+                         hdr_saturation_gray=config.hdr_saturation_gray, hdr_min_amplitude=config.hdr_min_amplitude)
+
+
+class JSLAB_PhaseShiftDecoderV2_GPU(JSLAB_PhaseShiftDecoder):
+    """JSLAB_PhaseShiftDecoderV2_GPU (JSLAB_PhaseShiftDecoder_V2_GPU.h:13-33) on zim_decode."""
+
+    def __init__(self, config: JSLAB_PhaseShiftDecoder.Config, ctx: Optional[Context] = None):
+        self.m_config = config
+        self._cfg = _config_struct(config)
+        self._ctx = ctx or Context(torch.cuda.current_device())
+        self._frames = None
+        self._dec: Optional[DecodedPhase] = None
+
+    def setImages(self, images):
+        """images: a (F, H, W) tensor/array or a list of F (H, W) frames, frequency-major order."""
+        n = frame_count(self._cfg)
+        if isinstance(images, (list, tuple)):
+            if len(images) != n:
+                raise ZimError(_lib.ERR_INVALID_ARG, f"expected {n} images, got {len(images)}")
+            images = torch.stack([torch.as_tensor(np.asarray(i)) if not isinstance(i, torch.Tensor) else i
+                                  for i in images])
+        elif not isinstance(images, torch.Tensor):
+            images = torch.as_tensor(np.asarray(images))
+        if images.dim() != 3 or images.shape[0] != n:
+            raise ZimError(_lib.ERR_INVALID_ARG, "image stack shape mismatch")
+        self._frames = images.to("cuda", non_blocking=True).contiguous()
+
+    def startCalculate(self) -> torch.Tensor:
+        """Decodes and returns the absolute phase (float64, post-smoothed if configured)."""
+        if self._frames is None:
+            raise ZimError(_lib.ERR_INVALID_ARG, "setImages first")
+        d = decode(self._ctx, self._cfg, self._frames)
+        self._dec = DecodedPhase(d["order"], d["residual"], d["mod"], d["valid"], bool(self.m_config.post_smooth))
+        return decode_phase_f64(self._ctx, d["order"], d["residual"], self.m_config.post_smooth)
+
+    def getOrderMap(self) -> torch.Tensor:
+        return self._dec.order.clone()
+
+    def getModulationMap(self) -> torch.Tensor:
+        return self._dec.mod.to(torch.float64)
+
+    def getDecoded(self) -> DecodedPhase:
+        return self._dec
+
+
+@dataclass
+class JSLAB_StereoCalibParams_V1:
+    """Mirror of JSLAB_StereoCalibParams_V1 (JSLAB_StereoCalibParams_V1.h:9-20)."""
+    camera_matrix: list = field(default_factory=lambda: [np.eye(3), np.eye(3)])
+    dist_coeffs: list = field(default_factory=lambda: [np.zeros(5), np.zeros(5)])
+    R: np.ndarray = field(default_factory=lambda: np.eye(3))
+    t: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    image_size: tuple = (0, 0)  # (width, height) like cv::Size
+
+    def as_struct(self):
+        return calib_struct(self.camera_matrix, self.dist_coeffs, self.R, self.t, self.image_size[0],
+                            self.image_size[1])
+
+
+class JSLAB_PhaseEpipolarReconstructor_V2:
+    """Mirror of JSLAB_PhaseEpipolarReconstructor_V2 (JSLAB_PhaseEpipolarReconstructor_V2.h:11-171)."""
+
+    @dataclass
+    class Config:
+        min_depth: float = 0.0
+        max_depth: float = 1000.0
+        min_phase_diff: float = 0.03
+        max_phase_diff: float = 0.4
+        grad_threshold: float = 1.0
+        use_rectified_coords: bool = True
+        use_disp_median_filter: bool = True
+        use_full_left_rectification: bool = True
+        radius_search: float = 0.7
+        radius_min_neighbors: int = 10
+        radius_window_size: int = 10
+        use_mls: bool = False
+        mls_window_size: int = 30
+        mls_spatial_sigma: float = 0.6
+        use_gpu_mls: bool = True
+        mls_polynomial_order: int = 1
+        mls_max_radius: float = 0.0
+        mls_iterations: int = 3
+        # additions of this path
+        use_px_gaussian: bool = True
+        px_gaussian_updates_mask: bool = False
+        use_ror: bool = True
+        use_sor: bool = False
+        sor_mean_k: int = 50
+        sor_std_mul: float = 1.0
+        use_metric_gaussian: bool = False
+        metric_gaussian_sigma: float = 0.5
+
+        def as_struct(self):
+            kw = {f.name: getattr(self, f.name) for f in fields(self) if f.name != "use_gpu_mls"}
+            for k, v in kw.items():
+                if isinstance(v, bool):
+                    kw[k] = int(v)
+            return recon_config(**kw)
+
+    def __init__(self, config: "JSLAB_PhaseEpipolarReconstructor_V2.Config" = None, ctx: Optional[Context] = None):
+        self.m_config = config or JSLAB_PhaseEpipolarReconstructor_V2.Config()
+        self._ctx = ctx or Context(torch.cuda.current_device())
+        self._rect = None
+        self._pha_f = 0
+        self._disp = None
+
+    @property
+    def context(self) -> Context:
+        return self._ctx
+
+    def setCalibrationParams(self, params: JSLAB_StereoCalibParams_V1):
+        self._ctx.set_calibration(params.as_struct(), self.m_config.use_full_left_rectification)
+
+    def setData(self, left, right, left_k=None, right_k=None, left_mod=None, pha_f: int = 0):
+        """left/right: DecodedPhase (exact path) or float64 absolute-phase maps with left_k/right_k.
+
+        A float64 map is taken as already post-smoothed (the reference's decoder
+        output); it is split into order + residual and rectified without a
+        second smoothing.
+        """
+        cams = []
+        for cam, (ph, k) in enumerate(((left, left_k), (right, right_k))):
+            if isinstance(ph, DecodedPhase):
+                cams.append(rectify(self._ctx, cam, ph.order, ph.residual, ph.post_smooth))
+                ords = ph.order
+            else:
+                ph = torch.as_tensor(ph).to("cuda", torch.float64)
+                k = torch.as_tensor(k).to("cuda", torch.int32).contiguous()
+                res = (ph - 2 * math.pi * k.to(torch.float64)).to(torch.float32).contiguous()
+                cams.append(rectify(self._ctx, cam, k, res, False))
+        self._rect = cams
+        self._pha_f = int(pha_f)
+
+    def startCalculate(self):
+        """Runs match -> median -> reproject -> filters; returns (xyz, P)."""
+        if self._rect is None:
+            raise ZimError(_lib.ERR_INVALID_ARG, "setData first")
+        c = self.m_config
+        rc = c.as_struct()
+        disp, _ = match(self._ctx, self._rect[0], self._rect[1], self._pha_f, c.grad_threshold, want_best=False)
+        dmed, xyz, mask = median_reproject(self._ctx, rc, disp)
+        self._disp = dmed
+        if c.use_px_gaussian:
+            xyz, mask = filter_px_gaussian(self._ctx, xyz, mask, c.px_gaussian_updates_mask)
+        if c.use_ror:
+            xyz, mask = filter_ror(self._ctx, xyz, mask, c.radius_search, c.radius_min_neighbors,
+                                   c.radius_window_size)
+        if c.use_sor:
+            mask, _ = filter_sor(self._ctx, xyz, mask, c.sor_mean_k, c.sor_std_mul)
+            xyz = xyz * mask.unsqueeze(-1).to(xyz.dtype)
+        if c.use_mls:
+            xyz = filter_mls(self._ctx, xyz, mask, c.mls_window_size, c.mls_spatial_sigma, c.mls_polynomial_order,
+                             c.mls_max_radius, c.mls_iterations)
+        if c.use_metric_gaussian:
+            xyz = filter_metric_gaussian(self._ctx, xyz, mask, c.metric_gaussian_sigma)
+        return xyz, mask
+
+    def getDisparityMap(self) -> torch.Tensor:
+        return self._disp.clone()

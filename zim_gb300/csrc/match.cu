@@ -1,0 +1,126 @@
+// match.cu -- row-wise order-constrained absolute-phase matching with
+// three-point sub-pixel refinement.
+//
+// Reference: PhaseShiftGrayCode3D/src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:933-1006
+// (stereoMatch) and the GPU span-table variant
+// JSLAB_PhaseEpipolarReconstructor_V2_GPU.cu:18-113.
+//
+// One CTA per rectified row.  The right row (order, phase base, residual) is
+// staged in shared memory; the per-order column span [lo, hi] is built with
+// shared-memory atomics; each left pixel of order k in [1, pha_f] scans the
+// span for right pixels of order k and keeps the first column of minimum
+// |phase_R - phase_L| (strict <, so the smallest column wins ties), rejects
+// min >= grad_threshold and columns < 2 or >= cols - 1, then refines with the
+// parabola through the costs of columns best-1, best, best+1.
+#include <climits>
+
+#include "zim_internal.cuh"
+
+namespace {
+
+constexpr int MATCH_THREADS = 256;
+
+__device__ __forceinline__ float phase_diff(int bR, float rR, int bL, float rL) {
+    // (2 pi bR + rR) - (2 pi bL + rL) with the integer cycles subtracted exactly
+    return fmaf((float)(bR - bL), ZIM_TWO_PI_F, rR - rL);
+}
+
+__global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
+    const int32_t* __restrict__ l_base, const float* __restrict__ l_res, const int32_t* __restrict__ l_order,
+    const int32_t* __restrict__ r_base, const float* __restrict__ r_res, const int32_t* __restrict__ r_order,
+    int cols, int pha_f, float grad_threshold, float* __restrict__ disp, int32_t* __restrict__ best_col) {
+    extern __shared__ int4 smem_raw[];
+    int* s_ord = reinterpret_cast<int*>(smem_raw);
+    int* s_base = s_ord + cols;
+    float* s_res = reinterpret_cast<float*>(s_base + cols);
+    int* s_lo = reinterpret_cast<int*>(s_res + cols);
+    int* s_hi = s_lo + (pha_f + 1);
+
+    const int row = blockIdx.x;
+    const size_t ro = (size_t)row * cols;
+    for (int k = threadIdx.x; k <= pha_f; k += blockDim.x) {
+        s_lo[k] = INT_MAX;
+        s_hi[k] = -1;
+    }
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        s_ord[j] = r_order[ro + j];
+        s_base[j] = r_base[ro + j];
+        s_res[j] = r_res[ro + j];
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        int k = s_ord[j];
+        if (k >= 0 && k <= pha_f) {
+            atomicMin(&s_lo[k], j);
+            atomicMax(&s_hi[k], j);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        const int k = l_order[ro + j];
+        float d = 0.f;
+        int best = -1;
+        if (k >= 1 && k <= pha_f) {
+            const int lo = s_lo[k], hi = s_hi[k];
+            if (lo <= hi) {
+                const int bL = l_base[ro + j];
+                const float rL = l_res[ro + j];
+                float min_cost = 1e9f;
+                int bj = -1;
+                for (int c = lo; c <= hi; c++) {
+                    if (s_ord[c] != k) continue;
+                    float diff = fabsf(phase_diff(s_base[c], s_res[c], bL, rL));
+                    if (diff < min_cost) {
+                        min_cost = diff;
+                        bj = c;
+                    }
+                }
+                if (bj >= 0 && min_cost < grad_threshold && bj >= 2 && bj < cols - 1) {
+                    float c0 = phase_diff(s_base[bj - 1], s_res[bj - 1], bL, rL);
+                    float c1 = phase_diff(s_base[bj], s_res[bj], bL, rL);
+                    float c2 = phase_diff(s_base[bj + 1], s_res[bj + 1], bL, rL);
+                    float num = c1 * (c0 - c2);
+                    float den = 2.0f * (c0 - c1) * (c1 - c2);
+                    float delta = fabsf(den) > 1e-9f ? num / den : 0.f;
+                    d = (float)(j - bj) - delta;
+                    best = bj;
+                }
+            }
+        }
+        disp[ro + j] = d;
+        if (best_col) best_col[ro + j] = best;
+    }
+}
+
+}  // namespace
+
+zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_res, const int32_t* l_order,
+                            const int32_t* r_base, const float* r_res, const int32_t* r_order, int rows, int cols,
+                            int pha_f, double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st) {
+    size_t smem = (size_t)cols * 12 + (size_t)(pha_f + 1) * 8;
+    static int configured_for = 0;
+    if ((int)smem > 48 * 1024 && (int)smem > configured_for) {
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured_for = (int)smem;
+    }
+    match_kernel<<<rows, MATCH_THREADS, smem, st>>>(l_base, l_res, l_order, r_base, r_res, r_order, cols, pha_f,
+                                                    (float)grad_threshold, disp, best_col);
+    ctx->launches += 1;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_match(zim_ctx* ctx, const int32_t* l_base, const float* l_res,
+                                        const int32_t* l_order, const int32_t* r_base, const float* r_res,
+                                        const int32_t* r_order, int rows, int cols, int pha_f, double grad_threshold,
+                                        float* disp, int32_t* best_col, void* stream) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    if (!l_base || !l_res || !l_order || !r_base || !r_res || !r_order || !disp)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "null argument");
+    if (rows <= 0 || cols <= 0 || cols > ZIM_MAX_MATCH_COLS)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "cols must be in [1, %d]", ZIM_MAX_MATCH_COLS);
+    if (pha_f < 0 || pha_f > ZIM_MAX_ORDER) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pha_f out of range");
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return zim_match_launch(ctx, l_base, l_res, l_order, r_base, r_res, r_order, rows, cols, pha_f, grad_threshold,
+                            disp, best_col, zim_stream(stream));
+}
