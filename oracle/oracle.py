@@ -245,13 +245,26 @@ def ror(xyz, mask, radius, min_neighbors, window_size, eps=1e-5):
     return out, mo, near
 
 
-def mls(xyz, mask, window, sigma, order, max_radius=0.0, iterations=1, eps=1e-5):
+def mls(xyz, mask, window, sigma, order, max_radius=0.0, iterations=1, eps=1e-5, jitter=0.0, seed=0):
     xyz = _c(xyz, np.float32); mask = _c(mask, np.uint8)
     H, W = mask.shape
-    out = np.empty_like(xyz); near = np.zeros_like(mask)
+    out = np.empty(xyz.shape, np.float64); near = np.zeros_like(mask)
     lib().zo_mls(_p(xyz), _p(mask), C.c_int(H), C.c_int(W), C.c_int(window), C.c_float(sigma), C.c_int(order),
-                 C.c_float(max_radius), C.c_int(iterations), _p(out), _p(near), C.c_double(eps))
+                 C.c_float(max_radius), C.c_int(iterations), _p(out), _p(near), C.c_double(eps),
+                 C.c_double(jitter), C.c_ulonglong(seed))
     return out, near
+
+
+def mls_sensitivity(xyz, mask, window, sigma, order, max_radius=0.0, iterations=1, jitter=1e-6, runs=2):
+    """Largest output change (mm) when every neighbour offset is perturbed by a
+    relative `jitter` -- the size of FP32 rounding in the offsets.  Points where
+    it is large are ill-conditioned (e.g. three nearly collinear neighbours)."""
+    base, _ = mls(xyz, mask, window, sigma, order, max_radius, iterations)
+    sens = np.zeros(mask.shape)
+    for s in range(1, runs + 1):
+        o, _ = mls(xyz, mask, window, sigma, order, max_radius, iterations, jitter=jitter, seed=s)
+        sens = np.maximum(sens, np.abs(o - base).max(axis=-1))
+    return sens
 
 
 def sor(xyz, mask, k, std_mul=1.0, eps=1e-5):

@@ -708,7 +708,7 @@ void zo_ror(const float* xyz, const uint8_t* mask, int rows, int cols, float rad
                     double dx = (double)xyz[3 * o] - xyz[3 * q], dy = (double)xyz[3 * o + 1] - xyz[3 * q + 1],
                            dz = (double)xyz[3 * o + 2] - xyz[3 * q + 2];
                     double d2 = dx * dx + dy * dy + dz * dz;
-                    if (fabs(d2 - r2) < eps * (1 + r2)) maybe++;
+                    if (fabs(d2 - r2) < 0.1 * eps * r2) maybe++; /* FP32 |d|^2 is good to ~3e-7 relative */
                     else if (d2 <= r2) sure++;
                 }
             if (near && sure < min_neighbors && sure + maybe >= min_neighbors) near[o] = 1;
@@ -819,14 +819,26 @@ static int cholesky_solve(double A[6][6], const double b[6], double x[6], int nc
     return 1;
 }
 
+/* Deterministic factor in [1 - j, 1 + j] for neighbour q of point o (jitter
+ * used to estimate a point's sensitivity to rounding; 1 when j == 0). */
+static inline double jit(double j, uint64_t seed, size_t o, size_t q) {
+    if (j == 0) return 1.0;
+    uint64_t h = seed * 0x9E3779B97F4A7C15ull ^ (o * 0xBF58476D1CE4E5B9ull) ^ (q * 0x94D049BB133111EBull);
+    h ^= h >> 31; h *= 0xD6E8FEB86659FD93ull; h ^= h >> 32;
+    return 1.0 + j * (((double)(h >> 11) / 9007199254740992.0) * 2.0 - 1.0);
+}
+
 /* One MLS pass, src/JSLAB_MLS_Filter.cpp:161-391 (CPU order fallback: order
- * drops to 0 when fewer than min_neighbors[order] neighbours, :277-280). */
+ * drops to 0 when fewer than min_neighbors[order] neighbours, :277-280).
+ * jitter > 0 scales every neighbour offset q - p by a pseudo-random factor in
+ * [1 - jitter, 1 + jitter] (sensitivity estimate only). */
 static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, int hw, double sigma,
-                     int order_in, double r2c, float* dst, uint8_t* near, double eps) {
+                     int order_in, double r2c, double* dst, uint8_t* near, double eps, double jitter,
+                     uint64_t seed) {
     const double inv_2s2 = 1.0 / (2.0 * sigma * sigma);
     const int min_nb[3] = {3, 5, 8};
     const int order = order_in < 0 ? 0 : (order_in > 2 ? 2 : order_in);
-    memcpy(dst, src, sizeof(float) * 3 * (size_t)rows * cols);
+    for (size_t i = 0; i < 3 * (size_t)rows * cols; i++) dst[i] = src[i];
 #pragma omp parallel for schedule(dynamic, 2)
     for (int irow = 0; irow < rows; irow++) {
         for (int jcol = 0; jcol < cols; jcol++) {
@@ -842,12 +854,15 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
                 for (int jc = c0; jc < c1; jc++) {
                     size_t q = (size_t)ir * cols + jc;
                     if (!mask[q]) continue;
-                    double dx = src[3 * q] - px, dy = src[3 * q + 1] - py, dz = src[3 * q + 2] - pz;
+                    const double jf = jit(jitter, seed, o, q);
+                    const double qx = px + (src[3 * q] - px) * jf, qy = py + (src[3 * q + 1] - py) * jf,
+                                 qz = pz + (src[3 * q + 2] - pz) * jf;
+                    double dx = qx - px, dy = qy - py, dz = qz - pz;
                     double d2 = dx * dx + dy * dy + dz * dz;
-                    if (fabs(d2 - r2c) < eps * (1 + r2c)) nf = 1;
+                    if (fabs(d2 - r2c) < 0.1 * eps * r2c) nf = 1;
                     if (d2 > r2c) continue;
                     double w = exp(-d2 * inv_2s2);
-                    cx += w * src[3 * q]; cy += w * src[3 * q + 1]; cz += w * src[3 * q + 2];
+                    cx += w * qx; cy += w * qy; cz += w * qz;
                     wsum += w;
                     nv++;
                 }
@@ -860,11 +875,14 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
                 for (int jc = c0; jc < c1; jc++) {
                     size_t q = (size_t)ir * cols + jc;
                     if (!mask[q]) continue;
-                    double dx = src[3 * q] - px, dy = src[3 * q + 1] - py, dz = src[3 * q + 2] - pz;
+                    const double jf = jit(jitter, seed, o, q);
+                    const double qx = px + (src[3 * q] - px) * jf, qy = py + (src[3 * q + 1] - py) * jf,
+                                 qz = pz + (src[3 * q + 2] - pz) * jf;
+                    double dx = qx - px, dy = qy - py, dz = qz - pz;
                     double d2 = dx * dx + dy * dy + dz * dz;
                     if (d2 > r2c) continue;
                     double w = exp(-d2 * inv_2s2);
-                    double ex = src[3 * q] - cx, ey = src[3 * q + 1] - cy, ez = src[3 * q + 2] - cz;
+                    double ex = qx - cx, ey = qy - cy, ez = qz - cz;
                     cov[0][0] += w * ex * ex; cov[0][1] += w * ex * ey; cov[0][2] += w * ex * ez;
                     cov[1][1] += w * ey * ey; cov[1][2] += w * ey * ez; cov[2][2] += w * ez * ez;
                 }
@@ -875,10 +893,17 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
             double t1x = E[1][0], t1y = E[1][1], t1z = E[1][2];
             double t2x = E[2][0], t2y = E[2][1], t2z = E[2][2];
             int cur = (nv >= min_nb[order]) ? order : 0;
-            float* out = dst + 3 * o;
+            /* FP32 conditioning of the frame: a covariance known to a relative 2^-23
+             * turns the normal by about 2^-23 * l2 / (l1 - l0); flag the point when
+             * that moves the projection by more than eps (mm). */
+            const double lever = sqrt((px - cx) * (px - cx) + (py - cy) * (py - cy) + (pz - cz) * (pz - cz)) +
+                                 sqrt(fmax(ev[2], 0.0) / wsum);
+            const double kappa = fabs(ev[2]) / fmax(ev[1] - ev[0], 1e-300);
+            if (near && 4.0 * 1.2e-7 * kappa * lever > eps) near[o] = 1;
+            double* out = dst + 3 * o;
             if (cur == 0) {
                 double dot = (px - cx) * nx + (py - cy) * ny + (pz - cz) * nz;
-                out[0] = (float)(px - dot * nx); out[1] = (float)(py - dot * ny); out[2] = (float)(pz - dot * nz);
+                out[0] = px - dot * nx; out[1] = py - dot * ny; out[2] = pz - dot * nz;
                 continue;
             }
             const int nc = (cur == 1) ? 3 : 6;
@@ -887,11 +912,14 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
                 for (int jc = c0; jc < c1; jc++) {
                     size_t q = (size_t)ir * cols + jc;
                     if (!mask[q]) continue;
-                    double dx = src[3 * q] - px, dy = src[3 * q + 1] - py, dz = src[3 * q + 2] - pz;
+                    const double jf = jit(jitter, seed, o, q);
+                    const double qx = px + (src[3 * q] - px) * jf, qy = py + (src[3 * q + 1] - py) * jf,
+                                 qz = pz + (src[3 * q + 2] - pz) * jf;
+                    double dx = qx - px, dy = qy - py, dz = qz - pz;
                     double d2 = dx * dx + dy * dy + dz * dz;
                     if (d2 > r2c) continue;
                     double w = exp(-d2 * inv_2s2);
-                    double ex = src[3 * q] - cx, ey = src[3 * q + 1] - cy, ez = src[3 * q + 2] - cz;
+                    double ex = qx - cx, ey = qy - cy, ez = qz - cz;
                     double u = ex * t1x + ey * t1y + ez * t1z;
                     double v = ex * t2x + ey * t2y + ez * t2z;
                     double f = ex * nx + ey * ny + ez * nz;
@@ -903,6 +931,31 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
                 }
             for (int a = 0; a < nc; a++)
                 for (int b = 0; b < a; b++) AtWA[a][b] = AtWA[b][a];
+            if (near) {
+                /* FP32 conditioning of the normal equations in a basis scaled by the
+                 * cut-off radius: pivot ratio of the scaled Cholesky factor. */
+                static const int deg[6] = {0, 1, 1, 2, 2, 2};
+                double h = sqrt(r2c), S[6][6], L[6][6] = {{0}}, lmin = DBL_MAX, lmax = 0;
+                int ok = 1;
+                for (int a = 0; a < nc; a++)
+                    for (int b = 0; b < nc; b++) S[a][b] = AtWA[a][b] / pow(h, deg[a] + deg[b]);
+                for (int i = 0; i < nc && ok; i++)
+                    for (int j = 0; j <= i; j++) {
+                        double s = S[i][j];
+                        for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
+                        if (i == j) {
+                            if (s <= 0) { ok = 0; break; }
+                            L[i][i] = sqrt(s);
+                            lmin = fmin(lmin, L[i][i]);
+                            lmax = fmax(lmax, L[i][i]);
+                        } else {
+                            L[i][j] = s / L[j][j];
+                        }
+                    }
+                double condA = ok ? (lmax / lmin) * (lmax / lmin) : 1e300;
+                double fscale = sqrt(fmax(ev[0], 0.0) / wsum);
+                if (4.0 * 1.2e-7 * condA * fscale > eps) near[o] = 1;
+            }
             double co[6] = {0};
             int solved = cholesky_solve(AtWA, AtWf, co, nc);
             if (!solved && cur == 2) {
@@ -916,7 +969,7 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
             }
             if (!solved) {
                 double dot = (px - cx) * nx + (py - cy) * ny + (pz - cz) * nz;
-                out[0] = (float)(px - dot * nx); out[1] = (float)(py - dot * ny); out[2] = (float)(pz - dot * nz);
+                out[0] = px - dot * nx; out[1] = py - dot * ny; out[2] = pz - dot * nz;
                 continue;
             }
             double ex0 = px - cx, ey0 = py - cy, ez0 = pz - cz;
@@ -924,15 +977,16 @@ static void mls_pass(const float* src, const uint8_t* mask, int rows, int cols, 
             double v0 = ex0 * t2x + ey0 * t2y + ez0 * t2z;
             double ff = co[0] + co[1] * u0 + co[2] * v0;
             if (cur == 2) ff += co[3] * u0 * u0 + co[4] * u0 * v0 + co[5] * v0 * v0;
-            out[0] = (float)(cx + u0 * t1x + v0 * t2x + ff * nx);
-            out[1] = (float)(cy + u0 * t1y + v0 * t2y + ff * ny);
-            out[2] = (float)(cz + u0 * t1z + v0 * t2z + ff * nz);
+            out[0] = cx + u0 * t1x + v0 * t2x + ff * nx;
+            out[1] = cy + u0 * t1y + v0 * t2y + ff * ny;
+            out[2] = cz + u0 * t1z + v0 * t2z + ff * nz;
         }
     }
 }
 
 void zo_mls(const float* xyz, const uint8_t* mask, int rows, int cols, int window, float sigma, int order,
-            float max_radius, int iterations, float* out, uint8_t* near, double eps) {
+            float max_radius, int iterations, double* out, uint8_t* near, double eps, double jitter,
+            unsigned long long seed) {
     /* src/JSLAB_MLS_Filter.cpp:397-415: cut-off max_radius^2, or 9 sigma^2 when 0. */
     const double r2c = (max_radius > 0.0f) ? (double)max_radius * max_radius : 9.0 * (double)sigma * sigma;
     const int n_iter = iterations < 1 ? 1 : iterations;
@@ -941,10 +995,11 @@ void zo_mls(const float* xyz, const uint8_t* mask, int rows, int cols, int windo
     memcpy(cur, xyz, sizeof(float) * n);
     uint8_t* nf = near ? (uint8_t*)calloc((size_t)rows * cols, 1) : NULL;
     for (int it = 0; it < n_iter; it++) {
-        mls_pass(cur, mask, rows, cols, window, sigma, order, r2c, out, nf, eps);
+        mls_pass(cur, mask, rows, cols, window, sigma, order, r2c, out, nf, eps, jitter, seed + it);
         if (near)
             for (size_t i = 0; i < (size_t)rows * cols; i++) near[i] |= nf[i];
-        if (it + 1 < n_iter) memcpy(cur, out, sizeof(float) * n);
+        if (it + 1 < n_iter)
+            for (size_t i = 0; i < n; i++) cur[i] = (float)out[i]; /* the reference iterates on CV_32F */
     }
     free(cur);
     free(nf);
@@ -1127,7 +1182,7 @@ static void rad_visit(void* vs, int id) {
     rad_state* s = (rad_state*)vs;
     double dx = s->p[3 * id] - s->qx, dy = s->p[3 * id + 1] - s->qy, dz = s->p[3 * id + 2] - s->qz;
     double d2 = dx * dx + dy * dy + dz * dz;
-    if (fabs(d2 - s->r2) < s->eps * (1 + s->r2)) s->near = 1;
+    if (fabs(d2 - s->r2) < 0.1 * s->eps * s->r2) s->near = 1;
     if (d2 > s->r2) return;
     double w = exp(-d2 * s->inv2s2);
     s->sx += w * dx; s->sy += w * dy; s->sz += w * dz; s->sw += w;

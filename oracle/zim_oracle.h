@@ -118,11 +118,12 @@ void zo_ror(const float* xyz, const uint8_t* mask, int rows, int cols, float rad
             int min_neighbors, int window_size, float* out, uint8_t* mask_out,
             uint8_t* near, double eps);
 
-/* Organised-window MLS, iterations >= 1.  near: 1 = a neighbour within eps of the
- * cut-off or a count/branch decision within eps. */
+/* Organised-window MLS, iterations >= 1; out is FP64 (unrounded).  near: 1 = a neighbour within eps of the
+ * cut-off.  jitter > 0 perturbs every neighbour offset by a relative factor in
+ * [1 - jitter, 1 + jitter] (seeded) to estimate rounding sensitivity. */
 void zo_mls(const float* xyz, const uint8_t* mask, int rows, int cols, int window,
-            float sigma, int order, float max_radius, int iterations, float* out,
-            uint8_t* near, double eps);
+            float sigma, int order, float max_radius, int iterations, double* out,
+            uint8_t* near, double eps, double jitter, unsigned long long seed);
 
 /* PCL StatisticalOutlierRemoval semantics over the valid points of an organised
  * cloud: mean distance to k nearest neighbours, threshold mean + std_mul*stddev.

@@ -31,8 +31,12 @@ def cloud(ctx, oracle, name="config1", width=612, height=512):
     return xyz, mask
 
 
-def point_tol(ref):
-    return POINT_TOL_MM + 2 * np.spacing(np.abs(ref).astype(np.float32))
+def point_tol(ref, iterations=1):
+    """Per-point tolerance (N, 1): POINT_TOL_MM plus 2 float ulps of the
+    point's largest coordinate per pass (a pass feeds FP32-rounded points into
+    the next, so one ulp at 900 mm can move every coordinate of the next pass)."""
+    big = np.abs(ref).max(axis=-1, keepdims=True).astype(np.float32)
+    return POINT_TOL_MM + 2 * iterations * np.spacing(big)
 
 
 def report(tag, got, ref, sel):
@@ -60,20 +64,26 @@ def test_px_gaussian_parity(ctx, oracle_lib, update_mask):
 def test_ror_parity(ctx, oracle_lib):
     from zim_gb300 import api
     xyz, mask = cloud(ctx, oracle_lib)
-    for (r, mn, win) in ((0.7, 10, 10), (0.5, 5, 5), (2.0, 30, 15)):
+    for (r, mn, win) in ((5.0, 10, 10), (3.0, 5, 5), (8.0, 30, 15)):
         out, mo = api.filter_ror(ctx, xyz, mask, r, mn, win)
         ox, om, near = oracle_lib.ror(xyz.cpu().numpy(), mask.cpu().numpy(), r, mn, win, eps=EPS)
         gm = mo.cpu().numpy()
         mis = gm != om
         print("ror", r, mn, win, "kept", int(om.sum()), "mismatch", int(mis.sum()), "near", int(near.sum()))
         assert (mis & (near == 0)).sum() == 0
+        assert 0.5 * mask.sum().item() < om.sum()
         assert np.array_equal(out.cpu().numpy()[~mis], ox[~mis])
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("order,window,sigma,radius,iters", [(2, 7, 1.41421356, 2.0, 1), (1, 5, 0.6, 0.0, 2),
-                                                               (0, 4, 0.5, 0.0, 1)])
+# The test scene is 612 px wide (1.5 mm pixel spacing, 4x the 5 MP scene's), so
+# the 5 MP settings (radius 2 mm, sigma 2/sqrt(2)) are scaled by 4 here.
+@pytest.mark.parametrize("order,window,sigma,radius,iters", [(2, 7, 5.656854, 8.0, 1), (1, 5, 2.4, 0.0, 2),
+                                                               (0, 4, 2.0, 0.0, 1)])
 def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters):
+    """Points the oracle flags (a neighbour within 1e-6 of the cut-off, or a
+    frame / normal-equation conditioning at which FP32 rounding alone moves the
+    result by more than 1e-5 mm) are counted; all others must agree."""
     from zim_gb300 import api
     xyz, mask = cloud(ctx, oracle_lib)
     out = api.filter_mls(ctx, xyz, mask, window, sigma, order, radius, iters)
@@ -82,10 +92,13 @@ def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters):
     m = mask.cpu().numpy() > 0
     sel = m & (near == 0)
     err = report(f"mls o{order} w{window}", g, ox, sel)
-    tol = point_tol(ox[sel])
+    tol = point_tol(ox[sel], iters)
     bad = (err > tol).any(axis=1)
-    print("  points beyond tolerance:", int(bad.sum()), "of", int(sel.sum()))
-    assert bad.mean() <= 1e-3
+    allerr = np.abs(g[m].astype(np.float64) - ox[m]).max(axis=1)
+    print("  flagged:", int((m & (near > 0)).sum()), "of", int(m.sum()), " beyond tolerance:", int(bad.sum()),
+          " all-points max/rms err mm:", float(allerr.max()), float(np.sqrt((allerr ** 2).mean())))
+    assert bad.sum() == 0
+    assert (m & (near > 0)).sum() <= 0.05 * m.sum()
     assert np.array_equal(g[~m], xyz.cpu().numpy()[~m])
 
 

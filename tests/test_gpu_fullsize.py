@@ -1,0 +1,95 @@
+"""The 5 MP workload itself (2448x2048, hierarchical 1/8/64, u16 12-bit).
+
+At full size the oracle still decodes in seconds, so decode parity is checked
+directly; the rest of the path is checked through size-independent properties:
+depth against the renderer's ground truth, coverage, bounds of every order,
+and run-to-run stability.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import scene_data
+
+EPS = 1e-5
+
+
+@pytest.fixture(scope="module")
+def full():
+    return scene_data("config1")
+
+
+@pytest.mark.gpu
+def test_fullsize_decode_parity(ctx, oracle_lib, full):
+    from zim_gb300 import api
+    spec, L, R, _ = full
+    cfg = api.decode_config(**spec.decode_kwargs())
+    d = api.decode(ctx, cfg, torch.from_numpy(L).cuda())
+    g = {k: v.cpu().numpy() for k, v in d.items()}
+    ph, k, mod, valid, near = oracle_lib.decode(oracle_lib.make_decode_cfg(**spec.decode_kwargs()), L, eps=EPS)
+    nb = near != 0
+    vm = g["valid"] != valid
+    om = (g["order"] != k) & (valid > 0) & (g["valid"] > 0)
+    print("5MP decode: valid", int(valid.sum()), "near", int(nb.sum()), "valid mismatch", int(vm.sum()),
+          "order mismatch", int(om.sum()))
+    assert (vm & ~nb).sum() == 0 and (om & ~nb).sum() == 0
+    assert nb.sum() <= 1e-4 * valid.size
+    ok = (valid > 0) & (g["valid"] > 0) & ~nb & ~om
+    err = np.abs(g["residual"].astype(np.float64) - (ph - 2 * math.pi * k))[ok]
+    print("5MP decode phase max/rms err", err.max(), np.sqrt((err ** 2).mean()))
+    assert err.max() <= 1e-5
+    assert g["order"].min() >= -1 and g["order"].max() <= 64
+
+
+def config1_recon(api):
+    return api.recon_config(use_px_gaussian=0, use_ror=0, use_sor=1, sor_mean_k=30, use_mls=1, mls_window_size=7,
+                            mls_spatial_sigma=2.0 / math.sqrt(2.0), mls_polynomial_order=2, mls_max_radius=2.0,
+                            mls_iterations=1, use_metric_gaussian=1, metric_gaussian_sigma=0.5)
+
+
+@pytest.mark.gpu
+def test_fullsize_pair_against_ground_truth(ctx, oracle_lib, full):
+    from zim_gb300 import api
+    spec, L, R, gt = full
+    ctx.set_calibration(spec.rig.as_dict(), True)
+    dcfg = api.decode_config(**spec.decode_kwargs())
+    rcfg = config1_recon(api)
+    dL, dR = torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda()
+    xyz, mask, _ = api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR)
+    xyz2, mask2, _ = api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR)
+    x, m = xyz.cpu().numpy(), mask.cpu().numpy()
+    n = int(m.sum())
+    print("5MP pair points", n, "of", m.size)
+    assert n > 0.6 * L.shape[1] * L.shape[2]
+    # run-to-run: bit-identical (SOR statistics are summed in a fixed order and
+    # the Gaussian accumulates in fixed point, whatever the hash-bucket order)
+    assert torch.equal(mask, mask2) and torch.equal(xyz, xyz2)
+    # depth against the renderer's ground truth: rectified -> left camera -> pixel
+    P = x[m > 0].astype(np.float64) @ ctx.R1
+    K = spec.rig.K[0]
+    D = spec.rig.D[0]
+    xn, yn = P[:, 0] / P[:, 2], P[:, 1] / P[:, 2]
+    r2 = xn * xn + yn * yn
+    kr = 1 + (D[1] * r2 + D[0]) * r2
+    u = np.clip(np.rint(K[0, 0] * xn * kr + K[0, 2]).astype(int), 0, spec.rig.width - 1)
+    v = np.clip(np.rint(K[1, 1] * yn * kr + K[1, 2]).astype(int), 0, spec.rig.height - 1)
+    dz = np.abs(P[:, 2] - gt[v, u, 2])
+    print("5MP |dz| vs ground truth: median %.4f mm, p95 %.4f, p99 %.4f" % (np.median(dz), *np.percentile(dz, [95, 99])))
+    assert np.median(dz) < 0.1
+    assert np.percentile(dz, 95) < 0.5
+    assert ctx.check_device() == 0
+
+
+@pytest.mark.gpu
+def test_fullsize_host_entry(ctx, oracle_lib, full):
+    """The host-buffer entry on the 5 MP pair equals the device entry."""
+    from zim_gb300 import api
+    spec, L, R, _ = full
+    ctx.set_calibration(spec.rig.as_dict(), True)
+    dcfg = api.decode_config(**spec.decode_kwargs())
+    rcfg = api.recon_config(use_px_gaussian=1, use_ror=1, radius_search=1.5, radius_min_neighbors=10)
+    xyz, mask, _ = api.reconstruct_pair(ctx, dcfg, rcfg, torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda())
+    hx, hm, _ = api.reconstruct_pair_host(ctx, dcfg, rcfg, L, R)
+    assert np.array_equal(hm, mask.cpu().numpy()) and np.array_equal(hx, xyz.cpu().numpy())

@@ -47,7 +47,8 @@ def test_pair_matches_oracle_end_to_end(ctx, oracle_lib, name, kw):
     from zim_gb300 import api
     spec, L, R, _ = scene_data(name, **kw)
     ctx.set_calibration(spec.rig.as_dict(), True)
-    rc = dict(use_px_gaussian=1, use_ror=1, radius_search=0.7, radius_min_neighbors=10, radius_window_size=10,
+    # ROR radius 5 mm: the test scenes' pixel spacing is 1-1.5 mm
+    rc = dict(use_px_gaussian=1, use_ror=1, radius_search=5.0, radius_min_neighbors=10, radius_window_size=10,
               min_depth=0.0, max_depth=1000.0)
     dcfg = api.decode_config(**spec.decode_kwargs())
     rcfg = api.recon_config(**rc)
@@ -55,6 +56,7 @@ def test_pair_matches_oracle_end_to_end(ctx, oracle_lib, name, kw):
     ox, om = oracle_pair(oracle_lib, spec, L, R, rc)
     s = compare_clouds(xyz.cpu().numpy(), mask.cpu().numpy(), ox, om)
     print(name, s)
+    assert s["points"] > 0.5 * om.size, s
     # end to end, FP32-vs-FP64 decisions near their thresholds propagate through
     # matching and the filters; they stay a tiny fraction of the image
     assert s["frac_mask_diff"] <= 2e-3, s

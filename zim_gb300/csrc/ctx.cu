@@ -331,12 +331,15 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
         if (s) return s;
         cx = ox; cm = om;
     }
+    // the grid filters carve their hash tables from the same region in turn
+    const size_t grid_mark = ctx->scratch_used;
     if (on[ST_SOR]) {
         uint8_t* om = next_m(ST_SOR);
         float* ox = next_x(ST_SOR);
         // removed points read as zero in the organised output
         s = zim_sor_launch(ctx, cx, cm, RH, RW, r->sor_mean_k, r->sor_std_mul, ox, om, nullptr, st);
         if (s) return s;
+        ctx->scratch_used = grid_mark;
         cx = ox; cm = om;
     }
     if (on[ST_MLS]) {
@@ -350,6 +353,7 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
         float* ox = next_x(ST_MG);
         s = zim_metric_gaussian_launch(ctx, cx, cm, RH, RW, r->metric_gaussian_sigma, ox, st);
         if (s) return s;
+        ctx->scratch_used = grid_mark;
         cx = ox;
     }
     if (cm != mask_out) ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(mask_out, cm, (size_t)RH * RW, cudaMemcpyDeviceToDevice, st));

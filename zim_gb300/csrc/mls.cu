@@ -71,14 +71,16 @@ __device__ void sym_eigen3(const float C[3][3], float ev[3], float E[3][3]) {
     }
 }
 
-__device__ bool cholesky_solve(float A[6][6], const float b[6], float x[6], int nc) {
+// Cholesky solve; thr[i] is the singular-pivot threshold of row i (the
+// reference's 1e-12 expressed in the scaled basis).
+__device__ bool cholesky_solve(float A[6][6], const float b[6], float x[6], int nc, const float thr[6]) {
     float L[6][6];
     for (int i = 0; i < nc; i++)
         for (int j = 0; j <= i; j++) {
             float s = A[i][j];
             for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
             if (i == j) {
-                if (s <= 1e-12f) return false;
+                if (s <= thr[i]) return false;
                 L[i][j] = sqrtf(s);
             } else {
                 L[i][j] = s / L[j][j];
@@ -145,9 +147,30 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     C[1][0] = C[0][1]; C[2][0] = C[0][2]; C[2][1] = C[1][2];
     float ev[3], E[3][3];
     sym_eigen3(C, ev, E);
-    const float nx = E[0][0], ny = E[0][1], nz = E[0][2];
-    const float t1x = E[1][0], t1y = E[1][1], t1z = E[1][2];
-    const float t2x = E[2][0], t2y = E[2][1], t2z = E[2][2];
+    // Orthonormal tangent frame: t1 is re-orthogonalised against the normal and
+    // t2 = n x t1.  Exact eigenvectors already satisfy this (up to sign, which
+    // the projection is invariant to); in FP32 it keeps the polynomial basis
+    // from degenerating when the two in-plane eigenvalues nearly coincide.
+    float nx = E[0][0], ny = E[0][1], nz = E[0][2];
+    float t1x = E[1][0], t1y = E[1][1], t1z = E[1][2];
+    float t2x = E[2][0], t2y = E[2][1], t2z = E[2][2];
+    {
+        float nn = nx * nx + ny * ny + nz * nz;
+        if (nn > 1e-30f) {
+            float in = rsqrtf(nn);
+            nx *= in; ny *= in; nz *= in;
+            float d = t1x * nx + t1y * ny + t1z * nz;
+            float ax = t1x - d * nx, ay = t1y - d * ny, az = t1z - d * nz;
+            float aa = ax * ax + ay * ay + az * az;
+            if (aa > 1e-30f) {
+                float ia = rsqrtf(aa);
+                t1x = ax * ia; t1y = ay * ia; t1z = az * ia;
+                t2x = ny * t1z - nz * t1y;
+                t2y = nz * t1x - nx * t1z;
+                t2z = nx * t1y - ny * t1x;
+            }
+        }
+    }
     const int min_nb = order == 2 ? 8 : (order == 1 ? 5 : 3);
     int cur = nv >= min_nb ? order : 0;
     // query point relative to the centroid: e0 = p - c = -c_rel
@@ -155,6 +178,14 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     float ox, oy, oz;  // correction added to p
     bool solved = false;
     float co[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
+    // radius): the fitted surface is the same, the normal equations are O(1).
+    const float is = rsqrtf(r2c);
+    float thr[6];
+    {
+        const float s2 = is * is, s4 = s2 * s2;  // pivot of degree-d row scales by h^(-2d)
+        thr[0] = 1e-12f; thr[1] = thr[2] = 1e-12f * s2; thr[3] = thr[4] = thr[5] = 1e-12f * s4;
+    }
     if (cur > 0) {
         const int nc = cur == 1 ? 3 : 6;
         float A[6][6], bv[6];
@@ -171,8 +202,8 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
                 if (d2 > r2c) continue;
                 float w = __expf(-d2 * inv_2s2);
                 float ex = dx - cx, ey = dy - cy, ez = dz - cz;
-                float u = ex * t1x + ey * t1y + ez * t1z;
-                float v = ex * t2x + ey * t2y + ez * t2z;
+                float u = (ex * t1x + ey * t1y + ez * t1z) * is;
+                float v = (ex * t2x + ey * t2y + ez * t2z) * is;
                 float f = ex * nx + ey * ny + ez * nz;
                 float bs[6] = {1.f, u, v, u * u, u * v, v * v};
 #pragma unroll
@@ -187,14 +218,14 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
             }
         for (int a = 0; a < nc; a++)
             for (int b = 0; b < a; b++) A[a][b] = A[b][a];
-        solved = cholesky_solve(A, bv, co, nc);
+        solved = cholesky_solve(A, bv, co, nc, thr);
         if (!solved && cur == 2) {
             float A1[6][6], b1[6];
             for (int a = 0; a < 3; a++) {
                 b1[a] = bv[a];
                 for (int b = 0; b < 3; b++) A1[a][b] = A[a][b];
             }
-            solved = cholesky_solve(A1, b1, co, 3);
+            solved = cholesky_solve(A1, b1, co, 3, thr);
             if (solved) cur = 1;
         }
     }
@@ -204,8 +235,9 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     } else {
         float u0 = ex0 * t1x + ey0 * t1y + ez0 * t1z;
         float v0 = ex0 * t2x + ey0 * t2y + ez0 * t2z;
-        float ff = co[0] + co[1] * u0 + co[2] * v0;
-        if (cur == 2) ff += co[3] * u0 * u0 + co[4] * u0 * v0 + co[5] * v0 * v0;
+        float us = u0 * is, vs = v0 * is;
+        float ff = co[0] + co[1] * us + co[2] * vs;
+        if (cur == 2) ff += co[3] * us * us + co[4] * us * vs + co[5] * vs * vs;
         // out = c + u0 t1 + v0 t2 + f n = p + (c_rel + u0 t1 + v0 t2 + f n)
         ox = cx + u0 * t1x + v0 * t2x + ff * nx;
         oy = cy + u0 * t1y + v0 * t2y + ff * ny;

@@ -127,6 +127,8 @@ __global__ void __launch_bounds__(RX* RY) median_reproject_kernel(const float* _
 
 // 3x3 point-cloud Gaussian (sigma 0.7 px): neighbour used if valid and
 // |x_n - x_c| < 3; output sum(w p) / sum(w) if sum(w) > 0.8, else 0; borders 0.
+// The weighted mean is accumulated as p_c + sum(w (p_n - p_c)) / sum(w), the
+// same value with millimetre-scale FP32 sums.
 __global__ void px_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
                                    float w00, float w01, float w11, float* __restrict__ out,
                                    uint8_t* __restrict__ mask_out) {
@@ -135,8 +137,11 @@ __global__ void px_gaussian_kernel(const float* __restrict__ xyz, const uint8_t*
     size_t o = (size_t)y * cols + x;
     float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
     bool inner = x >= 1 && y >= 1 && x < cols - 1 && y < rows - 1 && mask[o];
+    float cx = 0.f, cy = 0.f, cz = 0.f;
     if (inner) {
-        const float cx = __ldg(xyz + 3 * o);
+        cx = __ldg(xyz + 3 * o);
+        cy = __ldg(xyz + 3 * o + 1);
+        cz = __ldg(xyz + 3 * o + 2);
 #pragma unroll
         for (int a = -1; a <= 1; a++)
 #pragma unroll
@@ -146,17 +151,17 @@ __global__ void px_gaussian_kernel(const float* __restrict__ xyz, const uint8_t*
                 float nx = __ldg(xyz + 3 * q);
                 if (fabsf(nx - cx) < 3.0f) {
                     float w = (a == 0 && b == 0) ? w11 : ((a == 0 || b == 0) ? w01 : w00);
-                    sx = fmaf(nx, w, sx);
-                    sy = fmaf(__ldg(xyz + 3 * q + 1), w, sy);
-                    sz = fmaf(__ldg(xyz + 3 * q + 2), w, sz);
+                    sx = fmaf(nx - cx, w, sx);
+                    sy = fmaf(__ldg(xyz + 3 * q + 1) - cy, w, sy);
+                    sz = fmaf(__ldg(xyz + 3 * q + 2) - cz, w, sz);
                     cnt += w;
                 }
             }
     }
     bool keep = inner && cnt > 0.8f;
-    out[3 * o] = keep ? sx / cnt : 0.f;
-    out[3 * o + 1] = keep ? sy / cnt : 0.f;
-    out[3 * o + 2] = keep ? sz / cnt : 0.f;
+    out[3 * o] = keep ? cx + sx / cnt : 0.f;
+    out[3 * o + 1] = keep ? cy + sy / cnt : 0.f;
+    out[3 * o + 2] = keep ? cz + sz / cnt : 0.f;
     if (mask_out) mask_out[o] = keep ? 1 : 0;
 }
 
