@@ -221,6 +221,20 @@ ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz, const uint
                                       int rows, int cols, zim_point_xyz* points,
                                       uint64_t* count_dev, void* stream);
 
+/* zim_compact_points without any device allocation, for callers that may not
+ * call cudaMalloc (a host application that owns all device memory through its
+ * own pool, or a capture loop that cannot take the implicit synchronisation of
+ * cudaMalloc/cudaFree).  No counterpart in the reference.  Its scratch is a
+ * 256 KiB array in the library's device image, which limits it to
+ * rows * cols <= 64 Mi pixels (larger sizes return ZIM_ERR_INVALID_ARG) and is
+ * held by every GPU that loads the library until exit.  No context: it runs
+ * on the current device.  The first call on a device does a one-time set-up
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race, so serialise them. */
+ZIM_API zim_status zim_compact_points_noalloc(const float* xyz, const uint8_t* mask, int rows,
+                                              int cols, zim_point_xyz* points,
+                                              uint64_t* count_dev, void* stream);
+
 /* Whole plain per-pair path (decode L+R, rectify, match, median, reproject,
  * filters) on device buffers.  xyz/mask/disp are rect_h*rect_w.  pha_f <= 0
  * selects zim_decode_max_order(dcfg). */

@@ -78,6 +78,7 @@ PROTOTYPES = {
     "zim_filter_sor": (I, [V, V, V, I, I, I, D, V, V, V]),
     "zim_filter_metric_gaussian": (I, [V, V, V, I, I, D, V, V]),
     "zim_compact_points": (I, [V, V, V, I, I, V, V, V]),
+    "zim_compact_points_noalloc": (I, [V, V, I, I, V, V, V]),
     "zim_reconstruct_pair": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
     "zim_reconstruct_pair_host": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
 }
