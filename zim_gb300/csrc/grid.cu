@@ -9,16 +9,20 @@
 // nearest neighbours, threshold mean + std_mul * stddev, keep d <= threshold.
 //
 // Build (no host synchronisation): a trimmed mean of adjacent-pixel spacing
-// sets the finest cell on the device; up to four levels with cells
-// c, 4c, 16c, 64c are counting-sorted into power-of-two hash tables (count,
-// exclusive scan, scatter).  A kNN query visits Chebyshev rings of cells around
-// its cell and stops once it holds k + 1 candidates and the (k + 1)-th
-// distance is within the ring's guaranteed radius r * cell, so the result is
-// exact; a query that is not done after a few rings restarts one level
-// coarser, which bounds the work of isolated outliers.  A visited point's cell
-// is re-derived from its coordinates, so hash collisions never count a point
-// twice.  Both filters are deterministic: the SOR statistics are summed in a
-// fixed order and the Gaussian accumulates in 64-bit fixed point.
+// sets the finest cell on the device; levels with cells c, 4c, 16c, 64c are
+// counting-sorted into power-of-two hash tables of (offset, count) pairs.
+// A kNN query visits Chebyshev rings of cells around its own cell and stops
+// once it holds k + 1 candidates and the (k + 1)-th distance is within the
+// ring's guaranteed radius r * cell, so the result is exact.
+//   phase 1: one thread per point, finest level, rings <= 2 (almost all points);
+//   phase 2: one warp per remaining point (isolated outliers), coarser levels,
+//            the lanes splitting each ring's cells, cells farther than the
+//            current (k + 1)-th distance pruned, the lanes' sorted lists merged
+//            after each ring.
+// A visited point's cell is re-derived from its coordinates, so hash
+// collisions never count a point twice.  Both filters are deterministic: the
+// SOR statistics are summed in a fixed order, and the Gaussian's buckets are
+// sorted by pixel index before they are summed.
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -27,12 +31,14 @@
 
 namespace {
 
-constexpr int GB = 256;         // threads for pixel-parallel kernels
-constexpr int KNN_THREADS = 128;
-constexpr int KNN_MAX_K1 = 64;  // k + 1 <= 64
+constexpr int GB = 256;          // threads for pixel-parallel kernels
+constexpr int KNN_THREADS = 128; // phase-1 CTA
+constexpr int KNN_MAX_K1 = 64;   // k + 1 <= 64
 constexpr int SCAN_B = 1024;
 constexpr int MAX_LEVELS = 4;
-constexpr int LEVEL_RINGS = 3;  // rings tried on a level before going coarser
+constexpr int FINE_RINGS = 2;    // phase 1 rings on the finest level
+constexpr int COARSE_RINGS = 4;  // phase 2 rings per level before going coarser
+constexpr int P2_WARPS = 4;      // phase-2 warps per CTA
 
 struct GridStats {
     double sp_sum, sp_cnt;    // spacing pass 1
@@ -42,6 +48,7 @@ struct GridStats {
     float cell[MAX_LEVELS], inv_cell[MAX_LEVELS];
     int max_ring[MAX_LEVELS];
     int bbox_min[3], bbox_max[3];  // order-preserving float bits
+    unsigned n_deferred;
 };
 
 __device__ __forceinline__ int fbits(float f) {
@@ -55,25 +62,29 @@ __device__ __forceinline__ unsigned hash3(int x, int y, int z, unsigned tmask) {
 }
 
 // Deterministic block reduction (fixed shuffle tree); result valid in thread 0.
-template <typename T>
-__device__ T block_sum(T v) {
+template <typename T, typename Op>
+__device__ T block_reduce(T v, Op op, T ident) {
     __shared__ T ws[32];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    for (int off = 16; off; off >>= 1) v = op(v, __shfl_down_sync(0xffffffffu, v, off));
     if (lane == 0) ws[w] = v;
     __syncthreads();
-    T r = 0;
+    T r = ident;
     if (w == 0) {
-        r = lane < (int)(blockDim.x >> 5) ? ws[lane] : (T)0;
-        for (int off = 16; off; off >>= 1) r += __shfl_down_sync(0xffffffffu, r, off);
+        r = lane < (int)(blockDim.x >> 5) ? ws[lane] : ident;
+        for (int off = 16; off; off >>= 1) r = op(r, __shfl_down_sync(0xffffffffu, r, off));
     }
     __syncthreads();
     return r;
 }
+struct Add { template <typename T> __device__ T operator()(T a, T b) const { return a + b; } };
+struct Min { __device__ int operator()(int a, int b) const { return a < b ? a : b; } };
+struct Max { __device__ int operator()(int a, int b) const { return a > b ? a : b; } };
 
 __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
+    s->n_deferred = 0;
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
 
@@ -83,25 +94,32 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t n = (size_t)rows * cols;
     double d = 0, c = 0, nv = 0;
+    int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
     if (i < n && mask[i]) {
         nv = 1;
-        float px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
-        atomicMin(&s->bbox_min[0], fbits(px)); atomicMax(&s->bbox_max[0], fbits(px));
-        atomicMin(&s->bbox_min[1], fbits(py)); atomicMax(&s->bbox_max[1], fbits(py));
-        atomicMin(&s->bbox_min[2], fbits(pz)); atomicMax(&s->bbox_max[2], fbits(pz));
+        float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+        for (int a = 0; a < 3; a++) mn[a] = mx[a] = fbits(p[a]);
         if ((i % cols) + 1 < (size_t)cols && mask[i + 1]) {
-            float dx = xyz[3 * i + 3] - px, dy = xyz[3 * i + 4] - py, dz = xyz[3 * i + 5] - pz;
+            float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
             d = sqrtf(dx * dx + dy * dy + dz * dz);
             c = 1;
         }
     }
-    d = block_sum(d);
-    c = block_sum(c);
-    nv = block_sum(nv);
+    d = block_reduce(d, Add(), 0.0);
+    c = block_reduce(c, Add(), 0.0);
+    nv = block_reduce(nv, Add(), 0.0);
+    for (int a = 0; a < 3; a++) {
+        mn[a] = block_reduce(mn[a], Min(), INT_MAX);
+        mx[a] = block_reduce(mx[a], Max(), INT_MIN);
+    }
     if (threadIdx.x == 0) {
         atomicAdd(&s->sp_sum, d);
         atomicAdd(&s->sp_cnt, c);
         atomicAdd(&s->n_valid, nv);  // integer-valued: exact in any order
+        for (int a = 0; a < 3; a++) {
+            if (mn[a] != INT_MAX) atomicMin(&s->bbox_min[a], mn[a]);
+            if (mx[a] != INT_MIN) atomicMax(&s->bbox_max[a], mx[a]);
+        }
     }
 }
 
@@ -117,8 +135,8 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
         float v = sqrtf(dx * dx + dy * dy + dz * dz);
         if (v <= 3.0 * m1) { d = v; c = 1; }
     }
-    d = block_sum(d);
-    c = block_sum(c);
+    d = block_reduce(d, Add(), 0.0);
+    c = block_reduce(c, Add(), 0.0);
     if (threadIdx.x == 0) {
         atomicAdd(&s->sp2_sum, d);
         atomicAdd(&s->sp2_cnt, c);
@@ -162,7 +180,6 @@ __global__ void hash_count_kernel(const float* __restrict__ xyz, const uint8_t* 
     atomicAdd(&counts[hash3(cx, cy, cz, tmask)], 1u);
 }
 
-// exclusive scan, three phases
 __device__ __forceinline__ unsigned block_scan_incl(unsigned v, unsigned* ws) {
     unsigned x = v;
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -184,13 +201,14 @@ __device__ __forceinline__ unsigned block_scan_incl(unsigned v, unsigned* ws) {
     return x + (w ? ws[w - 1] : 0u);
 }
 
-__global__ void scan_blocks_kernel(const unsigned* __restrict__ in, unsigned* __restrict__ out, size_t n,
+// exclusive scan of the counts into tab[].x (per-block part), block totals
+__global__ void scan_blocks_kernel(const unsigned* __restrict__ counts, uint2* __restrict__ tab, size_t n,
                                    unsigned* __restrict__ block_tot) {
     __shared__ unsigned ws[32];
     size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
-    unsigned v = i < n ? in[i] : 0u;
+    unsigned v = i < n ? counts[i] : 0u;
     unsigned incl = block_scan_incl(v, ws);
-    if (i < n) out[i] = incl - v;
+    if (i < n) tab[i] = make_uint2(incl - v, v);
     if (threadIdx.x == SCAN_B - 1) block_tot[blockIdx.x] = incl;
 }
 
@@ -211,14 +229,14 @@ __global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb) {
     }
 }
 
-__global__ void scan_add_kernel(unsigned* __restrict__ out, size_t n, const unsigned* __restrict__ tot) {
+__global__ void scan_add_kernel(uint2* __restrict__ tab, size_t n, const unsigned* __restrict__ tot) {
     size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
-    if (i < n) out[i] += tot[blockIdx.x];
+    if (i < n) tab[i].x += tot[blockIdx.x];
 }
 
 __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                     const GridStats* __restrict__ s, int level, unsigned tmask,
-                                    const unsigned* __restrict__ off, unsigned* __restrict__ fill,
+                                    const uint2* __restrict__ tab, unsigned* __restrict__ fill,
                                     float4* __restrict__ pts) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !mask[i]) return;
@@ -226,13 +244,30 @@ __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t
     int cx, cy, cz;
     cell_of(x, y, z, s->inv_cell[level], cx, cy, cz);
     unsigned h = hash3(cx, cy, cz, tmask);
-    unsigned pos = off[h] + atomicAdd(&fill[h], 1u);
+    unsigned pos = tab[h].x + atomicAdd(&fill[h], 1u);
     pts[pos] = make_float4(x, y, z, __int_as_float((int)i));
 }
 
+// Sorts each bucket by pixel index, so bucket contents no longer depend on the
+// order of the scatter's atomics.
+__global__ void bucket_sort_kernel(const uint2* __restrict__ tab, unsigned T, float4* __restrict__ pts) {
+    unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= T) return;
+    const uint2 e = tab[h];
+    for (unsigned a = e.x + 1; a < e.x + e.y; a++) {
+        float4 v = pts[a];
+        int key = __float_as_int(v.w);
+        unsigned b = a;
+        while (b > e.x && __float_as_int(pts[b - 1].w) > key) {
+            pts[b] = pts[b - 1];
+            b--;
+        }
+        pts[b] = v;
+    }
+}
+
 struct Level {
-    const unsigned* off;  // exclusive offsets; bucket h spans [off[h], off[h] + cnt[h])
-    const unsigned* cnt;
+    const uint2* tab;  // (offset, count) per bucket
     const float4* pts;
     unsigned tmask;
 };
@@ -240,6 +275,10 @@ struct Levels {
     Level l[MAX_LEVELS];
     int n;
 };
+
+__device__ __forceinline__ uint2 bucket(const Level& g, int x, int y, int z) {
+    return __ldg(g.tab + hash3(x, y, z, g.tmask));
+}
 
 // Visits the points of all cells at Chebyshev distance exactly r from (cx, cy, cz).
 template <typename F>
@@ -250,9 +289,8 @@ __device__ __forceinline__ void visit_ring(const Level& g, float ic, int cx, int
             const int step = full ? 1 : 2 * r;
             for (int dx = -r; dx <= r; dx += step) {
                 int x = cx + dx, y = cy + dy, z = cz + dz;
-                unsigned h = hash3(x, y, z, g.tmask);
-                unsigned b = __ldg(g.off + h), e = b + __ldg(g.cnt + h);
-                for (unsigned t = b; t < e; t++) {
+                uint2 b = bucket(g, x, y, z);
+                for (unsigned t = b.x; t < b.x + b.y; t++) {
                     float4 p = __ldg(g.pts + t);
                     int px, py, pz;
                     cell_of(p.x, p.y, p.z, ic, px, py, pz);
@@ -263,72 +301,188 @@ __device__ __forceinline__ void visit_ring(const Level& g, float ic, int cx, int
         }
 }
 
-__global__ void __launch_bounds__(KNN_THREADS) sor_knn_kernel(const float* __restrict__ xyz,
-                                                              const uint8_t* __restrict__ mask, size_t n, int k,
-                                                              Levels lv, const GridStats* __restrict__ s,
-                                                              float* __restrict__ md_out, double* __restrict__ part,
-                                                              uint32_t* __restrict__ err) {
+// Phase 1: one thread per point on the finest level.  Points not resolved
+// within FINE_RINGS rings are appended to the deferred list (md = -1).
+__global__ void __launch_bounds__(KNN_THREADS) sor_knn_fine_kernel(const float* __restrict__ xyz,
+                                                                   const uint8_t* __restrict__ mask, size_t n, int k,
+                                                                   Level g, GridStats* s, float* __restrict__ md_out,
+                                                                   unsigned* __restrict__ deferred) {
     __shared__ float L[KNN_MAX_K1][KNN_THREADS];
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!mask[i] || s->n_valid <= k) {
+        md_out[i] = 0.f;
+        return;
+    }
+    const int K1 = k + 1, tid = threadIdx.x;
+    const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
+    int cnt = 0;
+    auto ins = [&](const float4& p) {
+        float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+        float d2 = dx * dx + dy * dy + dz * dz;
+        int j;
+        if (cnt < K1) j = cnt++;
+        else if (d2 < L[K1 - 1][tid]) j = K1 - 1;
+        else return;
+        while (j > 0 && L[j - 1][tid] > d2) {
+            L[j][tid] = L[j - 1][tid];
+            j--;
+        }
+        L[j][tid] = d2;
+    };
+    const float ic = s->inv_cell[0], cell = s->cell[0];
+    int cx, cy, cz;
+    cell_of(qx, qy, qz, ic, cx, cy, cz);
+    for (int r = 0; r <= FINE_RINGS; r++) {
+        visit_ring(g, ic, cx, cy, cz, r, ins);
+        float gr = r * cell;
+        if (cnt >= K1 && L[K1 - 1][tid] <= gr * gr) {
+            float sum = 0.f;
+            for (int j = 1; j < K1; j++) sum += sqrtf(L[j][tid]);
+            md_out[i] = sum / (float)k;
+            return;
+        }
+    }
+    md_out[i] = -1.f;
+    unsigned slot = atomicAdd(&s->n_deferred, 1u);
+    deferred[slot] = (unsigned)i;
+}
+
+// Cell t (0 <= t < 24 r^2 + 2) of the Chebyshev ring r around the origin.
+__device__ __forceinline__ void ring_cell(int r, int t, int& dx, int& dy, int& dz) {
+    if (r == 0) { dx = dy = dz = 0; return; }
+    const int side = 2 * r + 1, face = side * side;
+    if (t < 2 * face) {
+        dz = t < face ? -r : r;
+        int q = t < face ? t : t - face;
+        dy = q / side - r;
+        dx = q % side - r;
+        return;
+    }
+    t -= 2 * face;
+    const int per = 8 * r;
+    dz = t / per - (r - 1);
+    int p = t % per;
+    if (p < side) { dx = p - r; dy = -r; return; }
+    p -= side;
+    if (p < side) { dx = p - r; dy = r; return; }
+    p -= side;
+    dy = (p >> 1) - (r - 1);
+    dx = (p & 1) ? r : -r;
+}
+
+// Phase 2: one warp per deferred point, coarser levels.  Each lane keeps a
+// sorted list of its K1 best; after every ring the lists are merged to find
+// the (k+1)-th distance (termination and pruning bound) and the mean.
+__global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_coarse_kernel(const float* __restrict__ xyz, int k, Levels lv,
+                                                                        const GridStats* __restrict__ s,
+                                                                        const unsigned* __restrict__ deferred,
+                                                                        float* __restrict__ md_out,
+                                                                        uint32_t* __restrict__ err) {
+    __shared__ float L[P2_WARPS][KNN_MAX_K1][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int K1 = k + 1;
-    const int tid = threadIdx.x;
-    double md = 0.0, md2 = 0.0;
-    if (i < n && mask[i] && s->n_valid > k) {
+    const unsigned nd = s->n_deferred;
+    for (unsigned item = blockIdx.x * P2_WARPS + w; item < nd; item += gridDim.x * P2_WARPS) {
+        const unsigned i = deferred[item];
         const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
-        int cnt = 0;
-        auto ins = [&](const float4& p) {
-            float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-            float d2 = dx * dx + dy * dy + dz * dz;
-            int j;
-            if (cnt < K1) j = cnt++;
-            else if (d2 < L[K1 - 1][tid]) j = K1 - 1;
-            else return;
-            while (j > 0 && L[j - 1][tid] > d2) {
-                L[j][tid] = L[j - 1][tid];
-                j--;
-            }
-            L[j][tid] = d2;
-        };
         bool done = false;
-        for (int l = 0; l < lv.n && !done; l++) {
-            cnt = 0;
+        float md = 0.f;
+        for (int l = (lv.n > 1 ? 1 : 0); l < lv.n && !done; l++) {
+            const Level& g = lv.l[l];
             const float ic = s->inv_cell[l], cell = s->cell[l];
             int cx, cy, cz;
             cell_of(qx, qy, qz, ic, cx, cy, cz);
-            const int rmax = (l == lv.n - 1) ? s->max_ring[l] : LEVEL_RINGS;
-            for (int r = 0; r <= rmax; r++) {
-                visit_ring(lv.l[l], ic, cx, cy, cz, r, ins);
-                float gr = r * cell;
-                if (cnt >= K1 && L[K1 - 1][tid] <= gr * gr) { done = true; break; }
+            int cnt = 0;
+            float bound = INFINITY;  // current (k+1)-th squared distance over the warp
+            const int rmax = (l == lv.n - 1) ? s->max_ring[l] : COARSE_RINGS;
+            for (int r = 0; r <= rmax && !done; r++) {
+                const int ncell = r == 0 ? 1 : 24 * r * r + 2;
+                for (int t = lane; t < ncell; t += 32) {
+                    int dx, dy, dz;
+                    ring_cell(r, t, dx, dy, dz);
+                    const int x = cx + dx, y = cy + dy, z = cz + dz;
+                    // squared distance from q to the cell box (pruning), slightly shrunk
+                    float ex = fmaxf(fmaxf(x * cell - qx, qx - (x + 1) * cell), 0.f);
+                    float ey = fmaxf(fmaxf(y * cell - qy, qy - (y + 1) * cell), 0.f);
+                    float ez = fmaxf(fmaxf(z * cell - qz, qz - (z + 1) * cell), 0.f);
+                    float bd = fmaxf(sqrtf(ex * ex + ey * ey + ez * ez) - 1e-4f * cell, 0.f);
+                    if (bd * bd > bound) continue;
+                    uint2 b = bucket(g, x, y, z);
+                    for (unsigned u = b.x; u < b.x + b.y; u++) {
+                        float4 p = __ldg(g.pts + u);
+                        int px, py, pz;
+                        cell_of(p.x, p.y, p.z, ic, px, py, pz);
+                        if (px != x || py != y || pz != z) continue;
+                        float ddx = p.x - qx, ddy = p.y - qy, ddz = p.z - qz;
+                        float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        int j;
+                        if (cnt < K1) j = cnt++;
+                        else if (d2 < L[w][K1 - 1][lane]) j = K1 - 1;
+                        else continue;
+                        while (j > 0 && L[w][j - 1][lane] > d2) {
+                            L[w][j][lane] = L[w][j - 1][lane];
+                            j--;
+                        }
+                        L[w][j][lane] = d2;
+                    }
+                }
+                __syncwarp();
+                // merge: the K1 smallest over all lanes, in order
+                int head = 0;
+                float kth = INFINITY, sum = 0.f;
+                for (int round = 0; round < K1; round++) {
+                    float v = head < cnt ? L[w][head][lane] : INFINITY;
+                    int who = lane;
+                    for (int off = 16; off; off >>= 1) {
+                        float ov = __shfl_xor_sync(0xffffffffu, v, off);
+                        int ow = __shfl_xor_sync(0xffffffffu, who, off);
+                        if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
+                    }
+                    if (lane == who) head++;
+                    if (round > 0) sum += sqrtf(v);
+                    if (round == K1 - 1) kth = v;
+                }
+                bound = kth;
+                const float gr = r * cell;
+                if (kth <= gr * gr) {
+                    done = true;
+                    md = sum / (float)k;
+                }
+                __syncwarp();
             }
         }
-        if (!done && cnt < K1) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
-        float sum = 0.f;
-        for (int j = 1; j < min(cnt, K1); j++) sum += sqrtf(L[j][tid]);
-        float m = sum / (float)k;
-        md_out[i] = m;
-        md = m;
-        md2 = (double)(m * m);  // PCL: float square, double sum
-    } else if (i < n) {
-        md_out[i] = 0.f;
-    }
-    md = block_sum(md);
-    md2 = block_sum(md2);
-    if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = md;
-        part[2 * blockIdx.x + 1] = md2;
+        if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
+        if (lane == 0) md_out[i] = md;
     }
 }
 
-// Sums the per-block partials in a fixed order (one CTA).
+// Per-block sums of the mean distances (valid pixels), then a fixed-order total.
+__global__ void sor_partial_kernel(const uint8_t* __restrict__ mask, const float* __restrict__ md, size_t n,
+                                   double* __restrict__ part) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0, b = 0;
+    if (i < n && mask[i]) {
+        float m = md[i];
+        a = m;
+        b = (double)(m * m);  // PCL: float square, double sum
+    }
+    a = block_reduce(a, Add(), 0.0);
+    b = block_reduce(b, Add(), 0.0);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+
 __global__ void sor_stats_kernel(const double* __restrict__ part, int nb, GridStats* s) {
     double a = 0, b = 0;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
         a += part[2 * i];
         b += part[2 * i + 1];
     }
-    a = block_sum(a);
-    b = block_sum(b);
+    a = block_reduce(a, Add(), 0.0);
+    b = block_reduce(b, Add(), 0.0);
     if (threadIdx.x == 0) {
         s->md_sum = a;
         s->md_sq = b;
@@ -359,11 +513,11 @@ __global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t
     }
 }
 
-// Radius-3-sigma Gaussian: out = p + sum w (q - p) / sum w, accumulated in
-// 64-bit fixed point (scale fx) so the result does not depend on the order in
-// which the hash buckets hold the neighbours.
+// Radius-3-sigma Gaussian: out = p + sum w (q - p) / sum w over the 27 cells of
+// side 3 sigma around p; buckets are index-sorted, so the FP32 sums are
+// deterministic.
 __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
-                                       float r2, float inv2s2, double fx, Level g, const GridStats* __restrict__ s,
+                                       float r2, float inv2s2, Level g, const GridStats* __restrict__ s,
                                        float* __restrict__ out) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -373,80 +527,82 @@ __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint
         return;
     }
     const float ic = s->inv_cell[0];
-    const float ffx = (float)fx;
     int cx, cy, cz;
     cell_of(qx, qy, qz, ic, cx, cy, cz);
-    long long sx = 0, sy = 0, sz = 0, sw = 0;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
     auto acc = [&](const float4& p) {
         float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
         float d2 = dx * dx + dy * dy + dz * dz;
         if (d2 > r2) return;
         float w = __expf(-d2 * inv2s2);
-        float wf = w * ffx;
-        sx += __float2ll_rn(wf * dx);
-        sy += __float2ll_rn(wf * dy);
-        sz += __float2ll_rn(wf * dz);
-        sw += __float2ll_rn(wf);
+        sx = fmaf(w, dx, sx); sy = fmaf(w, dy, sy); sz = fmaf(w, dz, sz);
+        sw += w;
     };
     visit_ring(g, ic, cx, cy, cz, 0, acc);
     visit_ring(g, ic, cx, cy, cz, 1, acc);
-    double iw = 1.0 / (double)sw;
-    out[3 * i] = qx + (float)((double)sx * iw);
-    out[3 * i + 1] = qy + (float)((double)sy * iw);
-    out[3 * i + 2] = qz + (float)((double)sz * iw);
+    float iw = 1.0f / sw;
+    out[3 * i] = qx + sx * iw;
+    out[3 * i + 1] = qy + sy * iw;
+    out[3 * i + 2] = qz + sz * iw;
 }
 
-unsigned table_size(size_t n) {
+unsigned table_size(size_t want) {
     unsigned t = 1024;
-    while (t < n && t < (1u << 30)) t <<= 1;
+    while (t < want && t < (1u << 30)) t <<= 1;
     return t;
 }
+
+// level l tables: about 4 points per bucket on the finest level, 16x fewer per level
+unsigned level_table(size_t n, int l) { return table_size((n / 4) >> (4 * l)); }
 
 struct GridScratch {
     GridStats* stats;
     int levels;
     unsigned tsize[MAX_LEVELS];
-    unsigned* counts[MAX_LEVELS];
-    unsigned* off[MAX_LEVELS];
+    uint2* tab[MAX_LEVELS];
     float4* pts[MAX_LEVELS];
+    unsigned* counts;  // shared by the levels' builds
     unsigned* tot;
     float* md;
+    unsigned* deferred;
     double* part;
 };
 
 size_t grid_bytes(size_t n, int levels) {
-    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) + zim_align256(((n + KNN_THREADS - 1) / KNN_THREADS) * 16);
-    size_t tmax = 0;
+    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(((n + GB - 1) / GB) * 16);
+    unsigned tmax = 1024;
     for (int l = 0; l < levels; l++) {
-        unsigned t = table_size(n >> (2 * l));
+        unsigned t = level_table(n, l);
         tmax = t > tmax ? t : tmax;
-        b += 2 * zim_align256((size_t)t * 4) + zim_align256(n * 16);
+        b += zim_align256((size_t)t * 8) + zim_align256(n * 16);
     }
-    b += zim_align256(((tmax + SCAN_B - 1) / SCAN_B) * 4);
-    return b + 2048;
+    b += zim_align256((size_t)tmax * 4) + zim_align256(((tmax + SCAN_B - 1) / SCAN_B) * 4);
+    return b + 4096;
 }
 
 zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     G.levels = levels;
     G.stats = (GridStats*)zim_scratch_take(ctx, sizeof(GridStats));
-    unsigned tmax = 0;
+    unsigned tmax = 1024;
     for (int l = 0; l < levels; l++) {
-        G.tsize[l] = table_size(n >> (2 * l));
+        G.tsize[l] = level_table(n, l);
         tmax = G.tsize[l] > tmax ? G.tsize[l] : tmax;
-        G.counts[l] = (unsigned*)zim_scratch_take(ctx, (size_t)G.tsize[l] * 4);
-        G.off[l] = (unsigned*)zim_scratch_take(ctx, (size_t)G.tsize[l] * 4);
+        G.tab[l] = (uint2*)zim_scratch_take(ctx, (size_t)G.tsize[l] * 8);
         G.pts[l] = (float4*)zim_scratch_take(ctx, n * 16);
-        if (!G.counts[l] || !G.off[l] || !G.pts[l]) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
+        if (!G.tab[l] || !G.pts[l]) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
     }
+    G.counts = (unsigned*)zim_scratch_take(ctx, (size_t)tmax * 4);
     G.tot = (unsigned*)zim_scratch_take(ctx, ((tmax + SCAN_B - 1) / SCAN_B) * 4);
     G.md = (float*)zim_scratch_take(ctx, n * 4);
-    G.part = (double*)zim_scratch_take(ctx, ((n + KNN_THREADS - 1) / KNN_THREADS) * 16);
-    if (!G.stats || !G.tot || !G.md || !G.part) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
+    G.deferred = (unsigned*)zim_scratch_take(ctx, n * 4);
+    G.part = (double*)zim_scratch_take(ctx, ((n + GB - 1) / GB) * 16);
+    if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.part)
+        return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
     return ZIM_OK;
 }
 
 zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
-                      float factor, GridScratch& G, cudaStream_t st) {
+                      float factor, bool sort_buckets, GridScratch& G, cudaStream_t st) {
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
@@ -456,14 +612,18 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     ctx->launches += 4;
     for (int l = 0; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
-        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts[l], 0, (size_t)T * 4, st));
-        hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts[l]);
-        scan_blocks_kernel<<<nb, SCAN_B, 0, st>>>(G.counts[l], G.off[l], T, G.tot);
+        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
+        hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts);
+        scan_blocks_kernel<<<nb, SCAN_B, 0, st>>>(G.counts, G.tab[l], T, G.tot);
         scan_totals_kernel<<<1, SCAN_B, 0, st>>>(G.tot, (int)nb);
-        scan_add_kernel<<<nb, SCAN_B, 0, st>>>(G.off[l], T, G.tot);
-        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts[l], 0, (size_t)T * 4, st));
-        hash_scatter_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.off[l], G.counts[l], G.pts[l]);
+        scan_add_kernel<<<nb, SCAN_B, 0, st>>>(G.tab[l], T, G.tot);
+        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
+        hash_scatter_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.tab[l], G.counts, G.pts[l]);
         ctx->launches += 5;
+        if (sort_buckets) {
+            bucket_sort_kernel<<<(T + GB - 1) / GB, GB, 0, st>>>(G.tab[l], T, G.pts[l]);
+            ctx->launches += 1;
+        }
     }
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
@@ -480,20 +640,23 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     zim_status s = carve_grid(ctx, n, MAX_LEVELS, G);
     if (s) return s;
     // finest cell ~ 3.5 x spacing: the (k+1)-th neighbour of a surface point
-    // usually lies within one ring for k <= 50
+    // lies within one ring for ~98% of points at k = 30
     float factor = 3.5f * sqrtf(fmaxf(1.0f, (float)mean_k / 30.0f));
-    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, G, st);
+    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, G, st);
     if (s) return s;
     Levels lv;
     lv.n = G.levels;
-    for (int l = 0; l < G.levels; l++) lv.l[l] = Level{G.off[l], G.counts[l], G.pts[l], G.tsize[l] - 1};
+    for (int l = 0; l < G.levels; l++) lv.l[l] = Level{G.tab[l], G.pts[l], G.tsize[l] - 1};
     float* md = mean_dist ? mean_dist : G.md;
-    unsigned nblk = (unsigned)((n + KNN_THREADS - 1) / KNN_THREADS);
-    sor_knn_kernel<<<nblk, KNN_THREADS, 0, st>>>(xyz, mask, n, mean_k, lv, G.stats, md, G.part, ctx->d_error);
+    sor_knn_fine_kernel<<<(unsigned)((n + KNN_THREADS - 1) / KNN_THREADS), KNN_THREADS, 0, st>>>(
+        xyz, mask, n, mean_k, lv.l[0], G.stats, md, G.deferred);
+    sor_knn_coarse_kernel<<<(unsigned)(2 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
+        xyz, mean_k, lv, G.stats, G.deferred, md, ctx->d_error);
+    const unsigned nblk = (unsigned)((n + GB - 1) / GB);
+    sor_partial_kernel<<<nblk, GB, 0, st>>>(mask, md, n, G.part);
     sor_stats_kernel<<<1, 1024, 0, st>>>(G.part, (int)nblk, G.stats);
-    sor_classify_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, mean_k, std_mul, G.stats, md,
-                                                                      mask_out, xyz_out);
-    ctx->launches += 3;
+    sor_classify_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, mean_k, std_mul, G.stats, md, mask_out, xyz_out);
+    ctx->launches += 5;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
 }
@@ -505,13 +668,11 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     zim_status s = carve_grid(ctx, n, 1, G);
     if (s) return s;
     const float rad = (float)(3.0 * sigma);
-    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, G, st);
+    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, true, G, st);
     if (s) return s;
-    Level g{G.off[0], G.counts[0], G.pts[0], G.tsize[0] - 1};
-    // fixed-point scale: |w (q - p)| <= rad per term, ~1e4 terms stay below 2^62
-    const double fx = std::ldexp(1.0, 40) / fmax(1.0, (double)rad);
+    Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
     metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(
-        xyz, mask, n, rad * rad, (float)(1.0 / (2.0 * sigma * sigma)), fx, g, G.stats, out);
+        xyz, mask, n, rad * rad, (float)(1.0 / (2.0 * sigma * sigma)), g, G.stats, out);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
