@@ -211,6 +211,15 @@ ZIM_API zim_status zim_filter_mls(zim_ctx* ctx, const float* xyz, const uint8_t*
 ZIM_API zim_status zim_filter_sor(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
                                   int cols, int mean_k, double std_mul, uint8_t* mask_out,
                                   float* mean_dist, void* stream);
+/* Statistics of the last SOR run on this context (zim_filter_sor or the SOR
+ * stage of zim_reconstruct_pair): valid points, mean and standard deviation of
+ * the per-point mean k-NN distance, the threshold mean + std_mul * stddev, and
+ * how many points needed the second (outlier) search phase.  Synchronises. */
+typedef struct zim_sor_stats {
+    double n_valid, mean, stddev, threshold;
+    uint32_t n_far_search;
+} zim_sor_stats;
+ZIM_API zim_status zim_filter_sor_stats(zim_ctx* ctx, zim_sor_stats* out);
 ZIM_API zim_status zim_filter_metric_gaussian(zim_ctx* ctx, const float* xyz, const uint8_t* mask,
                                               int rows, int cols, double sigma, float* out,
                                               void* stream);

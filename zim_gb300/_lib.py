@@ -41,6 +41,11 @@ class ReconConfig(C.Structure):
                 ("use_metric_gaussian", C.c_int), ("metric_gaussian_sigma", C.c_double)]
 
 
+class SorStats(C.Structure):
+    _fields_ = [("n_valid", C.c_double), ("mean", C.c_double), ("stddev", C.c_double), ("threshold", C.c_double),
+                ("n_far_search", C.c_uint32)]
+
+
 class PointXYZ(C.Structure):
     _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("pad", C.c_float)]
 
@@ -76,6 +81,7 @@ PROTOTYPES = {
     "zim_filter_ror": (I, [V, V, V, I, I, Fl, I, I, V, V, V]),
     "zim_filter_mls": (I, [V, V, V, I, I, I, Fl, I, Fl, I, V, V]),
     "zim_filter_sor": (I, [V, V, V, I, I, I, D, V, V, V]),
+    "zim_filter_sor_stats": (I, [V, V]),
     "zim_filter_metric_gaussian": (I, [V, V, V, I, I, D, V, V]),
     "zim_compact_points": (I, [V, V, V, I, I, V, V, V]),
     "zim_compact_points_noalloc": (I, [V, V, I, I, V, V, V]),

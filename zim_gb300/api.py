@@ -264,6 +264,14 @@ def filter_sor(ctx, xyz, mask, mean_k, std_mul=1.0, want_mean_dist=False):
     return mo, md
 
 
+def sor_stats(ctx) -> dict:
+    """Statistics of the last SOR run on this context (synchronises)."""
+    st = _lib.SorStats()
+    ctx.check(_lib.load().zim_filter_sor_stats(ctx.h, C.byref(st)))
+    return dict(n_valid=st.n_valid, mean=st.mean, stddev=st.stddev, threshold=st.threshold,
+                n_far_search=st.n_far_search)
+
+
 def filter_metric_gaussian(ctx, xyz, mask, sigma):
     H, W = mask.shape
     out = torch.empty_like(xyz)

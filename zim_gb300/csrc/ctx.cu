@@ -139,6 +139,7 @@ extern "C" ZIM_API zim_status zim_create(int device, zim_ctx** out) {
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaFree(0) != cudaSuccess || cudaMalloc(&ctx->d_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->d_error, 0, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_sor_stats, 256) != cudaSuccess ||
         cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess) {
         delete ctx;
         return ZIM_ERR_CUDA;
@@ -155,6 +156,7 @@ extern "C" ZIM_API void zim_destroy(zim_ctx* ctx) {
         for (int m = 0; m < 2; m++) cudaFree(ctx->d_map[c][m]);
     cudaFree(ctx->scratch);
     cudaFree(ctx->d_error);
+    cudaFree(ctx->d_sor_stats);
     cudaFreeHost(ctx->h_pinned);
     delete ctx;
 }

@@ -9,17 +9,20 @@
 // nearest neighbours, threshold mean + std_mul * stddev, keep d <= threshold.
 //
 // Build (no host synchronisation): a trimmed mean of adjacent-pixel spacing
-// sets the finest cell on the device; levels with cells c, 4c, 16c, 64c are
-// counting-sorted into power-of-two hash tables of (offset, count) pairs.
-// A kNN query visits Chebyshev rings of cells around its own cell and stops
-// once it holds k + 1 candidates and the (k + 1)-th distance is within the
-// ring's guaranteed radius r * cell, so the result is exact.
-//   phase 1: one thread per point, finest level, rings <= 2 (almost all points);
-//   phase 2: one warp per remaining point (isolated outliers), coarser levels,
-//            the lanes splitting each ring's cells, cells farther than the
-//            current (k + 1)-th distance pruned, the lanes' sorted lists merged
-//            after each ring.
-// A visited point's cell is re-derived from its coordinates, so hash
+// sets the finest cell c on the device; the finest level (cell c) is
+// counting-sorted into a power-of-two hash table of (offset, count) pairs, the
+// coarse level (cell >= 16c) into a dense grid over the bounding box.  Exact
+// k-nearest neighbours in two phases:
+//   phase 1: one CTA per 16x8 pixel tile gathers the finest-level points of
+//            the tile's cell box (dilated by TILE_DILATE cells) into shared
+//            memory; every thread scans the same candidate list and is exact
+//            once it holds k + 1 candidates within its distance to the box
+//            boundary;
+//   phase 2: one warp per remaining point (isolated outliers) searches the
+//            coarse level best-first: occupied cells in order of the distance
+//            to their cube, until the next cube is farther than the current
+//            (k + 1)-th distance.
+// A visited point's finest cell is re-derived from its coordinates, so hash
 // collisions never count a point twice.  Both filters are deterministic: the
 // SOR statistics are summed in a fixed order, and the Gaussian's buckets are
 // sorted by pixel index before they are summed.
@@ -32,13 +35,17 @@
 namespace {
 
 constexpr int GB = 256;          // threads for pixel-parallel kernels
-constexpr int KNN_THREADS = 128; // phase-1 CTA
 constexpr int KNN_MAX_K1 = 64;   // k + 1 <= 64
 constexpr int SCAN_B = 1024;
-constexpr int MAX_LEVELS = 4;
-constexpr int FINE_RINGS = 2;    // phase 1 rings on the finest level
-constexpr int COARSE_RINGS = 4;  // phase 2 rings per level before going coarser
+constexpr int MAX_LEVELS = 2;    // finest + one coarse level
+constexpr int FINE_RINGS = 2;    // phase-1 fallback rings on the finest level
 constexpr int P2_WARPS = 4;      // phase-2 warps per CTA
+constexpr int TILE_X = 16, TILE_Y = 8, TILE_T = TILE_X * TILE_Y;
+constexpr int TILE_DILATE = 2;        // cells added around a tile's box
+constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
+constexpr int TILE_MAX_CAND = 2048;   // gathered points per tile
+constexpr int COARSE_MULT = 16;       // coarse level cell = 16 x finest
+constexpr long long DENSE_MAX = 1 << 21;  // cells of the dense coarse level
 
 struct GridStats {
     double sp_sum, sp_cnt;    // spacing pass 1
@@ -48,7 +55,10 @@ struct GridStats {
     float cell[MAX_LEVELS], inv_cell[MAX_LEVELS];
     int max_ring[MAX_LEVELS];
     int bbox_min[3], bbox_max[3];  // order-preserving float bits
-    unsigned n_deferred;
+    float org[3];                  // coarse (dense) level: origin and dimensions
+    int dims[3];
+    float amax;                    // largest |coordinate| of the bounding box
+    unsigned n_deferred, n_occ, p2_next;
 };
 
 __device__ __forceinline__ int fbits(float f) {
@@ -84,25 +94,32 @@ struct Max { __device__ int operator()(int a, int b) const { return a > b ? a : 
 __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
-    s->n_deferred = 0;
+    s->n_deferred = s->n_occ = s->p2_next = 0;
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
+
+// Blocks of the spacing passes (grid-stride): few enough that the per-block
+// atomics do not queue on the shared statistics.
+constexpr int SPACING_BLOCKS = 1024;
 
 // pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count
 __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
                                 GridStats* s) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t n = (size_t)rows * cols;
+    const size_t n = (size_t)rows * cols;
     double d = 0, c = 0, nv = 0;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-    if (i < n && mask[i]) {
-        nv = 1;
-        float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-        for (int a = 0; a < 3; a++) mn[a] = mx[a] = fbits(p[a]);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!mask[i]) continue;
+        nv += 1;
+        const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+        for (int a = 0; a < 3; a++) {
+            mn[a] = min(mn[a], fbits(p[a]));
+            mx[a] = max(mx[a], fbits(p[a]));
+        }
         if ((i % cols) + 1 < (size_t)cols && mask[i + 1]) {
             float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
-            d = sqrtf(dx * dx + dy * dy + dz * dz);
-            c = 1;
+            d += sqrtf(dx * dx + dy * dy + dz * dz);
+            c += 1;
         }
     }
     d = block_reduce(d, Add(), 0.0);
@@ -126,14 +143,14 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
 // pass 2: mean spacing over pairs closer than 3x the pass-1 mean
 __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
                                 GridStats* s) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t n = (size_t)rows * cols;
+    const size_t n = (size_t)rows * cols;
     const double m1 = s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 0.0;
     double d = 0, c = 0;
-    if (i < n && mask[i] && (i % cols) + 1 < (size_t)cols && mask[i + 1]) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!(mask[i] && (i % cols) + 1 < (size_t)cols && mask[i + 1])) continue;
         float dx = xyz[3 * i + 3] - xyz[3 * i], dy = xyz[3 * i + 4] - xyz[3 * i + 1], dz = xyz[3 * i + 5] - xyz[3 * i + 2];
         float v = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (v <= 3.0 * m1) { d = v; c = 1; }
+        if (v <= 3.0 * m1) { d += v; c += 1; }
     }
     d = block_reduce(d, Add(), 0.0);
     c = block_reduce(c, Add(), 0.0);
@@ -143,24 +160,46 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
     }
 }
 
-// finest cell = fixed_cell if > 0, else factor * trimmed mean spacing; level l
-// has cell * 4^l.  The cell size only affects speed, never the result.
+// Finest cell = fixed_cell if > 0, else factor * trimmed mean spacing (a
+// hashed level).  The coarse level is a dense grid over the bounding box with
+// cells of COARSE_MULT finest cells, enlarged until it has at most DENSE_MAX
+// cells.  The cell sizes only affect speed, never the result.
 __global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int levels) {
     float cell = fixed_cell;
     if (!(cell > 0.f)) {
         double sp = s->sp2_cnt > 0 ? s->sp2_sum / s->sp2_cnt : 1.0;
         cell = (float)(factor * sp);
     }
-    float ext = 0.f;
+    float ext = 0.f, e[3] = {0.f, 0.f, 0.f}, amax = 0.f;
     for (int a = 0; a < 3; a++)
-        if (s->bbox_max[a] >= s->bbox_min[a]) ext = fmaxf(ext, bitsf(s->bbox_max[a]) - bitsf(s->bbox_min[a]));
+        if (s->bbox_max[a] >= s->bbox_min[a]) {
+            e[a] = bitsf(s->bbox_max[a]) - bitsf(s->bbox_min[a]);
+            ext = fmaxf(ext, e[a]);
+            s->org[a] = bitsf(s->bbox_min[a]);
+            amax = fmaxf(amax, fmaxf(fabsf(bitsf(s->bbox_min[a])), fabsf(bitsf(s->bbox_max[a]))));
+        } else {
+            s->org[a] = 0.f;
+        }
+    s->amax = amax;
     cell = fmaxf(cell, ext * 1e-5f);
     cell = fmaxf(cell, 1e-6f);
-    for (int l = 0; l < MAX_LEVELS; l++) {
-        float c = l < levels ? cell * (float)(1 << (2 * l)) : cell;
-        s->cell[l] = c;
-        s->inv_cell[l] = 1.0f / c;
-        s->max_ring[l] = (int)ceilf(ext / c) + 2;
+    s->cell[0] = cell;
+    s->inv_cell[0] = 1.0f / cell;
+    s->max_ring[0] = (int)ceilf(ext / cell) + 2;
+    if (levels > 1) {
+        float c = cell * (float)COARSE_MULT;
+        for (;;) {
+            long long v = 1;
+            for (int a = 0; a < 3; a++) {
+                s->dims[a] = (int)floorf(e[a] / c) + 1;
+                v *= s->dims[a];
+            }
+            if (v <= DENSE_MAX) break;
+            c *= 1.26f;
+        }
+        s->cell[1] = c;
+        s->inv_cell[1] = 1.0f / c;
+        s->max_ring[1] = (int)ceilf(ext / c) + 2;
     }
 }
 
@@ -170,14 +209,32 @@ __device__ __forceinline__ void cell_of(float x, float y, float z, float ic, int
     cz = __float2int_rd(z * ic);
 }
 
+// Table slot of a point: hashed cell on the finest level, dense cell index on
+// the coarse level.
+__device__ __forceinline__ unsigned grid_slot(const GridStats* __restrict__ s, int level, unsigned tmask, float x,
+                                              float y, float z) {
+    if (level == 0) {
+        int cx, cy, cz;
+        cell_of(x, y, z, s->inv_cell[0], cx, cy, cz);
+        return hash3(cx, cy, cz, tmask);
+    }
+    const float ic = s->inv_cell[1];
+    int ix = min(max(__float2int_rd((x - s->org[0]) * ic), 0), s->dims[0] - 1);
+    int iy = min(max(__float2int_rd((y - s->org[1]) * ic), 0), s->dims[1] - 1);
+    int iz = min(max(__float2int_rd((z - s->org[2]) * ic), 0), s->dims[2] - 1);
+    return ((unsigned)iz * (unsigned)s->dims[1] + (unsigned)iy) * (unsigned)s->dims[0] + (unsigned)ix;
+}
+
+// Neighbouring pixels mostly share a cell, so the lanes of a warp that hit the
+// same slot add to it once (the lowest such lane).
 __global__ void hash_count_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                   const GridStats* __restrict__ s, int level, unsigned tmask,
                                   unsigned* __restrict__ counts) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !mask[i]) return;
-    int cx, cy, cz;
-    cell_of(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s->inv_cell[level], cx, cy, cz);
-    atomicAdd(&counts[hash3(cx, cy, cz, tmask)], 1u);
+    const bool v = i < n && mask[i];
+    const unsigned h = v ? grid_slot(s, level, tmask, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) : 0xffffffffu;
+    const unsigned grp = __match_any_sync(0xffffffffu, h);
+    if (v && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[h], (unsigned)__popc(grp));
 }
 
 __device__ __forceinline__ unsigned block_scan_incl(unsigned v, unsigned* ws) {
@@ -239,12 +296,21 @@ __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t
                                     const uint2* __restrict__ tab, unsigned* __restrict__ fill,
                                     float4* __restrict__ pts) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !mask[i]) return;
-    float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
-    int cx, cy, cz;
-    cell_of(x, y, z, s->inv_cell[level], cx, cy, cz);
-    unsigned h = hash3(cx, cy, cz, tmask);
-    unsigned pos = tab[h].x + atomicAdd(&fill[h], 1u);
+    const bool v = i < n && mask[i];
+    float x = 0.f, y = 0.f, z = 0.f;
+    unsigned h = 0xffffffffu;
+    if (v) {
+        x = xyz[3 * i]; y = xyz[3 * i + 1]; z = xyz[3 * i + 2];
+        h = grid_slot(s, level, tmask, x, y, z);
+    }
+    // one atomic per slot and warp; lanes take consecutive places in lane order
+    const unsigned grp = __match_any_sync(0xffffffffu, h);
+    const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+    unsigned base = 0;
+    if (v && lane == leader) base = atomicAdd(&fill[h], (unsigned)__popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!v) return;
+    const unsigned pos = tab[h].x + base + (unsigned)__popc(grp & ((1u << lane) - 1u));
     pts[pos] = make_float4(x, y, z, __int_as_float((int)i));
 }
 
@@ -270,10 +336,6 @@ struct Level {
     const uint2* tab;  // (offset, count) per bucket
     const float4* pts;
     unsigned tmask;
-};
-struct Levels {
-    Level l[MAX_LEVELS];
-    int n;
 };
 
 __device__ __forceinline__ uint2 bucket(const Level& g, int x, int y, int z) {
@@ -301,46 +363,231 @@ __device__ __forceinline__ void visit_ring(const Level& g, float ic, int cx, int
         }
 }
 
-// Phase 1: one thread per point on the finest level.  Points not resolved
-// within FINE_RINGS rings are appended to the deferred list (md = -1).
-__global__ void __launch_bounds__(KNN_THREADS) sor_knn_fine_kernel(const float* __restrict__ xyz,
-                                                                   const uint8_t* __restrict__ mask, size_t n, int k,
-                                                                   Level g, GridStats* s, float* __restrict__ md_out,
-                                                                   unsigned* __restrict__ deferred) {
-    __shared__ float L[KNN_MAX_K1][KNN_THREADS];
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (!mask[i] || s->n_valid <= k) {
-        md_out[i] = 0.f;
-        return;
-    }
-    const int K1 = k + 1, tid = threadIdx.x;
-    const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
-    int cnt = 0;
-    auto ins = [&](const float4& p) {
-        float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-        float d2 = dx * dx + dy * dy + dz * dz;
-        int j;
-        if (cnt < K1) j = cnt++;
-        else if (d2 < L[K1 - 1][tid]) j = K1 - 1;
-        else return;
-        while (j > 0 && L[j - 1][tid] > d2) {
-            L[j][tid] = L[j - 1][tid];
-            j--;
-        }
-        L[j][tid] = d2;
-    };
+// Pixel offsets within WIN_R of the centre, ordered by length.
+constexpr int WIN_R = 4;
+constexpr int WIN_W = TILE_X + 2 * WIN_R, WIN_H = TILE_Y + 2 * WIN_R;
+constexpr int WIN_N = (2 * WIN_R + 1) * (2 * WIN_R + 1) - 1;
+__constant__ signed char c_spiral[WIN_N][2] = {
+    {0, -1}, {-1, 0}, {1, 0}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0},
+    {2, 0}, {0, 2}, {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2},
+    {-2, -2}, {2, -2}, {-2, 2}, {2, 2}, {0, -3}, {-3, 0}, {3, 0}, {0, 3}, {-1, -3}, {1, -3},
+    {-3, -1}, {3, -1}, {-3, 1}, {3, 1}, {-1, 3}, {1, 3}, {-2, -3}, {2, -3}, {-3, -2}, {3, -2},
+    {-3, 2}, {3, 2}, {-2, 3}, {2, 3}, {0, -4}, {-4, 0}, {4, 0}, {0, 4}, {-1, -4}, {1, -4},
+    {-4, -1}, {4, -1}, {-4, 1}, {4, 1}, {-1, 4}, {1, 4}, {-3, -3}, {3, -3}, {-3, 3}, {3, 3},
+    {-2, -4}, {2, -4}, {-4, -2}, {4, -2}, {-4, 2}, {4, 2}, {-2, 4}, {2, 4}, {-3, -4}, {3, -4},
+    {-4, -3}, {4, -3}, {-4, 3}, {4, 3}, {-3, 4}, {3, 4}, {-4, -4}, {4, -4}, {-4, 4}, {4, 4}};
+static_assert(WIN_W * WIN_H <= TILE_MAX_CAND, "pixel window staged in the candidate buffer");
+static_assert(TILE_MAX_CELLS <= 8 * TILE_T, "cell scan: eight cells per thread");
+
+// Phase 1: one CTA per 16 x 8 pixel tile on the finest level.
+//  - Window bound: the query and its k nearest valid pixels (in pixel
+//    distance, within WIN_R) are k + 1 real points, so the largest of their
+//    squared distances, tau0, bounds the (k + 1)-th nearest squared distance.
+//  - Box: the tile's points, minus depth outliers (a trimmed mean of their z
+//    cells), span a box of cells; the CTA gathers every point of that box
+//    dilated by TILE_DILATE cells into shared memory, sorted by cell.  All
+//    points within distance g of a query lie in the box, g being the query's
+//    distance to the box boundary.
+//  - Each in-box query scans only the cells its ball of squared radius
+//    min(tau0, g^2) touches; holding k + 1 candidates within that ball, it is
+//    exact.
+// Out-of-box points run a per-thread ring search.  Unresolved queries are
+// appended to the deferred list with md = -1.
+__global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __restrict__ xyz,
+                                                              const uint8_t* __restrict__ mask, int rows, int cols,
+                                                              int k, Level g, GridStats* s, float* __restrict__ md_out,
+                                                              unsigned* __restrict__ deferred) {
+    extern __shared__ float4 tile_smem[];
+    float4* cand = tile_smem;                                         // TILE_MAX_CAND
+    float* Ls = reinterpret_cast<float*>(tile_smem + TILE_MAX_CAND);  // (k + 1) x TILE_T
+    __shared__ int s_off[TILE_MAX_CELLS + 1];  // candidate offset of each box cell
+    __shared__ unsigned s_ws[32];
+    __shared__ int s_box[6];
+    __shared__ float s_zc;
+    __shared__ unsigned s_total;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+    const int x = x0 + (tid % TILE_X), y = y0 + (tid / TILE_X);
+    const bool in = x < cols && y < rows;
+    const size_t i = in ? (size_t)y * cols + x : 0;
+    const bool active = in && mask[i] && s->n_valid > k;
     const float ic = s->inv_cell[0], cell = s->cell[0];
-    int cx, cy, cz;
-    cell_of(qx, qy, qz, ic, cx, cy, cz);
-    for (int r = 0; r <= FINE_RINGS; r++) {
-        visit_ring(g, ic, cx, cy, cz, r, ins);
-        float gr = r * cell;
-        if (cnt >= K1 && L[K1 - 1][tid] <= gr * gr) {
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    int c[3] = {0, 0, 0};
+    if (active) {
+        qx = xyz[3 * i]; qy = xyz[3 * i + 1]; qz = xyz[3 * i + 2];
+        cell_of(qx, qy, qz, ic, c[0], c[1], c[2]);
+    }
+    if (in && !active) md_out[i] = 0.f;
+    // window bound tau0 from the pixel neighbourhood (staged in cand; w = 0 marks invalid)
+    for (int t = tid; t < WIN_W * WIN_H; t += TILE_T) {
+        const int wx = x0 - WIN_R + t % WIN_W, wy = y0 - WIN_R + t / WIN_W;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
+            const size_t j = (size_t)wy * cols + wx;
+            if (mask[j]) v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
+        }
+        cand[t] = v;
+    }
+    __syncthreads();
+    float tau0 = INFINITY;
+    if (active) {
+        const int wc = (tid / TILE_X + WIN_R) * WIN_W + tid % TILE_X + WIN_R;
+        int found = 0;
+        float m = 0.f;
+        for (int o = 0; o < WIN_N && found < k; o++) {
+            const float4 p = cand[wc + c_spiral[o][1] * WIN_W + c_spiral[o][0]];
+            if (p.w == 0.f) continue;
+            const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+            m = fmaxf(m, dx * dx + dy * dy + dz * dz);
+            found++;
+        }
+        if (found == k) tau0 = m;
+    }
+    __syncthreads();
+    // trimmed mean of the z cells: mean, then mean of those within 8 cells of it
+    float n1 = block_reduce(active ? 1.f : 0.f, Add(), 0.f);
+    float z1 = block_reduce(active ? (float)c[2] : 0.f, Add(), 0.f);
+    if (tid == 0) s_zc = n1 > 0 ? z1 / n1 : 0.f;
+    __syncthreads();
+    bool near1 = active && fabsf((float)c[2] - s_zc) <= 8.f;
+    float n2 = block_reduce(near1 ? 1.f : 0.f, Add(), 0.f);
+    float z2 = block_reduce(near1 ? (float)c[2] : 0.f, Add(), 0.f);
+    __syncthreads();
+    if (tid == 0) s_zc = n2 > 0 ? z2 / n2 : s_zc;
+    __syncthreads();
+    const bool inbox = active && fabsf((float)c[2] - s_zc) <= 4.f;
+    for (int a = 0; a < 3; a++) {
+        int lo = block_reduce(inbox ? c[a] : INT_MAX, Min(), INT_MAX);
+        int hi = block_reduce(inbox ? c[a] : INT_MIN, Max(), INT_MIN);
+        if (tid == 0) { s_box[a] = lo; s_box[3 + a] = hi; }
+    }
+    __syncthreads();
+    const bool any = s_box[0] != INT_MAX;
+    const int lo0 = s_box[0] - TILE_DILATE, lo1 = s_box[1] - TILE_DILATE, lo2 = s_box[2] - TILE_DILATE;
+    const long long ex = any ? (long long)s_box[3] - s_box[0] + 1 + 2 * TILE_DILATE : 0;
+    const long long ey = any ? (long long)s_box[4] - s_box[1] + 1 + 2 * TILE_DILATE : 0;
+    const long long ez = any ? (long long)s_box[5] - s_box[2] + 1 + 2 * TILE_DILATE : 0;
+    const long long V = ex * ey * ez;
+    bool fast = any && V <= TILE_MAX_CELLS;  // uniform over the CTA
+    if (fast) {
+        // counting sort of the box's points by cell: count, scan, place
+        for (int t = tid; t < V; t += TILE_T) {
+            const int ix = lo0 + (int)(t % ex), iy = lo1 + (int)((t / ex) % ey), iz = lo2 + (int)(t / (ex * ey));
+            const uint2 b = bucket(g, ix, iy, iz);
+            int n_in = 0;
+            for (unsigned u = b.x; u < b.x + b.y; u++) {
+                const float4 p = __ldg(g.pts + u);
+                int px, py, pz;
+                cell_of(p.x, p.y, p.z, ic, px, py, pz);
+                n_in += (px == ix && py == iy && pz == iz);
+            }
+            s_off[t] = n_in;
+        }
+        __syncthreads();
+        unsigned v8[8], own = 0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = tid * 8 + u;
+            v8[u] = t < V ? (unsigned)s_off[t] : 0u;
+            own += v8[u];
+        }
+        const unsigned incl = block_scan_incl(own, s_ws);
+        unsigned run = incl - own;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = tid * 8 + u;
+            if (t < V) s_off[t] = (int)run;
+            run += v8[u];
+        }
+        if (tid == TILE_T - 1) {
+            s_total = incl;
+            s_off[V] = (int)incl;
+        }
+        __syncthreads();
+        fast = s_total <= (unsigned)TILE_MAX_CAND;
+        if (fast) {
+            for (int t = tid; t < V; t += TILE_T) {
+                const int ix = lo0 + (int)(t % ex), iy = lo1 + (int)((t / ex) % ey), iz = lo2 + (int)(t / (ex * ey));
+                const uint2 b = bucket(g, ix, iy, iz);
+                int pos = s_off[t];
+                for (unsigned u = b.x; u < b.x + b.y; u++) {
+                    const float4 p = __ldg(g.pts + u);
+                    int px, py, pz;
+                    cell_of(p.x, p.y, p.z, ic, px, py, pz);
+                    if (px == ix && py == iy && pz == iz) cand[pos++] = p;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    const int K1 = k + 1;
+    // margin for the float rounding of the cell mapping (|p| * 2^-23 << 1e-3 cell)
+    const float margin = fmaxf(1e-3f * cell, 4e-7f * fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))));
+    if (fast && inbox) {
+        float gmin = fminf(fminf(qx - lo0 * cell, (lo0 + ex) * cell - qx),
+                           fminf(fminf(qy - lo1 * cell, (lo1 + ey) * cell - qy),
+                                 fminf(qz - lo2 * cell, (lo2 + ez) * cell - qz)));
+        gmin = fmaxf(gmin - margin, 0.f);
+        // every point with d2 <= thr lies in the cells the ball of radius R touches
+        const float thr = fminf(tau0, gmin * gmin);
+        const float R = sqrtf(thr) + margin;
+        const int ax0 = max(lo0, __float2int_rd((qx - R) * ic)), ax1 = min(lo0 + (int)ex - 1, __float2int_rd((qx + R) * ic));
+        const int ay0 = max(lo1, __float2int_rd((qy - R) * ic)), ay1 = min(lo1 + (int)ey - 1, __float2int_rd((qy + R) * ic));
+        const int az0 = max(lo2, __float2int_rd((qz - R) * ic)), az1 = min(lo2 + (int)ez - 1, __float2int_rd((qz + R) * ic));
+        int cnt = 0;
+        for (int iz = az0; iz <= az1; iz++)
+            for (int iy = ay0; iy <= ay1; iy++) {
+                const int row = (int)(((long long)(iz - lo2) * ey + (iy - lo1)) * ex) - lo0;
+                const int j1 = s_off[row + ax1 + 1];
+                for (int j = s_off[row + ax0]; j < j1; j++) {
+                    const float4 p = cand[j];
+                    const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 > thr) continue;
+                    int jj;
+                    if (cnt < K1) jj = cnt++;
+                    else if (d2 < Ls[(K1 - 1) * TILE_T + tid]) jj = K1 - 1;
+                    else continue;
+                    while (jj > 0 && Ls[(jj - 1) * TILE_T + tid] > d2) {
+                        Ls[jj * TILE_T + tid] = Ls[(jj - 1) * TILE_T + tid];
+                        jj--;
+                    }
+                    Ls[jj * TILE_T + tid] = d2;
+                }
+            }
+        if (cnt >= K1) {
             float sum = 0.f;
-            for (int j = 1; j < K1; j++) sum += sqrtf(L[j][tid]);
+            for (int j = 1; j < K1; j++) sum += sqrtf(Ls[j * TILE_T + tid]);
             md_out[i] = sum / (float)k;
             return;
+        }
+    } else {
+        // per-thread ring search on the finest level
+        int cnt = 0;
+        auto ins = [&](const float4& p) {
+            float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+            float d2 = dx * dx + dy * dy + dz * dz;
+            int jj;
+            if (cnt < K1) jj = cnt++;
+            else if (d2 < Ls[(K1 - 1) * TILE_T + tid]) jj = K1 - 1;
+            else return;
+            while (jj > 0 && Ls[(jj - 1) * TILE_T + tid] > d2) {
+                Ls[jj * TILE_T + tid] = Ls[(jj - 1) * TILE_T + tid];
+                jj--;
+            }
+            Ls[jj * TILE_T + tid] = d2;
+        };
+        for (int r = 0; r <= FINE_RINGS; r++) {
+            visit_ring(g, ic, c[0], c[1], c[2], r, ins);
+            float gr = fmaxf(r * cell - margin, 0.f);
+            if (cnt >= K1 && Ls[(K1 - 1) * TILE_T + tid] <= gr * gr) {
+                float sum = 0.f;
+                for (int j = 1; j < K1; j++) sum += sqrtf(Ls[j * TILE_T + tid]);
+                md_out[i] = sum / (float)k;
+                return;
+            }
         }
     }
     md_out[i] = -1.f;
@@ -348,112 +595,118 @@ __global__ void __launch_bounds__(KNN_THREADS) sor_knn_fine_kernel(const float* 
     deferred[slot] = (unsigned)i;
 }
 
-// Cell t (0 <= t < 24 r^2 + 2) of the Chebyshev ring r around the origin.
-__device__ __forceinline__ void ring_cell(int r, int t, int& dx, int& dy, int& dz) {
-    if (r == 0) { dx = dy = dz = 0; return; }
-    const int side = 2 * r + 1, face = side * side;
-    if (t < 2 * face) {
-        dz = t < face ? -r : r;
-        int q = t < face ? t : t - face;
-        dy = q / side - r;
-        dx = q % side - r;
-        return;
-    }
-    t -= 2 * face;
-    const int per = 8 * r;
-    dz = t / per - (r - 1);
-    int p = t % per;
-    if (p < side) { dx = p - r; dy = -r; return; }
-    p -= side;
-    if (p < side) { dx = p - r; dy = r; return; }
-    p -= side;
-    dy = (p >> 1) - (r - 1);
-    dx = (p & 1) ? r : -r;
+// Occupied cells of the coarse (dense) level: (cell index, offset, count).
+__global__ void occupied_cells_kernel(const uint2* __restrict__ tab, GridStats* s, uint4* __restrict__ occ) {
+    const unsigned used = (unsigned)s->dims[0] * (unsigned)s->dims[1] * (unsigned)s->dims[2];
+    unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= used) return;
+    const uint2 e = tab[h];
+    if (e.y == 0) return;
+    occ[atomicAdd(&s->n_occ, 1u)] = make_uint4(h, e.x, e.y, 0u);
 }
 
-// Phase 2: one warp per deferred point, coarser levels.  Each lane keeps a
-// sorted list of its K1 best; after every ring the lists are merged to find
-// the (k+1)-th distance (termination and pruning bound) and the mean.
-__global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_coarse_kernel(const float* __restrict__ xyz, int k, Levels lv,
-                                                                        const GridStats* __restrict__ s,
-                                                                        const unsigned* __restrict__ deferred,
-                                                                        float* __restrict__ md_out,
-                                                                        uint32_t* __restrict__ err) {
+// Squared distance from q to a coarse cell's cube, the cube grown by a margin
+// that covers the float rounding of the cell mapping.
+__device__ __forceinline__ float cell_box_d2(unsigned idx, const GridStats* __restrict__ s, float qx, float qy,
+                                             float qz, float margin) {
+    const unsigned nx = (unsigned)s->dims[0], ny = (unsigned)s->dims[1];
+    const float c = s->cell[1];
+    const float lx = s->org[0] + (float)(idx % nx) * c - margin;
+    const float ly = s->org[1] + (float)((idx / nx) % ny) * c - margin;
+    const float lz = s->org[2] + (float)(idx / (nx * ny)) * c - margin;
+    const float w = c + 2.f * margin;
+    float ex = fmaxf(fmaxf(lx - qx, qx - (lx + w)), 0.f);
+    float ey = fmaxf(fmaxf(ly - qy, qy - (ly + w)), 0.f);
+    float ez = fmaxf(fmaxf(lz - qz, qz - (lz + w)), 0.f);
+    return ex * ex + ey * ey + ez * ez;
+}
+
+// Phase 2: one warp per deferred point, best-first over the coarse level's
+// occupied cells: repeatedly take the nearest unvisited cell (by distance to
+// its cube), scan its points with the lanes splitting them, merge the lanes'
+// sorted lists, and stop when the next cell is farther than the current
+// (k + 1)-th distance.  Work is handed out through an atomic counter.
+__global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float* __restrict__ xyz, int k,
+                                                                     GridStats* s,
+                                                                     const uint4* __restrict__ occ,
+                                                                     const float4* __restrict__ pts,
+                                                                     const unsigned* __restrict__ deferred,
+                                                                     float* __restrict__ md_out,
+                                                                     uint32_t* __restrict__ err) {
     __shared__ float L[P2_WARPS][KNN_MAX_K1][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int K1 = k + 1;
-    const unsigned nd = s->n_deferred;
-    for (unsigned item = blockIdx.x * P2_WARPS + w; item < nd; item += gridDim.x * P2_WARPS) {
+    const unsigned nd = s->n_deferred, nocc = s->n_occ;
+    for (;;) {
+        unsigned item = 0;
+        if (lane == 0) item = atomicAdd(&s->p2_next, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nd) break;
         const unsigned i = deferred[item];
         const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
+        // the cell mapping (x - org) * inv_cell and the cube corners org + i * cell
+        // round by a few ulps of the largest coordinate
+        const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
+        int cnt = 0;
+        float kth = INFINITY, sum = 0.f;
+        float last_d = -1.f;
+        int last_j = -1;
         bool done = false;
-        float md = 0.f;
-        for (int l = (lv.n > 1 ? 1 : 0); l < lv.n && !done; l++) {
-            const Level& g = lv.l[l];
-            const float ic = s->inv_cell[l], cell = s->cell[l];
-            int cx, cy, cz;
-            cell_of(qx, qy, qz, ic, cx, cy, cz);
-            int cnt = 0;
-            float bound = INFINITY;  // current (k+1)-th squared distance over the warp
-            const int rmax = (l == lv.n - 1) ? s->max_ring[l] : COARSE_RINGS;
-            for (int r = 0; r <= rmax && !done; r++) {
-                const int ncell = r == 0 ? 1 : 24 * r * r + 2;
-                for (int t = lane; t < ncell; t += 32) {
-                    int dx, dy, dz;
-                    ring_cell(r, t, dx, dy, dz);
-                    const int x = cx + dx, y = cy + dy, z = cz + dz;
-                    // squared distance from q to the cell box (pruning), slightly shrunk
-                    float ex = fmaxf(fmaxf(x * cell - qx, qx - (x + 1) * cell), 0.f);
-                    float ey = fmaxf(fmaxf(y * cell - qy, qy - (y + 1) * cell), 0.f);
-                    float ez = fmaxf(fmaxf(z * cell - qz, qz - (z + 1) * cell), 0.f);
-                    float bd = fmaxf(sqrtf(ex * ex + ey * ey + ez * ez) - 1e-4f * cell, 0.f);
-                    if (bd * bd > bound) continue;
-                    uint2 b = bucket(g, x, y, z);
-                    for (unsigned u = b.x; u < b.x + b.y; u++) {
-                        float4 p = __ldg(g.pts + u);
-                        int px, py, pz;
-                        cell_of(p.x, p.y, p.z, ic, px, py, pz);
-                        if (px != x || py != y || pz != z) continue;
-                        float ddx = p.x - qx, ddy = p.y - qy, ddz = p.z - qz;
-                        float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                        int j;
-                        if (cnt < K1) j = cnt++;
-                        else if (d2 < L[w][K1 - 1][lane]) j = K1 - 1;
-                        else continue;
-                        while (j > 0 && L[w][j - 1][lane] > d2) {
-                            L[w][j][lane] = L[w][j - 1][lane];
-                            j--;
-                        }
-                        L[w][j][lane] = d2;
-                    }
-                }
-                __syncwarp();
-                // merge: the K1 smallest over all lanes, in order
-                int head = 0;
-                float kth = INFINITY, sum = 0.f;
-                for (int round = 0; round < K1; round++) {
-                    float v = head < cnt ? L[w][head][lane] : INFINITY;
-                    int who = lane;
-                    for (int off = 16; off; off >>= 1) {
-                        float ov = __shfl_xor_sync(0xffffffffu, v, off);
-                        int ow = __shfl_xor_sync(0xffffffffu, who, off);
-                        if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
-                    }
-                    if (lane == who) head++;
-                    if (round > 0) sum += sqrtf(v);
-                    if (round == K1 - 1) kth = v;
-                }
-                bound = kth;
-                const float gr = r * cell;
-                if (kth <= gr * gr) {
-                    done = true;
-                    md = sum / (float)k;
-                }
-                __syncwarp();
+        for (unsigned iter = 0; iter <= nocc; iter++) {
+            // nearest cell after (last_d, last_j) in (distance, index) order
+            float bd = INFINITY;
+            int bj = INT_MAX;
+            for (unsigned j = lane; j < nocc; j += 32) {
+                float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
+                bool after = d > last_d || (d == last_d && (int)j > last_j);
+                if (after && (d < bd || (d == bd && (int)j < bj))) { bd = d; bj = (int)j; }
             }
+            for (int off = 16; off; off >>= 1) {
+                float od = __shfl_xor_sync(0xffffffffu, bd, off);
+                int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+                if (od < bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
+            }
+            if (bj == INT_MAX || bd > kth) { done = bj == INT_MAX ? kth < INFINITY : true; break; }
+            const uint4 o = occ[bj];
+            const unsigned b0 = o.y, bn = o.z;
+            for (unsigned u = b0 + lane; u < b0 + bn; u += 32) {
+                float4 p = __ldg(pts + u);
+                float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+                float d2 = dx * dx + dy * dy + dz * dz;
+                int jj;
+                if (cnt < K1) jj = cnt++;
+                else if (d2 < L[w][K1 - 1][lane]) jj = K1 - 1;
+                else continue;
+                while (jj > 0 && L[w][jj - 1][lane] > d2) {
+                    L[w][jj][lane] = L[w][jj - 1][lane];
+                    jj--;
+                }
+                L[w][jj][lane] = d2;
+            }
+            __syncwarp();
+            // merge: the K1 smallest over all lanes, in order
+            int head = 0;
+            float acc = 0.f, kk = INFINITY;
+            for (int round = 0; round < K1; round++) {
+                float v = head < cnt ? L[w][head][lane] : INFINITY;
+                int who = lane;
+                for (int off = 16; off; off >>= 1) {
+                    float ov = __shfl_xor_sync(0xffffffffu, v, off);
+                    int ow = __shfl_xor_sync(0xffffffffu, who, off);
+                    if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
+                }
+                if (lane == who) head++;
+                if (round > 0) acc += sqrtf(v);
+                if (round == K1 - 1) kk = v;
+            }
+            kth = kk;
+            sum = acc;
+            last_d = bd;
+            last_j = bj;
+            __syncwarp();
         }
         if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
-        if (lane == 0) md_out[i] = md;
+        if (lane == 0) md_out[i] = kth < INFINITY ? sum / (float)k : 0.f;
     }
 }
 
@@ -552,8 +805,9 @@ unsigned table_size(size_t want) {
     return t;
 }
 
-// level l tables: about 4 points per bucket on the finest level, 16x fewer per level
-unsigned level_table(size_t n, int l) { return table_size((n / 4) >> (4 * l)); }
+// level tables: about 4 points per bucket on the hashed finest level; the
+// coarse level is a dense grid of at most DENSE_MAX cells
+unsigned level_table(size_t n, int l) { return l == 0 ? table_size(n / 4) : (unsigned)DENSE_MAX; }
 
 struct GridScratch {
     GridStats* stats;
@@ -566,10 +820,12 @@ struct GridScratch {
     float* md;
     unsigned* deferred;
     double* part;
+    uint4* occ;  // occupied coarse cells: (cell index, offset, count, 0)
 };
 
 size_t grid_bytes(size_t n, int levels) {
-    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(((n + GB - 1) / GB) * 16);
+    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(((n + GB - 1) / GB) * 16) +
+               zim_align256((size_t)level_table(n, levels - 1) * sizeof(uint4));
     unsigned tmax = 1024;
     for (int l = 0; l < levels; l++) {
         unsigned t = level_table(n, l);
@@ -596,7 +852,8 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     G.md = (float*)zim_scratch_take(ctx, n * 4);
     G.deferred = (unsigned*)zim_scratch_take(ctx, n * 4);
     G.part = (double*)zim_scratch_take(ctx, ((n + GB - 1) / GB) * 16);
-    if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.part)
+    G.occ = (uint4*)zim_scratch_take(ctx, (size_t)G.tsize[levels - 1] * sizeof(uint4));
+    if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.part || !G.occ)
         return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
     return ZIM_OK;
 }
@@ -606,8 +863,9 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
-    spacing1_kernel<<<nblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
-    spacing2_kernel<<<nblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
+    const unsigned sblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
+    spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
+    spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
     cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
     ctx->launches += 4;
     for (int l = 0; l < G.levels; l++) {
@@ -644,19 +902,26 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     float factor = 3.5f * sqrtf(fmaxf(1.0f, (float)mean_k / 30.0f));
     s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, G, st);
     if (s) return s;
-    Levels lv;
-    lv.n = G.levels;
-    for (int l = 0; l < G.levels; l++) lv.l[l] = Level{G.tab[l], G.pts[l], G.tsize[l] - 1};
+    const Level fine{G.tab[0], G.pts[0], G.tsize[0] - 1};
     float* md = mean_dist ? mean_dist : G.md;
-    sor_knn_fine_kernel<<<(unsigned)((n + KNN_THREADS - 1) / KNN_THREADS), KNN_THREADS, 0, st>>>(
-        xyz, mask, n, mean_k, lv.l[0], G.stats, md, G.deferred);
-    sor_knn_coarse_kernel<<<(unsigned)(2 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
-        xyz, mean_k, lv, G.stats, G.deferred, md, ctx->d_error);
+    occupied_cells_kernel<<<(unsigned)((DENSE_MAX + GB - 1) / GB), GB, 0, st>>>(G.tab[1], G.stats, G.occ);
+    dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
+    const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * sizeof(float);
+    // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
+    sor_knn_far_kernel<<<(unsigned)(4 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
+        xyz, mean_k, G.stats, G.occ, G.pts[1], G.deferred, md, ctx->d_error);
+    ctx->launches += 3;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
     sor_partial_kernel<<<nblk, GB, 0, st>>>(mask, md, n, G.part);
     sor_stats_kernel<<<1, 1024, 0, st>>>(G.part, (int)nblk, G.stats);
     sor_classify_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, mean_k, std_mul, G.stats, md, mask_out, xyz_out);
-    ctx->launches += 5;
+    ctx->launches += 3;
+    static_assert(sizeof(GridStats) <= 256, "stats snapshot buffer");
+    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_sor_stats, G.stats, sizeof(GridStats), cudaMemcpyDeviceToDevice, st));
+    ctx->have_sor_stats = true;
+    ctx->last_sor_std_mul = std_mul;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
 }
@@ -689,6 +954,21 @@ extern "C" ZIM_API zim_status zim_filter_sor(zim_ctx* ctx, const float* xyz, con
     if (s) return s;
     zim_scratch_reset(ctx);
     return zim_sor_launch(ctx, xyz, mask, rows, cols, mean_k, std_mul, nullptr, mask_out, mean_dist, zim_stream(stream));
+}
+
+extern "C" ZIM_API zim_status zim_filter_sor_stats(zim_ctx* ctx, zim_sor_stats* out) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    if (!out || !ctx->have_sor_stats) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "no SOR run on this context");
+    GridStats h;
+    ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    ZIM_CUDA_TRY(ctx, cudaMemcpy(&h, ctx->d_sor_stats, sizeof h, cudaMemcpyDeviceToHost));
+    const double nv = h.n_valid;
+    out->n_valid = nv;
+    out->mean = nv > 0 ? h.md_sum / nv : 0.0;
+    out->stddev = nv > 1 ? sqrt((h.md_sq - h.md_sum * h.md_sum / nv) / (nv - 1)) : 0.0;
+    out->threshold = out->mean + ctx->last_sor_std_mul * out->stddev;
+    out->n_far_search = h.n_deferred;
+    return ZIM_OK;
 }
 
 extern "C" ZIM_API zim_status zim_filter_metric_gaussian(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,

@@ -98,11 +98,8 @@ zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_
                             const int32_t* r_base, const float* r_res, const int32_t* r_order, int rows, int cols,
                             int pha_f, double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st) {
     size_t smem = (size_t)cols * 12 + (size_t)(pha_f + 1) * 8;
-    static int configured_for = 0;
-    if ((int)smem > 48 * 1024 && (int)smem > configured_for) {
-        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured_for = (int)smem;
-    }
+    // the attribute is per device and per function: set it on every call
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     match_kernel<<<rows, MATCH_THREADS, smem, st>>>(l_base, l_res, l_order, r_base, r_res, r_order, cols, pha_f,
                                                     (float)grad_threshold, disp, best_col);
     ctx->launches += 1;

@@ -38,6 +38,9 @@ struct zim_ctx {
     uint32_t* d_error = nullptr;  // device error word
     void* h_pinned = nullptr;     // small pinned staging (counts)
     unsigned long long launches = 0;  // kernels this context has launched
+    void* d_sor_stats = nullptr;      // device copy of the last SOR run's statistics (256 B)
+    bool have_sor_stats = false;
+    double last_sor_std_mul = 1.0;
 };
 
 // Records a formatted error on the context and returns the status.
