@@ -43,7 +43,7 @@ constexpr int P2_WARPS = 4;      // phase-2 warps per CTA
 constexpr int TILE_X = 16, TILE_Y = 8, TILE_T = TILE_X * TILE_Y;
 constexpr int TILE_DILATE = 2;        // cells added around a tile's box
 constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
-constexpr int TILE_MAX_CAND = 2048;   // gathered points per tile
+constexpr int TILE_MAX_CAND = 1536;   // gathered points per tile (a surface tile gathers ~800)
 constexpr int COARSE_MULT = 16;       // coarse level cell = 16 x finest
 constexpr long long DENSE_MAX = 1 << 21;  // cells of the dense coarse level
 
@@ -73,7 +73,7 @@ __device__ __forceinline__ unsigned hash3(int x, int y, int z, unsigned tmask) {
 
 // Deterministic block reduction (fixed shuffle tree); result valid in thread 0.
 template <typename T, typename Op>
-__device__ T block_reduce(T v, Op op, T ident) {
+__device__ __forceinline__ T block_reduce(T v, Op op, T ident) {
     __shared__ T ws[32];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int off = 16; off; off >>= 1) v = op(v, __shfl_down_sync(0xffffffffu, v, off));
@@ -98,13 +98,14 @@ __global__ void stats_init_kernel(GridStats* s) {
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
 
-// Blocks of the spacing passes (grid-stride): few enough that the per-block
-// atomics do not queue on the shared statistics.
+// Blocks of the spacing passes (grid-stride).  Each block writes its partial
+// sums; spacing_total_kernel adds them in a fixed order, so the cell size does
+// not depend on the order blocks finish in.
 constexpr int SPACING_BLOCKS = 1024;
 
 // pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count
 __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                                GridStats* s) {
+                                GridStats* s, double* __restrict__ part) {
     const size_t n = (size_t)rows * cols;
     double d = 0, c = 0, nv = 0;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
@@ -130,9 +131,9 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
         mx[a] = block_reduce(mx[a], Max(), INT_MIN);
     }
     if (threadIdx.x == 0) {
-        atomicAdd(&s->sp_sum, d);
-        atomicAdd(&s->sp_cnt, c);
-        atomicAdd(&s->n_valid, nv);  // integer-valued: exact in any order
+        part[3 * blockIdx.x] = d;
+        part[3 * blockIdx.x + 1] = c;
+        part[3 * blockIdx.x + 2] = nv;
         for (int a = 0; a < 3; a++) {
             if (mn[a] != INT_MAX) atomicMin(&s->bbox_min[a], mn[a]);
             if (mx[a] != INT_MIN) atomicMax(&s->bbox_max[a], mx[a]);
@@ -142,7 +143,7 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
 
 // pass 2: mean spacing over pairs closer than 3x the pass-1 mean
 __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                                GridStats* s) {
+                                const GridStats* __restrict__ s, double* __restrict__ part) {
     const size_t n = (size_t)rows * cols;
     const double m1 = s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 0.0;
     double d = 0, c = 0;
@@ -155,8 +156,31 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
     d = block_reduce(d, Add(), 0.0);
     c = block_reduce(c, Add(), 0.0);
     if (threadIdx.x == 0) {
-        atomicAdd(&s->sp2_sum, d);
-        atomicAdd(&s->sp2_cnt, c);
+        part[3 * blockIdx.x] = d;
+        part[3 * blockIdx.x + 1] = c;
+        part[3 * blockIdx.x + 2] = 0.0;
+    }
+}
+
+// Fixed-order total of the spacing passes' block partials (one block of
+// SPACING_BLOCKS threads).  pass 1 sets the mean spacing and the valid count,
+// pass 2 the trimmed mean spacing.
+__global__ void spacing_total_kernel(const double* __restrict__ part, int nblk, int pass, GridStats* s) {
+    const int t = threadIdx.x;
+    double d = t < nblk ? part[3 * t] : 0.0, c = t < nblk ? part[3 * t + 1] : 0.0;
+    double nv = t < nblk ? part[3 * t + 2] : 0.0;
+    d = block_reduce(d, Add(), 0.0);
+    c = block_reduce(c, Add(), 0.0);
+    nv = block_reduce(nv, Add(), 0.0);
+    if (t == 0) {
+        if (pass == 1) {
+            s->sp_sum = d;
+            s->sp_cnt = c;
+            s->n_valid = nv;
+        } else {
+            s->sp2_sum = d;
+            s->sp2_cnt = c;
+        }
     }
 }
 
@@ -201,6 +225,25 @@ __global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int le
         s->inv_cell[1] = 1.0f / c;
         s->max_ring[1] = (int)ceilf(ext / c) + 2;
     }
+}
+
+// Squared distance with one fixed rounding sequence, so the same pair of
+// points gives the same value at every call site of the kNN search.
+__device__ __forceinline__ float sqdist(float dx, float dy, float dz) { return fmaf(dz, dz, fmaf(dy, dy, dx * dx)); }
+
+// Order-independent sum of the k + 1 nearest distances: each root, scaled by
+// 2^(56 - e) with sqrt(largest squared distance) < 2^e, is truncated to an
+// integer and the integers are added exactly, so every search path and every
+// visiting order gives the same bits.  (Roots below 2^(e - 56) count as 0.)
+__device__ __forceinline__ int root_exponent(float d2max) {
+    int e;
+    frexpf(sqrtf(d2max), &e);
+    return max(e, -60);  // keeps the scale 2^(56 - e) finite
+}
+__device__ __forceinline__ float root_scale(int e) { return ldexpf(1.0f, 56 - e); }
+__device__ __forceinline__ long long root_fixed(float d2, float scale) { return __float2ll_rz(sqrtf(d2) * scale); }
+__device__ __forceinline__ float fixed_mean(long long sum, int e, int k) {
+    return (float)(ldexp((double)sum, e - 56) / (double)k);
 }
 
 __device__ __forceinline__ void cell_of(float x, float y, float z, float ic, int& cx, int& cy, int& cz) {
@@ -379,6 +422,61 @@ __constant__ signed char c_spiral[WIN_N][2] = {
 static_assert(WIN_W * WIN_H <= TILE_MAX_CAND, "pixel window staged in the candidate buffer");
 static_assert(TILE_MAX_CELLS <= 8 * TILE_T, "cell scan: eight cells per thread");
 
+// Per-thread buffered selection of the K1 smallest squared distances, in
+// column tid of a [cap][TILE_T] shared array.  Values within the current bound
+// are appended unsorted; a full buffer is sorted, cut back to K1 entries and
+// the bound tightened to its K1-th value.  Appending keeps the lanes of a warp
+// in step; each lane sorts its own short list once at the end.
+constexpr int SEL_SLACK = 17;  // cap = K1 + SEL_SLACK
+struct KSel {
+    float* L;  // entry j at L[j * TILE_T]
+    int cnt, K1, cap;
+    float thr;
+    __device__ __forceinline__ float at(int j) const { return L[j * TILE_T]; }
+    __device__ __forceinline__ void sort() {
+        for (int a = 1; a < cnt; a++) {
+            const float v = L[a * TILE_T];
+            int b = a;
+            while (b > 0 && L[(b - 1) * TILE_T] > v) {
+                L[b * TILE_T] = L[(b - 1) * TILE_T];
+                b--;
+            }
+            L[b * TILE_T] = v;
+        }
+    }
+    __device__ __forceinline__ void push(float d2) {
+        if (d2 > thr) return;
+        L[cnt * TILE_T] = d2;
+        if (++cnt == cap) {
+            sort();
+            cnt = K1;
+            thr = L[(K1 - 1) * TILE_T];
+        }
+    }
+    // Mean distance to the k = K1 - 1 neighbours (needs cnt >= K1): drops the
+    // cnt - K1 largest entries, then sums the roots of the K1 smallest (the
+    // query's own zero among them) in fixed point.
+    __device__ __forceinline__ float mean_dist(int k) {
+        while (cnt > K1) {
+            int jm = 0;
+            float vm = L[0];
+            for (int j = 1; j < cnt; j++) {
+                const float v = L[j * TILE_T];
+                if (v > vm) { vm = v; jm = j; }
+            }
+            cnt--;
+            L[jm * TILE_T] = L[cnt * TILE_T];
+        }
+        float vmax = 0.f;
+        for (int j = 0; j < cnt; j++) vmax = fmaxf(vmax, L[j * TILE_T]);
+        const int e = root_exponent(vmax);
+        const float sc = root_scale(e);
+        long long sum = 0;
+        for (int j = 0; j < cnt; j++) sum += root_fixed(L[j * TILE_T], sc);
+        return fixed_mean(sum, e, k);
+    }
+};
+
 // Phase 1: one CTA per 16 x 8 pixel tile on the finest level.
 //  - Window bound: the query and its k nearest valid pixels (in pixel
 //    distance, within WIN_R) are k + 1 real points, so the largest of their
@@ -439,7 +537,7 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
             const float4 p = cand[wc + c_spiral[o][1] * WIN_W + c_spiral[o][0]];
             if (p.w == 0.f) continue;
             const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-            m = fmaxf(m, dx * dx + dy * dy + dz * dz);
+            m = fmaxf(m, sqdist(dx, dy, dz));
             found++;
         }
         if (found == k) tau0 = m;
@@ -457,6 +555,7 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
     if (tid == 0) s_zc = n2 > 0 ? z2 / n2 : s_zc;
     __syncthreads();
     const bool inbox = active && fabsf((float)c[2] - s_zc) <= 4.f;
+#pragma unroll
     for (int a = 0; a < 3; a++) {
         int lo = block_reduce(inbox ? c[a] : INT_MAX, Min(), INT_MAX);
         int hi = block_reduce(inbox ? c[a] : INT_MIN, Max(), INT_MIN);
@@ -521,72 +620,75 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
         }
         __syncthreads();
     }
-    if (!active) return;
     const int K1 = k + 1;
+    const bool fq = active && fast && inbox;
     // margin for the float rounding of the cell mapping (|p| * 2^-23 << 1e-3 cell)
     const float margin = fmaxf(1e-3f * cell, 4e-7f * fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))));
-    if (fast && inbox) {
+    float thr = -1.f;
+    int bx0 = INT_MAX, by0 = INT_MAX, bz0 = INT_MAX, bx1 = INT_MIN, by1 = INT_MIN, bz1 = INT_MIN;
+    if (fq) {
         float gmin = fminf(fminf(qx - lo0 * cell, (lo0 + ex) * cell - qx),
                            fminf(fminf(qy - lo1 * cell, (lo1 + ey) * cell - qy),
                                  fminf(qz - lo2 * cell, (lo2 + ez) * cell - qz)));
         gmin = fmaxf(gmin - margin, 0.f);
         // every point with d2 <= thr lies in the cells the ball of radius R touches
-        const float thr = fminf(tau0, gmin * gmin);
+        thr = fminf(tau0, gmin * gmin);
         const float R = sqrtf(thr) + margin;
-        const int ax0 = max(lo0, __float2int_rd((qx - R) * ic)), ax1 = min(lo0 + (int)ex - 1, __float2int_rd((qx + R) * ic));
-        const int ay0 = max(lo1, __float2int_rd((qy - R) * ic)), ay1 = min(lo1 + (int)ey - 1, __float2int_rd((qy + R) * ic));
-        const int az0 = max(lo2, __float2int_rd((qz - R) * ic)), az1 = min(lo2 + (int)ez - 1, __float2int_rd((qz + R) * ic));
-        int cnt = 0;
-        for (int iz = az0; iz <= az1; iz++)
-            for (int iy = ay0; iy <= ay1; iy++) {
+        bx0 = max(lo0, __float2int_rd((qx - R) * ic)); bx1 = min(lo0 + (int)ex - 1, __float2int_rd((qx + R) * ic));
+        by0 = max(lo1, __float2int_rd((qy - R) * ic)); by1 = min(lo1 + (int)ey - 1, __float2int_rd((qy + R) * ic));
+        bz0 = max(lo2, __float2int_rd((qz - R) * ic)); bz1 = min(lo2 + (int)ez - 1, __float2int_rd((qz + R) * ic));
+    }
+    // The warp scans the union of its queries' cell ranges in step: every lane
+    // reads the same candidate (a shared-memory broadcast) and keeps it when it
+    // lies within the lane's own bound.
+    const unsigned full = 0xffffffffu;
+    const int ux0 = __reduce_min_sync(full, bx0), ux1 = __reduce_max_sync(full, bx1);
+    const int uy0 = __reduce_min_sync(full, by0), uy1 = __reduce_max_sync(full, by1);
+    const int uz0 = __reduce_min_sync(full, bz0), uz1 = __reduce_max_sync(full, bz1);
+    if (ux0 != INT_MAX) {  // some lane of the warp is on the fast path
+        KSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, thr};
+        for (int iz = uz0; iz <= uz1; iz++)
+            for (int iy = uy0; iy <= uy1; iy++) {
                 const int row = (int)(((long long)(iz - lo2) * ey + (iy - lo1)) * ex) - lo0;
-                const int j1 = s_off[row + ax1 + 1];
-                for (int j = s_off[row + ax0]; j < j1; j++) {
+                const int j1 = s_off[row + ux1 + 1];
+                for (int j = s_off[row + ux0]; j < j1; j++) {
                     const float4 p = cand[j];
-                    const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if (d2 > thr) continue;
-                    int jj;
-                    if (cnt < K1) jj = cnt++;
-                    else if (d2 < Ls[(K1 - 1) * TILE_T + tid]) jj = K1 - 1;
-                    else continue;
-                    while (jj > 0 && Ls[(jj - 1) * TILE_T + tid] > d2) {
-                        Ls[jj * TILE_T + tid] = Ls[(jj - 1) * TILE_T + tid];
-                        jj--;
-                    }
-                    Ls[jj * TILE_T + tid] = d2;
+                    const float d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
+                    if (fq) sel.push(d2);
                 }
             }
-        if (cnt >= K1) {
-            float sum = 0.f;
-            for (int j = 1; j < K1; j++) sum += sqrtf(Ls[j * TILE_T + tid]);
-            md_out[i] = sum / (float)k;
+        if (fq && sel.cnt >= K1) {
+            md_out[i] = sel.mean_dist(k);
             return;
         }
-    } else {
+    }
+    if (!active) return;
+    if (!fq) {
         // per-thread ring search on the finest level
-        int cnt = 0;
-        auto ins = [&](const float4& p) {
-            float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-            float d2 = dx * dx + dy * dy + dz * dz;
-            int jj;
-            if (cnt < K1) jj = cnt++;
-            else if (d2 < Ls[(K1 - 1) * TILE_T + tid]) jj = K1 - 1;
-            else return;
-            while (jj > 0 && Ls[(jj - 1) * TILE_T + tid] > d2) {
-                Ls[jj * TILE_T + tid] = Ls[(jj - 1) * TILE_T + tid];
-                jj--;
-            }
-            Ls[jj * TILE_T + tid] = d2;
-        };
+        KSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, INFINITY};
         for (int r = 0; r <= FINE_RINGS; r++) {
-            visit_ring(g, ic, c[0], c[1], c[2], r, ins);
+            // cells at Chebyshev distance exactly r
+            for (int dz = -r; dz <= r; dz++)
+                for (int dy = -r; dy <= r; dy++) {
+                    const int step = (r == 0 || dz == -r || dz == r || dy == -r || dy == r) ? 1 : 2 * r;
+                    for (int dx = -r; dx <= r; dx += step) {
+                        const int cx = c[0] + dx, cy = c[1] + dy, cz = c[2] + dz;
+                        const uint2 b = bucket(g, cx, cy, cz);
+                        for (unsigned u = b.x; u < b.x + b.y; u++) {
+                            const float4 p = __ldg(g.pts + u);
+                            int px, py, pz;
+                            cell_of(p.x, p.y, p.z, ic, px, py, pz);
+                            if (px == cx && py == cy && pz == cz) sel.push(sqdist(p.x - qx, p.y - qy, p.z - qz));
+                        }
+                    }
+                }
             float gr = fmaxf(r * cell - margin, 0.f);
-            if (cnt >= K1 && Ls[(K1 - 1) * TILE_T + tid] <= gr * gr) {
-                float sum = 0.f;
-                for (int j = 1; j < K1; j++) sum += sqrtf(Ls[j * TILE_T + tid]);
-                md_out[i] = sum / (float)k;
-                return;
+            if (sel.cnt >= K1) {
+                sel.sort();
+                if (sel.at(K1 - 1) <= gr * gr) {
+                    md_out[i] = sel.mean_dist(k);
+                    return;
+                }
             }
         }
     }
@@ -634,6 +736,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                                                                      float* __restrict__ md_out,
                                                                      uint32_t* __restrict__ err) {
     __shared__ float L[P2_WARPS][KNN_MAX_K1][32];
+    __shared__ float M[P2_WARPS][KNN_MAX_K1];  // merged K1 smallest, ascending
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int K1 = k + 1;
     const unsigned nd = s->n_deferred, nocc = s->n_occ;
@@ -648,7 +751,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         // round by a few ulps of the largest coordinate
         const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
         int cnt = 0;
-        float kth = INFINITY, sum = 0.f;
+        float kth = INFINITY;
         float last_d = -1.f;
         int last_j = -1;
         bool done = false;
@@ -672,7 +775,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
             for (unsigned u = b0 + lane; u < b0 + bn; u += 32) {
                 float4 p = __ldg(pts + u);
                 float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-                float d2 = dx * dx + dy * dy + dz * dz;
+                float d2 = sqdist(dx, dy, dz);
                 int jj;
                 if (cnt < K1) jj = cnt++;
                 else if (d2 < L[w][K1 - 1][lane]) jj = K1 - 1;
@@ -684,9 +787,9 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                 L[w][jj][lane] = d2;
             }
             __syncwarp();
-            // merge: the K1 smallest over all lanes, in order
+            // merge: the K1 smallest over all lanes, in order, into M
             int head = 0;
-            float acc = 0.f, kk = INFINITY;
+            float kk = INFINITY;
             for (int round = 0; round < K1; round++) {
                 float v = head < cnt ? L[w][head][lane] : INFINITY;
                 int who = lane;
@@ -696,17 +799,26 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                     if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
                 }
                 if (lane == who) head++;
-                if (round > 0) acc += sqrtf(v);
+                if (lane == 0) M[w][round] = v;
                 if (round == K1 - 1) kk = v;
             }
             kth = kk;
-            sum = acc;
             last_d = bd;
             last_j = bj;
             __syncwarp();
         }
         if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
-        if (lane == 0) md_out[i] = kth < INFINITY ? sum / (float)k : 0.f;
+        float md = 0.f;
+        if (kth < INFINITY) {
+            const int e = root_exponent(kth);
+            const float sc = root_scale(e);
+            long long part = 0;
+            for (int j = lane; j < K1; j += 32) part += root_fixed(M[w][j], sc);
+            for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+            md = fixed_mean(part, e, k);
+        }
+        if (lane == 0) md_out[i] = md;
+        __syncwarp();
     }
 }
 
@@ -823,8 +935,14 @@ struct GridScratch {
     uint4* occ;  // occupied coarse cells: (cell index, offset, count, 0)
 };
 
+// block partials: the spacing passes' (3 per block), then the SOR statistics' (2 per block)
+size_t part_bytes(size_t n) {
+    const size_t sor = ((n + GB - 1) / GB) * 2 * sizeof(double), sp = (size_t)SPACING_BLOCKS * 3 * sizeof(double);
+    return sor > sp ? sor : sp;
+}
+
 size_t grid_bytes(size_t n, int levels) {
-    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(((n + GB - 1) / GB) * 16) +
+    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(part_bytes(n)) +
                zim_align256((size_t)level_table(n, levels - 1) * sizeof(uint4));
     unsigned tmax = 1024;
     for (int l = 0; l < levels; l++) {
@@ -851,7 +969,7 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     G.tot = (unsigned*)zim_scratch_take(ctx, ((tmax + SCAN_B - 1) / SCAN_B) * 4);
     G.md = (float*)zim_scratch_take(ctx, n * 4);
     G.deferred = (unsigned*)zim_scratch_take(ctx, n * 4);
-    G.part = (double*)zim_scratch_take(ctx, ((n + GB - 1) / GB) * 16);
+    G.part = (double*)zim_scratch_take(ctx, part_bytes(n));
     G.occ = (uint4*)zim_scratch_take(ctx, (size_t)G.tsize[levels - 1] * sizeof(uint4));
     if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.part || !G.occ)
         return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
@@ -864,10 +982,12 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
     const unsigned sblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
-    spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
-    spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats);
+    spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
+    spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats);
+    spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
+    spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats);
     cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
-    ctx->launches += 4;
+    ctx->launches += 6;
     for (int l = 0; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
         ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
@@ -906,7 +1026,8 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     float* md = mean_dist ? mean_dist : G.md;
     occupied_cells_kernel<<<(unsigned)((DENSE_MAX + GB - 1) / GB), GB, 0, st>>>(G.tab[1], G.stats, G.occ);
     dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
-    const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * sizeof(float);
+    const size_t tsm =
+        (size_t)TILE_MAX_CAND * sizeof(float4) + (size_t)(mean_k + 1 + SEL_SLACK) * TILE_T * sizeof(float);
     // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
