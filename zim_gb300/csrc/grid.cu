@@ -58,6 +58,9 @@ struct GridStats {
     float org[3];                  // coarse (dense) level: origin and dimensions
     int dims[3];
     float amax;                    // largest |coordinate| of the bounding box
+    double thr;                    // SOR threshold, and the largest float <= it
+    float thr_f;
+    int keep_all;
     unsigned n_deferred, n_occ, p2_next;
 };
 
@@ -723,11 +726,12 @@ __device__ __forceinline__ float cell_box_d2(unsigned idx, const GridStats* __re
     return ex * ex + ey * ey + ez * ez;
 }
 
-// Phase 2: one warp per deferred point, best-first over the coarse level's
-// occupied cells: repeatedly take the nearest unvisited cell (by distance to
-// its cube), scan its points with the lanes splitting them, merge the lanes'
-// sorted lists, and stop when the next cell is farther than the current
-// (k + 1)-th distance.  Work is handed out through an atomic counter.
+// Phase 2: one warp per deferred point over the coarse level's occupied cells.
+// Best-first (nearest cube first, lanes splitting each cell's points, lane
+// lists merged after each cell) until k + 1 points are held; the (k + 1)-th
+// distance then bounds the search, so one pass over the cells scans every
+// unvisited cell whose cube lies within it, and one merge ends the query.
+// Work is handed out through an atomic counter.
 __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float* __restrict__ xyz, int k,
                                                                      GridStats* s,
                                                                      const uint4* __restrict__ occ,
@@ -751,31 +755,12 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         // round by a few ulps of the largest coordinate
         const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
         int cnt = 0;
-        float kth = INFINITY;
-        float last_d = -1.f;
-        int last_j = -1;
-        bool done = false;
-        for (unsigned iter = 0; iter <= nocc; iter++) {
-            // nearest cell after (last_d, last_j) in (distance, index) order
-            float bd = INFINITY;
-            int bj = INT_MAX;
-            for (unsigned j = lane; j < nocc; j += 32) {
-                float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
-                bool after = d > last_d || (d == last_d && (int)j > last_j);
-                if (after && (d < bd || (d == bd && (int)j < bj))) { bd = d; bj = (int)j; }
-            }
-            for (int off = 16; off; off >>= 1) {
-                float od = __shfl_xor_sync(0xffffffffu, bd, off);
-                int oj = __shfl_xor_sync(0xffffffffu, bj, off);
-                if (od < bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
-            }
-            if (bj == INT_MAX || bd > kth) { done = bj == INT_MAX ? kth < INFINITY : true; break; }
-            const uint4 o = occ[bj];
-            const unsigned b0 = o.y, bn = o.z;
-            for (unsigned u = b0 + lane; u < b0 + bn; u += 32) {
-                float4 p = __ldg(pts + u);
-                float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-                float d2 = sqdist(dx, dy, dz);
+        // the lanes split a cell's points; each keeps its K1 smallest, sorted
+        auto scan_cell = [&](unsigned j) {
+            const uint4 o = occ[j];
+            for (unsigned u = o.y + lane; u < o.y + o.z; u += 32) {
+                const float4 p = __ldg(pts + u);
+                const float d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
                 int jj;
                 if (cnt < K1) jj = cnt++;
                 else if (d2 < L[w][K1 - 1][lane]) jj = K1 - 1;
@@ -787,7 +772,9 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                 L[w][jj][lane] = d2;
             }
             __syncwarp();
-            // merge: the K1 smallest over all lanes, in order, into M
+        };
+        // the K1 smallest over all lanes, in order, into M; returns the K1-th
+        auto merge = [&]() {
             int head = 0;
             float kk = INFINITY;
             for (int round = 0; round < K1; round++) {
@@ -802,10 +789,54 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                 if (lane == 0) M[w][round] = v;
                 if (round == K1 - 1) kk = v;
             }
-            kth = kk;
+            __syncwarp();
+            return kk;
+        };
+        float kth = INFINITY;
+        float last_d = -1.f;
+        int last_j = -1;
+        bool done = false;
+        // best-first until k + 1 points are held
+        for (unsigned iter = 0; iter <= nocc; iter++) {
+            // nearest cell after (last_d, last_j) in (distance, index) order
+            float bd = INFINITY;
+            int bj = INT_MAX;
+            for (unsigned j = lane; j < nocc; j += 32) {
+                float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
+                bool after = d > last_d || (d == last_d && (int)j > last_j);
+                if (after && (d < bd || (d == bd && (int)j < bj))) { bd = d; bj = (int)j; }
+            }
+            for (int off = 16; off; off >>= 1) {
+                float od = __shfl_xor_sync(0xffffffffu, bd, off);
+                int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+                if (od < bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
+            }
+            if (bj == INT_MAX) break;
+            scan_cell((unsigned)bj);
+            kth = merge();
             last_d = bd;
             last_j = bj;
-            __syncwarp();
+            if (kth < INFINITY) break;
+        }
+        if (kth < INFINITY) {
+            // every cell not yet visited whose cube lies within the current
+            // (k + 1)-th distance, in index order, then one merge
+            for (unsigned j0 = 0; j0 < nocc; j0 += 32) {
+                const unsigned j = j0 + lane;
+                bool take = false;
+                if (j < nocc) {
+                    const float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
+                    take = d <= kth && (d > last_d || (d == last_d && (int)j > last_j));
+                }
+                unsigned m = __ballot_sync(0xffffffffu, take);
+                while (m) {
+                    const int b = __ffs(m) - 1;
+                    m &= m - 1;
+                    scan_cell(j0 + (unsigned)b);
+                }
+            }
+            kth = merge();
+            done = true;
         }
         if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
         float md = 0.f;
@@ -822,15 +853,17 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
     }
 }
 
-// Per-block sums of the mean distances (valid pixels), then a fixed-order total.
+// Per-block sums of the mean distances (valid pixels, grid-stride over a fixed
+// number of blocks, so each thread's share is fixed), then a fixed-order total.
+// FP64 runs at a small fraction of the FP32 rate: two double adds per point.
 __global__ void sor_partial_kernel(const uint8_t* __restrict__ mask, const float* __restrict__ md, size_t n,
                                    double* __restrict__ part) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     double a = 0, b = 0;
-    if (i < n && mask[i]) {
-        float m = md[i];
-        a = m;
-        b = (double)(m * m);  // PCL: float square, double sum
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!mask[i]) continue;
+        const float m = md[i];
+        a += m;
+        b += (double)(m * m);  // PCL: float square, double sum
     }
     a = block_reduce(a, Add(), 0.0);
     b = block_reduce(b, Add(), 0.0);
@@ -840,7 +873,10 @@ __global__ void sor_partial_kernel(const uint8_t* __restrict__ mask, const float
     }
 }
 
-__global__ void sor_stats_kernel(const double* __restrict__ part, int nb, GridStats* s) {
+// Totals, then the threshold mean + std_mul * stddev once; the classifier
+// compares the float mean distances with thr_f, the largest float <= thr, which
+// decides exactly as (double)md > thr.
+__global__ void sor_stats_kernel(const double* __restrict__ part, int nb, int k, double std_mul, GridStats* s) {
     double a = 0, b = 0;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
         a += part[2 * i];
@@ -851,25 +887,23 @@ __global__ void sor_stats_kernel(const double* __restrict__ part, int nb, GridSt
     if (threadIdx.x == 0) {
         s->md_sum = a;
         s->md_sq = b;
+        const double nv = s->n_valid;
+        s->keep_all = nv <= k;  // too few points for a k-neighbourhood: nothing is removed
+        if (!s->keep_all) {
+            const double mean = a / nv;
+            const double var = (b - a * a / nv) / (nv - 1);
+            s->thr = mean + std_mul * sqrt(var);
+            s->thr_f = __double2float_rd(s->thr);
+        }
     }
 }
 
-__global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n, int k,
-                                    double std_mul, const GridStats* __restrict__ s, const float* __restrict__ md,
+__global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
+                                    const GridStats* __restrict__ s, const float* __restrict__ md,
                                     uint8_t* __restrict__ mask_out, float* __restrict__ xyz_out) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double nv = s->n_valid;
-    bool keep = false;
-    if (mask[i]) {
-        if (nv <= k) keep = true;  // too few points for a k-neighbourhood: nothing is removed
-        else {
-            double mean = s->md_sum / nv;
-            double var = (s->md_sq - s->md_sum * s->md_sum / nv) / (nv - 1);
-            double thr = mean + std_mul * sqrt(var);
-            keep = !((double)md[i] > thr);
-        }
-    }
+    const bool keep = mask[i] && (s->keep_all || !(md[i] > s->thr_f));
     mask_out[i] = keep ? 1 : 0;
     if (xyz_out) {
         xyz_out[3 * i] = keep ? xyz[3 * i] : 0.f;
@@ -1035,9 +1069,10 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         xyz, mean_k, G.stats, G.occ, G.pts[1], G.deferred, md, ctx->d_error);
     ctx->launches += 3;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
-    sor_partial_kernel<<<nblk, GB, 0, st>>>(mask, md, n, G.part);
-    sor_stats_kernel<<<1, 1024, 0, st>>>(G.part, (int)nblk, G.stats);
-    sor_classify_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, mean_k, std_mul, G.stats, md, mask_out, xyz_out);
+    const unsigned pblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
+    sor_partial_kernel<<<pblk, GB, 0, st>>>(mask, md, n, G.part);
+    sor_stats_kernel<<<1, 1024, 0, st>>>(G.part, (int)pblk, mean_k, std_mul, G.stats);
+    sor_classify_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, md, mask_out, xyz_out);
     ctx->launches += 3;
     static_assert(sizeof(GridStats) <= 256, "stats snapshot buffer");
     ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_sor_stats, G.stats, sizeof(GridStats), cudaMemcpyDeviceToDevice, st));
