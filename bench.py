@@ -262,6 +262,11 @@ def run_ours(args):
         }
         if cpu:
             result["cpu_baseline"] = cpu
+        if not args.no_diff:
+            result["diff"] = run_diff(api, local, steps=5, warmup=3,
+                                      want_cpu=world == 1 and not args.no_cpu_baseline)
+        if args.refine:
+            result["refine"] = run_refine(api, local, args.refine_poses, args.refine_iters)
         print(json.dumps(result))
     if dist:
         dist.barrier()
@@ -286,6 +291,141 @@ def cpu_baseline(spec, L, R, band_rows=256):
     return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": f"rectified rows [{y0},{y0 + band_rows}) of the same pair ({band_rows}/{rect.h} rows), "
                       f"whole path incl. filters, {dt:.2f} s"}
+
+
+DIFF_WORKLOAD = ("planar target at 8 seeded poses (tilt +-30 deg, depth 600-1200 mm), 2448x2048 x2 cams, "
+                 "config-1 rig; forward + adjoint of sub-pixel matching + reprojection w.r.t. 16 calibration "
+                 "parameters and per-pixel phase, point-to-plane loss, evaluated at the perturbed calibration "
+                 "(baseline +0.5%, cx0 +3 px, k1_0 +0.02)")
+
+
+def perturbed_theta(theta):
+    import numpy as np
+    th = np.array(theta, np.float64)
+    th[12] *= 1.005
+    th[2] += 3.0
+    th[4] += 0.02
+    return th
+
+
+def diff_poses(api, local, n_poses, seed=3):
+    """Renders n_poses planar-target poses, decodes them on the GPU (phase stays
+    resident) under the true calibration."""
+    from zim_gb300 import calib_refine as CR, synth
+    specs = [synth.pose_plane(seed=seed, pose=p) for p in range(n_poses)]
+    ctx = api.Context(local)
+    ctx.set_calibration(specs[0].rig.as_dict(), True)
+    dcfg = api.decode_config(**specs[0].decode_kwargs())
+    poses = []
+    for s in specs:
+        poses += CR.decode_views(ctx, dcfg, [(s.render(0), s.render(1))], [(s.plane_n, s.plane_d)])
+    return specs, ctx, poses
+
+
+def cpu_diff_baseline(spec, ctx, pose, theta):
+    """FP64 CPU forward + adjoint of one pose (the oracle restatement), timed;
+    its gradient is the reference the GPU gradient is checked against."""
+    import numpy as np
+    from oracle import oracle as O
+    rig = spec.rig
+    calib = O.make_calib(rig.K, rig.D, rig.R, rig.t, rig.width, rig.height)
+    R1, R2, P1, P2, Q, rw, rh = O.rectification(calib)
+    ir = [np.linalg.inv(P1[:, :3] @ R1), np.linalg.inv(P2[:, :3] @ R2)]
+    dist = [(rig.D[c][2], rig.D[c][3], rig.D[c][4]) for c in range(2)]
+    geom = O.diff_geom(ir, dist, Q, float(np.linalg.norm(rig.t)), rw, rh, rig.width, rig.height)
+    order = [o.cpu().numpy() for o in pose.order]
+    res = [r.cpu().numpy().astype(np.float64) for r in pose.residual]
+    t = time.perf_counter()
+    o = O.diff_eval(geom, theta, order[0], res[0], order[1], res[1], pose.best.cpu().numpy(), pose.plane)
+    dt = time.perf_counter() - t
+    return o, dt
+
+
+def run_diff(api, local, steps, warmup, want_cpu=True):
+    """Config 3: batched forward/adjoint over 8 poses at 5 MP."""
+    import numpy as np
+    import torch
+    from zim_gb300 import calib_refine as CR, diff
+    specs, ctx, poses = diff_poses(api, local, 8)
+    th = perturbed_theta(diff.nominal(ctx))
+    pha_f = specs[0].pha_f
+    CR.update_matches(ctx, th, poses, pha_f)
+    views = CR.views_of(poses)
+    for _ in range(warmup):
+        r = diff.backward(ctx, th, views)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(st)
+    for _ in range(steps):
+        r = diff.backward(ctx, th, views)
+    e1.record(st)
+    torch.cuda.synchronize()
+    bwd_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3) / steps
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        f = diff.forward(ctx, th, views)
+    fwd_ms = (time.perf_counter() - t0) * 1e3 / steps
+    t0 = time.perf_counter()
+    for _ in range(max(1, steps // 2)):
+        CR.update_matches(ctx, th, poses, pha_f)
+    torch.cuda.synchronize()
+    match_ms = (time.perf_counter() - t0) * 1e3 / max(1, steps // 2)
+    out = {"workload": DIFF_WORKLOAD, "poses": len(poses), "points": int(r["n_points"]),
+           "forward_ms": round(fwd_ms, 3), "forward_adjoint_ms": round(bwd_ms, 3),
+           "rematch_ms": round(match_ms, 3),
+           "forward_adjoint_mpoints_s": round(r["n_points"] / (bwd_ms * 1e-3) / 1e6, 2),
+           "reductions": "FP64, fixed order (bit-reproducible)"}
+    if want_cpu:
+        one = diff.backward(ctx, th, views[:1])
+        o, dt = cpu_diff_baseline(specs[0], ctx, poses[0], th)
+        g, go = one["grad"], o["grad"]
+        out["grad_err_vs_fp64"] = {"normwise_rel": float(np.linalg.norm(g - go) / np.linalg.norm(go)),
+                                   "worst_component_rel": float(np.max(np.abs(g - go) / np.abs(go))),
+                                   "loss_rel": float(abs(one["loss"] - o["loss"]) / o["loss"])}
+        out["cpu_baseline"] = {"value": round(o["n_points"] / dt / 1e6, 4), "unit": "Mpoints/s (forward+adjoint)",
+                               "cores": 1, "kind": "port", "sample": "pose 0 of 8, FP64 oracle, one thread",
+                               "seconds": round(dt, 3)}
+    return out
+
+
+def run_refine(api, local, n_poses=32, iterations=200):
+    """Config 4: calibration refinement from a perturbed calibration."""
+    import numpy as np
+    import torch
+    from zim_gb300 import calib_refine as CR, diff, synth
+    specs = [synth.pose_plane(seed=3, pose=p) for p in range(n_poses)]
+    rig = specs[0].rig.as_dict()
+    truth_ctx = api.Context(local)
+    truth_ctx.set_calibration(rig, True)
+    theta_true = diff.nominal(truth_ctx)
+    # start: the calibration perturbed as config 4 states; its rectified frame
+    # defines the virtual cameras, the truth is theta_true in that frame
+    pert = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in rig.items()}
+    pert["K"] = [k.copy() for k in rig["K"]]
+    pert["D"] = [d.copy() for d in rig["D"]]
+    pert["K"][0][0, 2] += 3.0
+    pert["D"][0][0] += 0.02
+    pert["t"] = rig["t"] * 1.005
+    ctx = api.Context(local)
+    ctx.set_calibration(pert, True)
+    dcfg = api.decode_config(**specs[0].decode_kwargs())
+    t_r = time.perf_counter()
+    poses = []
+    for s in specs:
+        poses += CR.decode_views(ctx, dcfg, [(s.render(0), s.render(1))], [(s.plane_n, s.plane_d)])
+    prep_s = time.perf_counter() - t_r
+    th0 = diff.nominal(ctx)
+    th, log = CR.refine(ctx, poses, th0, specs[0].pha_f, iterations=iterations)
+    names = diff.PARAM_NAMES
+    err0 = th0 - theta_true
+    err1 = th - theta_true
+    return {"poses": n_poses, "iterations": iterations, "seconds": round(log.seconds, 3),
+            "iterations_per_s": round(iterations / log.seconds, 3), "prepare_s": round(prep_s, 1),
+            "start_error": {names[k]: float(err0[k]) for k in (2, 4, 12)},
+            "final_error": {n: float(e) for n, e in zip(names, err1)},
+            "loss_start": log.losses[0] if log.losses else None, "loss_final": log.losses[-1] if log.losses else None}
 
 
 def run_reference(args):
@@ -327,6 +467,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-diff", action="store_true", help="skip the forward/adjoint leg (8 planar poses)")
+    ap.add_argument("--refine", action="store_true", help="also run calibration refinement (32 poses)")
+    ap.add_argument("--refine-poses", type=int, default=32)
+    ap.add_argument("--refine-iters", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -262,6 +262,84 @@ ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_conf
                                              int cols, int pha_f, float* xyz, uint8_t* mask,
                                              float* disp, void* stream);
 
+/* ---- differentiable sub-pixel matching + reprojection ----
+ * No counterpart in the reference (it has no gradients); the forward restates
+ * its sub-pixel refinement (JSLAB_PhaseEpipolarReconstructor_V2.cpp:985-1000)
+ * and reprojection (:414-461, rectified coordinates) on phase sampled with
+ * exact bilinear weights.  The integer decisions (fringe orders, match
+ * columns) are inputs and stay fixed; everything else is differentiated.
+ *
+ * Parameters (FP64 on the host).  Camera c (0 left, 1 right): fx, fy, cx, cy,
+ * k1, k2 of its intrinsics and distortion (p1, p2, k3 stay at the calibrated
+ * values); baseline = |t|; rot = rotation vector of a right-multiplied update
+ * of the right camera's rectifying rotation, R2 <- R2 * exp([rot]x) (an error
+ * of the relative rotation).  The rectified virtual cameras (their
+ * intrinsics, canvas and the left rectifying rotation) stay those of
+ * zim_set_calibration.  Gradient order: fx0 fy0 cx0 cy0 k1_0 k2_0 fx1 fy1 cx1
+ * cy1 k1_1 k2_1 baseline rot0 rot1 rot2. */
+#define ZIM_DIFF_NPARAMS 16
+typedef struct zim_diff_params {
+    double cam[2][6]; /* fx, fy, cx, cy, k1, k2 */
+    double baseline;
+    double rot[3];
+} zim_diff_params;
+
+/* The parameters of the calibration set by zim_set_calibration (rot = 0). */
+ZIM_API zim_status zim_diff_params_nominal(const zim_ctx* ctx, zim_diff_params* out);
+
+/* Rectifies one camera's decoded phase under `params`: bilinear sampling of
+ * 2*pi*order + residual with exact weights (a sample needs its four source
+ * taps inside the image and valid, order >= 1; else order 0), order by
+ * nearest neighbour; no post-smooth.  Feed both cameras' outputs to zim_match
+ * to fix the match columns for zim_diff_forward/backward. */
+ZIM_API zim_status zim_diff_rectify(zim_ctx* ctx, const zim_diff_params* params, int cam,
+                                    const int32_t* order, const float* residual, int rows,
+                                    int cols, int32_t* rect_base, float* rect_res,
+                                    int32_t* rect_order, void* stream);
+
+/* One view: both cameras' decoded phase (rows*cols, device), the match columns
+ * from zim_match (rect_h*rect_w, -1 = none) and a target plane: the loss of a
+ * view is sum over its points of (n . P + d)^2, P in the rectified left frame.
+ * A point enters when its four phase samples (left pixel, right columns
+ * best-1..best+1) are valid, |disparity| >= 1e-5 and z_min < Z < z_max.
+ * Optional device outputs: xyz (rect_h*rect_w*3, 0 where excluded) and mask
+ * from the forward; grad_phase[c] (rows*cols) from the backward, ACCUMULATED
+ * (+=) with FP32 atomics.  Optional input grad_xyz (rect_h*rect_w*3): an
+ * upstream gradient of the points, added to loss_weight * dLoss/dP. */
+typedef struct zim_diff_view {
+    const int32_t* order[2];
+    const float* residual[2];
+    const int32_t* best_col;
+    double plane[4];
+    float* xyz;
+    uint8_t* mask;
+    const float* grad_xyz;
+    float* grad_phase[2];
+} zim_diff_view;
+
+/* Sums over all views, reduced in FP64 in a fixed order (bit-reproducible):
+ * loss, points used, the gradient of loss_weight * loss (+ the grad_xyz
+ * terms) and J^T J of the point-to-plane distances (Gauss-Newton). */
+typedef struct zim_diff_result {
+    double loss;
+    double n_points;
+    double grad[ZIM_DIFF_NPARAMS];
+    double jtj[ZIM_DIFF_NPARAMS * ZIM_DIFF_NPARAMS];
+} zim_diff_result;
+
+/* Forward over n_views views of one rig in one launch: loss and n_points (the
+ * other result fields are zeroed), optional xyz/mask.  Synchronises `stream`. */
+ZIM_API zim_status zim_diff_forward(zim_ctx* ctx, const zim_diff_params* params,
+                                    const zim_diff_view* views, int n_views, int rows, int cols,
+                                    double z_min, double z_max, zim_diff_result* out,
+                                    void* stream);
+/* Adjoint (recomputes the forward): every field of *out, and grad_phase if
+ * requested.  Synchronises `stream`. */
+ZIM_API zim_status zim_diff_backward(zim_ctx* ctx, const zim_diff_params* params,
+                                     const zim_diff_view* views, int n_views, int rows, int cols,
+                                     double z_min, double z_max, double loss_weight,
+                                     zim_diff_result* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "libzim_oracle.so"
-SOURCES = [HERE / "zim_oracle.c", HERE / "zim_oracle.h"]
+SOURCES = [HERE / "zim_oracle.c", HERE / "zim_oracle_diff.c", HERE / "zim_oracle.h"]
 FLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=c11"]
 
 ENC_HETERODYNE3, ENC_HIERARCHICAL, ENC_GRAYCODE, ENC_GRAYCODE_COMPLEMENTARY = 0, 1, 2, 3
@@ -33,7 +33,8 @@ def build() -> Path:
     if LIB_PATH.exists() and stamp.exists() and stamp.read_text() == dig:
         return LIB_PATH
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    r = subprocess.run(["gcc", *FLAGS, str(SOURCES[0]), "-o", str(tmp), "-lm"], capture_output=True, text=True)
+    srcs = [str(s) for s in SOURCES if s.suffix == ".c"]
+    r = subprocess.run(["gcc", *FLAGS, *srcs, "-o", str(tmp), "-lm"], capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError("oracle build failed:\n" + r.stderr)
     os.replace(tmp, LIB_PATH)
@@ -284,6 +285,62 @@ def metric_gaussian(xyz, mask, sigma, eps=1e-5):
     lib().zo_metric_gaussian(_p(xyz), _p(mask), C.c_int(mask.size), C.c_double(sigma), _p(out), _p(near),
                              C.c_double(eps))
     return out, near
+
+
+class DiffGeom(C.Structure):
+    _fields_ = [("ir", (C.c_double * 9) * 2), ("dist", (C.c_double * 3) * 2), ("Q", C.c_double * 16),
+                ("baseline0", C.c_double), ("rect_w", C.c_int), ("rect_h", C.c_int), ("src_w", C.c_int),
+                ("src_h", C.c_int)]
+
+
+def diff_geom(ir, dist, Q, baseline0, rect_w, rect_h, src_w, src_h):
+    """Fixed geometry of the differentiable forward: ir[c] = (P_c[:, :3] R_c)^-1,
+    dist[c] = (p1, p2, k3), the nominal Q and baseline."""
+    g = DiffGeom()
+    for c in range(2):
+        for a in range(9):
+            g.ir[c][a] = float(np.asarray(ir[c]).ravel()[a])
+        for a in range(3):
+            g.dist[c][a] = float(dist[c][a])
+    for a in range(16):
+        g.Q[a] = float(np.asarray(Q).ravel()[a])
+    g.baseline0 = float(baseline0)
+    g.rect_w, g.rect_h, g.src_w, g.src_h = rect_w, rect_h, src_w, src_h
+    return g
+
+
+def diff_eval(geom, theta, order_l, res_l, order_r, res_r, best, plane, zmin=0.0, zmax=1e4, loss_weight=1.0,
+              want_grad=True, want_points=False, want_phase_grad=False, cells=None, cells_mode=0):
+    """FP64 loss of one view and (optionally) its analytic gradient, J^T J,
+    points and phase gradients.  cells: int32 array of rect_h*rect_w*8 for
+    cells_mode 1 (record) / 2 (reuse the recorded bilinear cells).  Returns a dict."""
+    th = _c(theta, np.float64)
+    ol, orr = _c(order_l, np.int32), _c(order_r, np.int32)
+    rl, rr = _c(res_l, np.float64), _c(res_r, np.float64)
+    bc = _c(best, np.int32)
+    pl = _c(plane, np.float64)
+    loss, npts = C.c_double(), C.c_double()
+    grad = np.zeros(16) if want_grad else None
+    jtj = np.zeros(256) if want_grad else None
+    xyz = np.zeros((geom.rect_h, geom.rect_w, 3)) if want_points else None
+    mask = np.zeros((geom.rect_h, geom.rect_w), np.uint8) if want_points else None
+    gl = np.zeros(ol.shape) if want_phase_grad else None
+    gr = np.zeros(ol.shape) if want_phase_grad else None
+    nul = C.c_void_p()
+    lib().zo_diff_eval(C.byref(geom), _p(th), _p(ol), _p(rl), _p(orr), _p(rr), _p(bc), _p(pl), C.c_double(zmin),
+                       C.c_double(zmax), C.c_double(loss_weight), C.byref(loss), C.byref(npts),
+                       _p(grad) if want_grad else nul, _p(jtj) if want_grad else nul,
+                       _p(xyz) if want_points else nul, _p(mask) if want_points else nul,
+                       _p(gl) if want_phase_grad else nul, _p(gr) if want_phase_grad else nul,
+                       _p(cells) if cells is not None else nul, C.c_int(cells_mode))
+    out = {"loss": loss.value, "n_points": npts.value}
+    if want_grad:
+        out["grad"], out["jtj"] = grad, jtj.reshape(16, 16)
+    if want_points:
+        out["xyz"], out["mask"] = xyz, mask
+    if want_phase_grad:
+        out["grad_phase"] = (gl, gr)
+    return out
 
 
 def _setup_prototypes():

@@ -135,6 +135,29 @@ int zo_sor(const float* xyz, const uint8_t* mask, int n, int k, double std_mul,
 void zo_metric_gaussian(const float* xyz, const uint8_t* mask, int n, double sigma,
                         float* out, uint8_t* near, double eps);
 
+/* Differentiable matching + reprojection (zim_oracle_diff.c).  Fixed geometry:
+ * nominal rectified-pixel -> ray matrices, p1 p2 k3 per camera, nominal Q and
+ * baseline, sizes. */
+typedef struct {
+    double ir[2][9];
+    double dist[2][3];
+    double Q[16];
+    double baseline0;
+    int rect_w, rect_h, src_w, src_h;
+} zo_diff_geom;
+
+/* Loss sum (n . P + d)^2 over the points of one view, their count, and (each
+ * optional, NULL to skip) the gradient of loss_weight * loss w.r.t. theta
+ * (zim_diff_params order), J^T J of the distances, the points / mask and the
+ * phase gradients (accumulated, +=).  cells (rect_w*rect_h*8 ints, may be
+ * NULL): cells_mode 1 records each sample's bilinear cell, 2 reuses recorded
+ * cells, so finite differences see one smooth patch per sample. */
+void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* order_l, const double* res_l,
+                  const int32_t* order_r, const double* res_r, const int32_t* best, const double plane[4],
+                  double zmin, double zmax, double loss_weight, double* loss, double* npts, double grad[16],
+                  double jtj[256], double* xyz, uint8_t* mask, double* gphase_l, double* gphase_r, int32_t* cells,
+                  int cells_mode);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,24 @@ class PointXYZ(C.Structure):
     _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("pad", C.c_float)]
 
 
+DIFF_NPARAMS = 16
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("cam", (C.c_double * 6) * 2), ("baseline", C.c_double), ("rot", C.c_double * 3)]
+
+
+class DiffView(C.Structure):
+    _fields_ = [("order", C.c_void_p * 2), ("residual", C.c_void_p * 2), ("best_col", C.c_void_p),
+                ("plane", C.c_double * 4), ("xyz", C.c_void_p), ("mask", C.c_void_p), ("grad_xyz", C.c_void_p),
+                ("grad_phase", C.c_void_p * 2)]
+
+
+class DiffResult(C.Structure):
+    _fields_ = [("loss", C.c_double), ("n_points", C.c_double), ("grad", C.c_double * DIFF_NPARAMS),
+                ("jtj", C.c_double * (DIFF_NPARAMS * DIFF_NPARAMS))]
+
+
 V = C.c_void_p
 I = C.c_int
 D = C.c_double
@@ -87,6 +105,10 @@ PROTOTYPES = {
     "zim_compact_points_noalloc": (I, [V, V, I, I, V, V, V]),
     "zim_reconstruct_pair": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
     "zim_reconstruct_pair_host": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
+    "zim_diff_params_nominal": (I, [V, V]),
+    "zim_diff_rectify": (I, [V, V, I, V, V, I, I, V, V, V, V]),
+    "zim_diff_forward": (I, [V, V, V, I, I, I, D, D, V, V]),
+    "zim_diff_backward": (I, [V, V, V, I, I, I, D, D, D, V, V]),
 }
 
 _lib = None

@@ -361,6 +361,7 @@ extern "C" ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo
         M3 iR = inverse(mul(A, R));
         MapParams p;
         std::memcpy(p.ir, iR.a, sizeof p.ir);
+        std::memcpy(ctx->ir[k], iR.a, sizeof ctx->ir[k]);
         const double* K = c->camera_matrix[k];
         const double* D = c->dist_coeffs[k];
         p.fx = K[0]; p.fy = K[4]; p.u0 = K[2]; p.v0 = K[5];

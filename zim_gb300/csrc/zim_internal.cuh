@@ -27,6 +27,7 @@ struct zim_ctx {
     bool calibrated = false;
     zim_stereo_calib calib{};
     double R1[9], R2[9], P1[12], P2[12], Q[16];
+    double ir[2][9];  // (P_c[:, :3] R_c)^-1: rectified pixel -> camera ray
     int src_w = 0, src_h = 0, rect_w = 0, rect_h = 0;
     float* d_map[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
 
