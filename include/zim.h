@@ -262,6 +262,61 @@ ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_conf
                                              int cols, int pha_f, float* xyz, uint8_t* mask,
                                              float* disp, void* stream);
 
+/* ---- batched path: many stereo pairs of uneven size and encoding ----
+ * No counterpart in the reference (it reconstructs one pair per call through
+ * JSLAB_PhaseEpipolarReconstructor_V2 / JSLAB_ReconstructPipeline_GPU).  One
+ * submission holds any number of pairs, each with its own decode config,
+ * sample type and one of the batch's calibrations.  Per pair it computes what
+ * zim_reconstruct_pair computes (bit-identical), for the pixel-domain stages:
+ * decode, rectify, match, 5x5 median, reprojection, 3x3 Gaussian and radius
+ * outlier filter.  The grid filters (SOR, MLS, metric Gaussian) work on whole
+ * clouds and run per pair afterwards (zim_filter_*).
+ * Execution: one persistent kernel per stage drains a device work queue of
+ * (pair, row band) items over all pairs (decode; rectify fused into match;
+ * median + reprojection; each pixel filter); the launch sequence is captured
+ * once as a CUDA graph and zim_batch_run replays it.  Band heights and
+ * persistent CTAs per SM are tunables, chosen by zim_batch_autotune. */
+typedef struct zim_batch zim_batch;
+
+typedef struct zim_batch_pair {
+    zim_decode_config decode;
+    int sample_type;         /* ZIM_SAMPLE_U8 / ZIM_SAMPLE_U16 */
+    int rows, cols;          /* camera image size: must equal its calibration's */
+    int calib;               /* index into the batch's calibrations */
+    int pha_f;               /* <= 0: zim_decode_max_order(&decode) */
+    const void* frames[2];   /* device frame stacks, left and right */
+    float* xyz;              /* device outputs, rect_h*rect_w of the calibration */
+    uint8_t* mask;
+    float* disp;             /* optional: the (median-filtered) disparity */
+} zim_batch_pair;
+
+typedef struct zim_batch_tuning {
+    int decode_rows;   /* 8-pixel tile rows per decode work item */
+    int match_rows;    /* rectified rows per rectify+match work item */
+    int filter_rows;   /* 8-pixel tile rows per median/filter work item */
+    int ctas_per_sm;   /* persistent CTAs per SM (capped by occupancy) */
+} zim_batch_tuning;
+
+/* Rectification of every calibration (as zim_set_calibration) into a batch
+ * bound to ctx's device. */
+ZIM_API zim_status zim_batch_create(zim_ctx* ctx, const zim_stereo_calib* calibs, int n_calibs,
+                                    int use_full_left_rectification, zim_batch** out);
+ZIM_API void zim_batch_destroy(zim_batch* batch);
+ZIM_API zim_status zim_batch_rect_size(const zim_batch* batch, int calib, int* rect_w, int* rect_h);
+/* Validates the pairs, allocates the intermediates, builds the work queues
+ * and captures the CUDA graph.  rcfg: zim_recon_config with use_sor, use_mls
+ * and use_metric_gaussian 0.  tuning NULL: the last autotuned (else default)
+ * tuning.  Replaces any previous submission; synchronises the device. */
+ZIM_API zim_status zim_batch_submit(zim_batch* batch, const zim_batch_pair* pairs, int n_pairs,
+                                    const zim_recon_config* rcfg, const zim_batch_tuning* tuning);
+/* Replays the submitted batch on `stream` (asynchronous). */
+ZIM_API zim_status zim_batch_run(zim_batch* batch, void* stream);
+/* Times candidate tunings on the submitted batch (each run several times),
+ * resubmits with the fastest and returns it and its time per run. */
+ZIM_API zim_status zim_batch_autotune(zim_batch* batch, void* stream, zim_batch_tuning* best,
+                                      double* best_ms);
+ZIM_API zim_status zim_batch_get_tuning(const zim_batch* batch, zim_batch_tuning* out);
+
 /* ---- differentiable sub-pixel matching + reprojection ----
  * No counterpart in the reference (it has no gradients); the forward restates
  * its sub-pixel refinement (JSLAB_PhaseEpipolarReconstructor_V2.cpp:985-1000)

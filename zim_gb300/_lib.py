@@ -50,6 +50,17 @@ class PointXYZ(C.Structure):
     _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("pad", C.c_float)]
 
 
+class BatchPair(C.Structure):
+    _fields_ = [("decode", DecodeConfig), ("sample_type", C.c_int), ("rows", C.c_int), ("cols", C.c_int),
+                ("calib", C.c_int), ("pha_f", C.c_int), ("frames", C.c_void_p * 2), ("xyz", C.c_void_p),
+                ("mask", C.c_void_p), ("disp", C.c_void_p)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("decode_rows", C.c_int), ("match_rows", C.c_int), ("filter_rows", C.c_int),
+                ("ctas_per_sm", C.c_int)]
+
+
 DIFF_NPARAMS = 16
 
 
@@ -105,6 +116,13 @@ PROTOTYPES = {
     "zim_compact_points_noalloc": (I, [V, V, I, I, V, V, V]),
     "zim_reconstruct_pair": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
     "zim_reconstruct_pair_host": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
+    "zim_batch_create": (I, [V, V, I, I, V]),
+    "zim_batch_destroy": (None, [V]),
+    "zim_batch_rect_size": (I, [V, I, V, V]),
+    "zim_batch_submit": (I, [V, V, I, V, V]),
+    "zim_batch_run": (I, [V, V]),
+    "zim_batch_autotune": (I, [V, V, V, V]),
+    "zim_batch_get_tuning": (I, [V, V]),
     "zim_diff_params_nominal": (I, [V, V]),
     "zim_diff_rectify": (I, [V, V, I, V, V, I, I, V, V, V, V]),
     "zim_diff_forward": (I, [V, V, V, I, I, I, D, D, V, V]),

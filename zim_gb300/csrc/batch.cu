@@ -1,0 +1,597 @@
+// batch.cu -- the batched path: many stereo pairs of uneven size, encoding and
+// calibration through persistent per-stage kernels that drain device work
+// queues, captured once as a CUDA graph.
+//
+// No counterpart in the reference (one pair per call:
+// PhaseShiftGrayCode3D/src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:397-480,
+// JSLAB_PhaseEpipolarReconstructor_V2_GPU.cu:352-480).  Per pair the stages
+// compute exactly what zim_reconstruct_pair computes (the same device code,
+// zim_tiles.cuh); what changes is the schedule:
+//   stage 1  decode:          item = (pair, camera, band of 8-row tile rows)
+//   stage 2  rectify + match: item = (pair, band of rectified rows); the right
+//            row is rectified straight into shared memory and each left pixel
+//            is rectified in registers, so no rectified phase reaches HBM
+//   stage 3  median + reprojection, stage 4 pixel Gaussian, stage 5 radius
+//            outlier filter: item = (pair, band of 8-row tile rows)
+// A persistent CTA takes items from its stage's queue (one atomic per item)
+// until the queue is empty, so small and large pairs share the GPU and no
+// per-pair launch or tail is paid.  Items are ordered largest pair first.
+// Stage order is kept by kernel boundaries (no inter-CTA waits).
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "zim_tiles.cuh"
+
+namespace {
+
+constexpr int BT = 256;  // threads per persistent CTA (one 32 x 8 tile)
+static_assert(BT == zt::DX * zt::DY && BT == zt::RX * zt::RY, "tile shape");
+
+enum { Q_DECODE, Q_MATCH, Q_REPROJ, Q_PXG, Q_ROR, NQ };
+
+struct PairDev {
+    zt::DecodeParams dp;
+    zt::ReprojParams rp;
+    int sample_type;
+    const void* frames[2];
+    const float* map[2][2];
+    int rows, cols, rw, rh;
+    int post_smooth, pha_f;
+    float grad_threshold;
+    int32_t* order[2];
+    float* res[2];
+    float* disp_raw;
+    float* disp_out;
+    float* x_rep;  // reprojection output
+    uint8_t* m_rep;
+    float* x_pxg;  // pixel Gaussian output (mask written only if it updates the mask)
+    uint8_t* m_pxg;
+    const float* x_ror_in;
+    const uint8_t* m_ror_in;
+    float* x_ror;
+    uint8_t* m_ror;
+    float pxg_w00, pxg_w01, pxg_w11;
+    float ror_r2;
+    int ror_min_nb, ror_hw;
+};
+
+struct Queues {
+    const int4* items[NQ];
+    int n[NQ];
+};
+
+// One item index per CTA: thread 0 takes it, everyone reads it.  The caller's
+// trailing __syncthreads keeps the next write behind every read.
+__device__ __forceinline__ int next_item(unsigned* counter, int* s_item) {
+    if (threadIdx.x == 0) *s_item = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    return *s_item;
+}
+
+__global__ void __launch_bounds__(BT) batch_decode_kernel(const PairDev* __restrict__ pairs, const int4* __restrict__ items,
+                                                          int n_items, unsigned* __restrict__ counter) {
+    __shared__ zt::DecodeSmem sm;
+    __shared__ zt::DecodeParams dp;
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];  // pair, camera, first tile row, tile rows
+        const PairDev& P = pairs[w.x];
+        {
+            const int* src = reinterpret_cast<const int*>(&P.dp);
+            int* dst = reinterpret_cast<int*>(&dp);
+            for (int k = tid; k < (int)(sizeof(zt::DecodeParams) / 4); k += BT) dst[k] = __ldg(src + k);
+        }
+        __syncthreads();
+        const int tiles_x = (P.cols + zt::DX - 1) / zt::DX;
+        const void* fr = P.frames[w.y];
+        int32_t* ord = P.order[w.y];
+        float* res = P.res[w.y];
+        for (int ty = w.z; ty < w.z + w.w; ty++)
+            for (int tx = 0; tx < tiles_x; tx++) {
+                if (P.sample_type == ZIM_SAMPLE_U8)
+                    zt::decode_tile<uint8_t>((const uint8_t*)fr, dp, tx, ty, tid, sm, ord, res, nullptr, nullptr);
+                else
+                    zt::decode_tile<uint16_t>((const uint16_t*)fr, dp, tx, ty, tid, sm, ord, res, nullptr, nullptr);
+            }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restrict__ pairs, const int4* __restrict__ items,
+                                                         int n_items, unsigned* __restrict__ counter, int max_cols) {
+    extern __shared__ int4 smem_raw[];
+    int* s_ord = reinterpret_cast<int*>(smem_raw);
+    int* s_base = s_ord + max_cols;
+    float* s_res = reinterpret_cast<float*>(s_base + max_cols);
+    int* s_lo = reinterpret_cast<int*>(s_res + max_cols);
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];  // pair, first rectified row, rows
+        const PairDev& P = pairs[w.x];
+        const int cols = P.rw, pha_f = P.pha_f;
+        int* s_hi = s_lo + (pha_f + 1);
+        for (int row = w.y; row < w.y + w.z; row++) {
+            const size_t ro = (size_t)row * cols;
+            for (int k = tid; k <= pha_f; k += BT) {
+                s_lo[k] = INT_MAX;
+                s_hi[k] = -1;
+            }
+            for (int j = tid; j < cols; j += BT) {
+                int32_t b, o;
+                float r;
+                zt::rectify_pixel(P.order[1], P.res[1], P.rows, P.cols, __ldg(P.map[1][0] + ro + j),
+                                  __ldg(P.map[1][1] + ro + j), P.post_smooth, b, r, o);
+                s_ord[j] = o;
+                s_base[j] = b;
+                s_res[j] = r;
+            }
+            __syncthreads();
+            zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, tid, BT);
+            __syncthreads();
+            for (int j = tid; j < cols; j += BT) {
+                int32_t bL, kL;
+                float rL;
+                zt::rectify_pixel(P.order[0], P.res[0], P.rows, P.cols, __ldg(P.map[0][0] + ro + j),
+                                  __ldg(P.map[0][1] + ro + j), P.post_smooth, bL, rL, kL);
+                float d;
+                int best;
+                zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, cols, pha_f, P.grad_threshold, d,
+                                best);
+                P.disp_raw[ro + j] = d;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BT) batch_reproject_kernel(const PairDev* __restrict__ pairs,
+                                                             const int4* __restrict__ items, int n_items,
+                                                             unsigned* __restrict__ counter) {
+    __shared__ zt::MedianSmem sm;
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];  // pair, first tile row, tile rows
+        const PairDev& P = pairs[w.x];
+        const int tiles_x = (P.rw + zt::RX - 1) / zt::RX;
+        for (int ty = w.y; ty < w.y + w.z; ty++)
+            for (int tx = 0; tx < tiles_x; tx++)
+                zt::median_reproject_tile(P.disp_raw, P.rh, P.rw, P.rp, tx, ty, tid, sm, P.disp_out, P.x_rep, P.m_rep);
+        __syncthreads();
+    }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(BT) batch_filter_kernel(const PairDev* __restrict__ pairs,
+                                                          const int4* __restrict__ items, int n_items,
+                                                          unsigned* __restrict__ counter) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];
+        const PairDev& P = pairs[w.x];
+        const int tiles_x = (P.rw + zt::RX - 1) / zt::RX;
+        for (int ty = w.y; ty < w.y + w.z; ty++)
+            for (int tx = 0; tx < tiles_x; tx++) {
+                const int x = tx * zt::RX + tid % zt::RX, y = ty * zt::RY + tid / zt::RX;
+                if (x >= P.rw || y >= P.rh) continue;
+                if (STAGE == Q_PXG)
+                    zt::px_gaussian_pixel(P.x_rep, P.m_rep, P.rh, P.rw, x, y, P.pxg_w00, P.pxg_w01, P.pxg_w11, P.x_pxg,
+                                          P.m_pxg);
+                else
+                    zt::ror_pixel(P.x_ror_in, P.m_ror_in, P.rh, P.rw, x, y, P.ror_r2, P.ror_min_nb, P.ror_hw, P.x_ror,
+                                  P.m_ror);
+            }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+struct zim_batch {
+    zim_ctx* ctx = nullptr;
+    std::vector<zim_rect_state> calibs;
+    std::vector<zim_batch_pair> pairs;
+    zim_recon_config rcfg{};
+    bool use_pxg = false, use_ror = false;
+    zim_batch_tuning tuning{4, 4, 4, 4};
+    bool tuned = false;
+    // device state of the submission
+    void* d_mem = nullptr;  // intermediates + descriptors + queues, one allocation
+    size_t d_bytes = 0;
+    PairDev* d_pairs = nullptr;
+    unsigned* d_counters = nullptr;
+    Queues q{};
+    int max_cols = 0, max_pha_f = 0;
+    size_t match_smem = 0;
+    int grid[NQ] = {0, 0, 0, 0, 0};
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    // host layout of the intermediates (for resubmission with another tuning)
+    std::vector<PairDev> host_pairs;
+    size_t items_off = 0;
+};
+
+namespace {
+
+void release_submission(zim_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    cudaFree(b->d_mem);
+    b->d_mem = nullptr;
+    b->d_bytes = 0;
+}
+
+int occupancy(const void* fn, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BT, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+// Builds the work items for a tuning (largest pair first) into host vectors.
+void build_items(const zim_batch* b, const zim_batch_tuning& t, std::vector<int4> (&items)[NQ]) {
+    std::vector<int> order(b->pairs.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return (size_t)b->pairs[a].rows * b->pairs[a].cols > (size_t)b->pairs[c].rows * b->pairs[c].cols;
+    });
+    for (int q = 0; q < NQ; q++) items[q].clear();
+    for (int pi : order) {
+        const zim_batch_pair& p = b->pairs[pi];
+        const zim_rect_state& C = b->calibs[p.calib];
+        const int trows = (p.rows + zt::DY - 1) / zt::DY;
+        for (int cam = 0; cam < 2; cam++)
+            for (int r = 0; r < trows; r += t.decode_rows)
+                items[Q_DECODE].push_back(make_int4(pi, cam, r, std::min(t.decode_rows, trows - r)));
+        for (int r = 0; r < C.rect_h; r += t.match_rows)
+            items[Q_MATCH].push_back(make_int4(pi, r, std::min(t.match_rows, C.rect_h - r), 0));
+        const int rtrows = (C.rect_h + zt::RY - 1) / zt::RY;
+        for (int r = 0; r < rtrows; r += t.filter_rows) {
+            const int4 it = make_int4(pi, r, std::min(t.filter_rows, rtrows - r), 0);
+            items[Q_REPROJ].push_back(it);
+            if (b->use_pxg) items[Q_PXG].push_back(it);
+            if (b->use_ror) items[Q_ROR].push_back(it);
+        }
+    }
+}
+
+zim_status capture(zim_batch* b) {
+    zim_ctx* ctx = b->ctx;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 152;
+    const int want = std::max(1, b->tuning.ctas_per_sm);
+    b->grid[Q_DECODE] = sms * std::min(want, occupancy((const void*)batch_decode_kernel, 0));
+    b->grid[Q_MATCH] = sms * std::min(want, occupancy((const void*)batch_match_kernel, b->match_smem));
+    b->grid[Q_REPROJ] = sms * std::min(want, occupancy((const void*)batch_reproject_kernel, 0));
+    b->grid[Q_PXG] = sms * std::min(want, occupancy((const void*)batch_filter_kernel<Q_PXG>, 0));
+    b->grid[Q_ROR] = sms * std::min(want, occupancy((const void*)batch_filter_kernel<Q_ROR>, 0));
+    cudaStream_t s = b->cap_stream;
+    ZIM_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(b->d_counters, 0, NQ * sizeof(unsigned), s);
+    const Queues& q = b->q;
+    if (q.n[Q_DECODE])
+        batch_decode_kernel<<<std::min(b->grid[Q_DECODE], q.n[Q_DECODE]), BT, 0, s>>>(
+            b->d_pairs, q.items[Q_DECODE], q.n[Q_DECODE], b->d_counters + Q_DECODE);
+    if (q.n[Q_MATCH])
+        batch_match_kernel<<<std::min(b->grid[Q_MATCH], q.n[Q_MATCH]), BT, b->match_smem, s>>>(
+            b->d_pairs, q.items[Q_MATCH], q.n[Q_MATCH], b->d_counters + Q_MATCH, b->max_cols);
+    if (q.n[Q_REPROJ])
+        batch_reproject_kernel<<<std::min(b->grid[Q_REPROJ], q.n[Q_REPROJ]), BT, 0, s>>>(
+            b->d_pairs, q.items[Q_REPROJ], q.n[Q_REPROJ], b->d_counters + Q_REPROJ);
+    if (q.n[Q_PXG])
+        batch_filter_kernel<Q_PXG><<<std::min(b->grid[Q_PXG], q.n[Q_PXG]), BT, 0, s>>>(
+            b->d_pairs, q.items[Q_PXG], q.n[Q_PXG], b->d_counters + Q_PXG);
+    if (q.n[Q_ROR])
+        batch_filter_kernel<Q_ROR><<<std::min(b->grid[Q_ROR], q.n[Q_ROR]), BT, 0, s>>>(
+            b->d_pairs, q.items[Q_ROR], q.n[Q_ROR], b->d_counters + Q_ROR);
+    cudaError_t le = cudaGetLastError();
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return zim_fail(ctx, ZIM_ERR_CUDA, "batch graph capture failed: %s",
+                        cudaGetErrorString(le != cudaSuccess ? le : e));
+    }
+    b->graph = g;
+    ZIM_CUDA_TRY(ctx, cudaGraphInstantiate(&b->exec, g, 0));
+    return ZIM_OK;
+}
+
+// Rebuilds the work queues for b->tuning (same pairs, same buffers) and recaptures.
+zim_status requeue(zim_batch* b) {
+    zim_ctx* ctx = b->ctx;
+    std::vector<int4> items[NQ];
+    build_items(b, b->tuning, items);
+    size_t need = 0;
+    for (int q = 0; q < NQ; q++) need += zim_align256(items[q].size() * sizeof(int4) + 16);
+    if (b->items_off + need > b->d_bytes) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "batch item space");
+    char* base = (char*)b->d_mem + b->items_off;
+    ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    for (int q = 0; q < NQ; q++) {
+        if (!items[q].empty())
+            ZIM_CUDA_TRY(ctx, cudaMemcpy(base, items[q].data(), items[q].size() * sizeof(int4), cudaMemcpyHostToDevice));
+        b->q.items[q] = (const int4*)base;
+        b->q.n[q] = (int)items[q].size();
+        base += zim_align256(items[q].size() * sizeof(int4) + 16);
+    }
+    return capture(b);
+}
+
+// Upper bound of the item space over the tunings the autotuner tries (1-row bands).
+size_t max_item_bytes(const zim_batch* b) {
+    size_t n[NQ] = {0, 0, 0, 0, 0};
+    for (const zim_batch_pair& p : b->pairs) {
+        const zim_rect_state& C = b->calibs[p.calib];
+        n[Q_DECODE] += 2 * (size_t)((p.rows + zt::DY - 1) / zt::DY);
+        n[Q_MATCH] += (size_t)C.rect_h;
+        const size_t rt = (C.rect_h + zt::RY - 1) / zt::RY;
+        n[Q_REPROJ] += rt;
+        n[Q_PXG] += rt;
+        n[Q_ROR] += rt;
+    }
+    size_t s = 0;
+    for (int q = 0; q < NQ; q++) s += zim_align256(n[q] * sizeof(int4) + 16);
+    return s;
+}
+
+bool tuning_ok(const zim_batch_tuning& t) {
+    return t.decode_rows >= 1 && t.decode_rows <= 1024 && t.match_rows >= 1 && t.match_rows <= 1024 &&
+           t.filter_rows >= 1 && t.filter_rows <= 1024 && t.ctas_per_sm >= 1 && t.ctas_per_sm <= 32;
+}
+
+}  // namespace
+
+extern "C" ZIM_API zim_status zim_batch_create(zim_ctx* ctx, const zim_stereo_calib* calibs, int n_calibs,
+                                               int use_full_left, zim_batch** out) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    if (!calibs || n_calibs < 1 || !out) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad argument");
+    *out = nullptr;
+    zim_batch* b = new zim_batch;
+    b->ctx = ctx;
+    for (int i = 0; i < n_calibs; i++) {
+        zim_rect_state st;
+        zim_status s = zim_rect_build(ctx, &calibs[i], use_full_left, st);
+        if (s) {
+            zim_batch_destroy(b);
+            return s;
+        }
+        b->calibs.push_back(st);
+    }
+    if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        zim_batch_destroy(b);
+        return zim_fail(ctx, ZIM_ERR_CUDA, "stream creation failed");
+    }
+    *out = b;
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API void zim_batch_destroy(zim_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    cudaDeviceSynchronize();
+    release_submission(b);
+    for (zim_rect_state& st : b->calibs) zim_rect_free(st);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    delete b;
+}
+
+extern "C" ZIM_API zim_status zim_batch_rect_size(const zim_batch* b, int calib, int* rw, int* rh) {
+    if (!b || calib < 0 || calib >= (int)b->calibs.size()) return ZIM_ERR_INVALID_ARG;
+    if (rw) *rw = b->calibs[calib].rect_w;
+    if (rh) *rh = b->calibs[calib].rect_h;
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pair* pairs, int n_pairs,
+                                               const zim_recon_config* rcfg, const zim_batch_tuning* tuning) {
+    if (!b) return ZIM_ERR_INVALID_ARG;
+    zim_ctx* ctx = b->ctx;
+    if (!pairs || n_pairs < 1 || !rcfg) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad argument");
+    if (rcfg->use_sor || rcfg->use_mls || rcfg->use_metric_gaussian)
+        return zim_fail(ctx, ZIM_ERR_UNSUPPORTED,
+                        "the batch runs the pixel-domain stages; run SOR / MLS / metric Gaussian per cloud after it");
+    if (rcfg->use_ror && (rcfg->radius_window_size < 0 || rcfg->radius_window_size > 64))
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, 64]");
+    if (tuning && !tuning_ok(*tuning)) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad tuning");
+    int max_cols = 1, max_pha = 0;
+    for (int i = 0; i < n_pairs; i++) {
+        const zim_batch_pair& p = pairs[i];
+        if (p.calib < 0 || p.calib >= (int)b->calibs.size())
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: bad calibration index", i);
+        const zim_rect_state& C = b->calibs[p.calib];
+        if (p.rows != C.src_h || p.cols != C.src_w)
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: image %dx%d differs from its calibration's %dx%d", i,
+                            p.cols, p.rows, C.src_w, C.src_h);
+        zim_status s = zim_decode_validate(&p.decode);
+        if (s) return zim_fail(ctx, s, "pair %d: invalid decode config", i);
+        if (p.sample_type != ZIM_SAMPLE_U8 && p.sample_type != ZIM_SAMPLE_U16)
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: bad sample type", i);
+        if (!p.frames[0] || !p.frames[1] || !p.xyz || !p.mask)
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: null frames or outputs", i);
+        if (C.rect_w > ZIM_MAX_MATCH_COLS) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: rectified width", i);
+        const int pf = p.pha_f > 0 ? p.pha_f : zim_decode_max_order(&p.decode);
+        if (pf < 0 || pf > ZIM_MAX_ORDER) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: pha_f out of range", i);
+        max_cols = std::max(max_cols, C.rect_w);
+        max_pha = std::max(max_pha, pf);
+    }
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    release_submission(b);
+    b->pairs.assign(pairs, pairs + n_pairs);
+    b->rcfg = *rcfg;
+    b->use_pxg = rcfg->use_px_gaussian != 0;
+    b->use_ror = rcfg->use_ror != 0;
+    if (tuning) b->tuning = *tuning;
+    b->max_cols = max_cols;
+    b->max_pha_f = max_pha;
+    b->match_smem = (size_t)max_cols * 12 + (size_t)(max_pha + 1) * 8;
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(batch_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)b->match_smem));
+
+    // memory plan: descriptors, counters, per-pair intermediates, items
+    const bool pxg_mask = b->use_pxg && rcfg->px_gaussian_updates_mask;
+    size_t bytes = zim_align256(sizeof(PairDev) * n_pairs) + 256;
+    for (const zim_batch_pair& p : b->pairs) {
+        const zim_rect_state& C = b->calibs[p.calib];
+        const size_t src = (size_t)p.rows * p.cols, dst = (size_t)C.rect_w * C.rect_h;
+        bytes += 2 * (zim_align256(src * 4) * 2) + zim_align256(dst * 4);
+        bytes += 2 * (zim_align256(dst * 12) + zim_align256(dst));  // two intermediate clouds at most
+    }
+    b->items_off = bytes;
+    bytes += max_item_bytes(b) + 4096;
+    if (cudaMalloc(&b->d_mem, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "batch allocation of %zu bytes failed", bytes);
+    }
+    b->d_bytes = bytes;
+    char* cur = (char*)b->d_mem;
+    auto take = [&](size_t n) {
+        char* p = cur;
+        cur += zim_align256(n);
+        return (void*)p;
+    };
+    b->d_pairs = (PairDev*)take(sizeof(PairDev) * n_pairs);
+    b->d_counters = (unsigned*)take(NQ * sizeof(unsigned));
+    float w00, w01, w11;
+    zt::px_gaussian_weights(w00, w01, w11);
+    b->host_pairs.assign(n_pairs, PairDev{});
+    for (int i = 0; i < n_pairs; i++) {
+        const zim_batch_pair& p = b->pairs[i];
+        const zim_rect_state& C = b->calibs[p.calib];
+        PairDev& D = b->host_pairs[i];
+        std::memset(&D, 0, sizeof D);
+        zt::decode_params(&p.decode, p.rows, p.cols, D.dp);
+        zt::reproj_params(C.Q, C.R1, rcfg, D.rp);
+        D.sample_type = p.sample_type;
+        D.rows = p.rows; D.cols = p.cols; D.rw = C.rect_w; D.rh = C.rect_h;
+        D.post_smooth = p.decode.post_smooth;
+        D.pha_f = p.pha_f > 0 ? p.pha_f : zim_decode_max_order(&p.decode);
+        D.grad_threshold = (float)rcfg->grad_threshold;
+        const size_t src = (size_t)p.rows * p.cols, dst = (size_t)C.rect_w * C.rect_h;
+        for (int c = 0; c < 2; c++) {
+            D.frames[c] = p.frames[c];
+            D.map[c][0] = C.d_map[c][0];
+            D.map[c][1] = C.d_map[c][1];
+            D.order[c] = (int32_t*)take(src * 4);
+            D.res[c] = (float*)take(src * 4);
+        }
+        D.disp_raw = (float*)take(dst * 4);
+        D.disp_out = p.disp;
+        // stage routing: the last writer of xyz / mask writes the caller's buffers
+        float* xbuf[2] = {(float*)take(dst * 12), (float*)take(dst * 12)};
+        uint8_t* mbuf[2] = {(uint8_t*)take(dst), (uint8_t*)take(dst)};
+        const bool last_rep = !b->use_pxg && !b->use_ror;
+        D.x_rep = last_rep ? p.xyz : xbuf[0];
+        D.m_rep = (!pxg_mask && !b->use_ror) ? p.mask : mbuf[0];
+        if (b->use_pxg) {
+            D.x_pxg = b->use_ror ? xbuf[1] : p.xyz;
+            D.m_pxg = pxg_mask ? (b->use_ror ? mbuf[1] : p.mask) : nullptr;
+            D.pxg_w00 = w00; D.pxg_w01 = w01; D.pxg_w11 = w11;
+        }
+        if (b->use_ror) {
+            D.x_ror_in = b->use_pxg ? D.x_pxg : D.x_rep;
+            D.m_ror_in = pxg_mask ? D.m_pxg : D.m_rep;
+            D.x_ror = p.xyz;
+            D.m_ror = p.mask;
+            D.ror_r2 = rcfg->radius_search * rcfg->radius_search;
+            D.ror_min_nb = rcfg->radius_min_neighbors;
+            D.ror_hw = rcfg->radius_window_size / 2;
+        }
+    }
+    if ((size_t)(cur - (char*)b->d_mem) > b->items_off)
+        return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "batch memory plan overflow");
+    b->items_off = (size_t)(cur - (char*)b->d_mem);
+    ZIM_CUDA_TRY(ctx, cudaMemcpy(b->d_pairs, b->host_pairs.data(), sizeof(PairDev) * n_pairs, cudaMemcpyHostToDevice));
+    return requeue(b);
+}
+
+extern "C" ZIM_API zim_status zim_batch_run(zim_batch* b, void* stream) {
+    if (!b) return ZIM_ERR_INVALID_ARG;
+    if (!b->exec) return zim_fail(b->ctx, ZIM_ERR_INVALID_ARG, "nothing submitted");
+    ZIM_CUDA_TRY(b->ctx, cudaGraphLaunch(b->exec, zim_stream(stream)));
+    for (int q = 0; q < NQ; q++) b->ctx->launches += b->q.n[q] > 0 ? 1 : 0;  // kernels in the graph
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_batch_get_tuning(const zim_batch* b, zim_batch_tuning* out) {
+    if (!b || !out) return ZIM_ERR_INVALID_ARG;
+    *out = b->tuning;
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_batch_autotune(zim_batch* b, void* stream, zim_batch_tuning* best, double* best_ms) {
+    if (!b) return ZIM_ERR_INVALID_ARG;
+    zim_ctx* ctx = b->ctx;
+    if (!b->exec) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "nothing submitted");
+    cudaStream_t st = zim_stream(stream);
+    cudaEvent_t e0, e1;
+    ZIM_CUDA_TRY(ctx, cudaEventCreate(&e0));
+    ZIM_CUDA_TRY(ctx, cudaEventCreate(&e1));
+    auto time_it = [&](double& ms) -> zim_status {
+        zim_status s = requeue(b);
+        if (s) return s;
+        ZIM_CUDA_TRY(ctx, cudaGraphLaunch(b->exec, st));  // warm-up
+        ZIM_CUDA_TRY(ctx, cudaEventRecord(e0, st));
+        const int reps = 3;
+        for (int r = 0; r < reps; r++) ZIM_CUDA_TRY(ctx, cudaGraphLaunch(b->exec, st));
+        ZIM_CUDA_TRY(ctx, cudaEventRecord(e1, st));
+        ZIM_CUDA_TRY(ctx, cudaEventSynchronize(e1));
+        float f = 0.f;
+        ZIM_CUDA_TRY(ctx, cudaEventElapsedTime(&f, e0, e1));
+        ms = f / reps;
+        return ZIM_OK;
+    };
+    // coordinate descent over the four tunables from the current tuning
+    zim_batch_tuning cur = b->tuning;
+    double cur_ms = 0;
+    b->tuning = cur;
+    zim_status s = time_it(cur_ms);
+    const int cand[4][5] = {{1, 2, 4, 8, 16}, {1, 2, 4, 8, 16}, {1, 2, 4, 8, 16}, {1, 2, 4, 8, 16}};
+    for (int pass = 0; pass < 2 && !s; pass++)
+        for (int k = 0; k < 4 && !s; k++)
+            for (int c = 0; c < 5 && !s; c++) {
+                zim_batch_tuning t = cur;
+                int* f = k == 0 ? &t.decode_rows : k == 1 ? &t.match_rows : k == 2 ? &t.filter_rows : &t.ctas_per_sm;
+                if (*f == cand[k][c]) continue;
+                *f = cand[k][c];
+                b->tuning = t;
+                double ms = 0;
+                s = time_it(ms);
+                if (!s && ms < cur_ms) {
+                    cur = t;
+                    cur_ms = ms;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->tuning = cur;
+    zim_status s2 = requeue(b);
+    if (s) return s;
+    if (s2) return s2;
+    b->tuned = true;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return ZIM_OK;
+}

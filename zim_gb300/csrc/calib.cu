@@ -10,7 +10,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "zim_internal.cuh"
+#include "zim_tiles.cuh"
 
 namespace {
 
@@ -250,40 +250,7 @@ __global__ void map_kernel(MapParams p, int w, int h, float* __restrict__ mx, fl
     my[(size_t)i * w + j] = (float)v;
 }
 
-// Post-smoothed phase at a source pixel in exact integer + FP32 form:
-// phase_s = 2*pi*K16/16 + R, K16 = sum (1 2 1)x(1 2 1) * order (BORDER_REPLICATE).
-__device__ __forceinline__ void smoothed_tap(const int32_t* __restrict__ order, const float* __restrict__ res,
-                                             int x, int y, int rows, int cols, int post_smooth, int& K16,
-                                             float& R) {
-    if (!post_smooth) {
-        size_t o = (size_t)y * cols + x;
-        K16 = 16 * __ldg(order + o);
-        R = __ldg(res + o);
-        return;
-    }
-    int k = 0;
-    float r = 0.f;
-#pragma unroll
-    for (int a = -1; a <= 1; a++) {
-        int yy = min(max(y + a, 0), rows - 1);
-        int ca = a == 0 ? 2 : 1;
-#pragma unroll
-        for (int b = -1; b <= 1; b++) {
-            int xx = min(max(x + b, 0), cols - 1);
-            int cw = ca * (b == 0 ? 2 : 1);
-            size_t o = (size_t)yy * cols + xx;
-            k += cw * __ldg(order + o);
-            r = fmaf((float)cw * 0.0625f, __ldg(res + o), r);
-        }
-    }
-    K16 = k;
-    R = r;
-}
-
-// setData remap of one camera: INTER_LINEAR of the (post-smoothed) phase with
-// OpenCV's 1/32-pixel quantised weights and BORDER_CONSTANT 0, INTER_NEAREST of
-// the order.  The phase is kept as an integer cycle count (exact: every weight
-// is a multiple of 1/16384) plus an FP32 residual.
+// setData remap of one camera (zt::rectify_pixel per rectified pixel).
 __global__ void rectify_kernel(const int32_t* __restrict__ order, const float* __restrict__ res, int srows,
                                int scols, const float* __restrict__ mapx, const float* __restrict__ mapy, int drows,
                                int dcols, int post_smooth, int32_t* __restrict__ rbase, float* __restrict__ rres,
@@ -292,39 +259,23 @@ __global__ void rectify_kernel(const int32_t* __restrict__ order, const float* _
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (j >= dcols || i >= drows) return;
     size_t o = (size_t)i * dcols + j;
-    float mx = mapx[o], my = mapy[o];
-    int nx = __float2int_rn(mx), ny = __float2int_rn(my);
-    int ko = 0;
-    if (nx >= 0 && ny >= 0 && nx < scols && ny < srows) ko = __ldg(order + (size_t)ny * scols + nx);
-    int sx = __float2int_rn(mx * 32.0f), sy = __float2int_rn(my * 32.0f);
-    int x0 = sx >> 5, y0 = sy >> 5;
-    int fx = sx & 31, fy = sy & 31;
-    long long I = 0;
-    float Rs = 0.f;
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-        int xx = x0 + (t & 1), yy = y0 + (t >> 1);
-        if (xx < 0 || yy < 0 || xx >= scols || yy >= srows) continue;
-        int wq = ((t >> 1) ? fy : 32 - fy) * ((t & 1) ? fx : 32 - fx);
-        if (wq == 0) continue;
-        int K16;
-        float R;
-        smoothed_tap(order, res, xx, yy, srows, scols, post_smooth, K16, R);
-        I += (long long)wq * K16;
-        Rs = fmaf((float)wq * (1.0f / 1024.0f), R, Rs);
-    }
-    // phase = 2*pi*I/16384 + Rs; split I = 16384*base + frac, frac in [-8192, 8192)
-    long long base = (I + 8192) >> 14;  // floor((I + 8192) / 16384)
-    int frac = (int)(I - (base << 14));
-    rbase[o] = (int32_t)base;
-    rres[o] = fmaf((float)frac, ZIM_TWO_PI_F / 16384.0f, Rs);
-    rorder[o] = ko;
+    zt::rectify_pixel(order, res, srows, scols, mapx[o], mapy[o], post_smooth, rbase[o], rres[o], rorder[o]);
 }
 
 }  // namespace
 
-extern "C" ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo_calib* c, int use_full_left) {
-    if (!ctx) return ZIM_ERR_INVALID_ARG;
+void zim_rect_free(zim_rect_state& st) {
+    for (int k = 0; k < 2; k++)
+        for (int m = 0; m < 2; m++) {
+            cudaFree(st.d_map[k][m]);
+            st.d_map[k][m] = nullptr;
+        }
+}
+
+// setCalibrationParams (JSLAB_PhaseEpipolarReconstructor_V2.cpp:292-339):
+// stereoRectify, the optional full-left canvas and the two cameras' float
+// rectification maps (FP64 on the device), into st (maps newly allocated).
+zim_status zim_rect_build(zim_ctx* ctx, const zim_stereo_calib* c, int use_full_left, zim_rect_state& st) {
     if (!c || c->width <= 0 || c->height <= 0 || c->width > 65536 || c->height > 65536)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad calibration image size");
     for (int k = 0; k < 2; k++)
@@ -332,55 +283,77 @@ extern "C" ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo
             return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad camera matrix %d", k);
     if (c->t[0] == 0 && c->t[1] == 0 && c->t[2] == 0) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "zero baseline");
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    double R1[9], R2[9], P1[12], P2[12], Q[16];
-    stereo_rectify(*c, R1, R2, P1, P2, Q);
+    st = zim_rect_state{};
+    stereo_rectify(*c, st.R1, st.R2, st.P1, st.P2, st.Q);
     int rw = c->width, rh = c->height;
-    if (use_full_left) full_left(*c, R1, P1, P2, Q, &rw, &rh);
+    if (use_full_left) full_left(*c, st.R1, st.P1, st.P2, st.Q, &rw, &rh);
     if (rw <= 0 || rh <= 0 || rw > 4 * c->width + 64 || rh > 4 * c->height + 64 || rw > 65536)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "degenerate rectification (%dx%d)", rw, rh);
-    ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
-    for (int k = 0; k < 2; k++)
-        for (int m = 0; m < 2; m++) {
-            cudaFree(ctx->d_map[k][m]);
-            ctx->d_map[k][m] = nullptr;
-        }
-    ctx->calibrated = false;
     size_t n = (size_t)rw * rh;
     for (int k = 0; k < 2; k++)
         for (int m = 0; m < 2; m++)
-            if (cudaMalloc(&ctx->d_map[k][m], n * sizeof(float)) != cudaSuccess) {
+            if (cudaMalloc(&st.d_map[k][m], n * sizeof(float)) != cudaSuccess) {
                 cudaGetLastError();
+                zim_rect_free(st);
                 return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "map allocation failed");
             }
     for (int k = 0; k < 2; k++) {
-        const double* Pk = k == 0 ? P1 : P2;
+        const double* Pk = k == 0 ? st.P1 : st.P2;
         M3 A, R;
         for (int r = 0; r < 3; r++)
             for (int q = 0; q < 3; q++) A(r, q) = Pk[r * 4 + q];
-        std::memcpy(R.a, k == 0 ? R1 : R2, sizeof R.a);
+        std::memcpy(R.a, k == 0 ? st.R1 : st.R2, sizeof R.a);
         M3 iR = inverse(mul(A, R));
         MapParams p;
         std::memcpy(p.ir, iR.a, sizeof p.ir);
-        std::memcpy(ctx->ir[k], iR.a, sizeof ctx->ir[k]);
+        std::memcpy(st.ir[k], iR.a, sizeof st.ir[k]);
         const double* K = c->camera_matrix[k];
         const double* D = c->dist_coeffs[k];
         p.fx = K[0]; p.fy = K[4]; p.u0 = K[2]; p.v0 = K[5];
         p.k1 = D[0]; p.k2 = D[1]; p.p1 = D[2]; p.p2 = D[3]; p.k3 = D[4];
         dim3 blk(256), grd((rw + 255) / 256, rh);
-        map_kernel<<<grd, blk>>>(p, rw, rh, ctx->d_map[k][0], ctx->d_map[k][1]);
-        ZIM_LAUNCH_CHECK(ctx);
+        map_kernel<<<grd, blk>>>(p, rw, rh, st.d_map[k][0], st.d_map[k][1]);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            zim_rect_free(st);
+            return zim_fail(ctx, ZIM_ERR_CUDA, "map kernel launch failed: %s", cudaGetErrorString(e));
+        }
     }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        zim_rect_free(st);
+        return zim_fail(ctx, ZIM_ERR_CUDA, "map kernel failed: %s", cudaGetErrorString(e));
+    }
+    st.src_w = c->width;
+    st.src_h = c->height;
+    st.rect_w = rw;
+    st.rect_h = rh;
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo_calib* c, int use_full_left) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    zim_rect_state st;
+    zim_status s = zim_rect_build(ctx, c, use_full_left, st);
+    if (s) return s;
+    for (int k = 0; k < 2; k++)
+        for (int m = 0; m < 2; m++) {
+            cudaFree(ctx->d_map[k][m]);
+            ctx->d_map[k][m] = st.d_map[k][m];
+        }
     ctx->calib = *c;
-    std::memcpy(ctx->R1, R1, sizeof R1);
-    std::memcpy(ctx->R2, R2, sizeof R2);
-    std::memcpy(ctx->P1, P1, sizeof P1);
-    std::memcpy(ctx->P2, P2, sizeof P2);
-    std::memcpy(ctx->Q, Q, sizeof Q);
-    ctx->src_w = c->width;
-    ctx->src_h = c->height;
-    ctx->rect_w = rw;
-    ctx->rect_h = rh;
+    std::memcpy(ctx->R1, st.R1, sizeof st.R1);
+    std::memcpy(ctx->R2, st.R2, sizeof st.R2);
+    std::memcpy(ctx->P1, st.P1, sizeof st.P1);
+    std::memcpy(ctx->P2, st.P2, sizeof st.P2);
+    std::memcpy(ctx->Q, st.Q, sizeof st.Q);
+    std::memcpy(ctx->ir, st.ir, sizeof st.ir);
+    ctx->src_w = st.src_w;
+    ctx->src_h = st.src_h;
+    ctx->rect_w = st.rect_w;
+    ctx->rect_h = st.rect_h;
     ctx->calibrated = true;
     return ZIM_OK;
 }

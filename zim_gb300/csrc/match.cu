@@ -14,16 +14,11 @@
 // parabola through the costs of columns best-1, best, best+1.
 #include <climits>
 
-#include "zim_internal.cuh"
+#include "zim_tiles.cuh"
 
 namespace {
 
 constexpr int MATCH_THREADS = 256;
-
-__device__ __forceinline__ float phase_diff(int bR, float rR, int bL, float rL) {
-    // (2 pi bR + rR) - (2 pi bL + rL) with the integer cycles subtracted exactly
-    return fmaf((float)(bR - bL), ZIM_TWO_PI_F, rR - rL);
-}
 
 __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
     const int32_t* __restrict__ l_base, const float* __restrict__ l_res, const int32_t* __restrict__ l_order,
@@ -48,45 +43,13 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
         s_res[j] = r_res[ro + j];
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-        int k = s_ord[j];
-        if (k >= 0 && k <= pha_f) {
-            atomicMin(&s_lo[k], j);
-            atomicMax(&s_hi[k], j);
-        }
-    }
+    zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, threadIdx.x, blockDim.x);
     __syncthreads();
     for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-        const int k = l_order[ro + j];
-        float d = 0.f;
-        int best = -1;
-        if (k >= 1 && k <= pha_f) {
-            const int lo = s_lo[k], hi = s_hi[k];
-            if (lo <= hi) {
-                const int bL = l_base[ro + j];
-                const float rL = l_res[ro + j];
-                float min_cost = 1e9f;
-                int bj = -1;
-                for (int c = lo; c <= hi; c++) {
-                    if (s_ord[c] != k) continue;
-                    float diff = fabsf(phase_diff(s_base[c], s_res[c], bL, rL));
-                    if (diff < min_cost) {
-                        min_cost = diff;
-                        bj = c;
-                    }
-                }
-                if (bj >= 0 && min_cost < grad_threshold && bj >= 2 && bj < cols - 1) {
-                    float c0 = phase_diff(s_base[bj - 1], s_res[bj - 1], bL, rL);
-                    float c1 = phase_diff(s_base[bj], s_res[bj], bL, rL);
-                    float c2 = phase_diff(s_base[bj + 1], s_res[bj + 1], bL, rL);
-                    float num = c1 * (c0 - c2);
-                    float den = 2.0f * (c0 - c1) * (c1 - c2);
-                    float delta = fabsf(den) > 1e-9f ? num / den : 0.f;
-                    d = (float)(j - bj) - delta;
-                    best = bj;
-                }
-            }
-        }
+        float d;
+        int best;
+        zt::match_pixel(j, l_order[ro + j], l_base[ro + j], l_res[ro + j], s_ord, s_base, s_res, s_lo, s_hi, cols,
+                        pha_f, grad_threshold, d, best);
         disp[ro + j] = d;
         if (best_col) best_col[ro + j] = best;
     }

@@ -103,6 +103,17 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
 zim_status zim_compact_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
                               int cols, zim_point_xyz* points, uint64_t* count_dev, cudaStream_t st);
 
+// Rectification of one calibration: stereoRectify (+ full-left canvas) and the
+// two cameras' float maps on the device (calib.cu).
+struct zim_rect_state {
+    double R1[9], R2[9], P1[12], P2[12], Q[16];
+    double ir[2][9];
+    int src_w = 0, src_h = 0, rect_w = 0, rect_h = 0;
+    float* d_map[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+};
+zim_status zim_rect_build(zim_ctx* ctx, const zim_stereo_calib* c, int use_full_left, zim_rect_state& st);
+void zim_rect_free(zim_rect_state& st);
+
 // Scratch bytes needed by the grid filters for n points.
 size_t zim_grid_scratch_bytes(size_t n_points);
 size_t zim_mls_scratch_bytes(size_t n_points);

@@ -1,0 +1,563 @@
+// zim_tiles.cuh -- per-tile / per-pixel device code shared by the plain
+// per-pair kernels and the persistent batch kernels, so both paths run the
+// same arithmetic (bit-identical results).  Every multiply-add that matters
+// is an explicit fmaf, so the results do not depend on a translation unit's
+// contraction flags.
+//
+// Reference: PhaseShiftGrayCode3D/src/JSLAB_PhaseShiftDecoder_V2.cpp:18-182
+// (pre-blur + decode body), JSLAB_PhaseEpipolarReconstructor_V2.cpp:368-395
+// (setData remap), :933-1006 (stereoMatch), :405-461 (median + reprojection),
+// :79-195 (pixel Gaussian, radius outlier filter).
+#pragma once
+
+#include <cmath>
+
+#include "zim_internal.cuh"
+
+namespace zt {
+
+// ---------------------------------------------------------------- decode ----
+
+constexpr int DX = 32, DY = 8;  // decode tile (threads of a block, as DX x DY)
+constexpr int DHX = DX + 2, DHY = DY + 2;
+
+struct DecodeParams {
+    int rows, cols, enc, n_ps;
+    int shift[4];
+    int fbase[4];      // first frame of each phase-shift frequency
+    float sinv[64];    // sin(2 pi k / N) per frame (reference LUT order)
+    float cosv[64];
+    float w2d[9];      // pre-blur weights k_a * k_b
+    float thr;
+    int avg3;
+    // heterodyne (integer fringe counts)
+    int f0, f1, f2, f12, f23, f1_gt_f2;
+    float f0_f12, f1_f23, f2_f23, inv_f12, inv_f23, inv_f1, inv_f2;
+    // hierarchical
+    int iratio[4];
+    float fratio[4];
+    // Gray code
+    int gray_bits, gray_base, complementary;
+};
+
+inline void decode_params(const zim_decode_config* c, int rows, int cols, DecodeParams& p) {
+    p = DecodeParams{};
+    p.rows = rows;
+    p.cols = cols;
+    p.enc = c->encoding;
+    p.n_ps = c->encoding == ZIM_ENC_HETERODYNE3 ? 3 : (c->encoding == ZIM_ENC_HIERARCHICAL ? c->n_freq : 1);
+    int f = 0;
+    for (int i = 0; i < p.n_ps; i++) {
+        p.shift[i] = c->shift_num[i];
+        p.fbase[i] = f;
+        for (int k = 0; k < c->shift_num[i]; k++, f++) {
+            // sin(2.0 * PI * k / inum) in double, as the reference builds its LUT
+            p.sinv[f] = (float)std::sin(2.0 * 3.14159265358979323846 * k / c->shift_num[i]);
+            p.cosv[f] = (float)std::cos(2.0 * 3.14159265358979323846 * k / c->shift_num[i]);
+        }
+    }
+    double kb[3];
+    if (c->preblur_sigma <= 0) { kb[0] = 0.25; kb[1] = 0.5; kb[2] = 0.25; }
+    else {
+        double t = std::exp(-0.5 / (c->preblur_sigma * c->preblur_sigma));
+        double mul = 1.0 / (2.0 * t + 1.0);
+        kb[0] = t * mul; kb[1] = mul; kb[2] = t * mul;
+    }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) p.w2d[a * 3 + b] = (float)(kb[a] * kb[b]);
+    p.thr = (float)c->modulation_threshold;
+    p.avg3 = c->avg_three_phase ? 1 : 0;
+    if (c->encoding == ZIM_ENC_HETERODYNE3) {
+        p.f0 = (int)c->freq[0]; p.f1 = (int)c->freq[1]; p.f2 = (int)c->freq[2];
+        p.f12 = std::abs(p.f0 - p.f1); p.f23 = std::abs(p.f1 - p.f2);
+        p.f1_gt_f2 = c->freq[1] > c->freq[2];
+        p.f0_f12 = (float)((double)p.f0 / p.f12);
+        p.f1_f23 = (float)((double)p.f1 / p.f23);
+        p.f2_f23 = (float)((double)p.f2 / p.f23);
+        p.inv_f12 = (float)(1.0 / p.f12);
+        p.inv_f23 = (float)(1.0 / p.f23);
+        p.inv_f1 = (float)(1.0 / p.f1);
+        p.inv_f2 = (float)(1.0 / p.f2);
+    } else if (c->encoding == ZIM_ENC_HIERARCHICAL) {
+        for (int i = 1; i < c->n_freq; i++) {
+            p.iratio[i] = (int)(c->freq[i] / c->freq[i - 1]);
+            p.fratio[i] = (float)p.iratio[i];
+        }
+    } else {
+        p.gray_bits = c->gray_bits;
+        p.gray_base = c->shift_num[0];
+        p.complementary = c->encoding == ZIM_ENC_GRAYCODE_COMPLEMENTARY;
+    }
+}
+
+__device__ __forceinline__ int floor_div(int a, int b) {  // b > 0
+    int q = a / b;
+    return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
+
+// Shared memory of one decode tile: the raw per-pixel sums of the tile + halo.
+struct DecodeSmem {
+    float S[DHY][DHX + 1], C[DHY][DHX + 1], M[DHY][DHX + 1];
+};
+
+// Decodes tile (bx, by) of DX x DY pixels with the DX * DY threads of a block
+// (tid = ty * DX + tx).  The pre-blur is linear, so the blurred sums
+// S = -sum sin_k I_k, C = sum cos_k I_k, sum I_k are the 3x3 blur of the raw
+// per-pixel sums: the tile computes them over its 1-pixel halo into shared
+// memory once per frequency.  Ends with every thread past its last shared
+// read, so the caller may start the next tile at once.
+template <typename T>
+__device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
+                                            int tid, DecodeSmem& sm, int32_t* __restrict__ order,
+                                            float* __restrict__ residual, float* __restrict__ mod_out,
+                                            uint8_t* __restrict__ valid_out) {
+    const int tx = tid % DX, ty = tid / DX;
+    const int x = bx * DX + tx, y = by * DY + ty;
+    const int gx0 = bx * DX - 1, gy0 = by * DY - 1;
+    const size_t npx = (size_t)p.rows * p.cols;
+
+    float wrap[4];
+    float mod0 = 0.f;
+    bool ok = true;
+    for (int i = 0; i < p.n_ps; i++) {
+        const int N = p.shift[i];
+        const T* fb = frames + (size_t)p.fbase[i] * npx;
+        const float* sv = p.sinv + p.fbase[i];
+        const float* cv = p.cosv + p.fbase[i];
+        for (int h = tid; h < DHX * DHY; h += DX * DY) {
+            int hy = h / DHX, hx = h - hy * DHX;
+            int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
+            const T* src = fb + (size_t)gy * p.cols + gx;
+            float s = 0.f, c = 0.f, m = 0.f;
+            for (int k = 0; k < N; k++) {
+                float v = (float)__ldg(src + (size_t)k * npx);
+                s = fmaf(-sv[k], v, s);
+                c = fmaf(cv[k], v, c);
+                m += v;
+            }
+            sm.S[hy][hx] = s;
+            sm.C[hy][hx] = c;
+            sm.M[hy][hx] = m;
+        }
+        __syncthreads();
+        float S = 0.f, C = 0.f, M = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                float w = p.w2d[a * 3 + b];
+                S = fmaf(w, sm.S[ty + a][tx + b], S);
+                C = fmaf(w, sm.C[ty + a][tx + b], C);
+                M = fmaf(w, sm.M[ty + a][tx + b], M);
+            }
+        __syncthreads();
+        if (ok) {
+            wrap[i] = atan2f(S, C);
+            float b = 2.0f * sqrtf(fmaf(S, S, C * C)) / (float)N;
+            float mean = M / (float)N;
+            float nm = mean > 1e-3f ? b / mean : 0.f;
+            if (i == 0) mod0 = nm;
+            if (nm < p.thr) ok = false;
+        }
+    }
+    if (x >= p.cols || y >= p.rows) return;
+    const size_t pix = (size_t)y * p.cols + x;
+    if (mod_out) mod_out[pix] = mod0;
+    int k = 0;
+    float r = 0.f;
+    if (ok) {
+        if (p.enc == ZIM_ENC_HETERODYNE3) {
+            const float w0 = wrap[0], w1 = wrap[1], w2 = wrap[2];
+            float p12 = w0 > w1 ? w0 - w1 : w0 - w1 + ZIM_TWO_PI_F;
+            float p23;
+            if (p.f1_gt_f2) p23 = w1 > w2 ? w1 - w2 : w1 - w2 + ZIM_TWO_PI_F;
+            else p23 = w2 > w1 ? w2 - w1 : w2 - w1 + ZIM_TWO_PI_F;
+            float p123 = p12 > p23 ? p12 - p23 : p12 - p23 + ZIM_TWO_PI_F;
+            // uphase12 = p12 + 2 pi m12;  k = round(m12 f0 / f12 + (p12 f0 / f12 - w0) / 2 pi)
+            int m12 = (int)roundf(fmaf(p123, (float)p.f12, -p12) * ZIM_INV_TWO_PI_F);
+            int num = m12 * p.f0;
+            int q = floor_div(num, p.f12);
+            int rem = num - q * p.f12;
+            k = q + (int)roundf(fmaf((float)rem, p.inv_f12, fmaf(p12, p.f0_f12, -w0) * ZIM_INV_TWO_PI_F));
+            r = w0;
+            if (p.avg3) {
+                int m23 = (int)roundf(fmaf(p123, (float)p.f23, -p23) * ZIM_INV_TWO_PI_F);
+                int n2 = m23 * p.f1, q2 = floor_div(n2, p.f23), r2i = n2 - q2 * p.f23;
+                int k2 = q2 + (int)roundf(fmaf((float)r2i, p.inv_f23, fmaf(p23, p.f1_f23, -w1) * ZIM_INV_TWO_PI_F));
+                int n3 = m23 * p.f2, q3 = floor_div(n3, p.f23), r3i = n3 - q3 * p.f23;
+                int k3 = q3 + (int)roundf(fmaf((float)r3i, p.inv_f23, fmaf(p23, p.f2_f23, -w2) * ZIM_INV_TWO_PI_F));
+                // (uphase2 f0 / f1 - 2 pi k) = (w1 f0 + 2 pi (k2 f0 - k f1)) / f1, same for 3
+                float r2 = fmaf((float)(k2 * p.f0 - k * p.f1), ZIM_TWO_PI_F, w1 * (float)p.f0) * p.inv_f1;
+                float r3 = fmaf((float)(k3 * p.f0 - k * p.f2), ZIM_TWO_PI_F, w2 * (float)p.f0) * p.inv_f2;
+                r = (w0 + r2 + r3) * (1.0f / 3.0f);
+            }
+        } else if (p.enc == ZIM_ENC_HIERARCHICAL) {
+            for (int i = 1; i < p.n_ps; i++) {
+                float a = fmaf(p.fratio[i], wrap[i - 1] + ZIM_PI_F, -(wrap[i] + ZIM_PI_F)) * ZIM_INV_TWO_PI_F;
+                k = p.iratio[i] * k + (int)roundf(a);
+            }
+            r = wrap[p.n_ps - 1];
+        } else {
+            const int N = p.shift[0];
+            int sum_raw = 0;
+            for (int t = 0; t < N; t++) sum_raw += (int)__ldg(frames + (size_t)t * npx + pix);
+            int bin = 0, v1 = 0;
+            for (int b = 0; b < p.gray_bits; b++) {
+                int g = N * (int)__ldg(frames + (size_t)(p.gray_base + b) * npx + pix) > sum_raw ? 1 : 0;
+                bin ^= g;
+                v1 = (v1 << 1) | bin;
+            }
+            k = v1;
+            if (p.complementary) {
+                int g = N * (int)__ldg(frames + (size_t)(p.gray_base + p.gray_bits) * npx + pix) > sum_raw ? 1 : 0;
+                int v2 = (v1 << 1) | (bin ^ g);
+                int k2 = (v2 + 1) >> 1;
+                float w = wrap[0];
+                if (w <= -0.5f * ZIM_PI_F) k = k2;
+                else if (w >= 0.5f * ZIM_PI_F) k = k2 - 1;
+            }
+            r = wrap[0];
+        }
+    }
+    order[pix] = k;
+    residual[pix] = r;
+    if (valid_out) valid_out[pix] = ok ? 1 : 0;
+}
+
+// --------------------------------------------------------------- rectify ----
+
+// Post-smoothed phase at a source pixel in exact integer + FP32 form:
+// phase_s = 2*pi*K16/16 + R, K16 = sum (1 2 1)x(1 2 1) * order (BORDER_REPLICATE).
+__device__ __forceinline__ void smoothed_tap(const int32_t* __restrict__ order, const float* __restrict__ res, int x,
+                                             int y, int rows, int cols, int post_smooth, int& K16, float& R) {
+    if (!post_smooth) {
+        size_t o = (size_t)y * cols + x;
+        K16 = 16 * __ldg(order + o);
+        R = __ldg(res + o);
+        return;
+    }
+    int k = 0;
+    float r = 0.f;
+#pragma unroll
+    for (int a = -1; a <= 1; a++) {
+        int yy = min(max(y + a, 0), rows - 1);
+        int ca = a == 0 ? 2 : 1;
+#pragma unroll
+        for (int b = -1; b <= 1; b++) {
+            int xx = min(max(x + b, 0), cols - 1);
+            int cw = ca * (b == 0 ? 2 : 1);
+            size_t o = (size_t)yy * cols + xx;
+            k += cw * __ldg(order + o);
+            r = fmaf((float)cw * 0.0625f, __ldg(res + o), r);
+        }
+    }
+    K16 = k;
+    R = r;
+}
+
+// setData remap of one rectified pixel: INTER_LINEAR of the (post-smoothed)
+// phase with OpenCV's 1/32-pixel quantised weights and BORDER_CONSTANT 0,
+// INTER_NEAREST of the order.  The phase is kept as an integer cycle count
+// (exact: every weight is a multiple of 1/16384) plus an FP32 residual.
+__device__ __forceinline__ void rectify_pixel(const int32_t* __restrict__ order, const float* __restrict__ res,
+                                              int srows, int scols, float mx, float my, int post_smooth,
+                                              int32_t& rbase, float& rres, int32_t& rorder) {
+    int nx = __float2int_rn(mx), ny = __float2int_rn(my);
+    int ko = 0;
+    if (nx >= 0 && ny >= 0 && nx < scols && ny < srows) ko = __ldg(order + (size_t)ny * scols + nx);
+    int sx = __float2int_rn(mx * 32.0f), sy = __float2int_rn(my * 32.0f);
+    int x0 = sx >> 5, y0 = sy >> 5;
+    int fx = sx & 31, fy = sy & 31;
+    long long I = 0;
+    float Rs = 0.f;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        int xx = x0 + (t & 1), yy = y0 + (t >> 1);
+        if (xx < 0 || yy < 0 || xx >= scols || yy >= srows) continue;
+        int wq = ((t >> 1) ? fy : 32 - fy) * ((t & 1) ? fx : 32 - fx);
+        if (wq == 0) continue;
+        int K16;
+        float R;
+        smoothed_tap(order, res, xx, yy, srows, scols, post_smooth, K16, R);
+        I += (long long)wq * K16;
+        Rs = fmaf((float)wq * (1.0f / 1024.0f), R, Rs);
+    }
+    // phase = 2*pi*I/16384 + Rs; split I = 16384*base + frac, frac in [-8192, 8192)
+    long long base = (I + 8192) >> 14;  // floor((I + 8192) / 16384)
+    int frac = (int)(I - (base << 14));
+    rbase = (int32_t)base;
+    rres = fmaf((float)frac, ZIM_TWO_PI_F / 16384.0f, Rs);
+    rorder = ko;
+}
+
+// ----------------------------------------------------------------- match ----
+
+__device__ __forceinline__ float phase_diff(int bR, float rR, int bL, float rL) {
+    // (2 pi bR + rR) - (2 pi bL + rL) with the integer cycles subtracted exactly
+    return fmaf((float)(bR - bL), ZIM_TWO_PI_F, rR - rL);
+}
+
+// One left pixel against a right row staged in shared memory (s_ord, s_base,
+// s_res) with the per-order column spans [s_lo, s_hi]: the first column of
+// minimum |phase_R - phase_L| among right pixels of the same order (strict <),
+// rejected if min >= grad_threshold or the column is < 2 or >= cols - 1, then
+// the reference's three-point sub-pixel refinement.
+__device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, const int* s_ord, const int* s_base,
+                                            const float* s_res, const int* s_lo, const int* s_hi, int cols, int pha_f,
+                                            float grad_threshold, float& d, int& best) {
+    d = 0.f;
+    best = -1;
+    if (k < 1 || k > pha_f) return;
+    const int lo = s_lo[k], hi = s_hi[k];
+    if (lo > hi) return;
+    float min_cost = 1e9f;
+    int bj = -1;
+    for (int c = lo; c <= hi; c++) {
+        if (s_ord[c] != k) continue;
+        float diff = fabsf(phase_diff(s_base[c], s_res[c], bL, rL));
+        if (diff < min_cost) {
+            min_cost = diff;
+            bj = c;
+        }
+    }
+    if (bj >= 0 && min_cost < grad_threshold && bj >= 2 && bj < cols - 1) {
+        float c0 = phase_diff(s_base[bj - 1], s_res[bj - 1], bL, rL);
+        float c1 = phase_diff(s_base[bj], s_res[bj], bL, rL);
+        float c2 = phase_diff(s_base[bj + 1], s_res[bj + 1], bL, rL);
+        float num = c1 * (c0 - c2);
+        float den = 2.0f * (c0 - c1) * (c1 - c2);
+        float delta = fabsf(den) > 1e-9f ? num / den : 0.f;
+        d = (float)(j - bj) - delta;
+        best = bj;
+    }
+}
+
+// Per-order column spans of a staged right row (shared atomics).  Callers sync
+// before and after.
+__device__ __forceinline__ void match_spans(const int* s_ord, int cols, int pha_f, int* s_lo, int* s_hi, int tid,
+                                            int nthreads) {
+    for (int j = tid; j < cols; j += nthreads) {
+        int k = s_ord[j];
+        if (k >= 0 && k <= pha_f) {
+            atomicMin(&s_lo[k], j);
+            atomicMax(&s_hi[k], j);
+        }
+    }
+}
+
+// -------------------------------------------------- median + reprojection ----
+
+constexpr int RX = 32, RY = 8;  // median/reprojection tile
+
+struct ReprojParams {
+    float q03, q13, q23, q32, q33;
+    double dq03, dq13, dq23, dq32, dq33;
+    float r1[9];
+    float min_depth, max_depth;
+    double dmin_depth, dmax_depth;
+    int use_rectified, use_median;
+};
+
+inline void reproj_params(const double Q[16], const double R1[9], const zim_recon_config* cfg, ReprojParams& p) {
+    p.q03 = (float)Q[3]; p.q13 = (float)Q[7]; p.q23 = (float)Q[11];
+    p.q32 = (float)Q[14]; p.q33 = (float)Q[15];
+    p.dq03 = Q[3]; p.dq13 = Q[7]; p.dq23 = Q[11]; p.dq32 = Q[14]; p.dq33 = Q[15];
+    for (int i = 0; i < 9; i++) p.r1[i] = (float)R1[i];
+    p.min_depth = (float)cfg->min_depth;
+    p.max_depth = (float)cfg->max_depth;
+    p.dmin_depth = cfg->min_depth;
+    p.dmax_depth = cfg->max_depth;
+    p.use_rectified = cfg->use_rectified_coords != 0;
+    p.use_median = cfg->use_disp_median_filter != 0;
+}
+
+__device__ __forceinline__ void cswap(float& a, float& b) {
+    float lo = fminf(a, b), hi = fmaxf(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Moves the minimum of w[0..n) to w[0] and the maximum to w[n-1].
+template <int N>
+__device__ __forceinline__ void minmax_ends(float* w) {
+#pragma unroll
+    for (int i = 1; i < N; i++) cswap(w[0], w[i]);
+#pragma unroll
+    for (int i = 1; i < N - 1; i++) cswap(w[i], w[N - 1]);
+}
+
+// Exact median of 25 values by forgetful selection: keep 14, drop min and max,
+// add one, repeat; every dropped value provably has rank != 13.
+__device__ __forceinline__ float median25(float* a) {
+    minmax_ends<14>(a);            // a[1..12] live
+    a[13] = a[14]; minmax_ends<13>(a + 1);  // live a[2..12]
+    a[1] = a[15];  minmax_ends<12>(a + 1);  // live a[2..11]
+    a[12] = a[16]; minmax_ends<11>(a + 2);  // live a[3..11]
+    a[2] = a[17];  minmax_ends<10>(a + 2);  // live a[3..10]
+    a[11] = a[18]; minmax_ends<9>(a + 3);   // live a[4..10]
+    a[3] = a[19];  minmax_ends<8>(a + 3);   // live a[4..9]
+    a[10] = a[20]; minmax_ends<7>(a + 4);   // live a[5..9]
+    a[4] = a[21];  minmax_ends<6>(a + 4);   // live a[5..8]
+    a[9] = a[22];  minmax_ends<5>(a + 5);   // live a[6..8]
+    a[5] = a[23];  minmax_ends<4>(a + 5);   // live a[6..7]
+    a[8] = a[24];  minmax_ends<3>(a + 6);   // live a[7]
+    return a[7];
+}
+
+struct MedianSmem {
+    float tile[RY + 4][RX + 5];
+};
+
+// 5x5 median (replicate border) + Q reprojection of tile (bx, by) with the
+// RX * RY threads of a block.  Ends past the last shared read.
+__device__ __forceinline__ void median_reproject_tile(const float* __restrict__ disp, int rows, int cols,
+                                                      const ReprojParams& p, int bx, int by, int tid, MedianSmem& sm,
+                                                      float* __restrict__ disp_out, float* __restrict__ xyz,
+                                                      uint8_t* __restrict__ mask) {
+    const int tx = tid % RX, ty = tid / RX;
+    const int x = bx * RX + tx, y = by * RY + ty;
+    float d = 0.f;
+    if (p.use_median) {
+        const int gx0 = bx * RX - 2, gy0 = by * RY - 2;
+        for (int h = tid; h < (RX + 4) * (RY + 4); h += RX * RY) {
+            int hy = h / (RX + 4), hx = h - hy * (RX + 4);
+            int gy = min(max(gy0 + hy, 0), rows - 1), gx = min(max(gx0 + hx, 0), cols - 1);
+            sm.tile[hy][hx] = __ldg(disp + (size_t)gy * cols + gx);
+        }
+        __syncthreads();
+        float a[25];
+#pragma unroll
+        for (int dy = 0; dy < 5; dy++)
+#pragma unroll
+            for (int dx = 0; dx < 5; dx++) a[dy * 5 + dx] = sm.tile[ty + dy][tx + dx];
+        __syncthreads();
+        d = median25(a);
+    } else if (x < cols && y < rows) {
+        d = disp[(size_t)y * cols + x];
+    }
+    if (x >= cols || y >= rows) return;
+    const size_t o = (size_t)y * cols + x;
+    if (disp_out) disp_out[o] = d;
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    uint8_t m = 0;
+    if (fabsf(d) >= 1e-5f) {
+        float X, Y, Z;
+        float w = fmaf(p.q32, d, p.q33);
+        if (fabsf(w) < 1e-2f * (fabsf(p.q32 * d) + fabsf(p.q33))) {
+            // near-zero disparity denominator: FP64 divide
+            double wd = fma(p.dq32, (double)d, p.dq33);
+            double iw = 1.0 / wd;
+            X = (float)(((double)x + p.dq03) * iw);
+            Y = (float)(((double)y + p.dq13) * iw);
+            Z = (float)(p.dq23 * iw);
+            double zz = p.dq23 * iw;
+            if (p.use_rectified) {
+                if (zz > p.dmin_depth && zz < p.dmax_depth) { ox = X; oy = Y; oz = Z; m = 1; }
+            } else {
+                double xx = ((double)x + p.dq03) * iw, yy = ((double)y + p.dq13) * iw;
+                double rx = fma((double)p.r1[0], xx, fma((double)p.r1[3], yy, (double)p.r1[6] * zz));
+                double ry = fma((double)p.r1[1], xx, fma((double)p.r1[4], yy, (double)p.r1[7] * zz));
+                double rz = fma((double)p.r1[2], xx, fma((double)p.r1[5], yy, (double)p.r1[8] * zz));
+                if (rz > p.dmin_depth && rz < p.dmax_depth) { ox = (float)rx; oy = (float)ry; oz = (float)rz; m = 1; }
+            }
+        } else {
+            float iw = 1.0f / w;
+            X = ((float)x + p.q03) * iw;
+            Y = ((float)y + p.q13) * iw;
+            Z = p.q23 * iw;
+            if (p.use_rectified) {
+                if (Z > p.min_depth && Z < p.max_depth) { ox = X; oy = Y; oz = Z; m = 1; }
+            } else {
+                float rx = fmaf(p.r1[0], X, fmaf(p.r1[3], Y, p.r1[6] * Z));
+                float ry = fmaf(p.r1[1], X, fmaf(p.r1[4], Y, p.r1[7] * Z));
+                float rz = fmaf(p.r1[2], X, fmaf(p.r1[5], Y, p.r1[8] * Z));
+                if (rz > p.min_depth && rz < p.max_depth) { ox = rx; oy = ry; oz = rz; m = 1; }
+            }
+        }
+    }
+    xyz[3 * o] = ox;
+    xyz[3 * o + 1] = oy;
+    xyz[3 * o + 2] = oz;
+    mask[o] = m;
+}
+
+// ------------------------------------------------- pixel-window filters ----
+
+// getGaussianKernel(3, 0.7, CV_32F) outer-product weights: corner, edge, centre.
+inline void px_gaussian_weights(float& w00, float& w01, float& w11) {
+    double t = std::exp(-0.5 / (0.7 * 0.7));
+    double mul = 1.0 / (2.0 * t + 1.0);
+    float k0 = (float)(t * mul), k1 = (float)mul;
+    w00 = k0 * k0;
+    w01 = k0 * k1;
+    w11 = k1 * k1;
+}
+
+// 3x3 point-cloud Gaussian (sigma 0.7 px) at (x, y): neighbour used if valid
+// and |x_n - x_c| < 3; output sum(w p) / sum(w) if sum(w) > 0.8, else 0;
+// borders 0.  The weighted mean is accumulated as p_c + sum(w (p_n - p_c)) /
+// sum(w), the same value with millimetre-scale FP32 sums.
+__device__ __forceinline__ void px_gaussian_pixel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask,
+                                                  int rows, int cols, int x, int y, float w00, float w01, float w11,
+                                                  float* __restrict__ out, uint8_t* __restrict__ mask_out) {
+    size_t o = (size_t)y * cols + x;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
+    bool inner = x >= 1 && y >= 1 && x < cols - 1 && y < rows - 1 && mask[o];
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    if (inner) {
+        cx = __ldg(xyz + 3 * o);
+        cy = __ldg(xyz + 3 * o + 1);
+        cz = __ldg(xyz + 3 * o + 2);
+#pragma unroll
+        for (int a = -1; a <= 1; a++)
+#pragma unroll
+            for (int b = -1; b <= 1; b++) {
+                size_t q = o + (ptrdiff_t)a * cols + b;
+                if (!__ldg(mask + q)) continue;
+                float nx = __ldg(xyz + 3 * q);
+                if (fabsf(nx - cx) < 3.0f) {
+                    float w = (a == 0 && b == 0) ? w11 : ((a == 0 || b == 0) ? w01 : w00);
+                    sx = fmaf(nx - cx, w, sx);
+                    sy = fmaf(__ldg(xyz + 3 * q + 1) - cy, w, sy);
+                    sz = fmaf(__ldg(xyz + 3 * q + 2) - cz, w, sz);
+                    cnt += w;
+                }
+            }
+    }
+    bool keep = inner && cnt > 0.8f;
+    out[3 * o] = keep ? cx + sx / cnt : 0.f;
+    out[3 * o + 1] = keep ? cy + sy / cnt : 0.f;
+    out[3 * o + 2] = keep ? cz + sz / cnt : 0.f;
+    if (mask_out) mask_out[o] = keep ? 1 : 0;
+}
+
+// Radius outlier filter at (x, y): keep if at least min_nb valid neighbours
+// (not self) of the (2 hw + 1)^2 window lie within sqrt(r2).
+__device__ __forceinline__ void ror_pixel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
+                                          int cols, int x, int y, float r2, int min_nb, int hw,
+                                          float* __restrict__ out, uint8_t* __restrict__ mask_out) {
+    size_t o = (size_t)y * cols + x;
+    bool keep = false;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (mask[o]) {
+        keep = min_nb <= 0;
+        px = xyz[3 * o]; py = xyz[3 * o + 1]; pz = xyz[3 * o + 2];
+        int cnt = 0;
+        int r0 = max(0, y - hw), r1 = min(rows, y + hw + 1), c0 = max(0, x - hw), c1 = min(cols, x + hw + 1);
+        for (int i = r0; i < r1 && !keep; i++)
+            for (int j = c0; j < c1; j++) {
+                size_t q = (size_t)i * cols + j;
+                if (q == o || !__ldg(mask + q)) continue;
+                float dx = px - __ldg(xyz + 3 * q), dy = py - __ldg(xyz + 3 * q + 1), dz = pz - __ldg(xyz + 3 * q + 2);
+                if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= r2) {
+                    if (++cnt >= min_nb) { keep = true; break; }
+                }
+            }
+    }
+    out[3 * o] = keep ? px : 0.f;
+    out[3 * o + 1] = keep ? py : 0.f;
+    out[3 * o + 2] = keep ? pz : 0.f;
+    mask_out[o] = keep ? 1 : 0;
+}
+
+}  // namespace zt
