@@ -8,6 +8,7 @@
 // compute exactly what zim_reconstruct_pair computes (the same device code,
 // zim_tiles.cuh); what changes is the schedule:
 //   stage 1  decode:          item = (pair, camera, band of 8-row tile rows)
+//   stage 1b post-smooth of the decoded phase (same items), when configured
 //   stage 2  rectify + match: item = (pair, band of rectified rows); the right
 //            row is rectified straight into shared memory and each left pixel
 //            is rectified in registers, so no rectified phase reaches HBM
@@ -29,7 +30,7 @@ namespace {
 constexpr int BT = 256;  // threads per persistent CTA (one 32 x 8 tile)
 static_assert(BT == zt::DX * zt::DY && BT == zt::RX * zt::RY, "tile shape");
 
-enum { Q_DECODE, Q_MATCH, Q_REPROJ, Q_PXG, Q_ROR, NQ };
+enum { Q_DECODE, Q_SMOOTH, Q_MATCH, Q_REPROJ, Q_PXG, Q_ROR, NQ };
 
 struct PairDev {
     zt::DecodeParams dp;
@@ -42,6 +43,8 @@ struct PairDev {
     float grad_threshold;
     int32_t* order[2];
     float* res[2];
+    int32_t* sk[2];  // post-smoothed taps (16 x cycles, residual), when post_smooth
+    float* sr[2];
     float* disp_raw;
     float* disp_out;
     float* x_rep;  // reprojection output
@@ -102,6 +105,27 @@ __global__ void __launch_bounds__(BT) batch_decode_kernel(const PairDev* __restr
     }
 }
 
+__global__ void __launch_bounds__(BT) batch_smooth_kernel(const PairDev* __restrict__ pairs,
+                                                          const int4* __restrict__ items, int n_items,
+                                                          unsigned* __restrict__ counter) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];  // pair, camera, first tile row, tile rows
+        const PairDev& P = pairs[w.x];
+        const int tiles_x = (P.cols + zt::DX - 1) / zt::DX;
+        for (int ty = w.z; ty < w.z + w.w; ty++)
+            for (int tx = 0; tx < tiles_x; tx++) {
+                const int x = tx * zt::DX + tid % zt::DX, y = ty * zt::DY + tid / zt::DX;
+                if (x < P.cols && y < P.rows) zt::smooth_pixel(P.order[w.y], P.res[w.y], P.rows, P.cols, x, y,
+                                                               P.sk[w.y], P.sr[w.y]);
+            }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restrict__ pairs, const int4* __restrict__ items,
                                                          int n_items, unsigned* __restrict__ counter, int max_cols) {
     extern __shared__ int4 smem_raw[];
@@ -127,8 +151,12 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
             for (int j = tid; j < cols; j += BT) {
                 int32_t b, o;
                 float r;
-                zt::rectify_pixel(P.order[1], P.res[1], P.rows, P.cols, __ldg(P.map[1][0] + ro + j),
-                                  __ldg(P.map[1][1] + ro + j), P.post_smooth, b, r, o);
+                if (P.post_smooth)
+                    zt::rectify_pixel_smoothed(P.sk[1], P.sr[1], P.order[1], P.rows, P.cols,
+                                               __ldg(P.map[1][0] + ro + j), __ldg(P.map[1][1] + ro + j), b, r, o);
+                else
+                    zt::rectify_pixel(P.order[1], P.res[1], P.rows, P.cols, __ldg(P.map[1][0] + ro + j),
+                                      __ldg(P.map[1][1] + ro + j), 0, b, r, o);
                 s_ord[j] = o;
                 s_base[j] = b;
                 s_res[j] = r;
@@ -139,8 +167,12 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
             for (int j = tid; j < cols; j += BT) {
                 int32_t bL, kL;
                 float rL;
-                zt::rectify_pixel(P.order[0], P.res[0], P.rows, P.cols, __ldg(P.map[0][0] + ro + j),
-                                  __ldg(P.map[0][1] + ro + j), P.post_smooth, bL, rL, kL);
+                if (P.post_smooth)
+                    zt::rectify_pixel_smoothed(P.sk[0], P.sr[0], P.order[0], P.rows, P.cols,
+                                               __ldg(P.map[0][0] + ro + j), __ldg(P.map[0][1] + ro + j), bL, rL, kL);
+                else
+                    zt::rectify_pixel(P.order[0], P.res[0], P.rows, P.cols, __ldg(P.map[0][0] + ro + j),
+                                      __ldg(P.map[0][1] + ro + j), 0, bL, rL, kL);
                 float d;
                 int best;
                 zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, cols, pha_f, P.grad_threshold, d,
@@ -171,10 +203,9 @@ __global__ void __launch_bounds__(BT) batch_reproject_kernel(const PairDev* __re
     }
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(BT) batch_filter_kernel(const PairDev* __restrict__ pairs,
-                                                          const int4* __restrict__ items, int n_items,
-                                                          unsigned* __restrict__ counter) {
+__global__ void __launch_bounds__(BT) batch_pxg_kernel(const PairDev* __restrict__ pairs,
+                                                       const int4* __restrict__ items, int n_items,
+                                                       unsigned* __restrict__ counter) {
     __shared__ int s_item;
     const int tid = threadIdx.x;
     for (;;) {
@@ -187,13 +218,29 @@ __global__ void __launch_bounds__(BT) batch_filter_kernel(const PairDev* __restr
             for (int tx = 0; tx < tiles_x; tx++) {
                 const int x = tx * zt::RX + tid % zt::RX, y = ty * zt::RY + tid / zt::RX;
                 if (x >= P.rw || y >= P.rh) continue;
-                if (STAGE == Q_PXG)
-                    zt::px_gaussian_pixel(P.x_rep, P.m_rep, P.rh, P.rw, x, y, P.pxg_w00, P.pxg_w01, P.pxg_w11, P.x_pxg,
-                                          P.m_pxg);
-                else
-                    zt::ror_pixel(P.x_ror_in, P.m_ror_in, P.rh, P.rw, x, y, P.ror_r2, P.ror_min_nb, P.ror_hw, P.x_ror,
-                                  P.m_ror);
+                zt::px_gaussian_pixel(P.x_rep, P.m_rep, P.rh, P.rw, x, y, P.pxg_w00, P.pxg_w01, P.pxg_w11, P.x_pxg,
+                                      P.m_pxg);
             }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BT) batch_ror_kernel(const PairDev* __restrict__ pairs,
+                                                       const int4* __restrict__ items, int n_items,
+                                                       unsigned* __restrict__ counter) {
+    extern __shared__ float4 ror_smem[];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= n_items) break;
+        const int4 w = items[it];
+        const PairDev& P = pairs[w.x];
+        const int tiles_x = (P.rw + zt::RX - 1) / zt::RX;
+        for (int ty = w.y; ty < w.y + w.z; ty++)
+            for (int tx = 0; tx < tiles_x; tx++)
+                zt::ror_tile(P.x_ror_in, P.m_ror_in, P.rh, P.rw, tx, ty, tid, P.ror_r2, P.ror_min_nb, P.ror_hw,
+                             ror_smem, P.x_ror, P.m_ror);
         __syncthreads();
     }
 }
@@ -216,7 +263,8 @@ struct zim_batch {
     Queues q{};
     int max_cols = 0, max_pha_f = 0;
     size_t match_smem = 0;
-    int grid[NQ] = {0, 0, 0, 0, 0};
+    size_t ror_smem = 0;
+    int grid[NQ] = {0, 0, 0, 0, 0, 0};
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -259,8 +307,11 @@ void build_items(const zim_batch* b, const zim_batch_tuning& t, std::vector<int4
         const zim_rect_state& C = b->calibs[p.calib];
         const int trows = (p.rows + zt::DY - 1) / zt::DY;
         for (int cam = 0; cam < 2; cam++)
-            for (int r = 0; r < trows; r += t.decode_rows)
-                items[Q_DECODE].push_back(make_int4(pi, cam, r, std::min(t.decode_rows, trows - r)));
+            for (int r = 0; r < trows; r += t.decode_rows) {
+                const int4 it = make_int4(pi, cam, r, std::min(t.decode_rows, trows - r));
+                items[Q_DECODE].push_back(it);
+                if (p.decode.post_smooth) items[Q_SMOOTH].push_back(it);
+            }
         for (int r = 0; r < C.rect_h; r += t.match_rows)
             items[Q_MATCH].push_back(make_int4(pi, r, std::min(t.match_rows, C.rect_h - r), 0));
         const int rtrows = (C.rect_h + zt::RY - 1) / zt::RY;
@@ -282,10 +333,11 @@ zim_status capture(zim_batch* b) {
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 152;
     const int want = std::max(1, b->tuning.ctas_per_sm);
     b->grid[Q_DECODE] = sms * std::min(want, occupancy((const void*)batch_decode_kernel, 0));
+    b->grid[Q_SMOOTH] = sms * std::min(want, occupancy((const void*)batch_smooth_kernel, 0));
     b->grid[Q_MATCH] = sms * std::min(want, occupancy((const void*)batch_match_kernel, b->match_smem));
     b->grid[Q_REPROJ] = sms * std::min(want, occupancy((const void*)batch_reproject_kernel, 0));
-    b->grid[Q_PXG] = sms * std::min(want, occupancy((const void*)batch_filter_kernel<Q_PXG>, 0));
-    b->grid[Q_ROR] = sms * std::min(want, occupancy((const void*)batch_filter_kernel<Q_ROR>, 0));
+    b->grid[Q_PXG] = sms * std::min(want, occupancy((const void*)batch_pxg_kernel, 0));
+    b->grid[Q_ROR] = sms * std::min(want, occupancy((const void*)batch_ror_kernel, b->ror_smem));
     cudaStream_t s = b->cap_stream;
     ZIM_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->d_counters, 0, NQ * sizeof(unsigned), s);
@@ -293,6 +345,9 @@ zim_status capture(zim_batch* b) {
     if (q.n[Q_DECODE])
         batch_decode_kernel<<<std::min(b->grid[Q_DECODE], q.n[Q_DECODE]), BT, 0, s>>>(
             b->d_pairs, q.items[Q_DECODE], q.n[Q_DECODE], b->d_counters + Q_DECODE);
+    if (q.n[Q_SMOOTH])
+        batch_smooth_kernel<<<std::min(b->grid[Q_SMOOTH], q.n[Q_SMOOTH]), BT, 0, s>>>(
+            b->d_pairs, q.items[Q_SMOOTH], q.n[Q_SMOOTH], b->d_counters + Q_SMOOTH);
     if (q.n[Q_MATCH])
         batch_match_kernel<<<std::min(b->grid[Q_MATCH], q.n[Q_MATCH]), BT, b->match_smem, s>>>(
             b->d_pairs, q.items[Q_MATCH], q.n[Q_MATCH], b->d_counters + Q_MATCH, b->max_cols);
@@ -300,10 +355,10 @@ zim_status capture(zim_batch* b) {
         batch_reproject_kernel<<<std::min(b->grid[Q_REPROJ], q.n[Q_REPROJ]), BT, 0, s>>>(
             b->d_pairs, q.items[Q_REPROJ], q.n[Q_REPROJ], b->d_counters + Q_REPROJ);
     if (q.n[Q_PXG])
-        batch_filter_kernel<Q_PXG><<<std::min(b->grid[Q_PXG], q.n[Q_PXG]), BT, 0, s>>>(
-            b->d_pairs, q.items[Q_PXG], q.n[Q_PXG], b->d_counters + Q_PXG);
+        batch_pxg_kernel<<<std::min(b->grid[Q_PXG], q.n[Q_PXG]), BT, 0, s>>>(b->d_pairs, q.items[Q_PXG], q.n[Q_PXG],
+                                                                            b->d_counters + Q_PXG);
     if (q.n[Q_ROR])
-        batch_filter_kernel<Q_ROR><<<std::min(b->grid[Q_ROR], q.n[Q_ROR]), BT, 0, s>>>(
+        batch_ror_kernel<<<std::min(b->grid[Q_ROR], q.n[Q_ROR]), BT, b->ror_smem, s>>>(
             b->d_pairs, q.items[Q_ROR], q.n[Q_ROR], b->d_counters + Q_ROR);
     cudaError_t le = cudaGetLastError();
     cudaGraph_t g = nullptr;
@@ -340,10 +395,11 @@ zim_status requeue(zim_batch* b) {
 
 // Upper bound of the item space over the tunings the autotuner tries (1-row bands).
 size_t max_item_bytes(const zim_batch* b) {
-    size_t n[NQ] = {0, 0, 0, 0, 0};
+    size_t n[NQ] = {0, 0, 0, 0, 0, 0};
     for (const zim_batch_pair& p : b->pairs) {
         const zim_rect_state& C = b->calibs[p.calib];
         n[Q_DECODE] += 2 * (size_t)((p.rows + zt::DY - 1) / zt::DY);
+        n[Q_SMOOTH] += 2 * (size_t)((p.rows + zt::DY - 1) / zt::DY);
         n[Q_MATCH] += (size_t)C.rect_h;
         const size_t rt = (C.rect_h + zt::RY - 1) / zt::RY;
         n[Q_REPROJ] += rt;
@@ -412,8 +468,8 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     if (rcfg->use_sor || rcfg->use_mls || rcfg->use_metric_gaussian)
         return zim_fail(ctx, ZIM_ERR_UNSUPPORTED,
                         "the batch runs the pixel-domain stages; run SOR / MLS / metric Gaussian per cloud after it");
-    if (rcfg->use_ror && (rcfg->radius_window_size < 0 || rcfg->radius_window_size > 64))
-        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, 64]");
+    if (rcfg->use_ror && (rcfg->radius_window_size < 0 || rcfg->radius_window_size > ZIM_MAX_ROR_WINDOW))
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, %d]", ZIM_MAX_ROR_WINDOW);
     if (tuning && !tuning_ok(*tuning)) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad tuning");
     int max_cols = 1, max_pha = 0;
     for (int i = 0; i < n_pairs; i++) {
@@ -449,6 +505,10 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     b->match_smem = (size_t)max_cols * 12 + (size_t)(max_pha + 1) * 8;
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(batch_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)b->match_smem));
+    b->ror_smem = b->use_ror ? zt::ror_smem_bytes(rcfg->radius_window_size / 2) : 0;
+    if (b->use_ror)
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(batch_ror_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)b->ror_smem));
 
     // memory plan: descriptors, counters, per-pair intermediates, items
     const bool pxg_mask = b->use_pxg && rcfg->px_gaussian_updates_mask;
@@ -456,7 +516,7 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     for (const zim_batch_pair& p : b->pairs) {
         const zim_rect_state& C = b->calibs[p.calib];
         const size_t src = (size_t)p.rows * p.cols, dst = (size_t)C.rect_w * C.rect_h;
-        bytes += 2 * (zim_align256(src * 4) * 2) + zim_align256(dst * 4);
+        bytes += 2 * (zim_align256(src * 4) * (p.decode.post_smooth ? 4 : 2)) + zim_align256(dst * 4);
         bytes += 2 * (zim_align256(dst * 12) + zim_align256(dst));  // two intermediate clouds at most
     }
     b->items_off = bytes;
@@ -496,6 +556,10 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
             D.map[c][1] = C.d_map[c][1];
             D.order[c] = (int32_t*)take(src * 4);
             D.res[c] = (float*)take(src * 4);
+            if (p.decode.post_smooth) {
+                D.sk[c] = (int32_t*)take(src * 4);
+                D.sr[c] = (float*)take(src * 4);
+            }
         }
         D.disp_raw = (float*)take(dst * 4);
         D.disp_out = p.disp;

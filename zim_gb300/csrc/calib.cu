@@ -262,6 +262,28 @@ __global__ void rectify_kernel(const int32_t* __restrict__ order, const float* _
     zt::rectify_pixel(order, res, srows, scols, mapx[o], mapy[o], post_smooth, rbase[o], rres[o], rorder[o]);
 }
 
+// Post-smooth once per source pixel (the reference smooths the decoded phase
+// map before setData, JSLAB_PhaseShiftDecoder_V2.cpp:274-295) ...
+__global__ void smooth_kernel(const int32_t* __restrict__ order, const float* __restrict__ res, int rows, int cols,
+                              int32_t* __restrict__ K16, float* __restrict__ R) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= cols || y >= rows) return;
+    zt::smooth_pixel(order, res, rows, cols, x, y, K16, R);
+}
+
+// ... then remap the smoothed taps.
+__global__ void rectify_smoothed_kernel(const int32_t* __restrict__ K16, const float* __restrict__ R,
+                                        const int32_t* __restrict__ order, int srows, int scols,
+                                        const float* __restrict__ mapx, const float* __restrict__ mapy, int drows,
+                                        int dcols, int32_t* __restrict__ rbase, float* __restrict__ rres,
+                                        int32_t* __restrict__ rorder) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= dcols || i >= drows) return;
+    size_t o = (size_t)i * dcols + j;
+    zt::rectify_pixel_smoothed(K16, R, order, srows, scols, mapx[o], mapy[o], rbase[o], rres[o], rorder[o]);
+}
+
 }  // namespace
 
 void zim_rect_free(zim_rect_state& st) {
@@ -384,11 +406,21 @@ extern "C" ZIM_API zim_status zim_get_rectify_maps(zim_ctx* ctx, int cam, float*
 }
 
 zim_status zim_rectify_launch(zim_ctx* ctx, int cam, const int32_t* order, const float* residual, int rows, int cols,
-                              int post_smooth, int32_t* rbase, float* rres, int32_t* rorder, cudaStream_t st) {
+                              int post_smooth, int32_t* smooth_k16, float* smooth_r, int32_t* rbase, float* rres,
+                              int32_t* rorder, cudaStream_t st) {
     dim3 blk(32, 8), grd((ctx->rect_w + 31) / 32, (ctx->rect_h + 7) / 8);
-    rectify_kernel<<<grd, blk, 0, st>>>(order, residual, rows, cols, ctx->d_map[cam][0], ctx->d_map[cam][1],
-                                        ctx->rect_h, ctx->rect_w, post_smooth, rbase, rres, rorder);
-    ctx->launches += 1;
+    if (post_smooth) {
+        dim3 sgrd((cols + 31) / 32, (rows + 7) / 8);
+        smooth_kernel<<<sgrd, blk, 0, st>>>(order, residual, rows, cols, smooth_k16, smooth_r);
+        rectify_smoothed_kernel<<<grd, blk, 0, st>>>(smooth_k16, smooth_r, order, rows, cols, ctx->d_map[cam][0],
+                                                     ctx->d_map[cam][1], ctx->rect_h, ctx->rect_w, rbase, rres,
+                                                     rorder);
+        ctx->launches += 2;
+    } else {
+        rectify_kernel<<<grd, blk, 0, st>>>(order, residual, rows, cols, ctx->d_map[cam][0], ctx->d_map[cam][1],
+                                            ctx->rect_h, ctx->rect_w, 0, rbase, rres, rorder);
+        ctx->launches += 1;
+    }
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
 }
@@ -403,6 +435,17 @@ extern "C" ZIM_API zim_status zim_rectify(zim_ctx* ctx, int cam, const int32_t* 
     if (rows != ctx->src_h || cols != ctx->src_w)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "image size differs from calibration");
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    return zim_rectify_launch(ctx, cam, order, residual, rows, cols, post_smooth, rbase, rres, rorder,
+    int32_t* sk = nullptr;
+    float* sr = nullptr;
+    if (post_smooth) {
+        const size_t src = (size_t)rows * cols;
+        zim_status s = zim_scratch_reserve(ctx, 2 * zim_align256(src * 4) + 1024);
+        if (s) return s;
+        zim_scratch_reset(ctx);
+        sk = (int32_t*)zim_scratch_take(ctx, src * 4);
+        sr = (float*)zim_scratch_take(ctx, src * 4);
+        if (!sk || !sr) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "rectify scratch");
+    }
+    return zim_rectify_launch(ctx, cam, order, residual, rows, cols, post_smooth, sk, sr, rbase, rres, rorder,
                               zim_stream(stream));
 }

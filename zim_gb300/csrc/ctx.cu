@@ -222,6 +222,8 @@ struct PairBuffers {
     int32_t* rbase[2];
     float* rres[2];
     int32_t* rorder[2];
+    int32_t* sk[2];  // post-smoothed taps (16 x cycles, residual)
+    float* sr[2];
     float* disp_raw;
     float* disp_med;
     float* xyz[2];
@@ -233,7 +235,7 @@ size_t pair_scratch_bytes(const zim_ctx* ctx, const zim_recon_config* r, int row
                           int sample_bytes, int frames, bool host) {
     size_t src = (size_t)rows * cols, dst = (size_t)ctx->rect_h * ctx->rect_w;
     size_t b = 0;
-    b += 2 * (zim_align256(src * 4) * 2);
+    b += 2 * (zim_align256(src * 4) * 4);
     b += 2 * (zim_align256(dst * 4) * 3);
     b += zim_align256(dst * 4);
     if (need_disp) b += zim_align256(dst * 4);
@@ -261,6 +263,8 @@ static zim_status check_pair_args(zim_ctx* ctx, const zim_decode_config* d, cons
                         ctx->src_w, ctx->src_h);
     if (r->use_mls && (r->mls_window_size < 0 || r->mls_window_size > 64))
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "mls_window_size out of range");
+    if (r->use_ror && (r->radius_window_size < 0 || r->radius_window_size > ZIM_MAX_ROR_WINDOW))
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, %d]", ZIM_MAX_ROR_WINDOW);
     return ZIM_OK;
 }
 
@@ -272,8 +276,8 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
     for (int c = 0; c < 2; c++) {
         s = zim_decode_launch(ctx, d, frames[c], sample_type, rows, cols, B.order[c], B.res[c], nullptr, nullptr, st);
         if (s) return s;
-        s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->post_smooth, B.rbase[c], B.rres[c],
-                               B.rorder[c], st);
+        s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->post_smooth, B.sk[c], B.sr[c],
+                               B.rbase[c], B.rres[c], B.rorder[c], st);
         if (s) return s;
     }
     const int RH = ctx->rect_h, RW = ctx->rect_w;
@@ -371,6 +375,8 @@ static zim_status carve_pair(zim_ctx* ctx, const zim_recon_config* r, int rows, 
     for (int c = 0; c < 2; c++) {
         B.order[c] = (int32_t*)zim_scratch_take(ctx, src * 4);
         B.res[c] = (float*)zim_scratch_take(ctx, src * 4);
+        B.sk[c] = (int32_t*)zim_scratch_take(ctx, src * 4);
+        B.sr[c] = (float*)zim_scratch_take(ctx, src * 4);
         B.rbase[c] = (int32_t*)zim_scratch_take(ctx, dst * 4);
         B.rres[c] = (float*)zim_scratch_take(ctx, dst * 4);
         B.rorder[c] = (int32_t*)zim_scratch_take(ctx, dst * 4);

@@ -30,11 +30,12 @@ __global__ void px_gaussian_kernel(const float* __restrict__ xyz, const uint8_t*
     zt::px_gaussian_pixel(xyz, mask, rows, cols, x, y, w00, w01, w11, out, mask_out);
 }
 
-__global__ void ror_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                           float r2, int min_nb, int hw, float* __restrict__ out, uint8_t* __restrict__ mask_out) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= cols || y >= rows) return;
-    zt::ror_pixel(xyz, mask, rows, cols, x, y, r2, min_nb, hw, out, mask_out);
+__global__ void __launch_bounds__(RX* RY) ror_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask,
+                                                     int rows, int cols, float r2, int min_nb, int hw,
+                                                     float* __restrict__ out, uint8_t* __restrict__ mask_out) {
+    extern __shared__ float4 ror_smem[];
+    zt::ror_tile(xyz, mask, rows, cols, blockIdx.x, blockIdx.y, threadIdx.y * RX + threadIdx.x, r2, min_nb, hw,
+                 ror_smem, out, mask_out);
 }
 
 constexpr int CB = 1024;  // compaction block
@@ -144,9 +145,11 @@ zim_status zim_px_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint8_t*
 
 zim_status zim_ror_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float radius,
                           int min_neighbors, int window_size, float* out, uint8_t* mask_out, cudaStream_t st) {
-    dim3 blk(32, 8), grd((cols + 31) / 32, (rows + 7) / 8);
-    ror_kernel<<<grd, blk, 0, st>>>(xyz, mask, rows, cols, radius * radius, min_neighbors, window_size / 2, out,
-                                    mask_out);
+    const int hw = window_size / 2;
+    const size_t smem = zt::ror_smem_bytes(hw);
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(ror_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 blk(RX, RY), grd((cols + RX - 1) / RX, (rows + RY - 1) / RY);
+    ror_kernel<<<grd, blk, smem, st>>>(xyz, mask, rows, cols, radius * radius, min_neighbors, hw, out, mask_out);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
@@ -196,7 +199,7 @@ extern "C" ZIM_API zim_status zim_filter_ror(zim_ctx* ctx, const float* xyz, con
                                              uint8_t* mask_out, void* stream) {
     zim_status s = check_cloud(ctx, xyz, mask, out, rows, cols);
     if (s) return s;
-    if (!mask_out || window_size < 0 || window_size > 128 || min_neighbors < 0)
+    if (!mask_out || window_size < 0 || window_size > ZIM_MAX_ROR_WINDOW || min_neighbors < 0)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad ROR argument");
     return zim_ror_launch(ctx, xyz, mask, rows, cols, radius, min_neighbors, window_size, out, mask_out,
                           zim_stream(stream));

@@ -17,6 +17,8 @@
 // Maximum rectified width handled by the one-CTA-per-row matcher.
 #define ZIM_MAX_MATCH_COLS 8192
 #define ZIM_MAX_ORDER 4095
+// Largest radius-filter window: its shared-memory tile must fit one CTA.
+#define ZIM_MAX_ROR_WINDOW 96
 
 struct zim_ctx {
     int device = 0;
@@ -77,9 +79,10 @@ struct zim_decode_params;  // decode.cu
 zim_status zim_decode_launch(zim_ctx* ctx, const zim_decode_config* cfg, const void* frames,
                              int sample_type, int rows, int cols, int32_t* order, float* residual,
                              float* mod, uint8_t* valid, cudaStream_t st);
+// post_smooth: smooth_k16 / smooth_r are rows*cols scratch for the smoothed taps.
 zim_status zim_rectify_launch(zim_ctx* ctx, int cam, const int32_t* order, const float* residual,
-                              int rows, int cols, int post_smooth, int32_t* rect_base,
-                              float* rect_res, int32_t* rect_order, cudaStream_t st);
+                              int rows, int cols, int post_smooth, int32_t* smooth_k16, float* smooth_r,
+                              int32_t* rect_base, float* rect_res, int32_t* rect_order, cudaStream_t st);
 zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_res,
                             const int32_t* l_order, const int32_t* r_base, const float* r_res,
                             const int32_t* r_order, int rows, int cols, int pha_f,

@@ -90,9 +90,14 @@ inline void decode_params(const zim_decode_config* c, int rows, int cols, Decode
     }
 }
 
-__device__ __forceinline__ int floor_div(int a, int b) {  // b > 0
-    int q = a / b;
-    return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+// floor(a / b) for b > 0 and |a / b| < 2^21, from the float reciprocal
+// inv_b = 1 / b: the float quotient is within one of the true one, and one
+// remainder check corrects it (an integer division costs ~40 instructions).
+__device__ __forceinline__ int floor_div(int a, int b, float inv_b) {
+    int q = __float2int_rd((float)a * inv_b);
+    const int r = a - q * b;
+    q += (r >= b) - (r < 0);
+    return q;
 }
 
 // Shared memory of one decode tile: the raw per-pixel sums of the tile + halo.
@@ -116,7 +121,7 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
     const int gx0 = bx * DX - 1, gy0 = by * DY - 1;
     const size_t npx = (size_t)p.rows * p.cols;
 
-    float wrap[4];
+    float wrap0 = 0.f, wrap1 = 0.f, wrap2 = 0.f, wrap3 = 0.f;  // named, so they stay in registers
     float mod0 = 0.f;
     bool ok = true;
     for (int i = 0; i < p.n_ps; i++) {
@@ -152,7 +157,11 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             }
         __syncthreads();
         if (ok) {
-            wrap[i] = atan2f(S, C);
+            const float wr = atan2f(S, C);
+            if (i == 0) wrap0 = wr;
+            else if (i == 1) wrap1 = wr;
+            else if (i == 2) wrap2 = wr;
+            else wrap3 = wr;
             float b = 2.0f * sqrtf(fmaf(S, S, C * C)) / (float)N;
             float mean = M / (float)N;
             float nm = mean > 1e-3f ? b / mean : 0.f;
@@ -167,7 +176,7 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
     float r = 0.f;
     if (ok) {
         if (p.enc == ZIM_ENC_HETERODYNE3) {
-            const float w0 = wrap[0], w1 = wrap[1], w2 = wrap[2];
+            const float w0 = wrap0, w1 = wrap1, w2 = wrap2;
             float p12 = w0 > w1 ? w0 - w1 : w0 - w1 + ZIM_TWO_PI_F;
             float p23;
             if (p.f1_gt_f2) p23 = w1 > w2 ? w1 - w2 : w1 - w2 + ZIM_TWO_PI_F;
@@ -176,15 +185,15 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             // uphase12 = p12 + 2 pi m12;  k = round(m12 f0 / f12 + (p12 f0 / f12 - w0) / 2 pi)
             int m12 = (int)roundf(fmaf(p123, (float)p.f12, -p12) * ZIM_INV_TWO_PI_F);
             int num = m12 * p.f0;
-            int q = floor_div(num, p.f12);
+            int q = floor_div(num, p.f12, p.inv_f12);
             int rem = num - q * p.f12;
             k = q + (int)roundf(fmaf((float)rem, p.inv_f12, fmaf(p12, p.f0_f12, -w0) * ZIM_INV_TWO_PI_F));
             r = w0;
             if (p.avg3) {
                 int m23 = (int)roundf(fmaf(p123, (float)p.f23, -p23) * ZIM_INV_TWO_PI_F);
-                int n2 = m23 * p.f1, q2 = floor_div(n2, p.f23), r2i = n2 - q2 * p.f23;
+                int n2 = m23 * p.f1, q2 = floor_div(n2, p.f23, p.inv_f23), r2i = n2 - q2 * p.f23;
                 int k2 = q2 + (int)roundf(fmaf((float)r2i, p.inv_f23, fmaf(p23, p.f1_f23, -w1) * ZIM_INV_TWO_PI_F));
-                int n3 = m23 * p.f2, q3 = floor_div(n3, p.f23), r3i = n3 - q3 * p.f23;
+                int n3 = m23 * p.f2, q3 = floor_div(n3, p.f23, p.inv_f23), r3i = n3 - q3 * p.f23;
                 int k3 = q3 + (int)roundf(fmaf((float)r3i, p.inv_f23, fmaf(p23, p.f2_f23, -w2) * ZIM_INV_TWO_PI_F));
                 // (uphase2 f0 / f1 - 2 pi k) = (w1 f0 + 2 pi (k2 f0 - k f1)) / f1, same for 3
                 float r2 = fmaf((float)(k2 * p.f0 - k * p.f1), ZIM_TWO_PI_F, w1 * (float)p.f0) * p.inv_f1;
@@ -192,11 +201,16 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
                 r = (w0 + r2 + r3) * (1.0f / 3.0f);
             }
         } else if (p.enc == ZIM_ENC_HIERARCHICAL) {
-            for (int i = 1; i < p.n_ps; i++) {
-                float a = fmaf(p.fratio[i], wrap[i - 1] + ZIM_PI_F, -(wrap[i] + ZIM_PI_F)) * ZIM_INV_TWO_PI_F;
-                k = p.iratio[i] * k + (int)roundf(a);
+            const float wr[4] = {wrap0, wrap1, wrap2, wrap3};
+#pragma unroll
+            for (int i = 1; i < 4; i++) {
+                if (i < p.n_ps) {
+                    float a = fmaf(p.fratio[i], wr[i - 1] + ZIM_PI_F, -(wr[i] + ZIM_PI_F)) * ZIM_INV_TWO_PI_F;
+                    k = p.iratio[i] * k + (int)roundf(a);
+                    r = wr[i];
+                }
             }
-            r = wrap[p.n_ps - 1];
+            if (p.n_ps == 1) r = wrap0;
         } else {
             const int N = p.shift[0];
             int sum_raw = 0;
@@ -212,11 +226,11 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
                 int g = N * (int)__ldg(frames + (size_t)(p.gray_base + p.gray_bits) * npx + pix) > sum_raw ? 1 : 0;
                 int v2 = (v1 << 1) | (bin ^ g);
                 int k2 = (v2 + 1) >> 1;
-                float w = wrap[0];
+                float w = wrap0;
                 if (w <= -0.5f * ZIM_PI_F) k = k2;
                 else if (w >= 0.5f * ZIM_PI_F) k = k2 - 1;
             }
-            r = wrap[0];
+            r = wrap0;
         }
     }
     order[pix] = k;
@@ -284,6 +298,50 @@ __device__ __forceinline__ void rectify_pixel(const int32_t* __restrict__ order,
     }
     // phase = 2*pi*I/16384 + Rs; split I = 16384*base + frac, frac in [-8192, 8192)
     long long base = (I + 8192) >> 14;  // floor((I + 8192) / 16384)
+    int frac = (int)(I - (base << 14));
+    rbase = (int32_t)base;
+    rres = fmaf((float)frac, ZIM_TWO_PI_F / 16384.0f, Rs);
+    rorder = ko;
+}
+
+// The same remap from phase that was post-smoothed once per source pixel
+// (smooth_pixel: K16 = 16 x smoothed cycles, R = smoothed residual), so a
+// rectified pixel reads 4 taps instead of 4 x 9.  Identical results: the taps
+// hold exactly what smoothed_tap computes.
+__device__ __forceinline__ void smooth_pixel(const int32_t* __restrict__ order, const float* __restrict__ res, int rows,
+                                             int cols, int x, int y, int32_t* __restrict__ K16,
+                                             float* __restrict__ R) {
+    int k;
+    float r;
+    smoothed_tap(order, res, x, y, rows, cols, 1, k, r);
+    const size_t o = (size_t)y * cols + x;
+    K16[o] = k;
+    R[o] = r;
+}
+
+__device__ __forceinline__ void rectify_pixel_smoothed(const int32_t* __restrict__ K16, const float* __restrict__ Rs_,
+                                                       const int32_t* __restrict__ order, int srows, int scols,
+                                                       float mx, float my, int32_t& rbase, float& rres,
+                                                       int32_t& rorder) {
+    int nx = __float2int_rn(mx), ny = __float2int_rn(my);
+    int ko = 0;
+    if (nx >= 0 && ny >= 0 && nx < scols && ny < srows) ko = __ldg(order + (size_t)ny * scols + nx);
+    int sx = __float2int_rn(mx * 32.0f), sy = __float2int_rn(my * 32.0f);
+    int x0 = sx >> 5, y0 = sy >> 5;
+    int fx = sx & 31, fy = sy & 31;
+    long long I = 0;
+    float Rs = 0.f;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        int xx = x0 + (t & 1), yy = y0 + (t >> 1);
+        if (xx < 0 || yy < 0 || xx >= scols || yy >= srows) continue;
+        int wq = ((t >> 1) ? fy : 32 - fy) * ((t & 1) ? fx : 32 - fx);
+        if (wq == 0) continue;
+        const size_t o = (size_t)yy * scols + xx;
+        I += (long long)wq * __ldg(K16 + o);
+        Rs = fmaf((float)wq * (1.0f / 1024.0f), __ldg(Rs_ + o), Rs);
+    }
+    long long base = (I + 8192) >> 14;
     int frac = (int)(I - (base << 14));
     rbase = (int32_t)base;
     rres = fmaf((float)frac, ZIM_TWO_PI_F / 16384.0f, Rs);
@@ -531,32 +589,55 @@ __device__ __forceinline__ void px_gaussian_pixel(const float* __restrict__ xyz,
     if (mask_out) mask_out[o] = keep ? 1 : 0;
 }
 
-// Radius outlier filter at (x, y): keep if at least min_nb valid neighbours
-// (not self) of the (2 hw + 1)^2 window lie within sqrt(r2).
-__device__ __forceinline__ void ror_pixel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
-                                          int cols, int x, int y, float r2, int min_nb, int hw,
-                                          float* __restrict__ out, uint8_t* __restrict__ mask_out) {
-    size_t o = (size_t)y * cols + x;
-    bool keep = false;
-    float px = 0.f, py = 0.f, pz = 0.f;
-    if (mask[o]) {
-        keep = min_nb <= 0;
-        px = xyz[3 * o]; py = xyz[3 * o + 1]; pz = xyz[3 * o + 2];
-        int cnt = 0;
-        int r0 = max(0, y - hw), r1 = min(rows, y + hw + 1), c0 = max(0, x - hw), c1 = min(cols, x + hw + 1);
-        for (int i = r0; i < r1 && !keep; i++)
-            for (int j = c0; j < c1; j++) {
-                size_t q = (size_t)i * cols + j;
-                if (q == o || !__ldg(mask + q)) continue;
-                float dx = px - __ldg(xyz + 3 * q), dy = py - __ldg(xyz + 3 * q + 1), dz = pz - __ldg(xyz + 3 * q + 2);
-                if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= r2) {
-                    if (++cnt >= min_nb) { keep = true; break; }
-                }
-            }
+// Radius outlier filter over tile (bx, by) of RX x RY pixels with the RX * RY
+// threads of a block: keep a valid point if at least min_nb valid neighbours
+// (not itself) of its (2 hw + 1)^2 window lie within sqrt(r2).  The tile and
+// its hw halo are staged in shared memory (ror_smem_bytes) as float4 with
+// invalid and off-image pixels NaN, so a neighbour test is one shared load
+// and an FP32 distance that compares false for NaN.  The point itself passes
+// its own test (distance 0), so the count including it must reach
+// min_nb + 1.  Ends past the last shared read.
+inline size_t ror_smem_bytes(int hw) { return (size_t)(RX + 2 * hw) * (RY + 2 * hw) * sizeof(float4); }
+
+__device__ __forceinline__ void ror_tile(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
+                                         int cols, int bx, int by, int tid, float r2, int min_nb, int hw, float4* sp,
+                                         float* __restrict__ out, uint8_t* __restrict__ mask_out) {
+    const int TW = RX + 2 * hw, TH = RY + 2 * hw;
+    const int gx0 = bx * RX - hw, gy0 = by * RY - hw;
+    for (int t = tid; t < TW * TH; t += RX * RY) {
+        const int ty = t / TW, tx = t - ty * TW;
+        const int gx = gx0 + tx, gy = gy0 + ty;
+        float4 v = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+        if (gx >= 0 && gy >= 0 && gx < cols && gy < rows) {
+            const size_t q = (size_t)gy * cols + gx;
+            if (__ldg(mask + q)) v = make_float4(__ldg(xyz + 3 * q), __ldg(xyz + 3 * q + 1), __ldg(xyz + 3 * q + 2), 1.f);
+        }
+        sp[t] = v;
     }
-    out[3 * o] = keep ? px : 0.f;
-    out[3 * o + 1] = keep ? py : 0.f;
-    out[3 * o + 2] = keep ? pz : 0.f;
+    __syncthreads();
+    const int tx = tid % RX, ty = tid / RX;
+    const int x = bx * RX + tx, y = by * RY + ty;
+    const float4 c = sp[(ty + hw) * TW + tx + hw];
+    bool keep = false;
+    if (x < cols && y < rows && c.w != 0.f) {
+        keep = min_nb <= 0;
+        int cnt = 0;
+        for (int i = 0; i <= 2 * hw && !keep; i++) {
+            const float4* row = sp + (ty + i) * TW + tx;
+            for (int j = 0; j <= 2 * hw; j++) {
+                const float4 p = row[j];
+                const float dx = c.x - p.x, dy = c.y - p.y, dz = c.z - p.z;
+                cnt += fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= r2 ? 1 : 0;
+            }
+            keep = cnt >= min_nb + 1;
+        }
+    }
+    __syncthreads();
+    if (x >= cols || y >= rows) return;
+    const size_t o = (size_t)y * cols + x;
+    out[3 * o] = keep ? c.x : 0.f;
+    out[3 * o + 1] = keep ? c.y : 0.f;
+    out[3 * o + 2] = keep ? c.z : 0.f;
     mask_out[o] = keep ? 1 : 0;
 }
 
