@@ -100,28 +100,23 @@ __device__ bool cholesky_solve(float A[6][6], const float b[6], float x[6], int 
     return true;
 }
 
-__global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ src, const uint8_t* __restrict__ mask,
-                                                     int rows, int cols, int hw, float inv_2s2, int order, float r2c,
-                                                     float* __restrict__ dst) {
-    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
-    if (x >= cols || y >= rows) return;
-    const size_t o = (size_t)y * cols + x;
-    const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
-    dst[3 * o] = px;
-    dst[3 * o + 1] = py;
-    dst[3 * o + 2] = pz;
-    if (!mask[o]) return;
+// MLS of one valid point at pixel (x, y).  nb(i, j, dx, dy, dz) yields the
+// offset of the neighbour at pixel (i, j) from the query point and whether it
+// is a valid point; the window runs row-major over the pixels of the image.
+template <typename Nb>
+__device__ __forceinline__ void mls_point(int x, int y, int rows, int cols, int hw, float inv_2s2, int order,
+                                          float r2c, Nb nb, float& ox, float& oy, float& oz, bool& moved) {
+    moved = false;
     const int r0 = max(0, y - hw), r1 = min(rows, y + hw + 1), c0 = max(0, x - hw), c1 = min(cols, x + hw + 1);
     // 1. weighted centroid (relative to p)
     float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
     int nv = 0;
     for (int i = r0; i < r1; i++)
         for (int j = c0; j < c1; j++) {
-            size_t q = (size_t)i * cols + j;
-            if (!__ldg(mask + q)) continue;
-            float dx = __ldg(src + 3 * q) - px, dy = __ldg(src + 3 * q + 1) - py, dz = __ldg(src + 3 * q + 2) - pz;
+            float dx, dy, dz;
+            if (!nb(i, j, dx, dy, dz)) continue;
             float d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 > r2c) continue;
+            if (!(d2 <= r2c)) continue;
             float w = __expf(-d2 * inv_2s2);
             cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
             ws += w;
@@ -134,11 +129,10 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     float C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     for (int i = r0; i < r1; i++)
         for (int j = c0; j < c1; j++) {
-            size_t q = (size_t)i * cols + j;
-            if (!__ldg(mask + q)) continue;
-            float dx = __ldg(src + 3 * q) - px, dy = __ldg(src + 3 * q + 1) - py, dz = __ldg(src + 3 * q + 2) - pz;
+            float dx, dy, dz;
+            if (!nb(i, j, dx, dy, dz)) continue;
             float d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 > r2c) continue;
+            if (!(d2 <= r2c)) continue;
             float w = __expf(-d2 * inv_2s2);
             float ex = dx - cx, ey = dy - cy, ez = dz - cz;
             C[0][0] = fmaf(w * ex, ex, C[0][0]); C[0][1] = fmaf(w * ex, ey, C[0][1]); C[0][2] = fmaf(w * ex, ez, C[0][2]);
@@ -175,7 +169,6 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     int cur = nv >= min_nb ? order : 0;
     // query point relative to the centroid: e0 = p - c = -c_rel
     const float ex0 = -cx, ey0 = -cy, ez0 = -cz;
-    float ox, oy, oz;  // correction added to p
     bool solved = false;
     float co[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
@@ -189,17 +182,18 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     if (cur > 0) {
         const int nc = cur == 1 ? 3 : 6;
         float A[6][6], bv[6];
+#pragma unroll
         for (int a = 0; a < 6; a++) {
             bv[a] = 0.f;
+#pragma unroll
             for (int b = 0; b < 6; b++) A[a][b] = 0.f;
         }
         for (int i = r0; i < r1; i++)
             for (int j = c0; j < c1; j++) {
-                size_t q = (size_t)i * cols + j;
-                if (!__ldg(mask + q)) continue;
-                float dx = __ldg(src + 3 * q) - px, dy = __ldg(src + 3 * q + 1) - py, dz = __ldg(src + 3 * q + 2) - pz;
+                float dx, dy, dz;
+                if (!nb(i, j, dx, dy, dz)) continue;
                 float d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 > r2c) continue;
+                if (!(d2 <= r2c)) continue;
                 float w = __expf(-d2 * inv_2s2);
                 float ex = dx - cx, ey = dy - cy, ez = dz - cz;
                 float u = (ex * t1x + ey * t1y + ez * t1z) * is;
@@ -208,12 +202,13 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
                 float bs[6] = {1.f, u, v, u * u, u * v, v * v};
 #pragma unroll
                 for (int a = 0; a < 6; a++) {
-                    if (a >= nc) break;
-                    float wa = w * bs[a];
-                    bv[a] = fmaf(wa, f, bv[a]);
+                    if (a < nc) {
+                        float wa = w * bs[a];
+                        bv[a] = fmaf(wa, f, bv[a]);
 #pragma unroll
-                    for (int b = 0; b < 6; b++)
-                        if (b >= a && b < nc) A[a][b] = fmaf(wa, bs[b], A[a][b]);
+                        for (int b = 0; b < 6; b++)
+                            if (b >= a && b < nc) A[a][b] = fmaf(wa, bs[b], A[a][b]);
+                    }
                 }
             }
         for (int a = 0; a < nc; a++)
@@ -243,9 +238,74 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
         oy = cy + u0 * t1y + v0 * t2y + ff * ny;
         oz = cz + u0 * t1z + v0 * t2z + ff * nz;
     }
-    dst[3 * o] = px + ox;
-    dst[3 * o + 1] = py + oy;
-    dst[3 * o + 2] = pz + oz;
+    moved = true;
+}
+
+// Neighbours straight from global memory (windows too wide for shared memory).
+__global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ src, const uint8_t* __restrict__ mask,
+                                                     int rows, int cols, int hw, float inv_2s2, int order, float r2c,
+                                                     float* __restrict__ dst) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= cols || y >= rows) return;
+    const size_t o = (size_t)y * cols + x;
+    const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    bool moved = false;
+    if (mask[o]) {
+        auto nb = [&](int i, int j, float& dx, float& dy, float& dz) {
+            const size_t q = (size_t)i * cols + j;
+            if (!__ldg(mask + q)) return false;
+            dx = __ldg(src + 3 * q) - px; dy = __ldg(src + 3 * q + 1) - py; dz = __ldg(src + 3 * q + 2) - pz;
+            return true;
+        };
+        mls_point(x, y, rows, cols, hw, inv_2s2, order, r2c, nb, ox, oy, oz, moved);
+    }
+    dst[3 * o] = moved ? px + ox : px;
+    dst[3 * o + 1] = moved ? py + oy : py;
+    dst[3 * o + 2] = moved ? pz + oz : pz;
+}
+
+// The tile and its hw halo staged in shared memory as float4, NaN for invalid
+// and off-image pixels (their distance test fails).
+inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * hw) * sizeof(float4); }
+
+__global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restrict__ src,
+                                                          const uint8_t* __restrict__ mask, int rows, int cols, int hw,
+                                                          float inv_2s2, int order, float r2c,
+                                                          float* __restrict__ dst) {
+    extern __shared__ float4 mls_sp[];
+    const int TW = MX + 2 * hw, TH = MY + 2 * hw;
+    const int gx0 = blockIdx.x * MX - hw, gy0 = blockIdx.y * MY - hw;
+    const int tid = threadIdx.y * MX + threadIdx.x;
+    for (int t = tid; t < TW * TH; t += MX * MY) {
+        const int ty = t / TW, tx = t - ty * TW;
+        const int gx = gx0 + tx, gy = gy0 + ty;
+        float4 v = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+        if (gx >= 0 && gy >= 0 && gx < cols && gy < rows) {
+            const size_t q = (size_t)gy * cols + gx;
+            if (__ldg(mask + q)) v = make_float4(__ldg(src + 3 * q), __ldg(src + 3 * q + 1), __ldg(src + 3 * q + 2), 1.f);
+        }
+        mls_sp[t] = v;
+    }
+    __syncthreads();
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= cols || y >= rows) return;
+    const size_t o = (size_t)y * cols + x;
+    const float4 c = mls_sp[(threadIdx.y + hw) * TW + threadIdx.x + hw];
+    const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    bool moved = false;
+    if (c.w != 0.f) {
+        auto nb = [&](int i, int j, float& dx, float& dy, float& dz) {
+            const float4 q = mls_sp[(i - gy0) * TW + (j - gx0)];
+            dx = q.x - px; dy = q.y - py; dz = q.z - pz;
+            return true;  // invalid neighbours are NaN and fail the distance test
+        };
+        mls_point(x, y, rows, cols, hw, inv_2s2, order, r2c, nb, ox, oy, oz, moved);
+    }
+    dst[3 * o] = moved ? px + ox : px;
+    dst[3 * o + 1] = moved ? py + oy : py;
+    dst[3 * o + 2] = moved ? pz + oz : pz;
 }
 
 }  // namespace
@@ -260,12 +320,19 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const int ord = order < 0 ? 0 : (order > 2 ? 2 : order);
     const int n_iter = iterations < 1 ? 1 : iterations;
     dim3 blk(MX, MY), grd((cols + MX - 1) / MX, (rows + MY - 1) / MY);
+    const size_t smem = mls_smem_bytes(window);
+    const bool use_smem = smem <= 96 * 1024;
+    if (use_smem)
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(mls_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // ping-pong so that the last pass lands in `out`
     const float* in = xyz;
     for (int it = 0; it < n_iter; it++) {
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
-        mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
+        if (use_smem)
+            mls_smem_kernel<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
+        else
+            mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;
         ZIM_LAUNCH_CHECK(ctx);
         in = dst;
