@@ -74,7 +74,8 @@ typedef struct zim_decode_config {
     double preblur_sigma;        /* 3x3 pre-blur sigma, default 3.0 (<= 0: OpenCV default kernel) */
     int avg_three_phase;         /* default 1 (heterodyne only) */
     int post_smooth;             /* default 1: 3x3 Gaussian of the absolute phase */
-    int enable_hdr;              /* default 0; 1 is not implemented (ZIM_ERR_UNSUPPORTED) */
+    int enable_hdr;              /* default 0; 1: HDR least squares on raw samples (heterodyne,
+                                    hierarchical; JSLAB_HDRPhaseFit.h), invalid orders -1 */
     double hdr_saturation_gray;
     double hdr_min_amplitude;
     int encoding;                /* zim_encoding, default ZIM_ENC_HETERODYNE3 */
@@ -181,7 +182,11 @@ ZIM_API zim_status zim_get_rectify_maps(zim_ctx* ctx, int cam, float* mapx, floa
 
 /* setData for one camera (JSLAB_PhaseEpipolarReconstructor_V2.cpp:368-395):
  * post-smooth (optional) + remap INTER_LINEAR of the phase, INTER_NEAREST of
- * the order.  Rectified phase = 2*pi*rect_base + rect_res (rect_h*rect_w). */
+ * the order.  Rectified phase = 2*pi*rect_base + rect_res (rect_h*rect_w).
+ * post_smooth (also for zim_decode_phase_f64): 0 none, 1 the 3x3 Gaussian;
+ * for an HDR decode (invalid pixels carry order -1 and phase 0) 2 the HDR
+ * post-smooth (blur normalised by the blurred validity,
+ * JSLAB_PhaseShiftDecoder_V2.cpp:280-291) and 3 none. */
 ZIM_API zim_status zim_rectify(zim_ctx* ctx, int cam, const int32_t* order, const float* residual,
                                int rows, int cols, int post_smooth, int32_t* rect_base,
                                float* rect_res, int32_t* rect_order, void* stream);

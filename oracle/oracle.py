@@ -45,7 +45,8 @@ def build() -> Path:
 class DecodeCfg(C.Structure):
     _fields_ = [("encoding", C.c_int), ("n_freq", C.c_int), ("freq", C.c_double * 4), ("shift_num", C.c_int * 4),
                 ("gray_bits", C.c_int), ("modulation_threshold", C.c_double), ("preblur_sigma", C.c_double),
-                ("avg_three_phase", C.c_int), ("post_smooth", C.c_int)]
+                ("avg_three_phase", C.c_int), ("post_smooth", C.c_int), ("enable_hdr", C.c_int),
+                ("hdr_saturation_gray", C.c_double), ("hdr_min_amplitude", C.c_double)]
 
 
 class Calib(C.Structure):
@@ -73,7 +74,8 @@ def _c(a, dtype):
 
 
 def make_decode_cfg(encoding=ENC_HETERODYNE3, freq=(121, 110, 120), shift_num=(8, 8, 8), gray_bits=0,
-                    modulation_threshold=1.0, preblur_sigma=3.0, avg_three_phase=True, post_smooth=True, n_freq=None):
+                    modulation_threshold=1.0, preblur_sigma=3.0, avg_three_phase=True, post_smooth=True, n_freq=None,
+                    enable_hdr=False, hdr_saturation_gray=255.0, hdr_min_amplitude=2.0):
     c = DecodeCfg()
     c.encoding = encoding
     c.n_freq = n_freq if n_freq is not None else (3 if encoding == ENC_HETERODYNE3 else
@@ -87,6 +89,9 @@ def make_decode_cfg(encoding=ENC_HETERODYNE3, freq=(121, 110, 120), shift_num=(8
     c.preblur_sigma = preblur_sigma
     c.avg_three_phase = int(bool(avg_three_phase))
     c.post_smooth = int(bool(post_smooth))
+    c.enable_hdr = int(bool(enable_hdr))
+    c.hdr_saturation_gray = float(hdr_saturation_gray)
+    c.hdr_min_amplitude = float(hdr_min_amplitude)
     return c
 
 
@@ -141,6 +146,14 @@ def post_smooth(phase):
     phase = _c(phase, np.float64)
     out = np.empty_like(phase)
     lib().zo_post_smooth(_p(phase), _p(out), C.c_int(phase.shape[0]), C.c_int(phase.shape[1]))
+    return out
+
+
+def post_smooth_hdr(phase, valid):
+    phase = _c(phase, np.float64)
+    valid = _c(valid, np.uint8)
+    out = np.empty_like(phase)
+    lib().zo_post_smooth_hdr(_p(phase), _p(valid), _p(out), C.c_int(phase.shape[0]), C.c_int(phase.shape[1]))
     return out
 
 
@@ -350,7 +363,11 @@ def _setup_prototypes():
     L.zo_frame_count.restype = C.c_int
 
 
-def rectify_decoded(phase_unsmoothed, order, mapx, mapy, post):
-    """setData for one camera: optional post-smooth, remap linear / nearest."""
-    ph = post_smooth(phase_unsmoothed) if post else phase_unsmoothed
+def rectify_decoded(phase_unsmoothed, order, mapx, mapy, post, hdr_valid=None):
+    """setData for one camera: optional post-smooth (HDR form when the decode
+    validity is given), remap linear / nearest."""
+    if post:
+        ph = post_smooth_hdr(phase_unsmoothed, hdr_valid) if hdr_valid is not None else post_smooth(phase_unsmoothed)
+    else:
+        ph = phase_unsmoothed
     return remap_linear(ph, mapx, mapy), remap_nearest(order, mapx, mapy)

@@ -66,8 +66,9 @@ def run_pair(decode_kwargs, pha_f, L, R, rect: Rectification, f: Filters = Filte
     cfg = O.make_decode_cfg(**decode_kwargs)
     r = []
     for cam, fr in enumerate((L, R)):
-        ph, k, _, _, _ = O.decode(cfg, fr)
-        r.append(O.rectify_decoded(ph, k, *rect.maps[cam], bool(cfg.post_smooth)))
+        ph, k, _, valid, _ = O.decode(cfg, fr)
+        r.append(O.rectify_decoded(ph, k, *rect.maps[cam], bool(cfg.post_smooth),
+                                   valid if cfg.enable_hdr else None))
     disp, _, _ = O.stereo_match(r[0][0], r[1][0], r[0][1], r[1][1], pha_f)
     d32 = disp.astype(np.float32)
     dm = O.median5(d32) if f.use_median else d32
@@ -86,8 +87,8 @@ def run_band(decode_kwargs, pha_f, L, R, rect: Rectification, y0: int, y1: int, 
         mxb, myb = mx[ya:yb], my[ya:yb]
         lo = int(max(0, math.floor(np.nanmin(myb)) - 3))
         hi = int(min(fr.shape[1], math.ceil(np.nanmax(myb)) + 4))
-        ph, k, _, _, _ = O.decode(cfg, np.ascontiguousarray(fr[:, lo:hi]))
-        r.append(O.rectify_decoded(ph, k, mxb, myb - lo, bool(cfg.post_smooth)))
+        ph, k, _, valid, _ = O.decode(cfg, np.ascontiguousarray(fr[:, lo:hi]))
+        r.append(O.rectify_decoded(ph, k, mxb, myb - lo, bool(cfg.post_smooth), valid if cfg.enable_hdr else None))
     disp, _, _ = O.stereo_match(r[0][0], r[1][0], r[0][1], r[1][1], pha_f)
     d32 = disp.astype(np.float32)
     dm = O.median5(d32) if f.use_median else d32

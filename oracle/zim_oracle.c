@@ -100,6 +100,47 @@ static double wrapped_phase(const double* const* fr, size_t pix, int inum, doubl
     return norm_mod;
 }
 
+/* HDR least squares of one frequency (JSLAB_HDRPhaseFit.h:10-61 applied as in
+ * JSLAB_PhaseShiftDecoder_V2.cpp:73-90): samples with 0 <= I < saturation fit
+ * I = A + C cos d - S sin d; the reference multiplies a cached pseudo-inverse
+ * of the subset's design, restated here as the normal equations of the same
+ * full-rank subset (the same least-squares solution).  Rejects fewer than 3
+ * samples, hypot(C, S) <= min_amp or A <= 1e-3.  Returns the normalised
+ * modulation (-1 if rejected); writes wrap. */
+static double hdr_wrapped_phase(const double* const* fr, size_t pix, int inum, double sat, double min_amp,
+                                double* wrap, uint8_t* nf, double eps) {
+    double M[3][3] = {{0}}, r[3] = {0};
+    int n = 0;
+    for (int k = 0; k < inum; k++) {
+        const double v = fr[k][pix];
+        if (!(v >= 0.0 && v < sat)) continue;
+        const double d = 2.0 * ZO_PI * k / inum;
+        const double x[3] = {1.0, cos(d), -sin(d)};
+        for (int a = 0; a < 3; a++) {
+            r[a] += x[a] * v;
+            for (int b = 0; b < 3; b++) M[a][b] += x[a] * x[b];
+        }
+        n++;
+    }
+    if (n < 3) return -1.0;
+    const double c00 = M[1][1] * M[2][2] - M[1][2] * M[2][1], c01 = M[0][2] * M[2][1] - M[0][1] * M[2][2],
+                 c02 = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+    const double det = M[0][0] * c00 + M[0][1] * c01 + M[0][2] * c02;
+    if (!(fabs(det) > 1e-10)) return -1.0;
+    const double c11 = M[0][0] * M[2][2] - M[0][2] * M[2][0], c12 = M[0][2] * M[1][0] - M[0][0] * M[1][2],
+                 c22 = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+    const double A = (c00 * r[0] + c01 * r[1] + c02 * r[2]) / det;
+    const double C = (c01 * r[0] + c11 * r[1] + c12 * r[2]) / det;
+    const double S = (c02 * r[0] + c12 * r[1] + c22 * r[2]) / det;
+    if (fabs(hypot(C, S) - min_amp) < eps * (1.0 + min_amp)) *nf |= ZO_NEAR_MOD;
+    if (!(hypot(C, S) > min_amp) || !(A > 1e-3)) return -1.0;
+    const double cos_sum = C * inum / 2.0, sin_sum = S * inum / 2.0, sum_gray = A * inum;
+    *wrap = atan2(sin_sum, cos_sum);
+    const double b = 2.0 * sqrt(sin_sum * sin_sum + cos_sum * cos_sum) / inum;
+    const double mean_val = sum_gray / inum;
+    return mean_val > 1e-3 ? b / mean_val : 0.0;
+}
+
 static inline uint8_t wrap_flag(double w, double eps) { return (ZO_PI - fabs(w) < eps) ? ZO_NEAR_WRAP : 0; }
 
 int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols, double* phase,
@@ -120,7 +161,12 @@ int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols
     double kb[3];
     zo_gaussian_kernel3(cfg->preblur_sigma, kb);
     double* blurred = (double*)malloc(sizeof(double) * npx * n_blur);
-    for (int f = 0; f < n_blur; f++) zo_blur3(frames + npx * f, blurred + npx * f, rows, cols, kb);
+    const int hdr = cfg->enable_hdr && (cfg->encoding == ZO_ENC_HETERODYNE3 || cfg->encoding == ZO_ENC_HIERARCHICAL);
+    for (int f = 0; f < n_blur; f++) {
+        /* HDR classifies saturation on the raw samples: no pre-blur */
+        if (hdr) memcpy(blurred + npx * f, frames + npx * f, sizeof(double) * npx);
+        else zo_blur3(frames + npx * f, blurred + npx * f, rows, cols, kb);
+    }
 
     const double TWO_PI = 2 * ZO_PI;
 #pragma omp parallel for schedule(dynamic, 4)
@@ -136,7 +182,14 @@ int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols
                 const int inum = cfg->shift_num[i];
                 for (int k = 0; k < inum; k++) fr[k] = blurred + npx * (base + k);
                 base += inum;
-                double nm = wrapped_phase(fr, pix, inum, &wrap[i]);
+                double nm;
+                if (hdr) {
+                    nm = hdr_wrapped_phase(fr, pix, inum, cfg->hdr_saturation_gray, cfg->hdr_min_amplitude, &wrap[i],
+                                           &nf, eps);
+                    if (nm < 0) { ok = 0; break; }
+                } else {
+                    nm = wrapped_phase(fr, pix, inum, &wrap[i]);
+                }
                 nf |= wrap_flag(wrap[i], eps);
                 if (fabs(nm - cfg->modulation_threshold) < eps) nf |= ZO_NEAR_MOD;
                 if (i == 0) m0 = nm;
@@ -144,7 +197,7 @@ int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols
             }
             mod[pix] = m0;
             phase[pix] = 0.0;
-            order[pix] = 0;
+            order[pix] = hdr ? -1 : 0;
             valid[pix] = 0;
             if (!ok) { if (near) near[pix] = nf; continue; }
 
@@ -236,6 +289,20 @@ int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols
     }
     free(blurred);
     return 0;
+}
+
+void zo_post_smooth_hdr(const double* src, const uint8_t* valid, double* dst, int rows, int cols) {
+    double k[3];
+    zo_gaussian_kernel3(0.0, k);
+    const size_t n = (size_t)rows * cols;
+    double* w = (double*)malloc(sizeof(double) * n);
+    double* bw = (double*)malloc(sizeof(double) * n);
+    for (size_t i = 0; i < n; i++) w[i] = valid[i] ? 1.0 : 0.0;
+    zo_blur3(src, dst, rows, cols, k);
+    zo_blur3(w, bw, rows, cols, k);
+    for (size_t i = 0; i < n; i++) dst[i] = valid[i] ? dst[i] / (bw[i] > 1e-12 ? bw[i] : 1e-12) : 0.0;
+    free(w);
+    free(bw);
 }
 
 void zo_post_smooth(const double* src, double* dst, int rows, int cols) {

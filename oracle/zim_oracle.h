@@ -45,6 +45,9 @@ typedef struct {
     double preblur_sigma;  /* 3x3 Gaussian pre-blur sigma (<=0: OpenCV default) */
     int avg_three_phase;
     int post_smooth;
+    int enable_hdr;        /* HDR least squares on raw samples (heterodyne / hierarchical) */
+    double hdr_saturation_gray;
+    double hdr_min_amplitude;
 } zo_decode_cfg;
 
 /* getGaussianKernel(3, sigma) (OpenCV imgproc, documented formula). */
@@ -57,14 +60,19 @@ void zo_blur3(const double* src, double* dst, int rows, int cols, const double k
 int zo_frame_count(const zo_decode_cfg* cfg);
 
 /* Decode one camera.  frames: F planes of rows*cols sample values.
- * phase = unsmoothed absolute phase (0 where invalid), order, mod (frequency-0
- * normalised modulation), valid (1/0), near (ZO_NEAR_* bits; may be NULL). */
+ * phase = unsmoothed absolute phase (0 where invalid), order (-1 where invalid
+ * with HDR, else 0), mod (frequency-0 normalised modulation), valid (1/0),
+ * near (ZO_NEAR_* bits; may be NULL).  With enable_hdr the phase-shift frames
+ * are not pre-blurred and each frequency is an HDR least-squares fit. */
 int zo_decode(const zo_decode_cfg* cfg, const double* frames, int rows, int cols,
               double* phase, int32_t* order, double* mod, uint8_t* valid, uint8_t* near,
               double eps);
 
 /* Post-decode smoothing: GaussianBlur(3x3, sigma 0) with BORDER_REPLICATE. */
 void zo_post_smooth(const double* src, double* dst, int rows, int cols);
+/* HDR post-smooth: the blur of the phase divided by the blur of the validity
+ * (clamped at 1e-12), 0 where invalid (JSLAB_PhaseShiftDecoder_V2.cpp:280-291). */
+void zo_post_smooth_hdr(const double* src, const uint8_t* valid, double* dst, int rows, int cols);
 
 /* ---- calibration / rectification (FP64) ---- */
 typedef struct {

@@ -61,7 +61,11 @@ def test_validate_like_reference_factory(native):
     for bad in ((0, 100, 94), (107, 0, 94), (107, 100, 0)):
         c = api.decode_config(freq=bad)
         assert L.zim_decode_validate(C.byref(c)) == _lib.ERR_INVALID_ARG
-    c = api.decode_config(enable_hdr=True)
+    c = api.decode_config(enable_hdr=True)  # HDR least squares: heterodyne and hierarchical
+    assert L.zim_decode_validate(C.byref(c)) == _lib.OK
+    c = api.decode_config(enable_hdr=True, shift_num=(13, 8, 8))  # the reference fit takes 3..12 steps
+    assert L.zim_decode_validate(C.byref(c)) == _lib.ERR_INVALID_ARG
+    c = api.decode_config(encoding=api.ENC_GRAYCODE, freq=(32,), shift_num=(4,), gray_bits=5, enable_hdr=True)
     assert L.zim_decode_validate(C.byref(c)) == _lib.ERR_UNSUPPORTED
     c = api.decode_config(shift_num=(2, 8, 8))
     assert L.zim_decode_validate(C.byref(c)) == _lib.ERR_INVALID_ARG

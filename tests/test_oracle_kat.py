@@ -69,6 +69,59 @@ def test_single_pixel_heterodyne(freqs):
         assert abs(ph[1, 1] - TWO_PI * freqs[0] * x) < 1e-9
 
 
+def test_hdr_least_squares_recovers_clipped_pixels():
+    """JSLAB_HDRPhaseFit semantics: samples at or above the saturation grey are
+    dropped and A + C cos d - S sin d is fitted to the rest, so a bright pixel
+    whose peaks clip still decodes exactly, where the plain sums are biased."""
+    rng = np.random.default_rng(1)
+    freqs = (121, 110, 120)
+    n_exact = 0
+    for x in rng.uniform(0.002, 0.998, 100):
+        raw = frames_for(np.array([x]), 200.0, 100.0, freqs, (8, 8, 8), 0.0)
+        clipped = np.minimum(raw, 255.0)  # 8-bit sensor: peaks saturate
+        img = np.repeat(np.repeat(clipped, 3, 1), 3, 2)
+        cfg = O.make_decode_cfg(O.ENC_HETERODYNE3, freqs, (8, 8, 8), modulation_threshold=0.3, enable_hdr=True,
+                                hdr_saturation_gray=255.0, hdr_min_amplitude=2.0)
+        ph, k, mod, valid, _ = O.decode(cfg, img)
+        assert valid[1, 1] == 1
+        assert k[1, 1] == round(121 * x)
+        assert abs(ph[1, 1] - TWO_PI * 121 * x) < 1e-9
+        assert abs(mod[1, 1] - 0.5) < 1e-9
+        n_exact += 1
+    assert n_exact == 100
+
+
+def test_hdr_rejects_and_marks_invalid_orders():
+    # all samples saturated -> fewer than three usable: invalid, order -1
+    img = np.full((24, 3, 3), 255.0)
+    cfg = O.make_decode_cfg(O.ENC_HETERODYNE3, (121, 110, 120), (8, 8, 8), modulation_threshold=0.3,
+                            enable_hdr=True, hdr_saturation_gray=255.0)
+    ph, k, mod, valid, _ = O.decode(cfg, img)
+    assert (valid == 0).all() and (k == -1).all() and (ph == 0).all()
+    # amplitude at the threshold is rejected (hypot(C, S) <= min_amp)
+    x = np.array([0.3])
+    img = np.repeat(np.repeat(frames_for(x, 100.0, 2.0, (121, 110, 120), (8, 8, 8), 0.0), 3, 1), 3, 2)
+    cfg = O.make_decode_cfg(O.ENC_HETERODYNE3, (121, 110, 120), (8, 8, 8), modulation_threshold=0.0,
+                            enable_hdr=True, hdr_min_amplitude=2.0 + 1e-9)
+    _, k, _, valid, _ = O.decode(cfg, img)
+    assert valid[1, 1] == 0 and k[1, 1] == -1
+
+
+def test_hdr_post_smooth_normalises_by_validity():
+    ph = np.arange(25, dtype=float).reshape(5, 5) + 100.0
+    valid = np.ones((5, 5), np.uint8)
+    valid[2, 3] = 0
+    ph[2, 3] = 0.0
+    out = O.post_smooth_hdr(ph, valid)
+    k = np.array([0.25, 0.5, 0.25])
+    pad = np.pad(ph, 1, mode="edge")
+    padv = np.pad(valid.astype(float), 1, mode="edge")
+    num = sum(k[a] * k[b] * pad[a:a + 5, b:b + 5] for a in range(3) for b in range(3))
+    den = sum(k[a] * k[b] * padv[a:a + 5, b:b + 5] for a in range(3) for b in range(3))
+    ref = np.where(valid > 0, num / den, 0.0)
+    assert np.allclose(out, ref, rtol=0, atol=1e-12)
+
+
 def test_hierarchical_1_8_64():
     for x in np.linspace(0.001, 0.999, 301):
         img = np.repeat(np.repeat(frames_for(np.array([x]), 2000.0, 1500.0, (1, 8, 64), (4, 4, 4), math.pi), 3, 1), 3,

@@ -189,11 +189,13 @@ def decode(ctx: Context, cfg, frames: torch.Tensor, want_mod=True, want_valid=Tr
     return dict(order=order, residual=res, mod=mod, valid=valid)
 
 
-def decode_phase_f64(ctx: Context, order, residual, post_smooth=True):
+def decode_phase_f64(ctx: Context, order, residual, post_smooth=True, hdr=False):
+    """startCalculate's CV_64F phase: 2 pi order + residual, optionally
+    post-smoothed (the HDR form for an HDR decode, whose invalid orders are -1)."""
     H, W = order.shape
     out = torch.empty((H, W), dtype=torch.float64, device=order.device)
-    ctx.check(_lib.load().zim_decode_phase_f64(ctx.h, _p(order), _p(residual), H, W, int(bool(post_smooth)), _p(out),
-                                               _stream()))
+    mode = (2 if post_smooth else 3) if hdr else (1 if post_smooth else 0)
+    ctx.check(_lib.load().zim_decode_phase_f64(ctx.h, _p(order), _p(residual), H, W, mode, _p(out), _stream()))
     return out
 
 
@@ -418,7 +420,8 @@ class JSLAB_PhaseShiftDecoderV2_GPU(JSLAB_PhaseShiftDecoder):
             raise ZimError(_lib.ERR_INVALID_ARG, "setImages first")
         d = decode(self._ctx, self._cfg, self._frames)
         self._dec = DecodedPhase(d["order"], d["residual"], d["mod"], d["valid"], bool(self.m_config.post_smooth))
-        return decode_phase_f64(self._ctx, d["order"], d["residual"], self.m_config.post_smooth)
+        return decode_phase_f64(self._ctx, d["order"], d["residual"], self.m_config.post_smooth,
+                                self.m_config.enable_hdr)
 
     def getOrderMap(self) -> torch.Tensor:
         return self._dec.order.clone()

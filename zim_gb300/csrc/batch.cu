@@ -119,8 +119,11 @@ __global__ void __launch_bounds__(BT) batch_smooth_kernel(const PairDev* __restr
         for (int ty = w.z; ty < w.z + w.w; ty++)
             for (int tx = 0; tx < tiles_x; tx++) {
                 const int x = tx * zt::DX + tid % zt::DX, y = ty * zt::DY + tid / zt::DX;
-                if (x < P.cols && y < P.rows) zt::smooth_pixel(P.order[w.y], P.res[w.y], P.rows, P.cols, x, y,
-                                                               P.sk[w.y], P.sr[w.y]);
+                if (x >= P.cols || y >= P.rows) continue;
+                if (P.post_smooth == 2)
+                    zt::smooth_pixel_hdr(P.order[w.y], P.res[w.y], P.rows, P.cols, x, y, P.sk[w.y], P.sr[w.y]);
+                else
+                    zt::smooth_pixel(P.order[w.y], P.res[w.y], P.rows, P.cols, x, y, P.sk[w.y], P.sr[w.y]);
             }
         __syncthreads();
     }
@@ -151,12 +154,12 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
             for (int j = tid; j < cols; j += BT) {
                 int32_t b, o;
                 float r;
-                if (P.post_smooth)
+                if (P.post_smooth == 1 || P.post_smooth == 2)
                     zt::rectify_pixel_smoothed(P.sk[1], P.sr[1], P.order[1], P.rows, P.cols,
                                                __ldg(P.map[1][0] + ro + j), __ldg(P.map[1][1] + ro + j), b, r, o);
                 else
                     zt::rectify_pixel(P.order[1], P.res[1], P.rows, P.cols, __ldg(P.map[1][0] + ro + j),
-                                      __ldg(P.map[1][1] + ro + j), 0, b, r, o);
+                                      __ldg(P.map[1][1] + ro + j), P.post_smooth, b, r, o);
                 s_ord[j] = o;
                 s_base[j] = b;
                 s_res[j] = r;
@@ -167,12 +170,12 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
             for (int j = tid; j < cols; j += BT) {
                 int32_t bL, kL;
                 float rL;
-                if (P.post_smooth)
+                if (P.post_smooth == 1 || P.post_smooth == 2)
                     zt::rectify_pixel_smoothed(P.sk[0], P.sr[0], P.order[0], P.rows, P.cols,
                                                __ldg(P.map[0][0] + ro + j), __ldg(P.map[0][1] + ro + j), bL, rL, kL);
                 else
                     zt::rectify_pixel(P.order[0], P.res[0], P.rows, P.cols, __ldg(P.map[0][0] + ro + j),
-                                      __ldg(P.map[0][1] + ro + j), 0, bL, rL, kL);
+                                      __ldg(P.map[0][1] + ro + j), P.post_smooth, bL, rL, kL);
                 float d;
                 int best;
                 zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, cols, pha_f, P.grad_threshold, d,
@@ -310,7 +313,7 @@ void build_items(const zim_batch* b, const zim_batch_tuning& t, std::vector<int4
             for (int r = 0; r < trows; r += t.decode_rows) {
                 const int4 it = make_int4(pi, cam, r, std::min(t.decode_rows, trows - r));
                 items[Q_DECODE].push_back(it);
-                if (p.decode.post_smooth) items[Q_SMOOTH].push_back(it);
+                if (p.decode.post_smooth) items[Q_SMOOTH].push_back(it);  // modes 1 and 2
             }
         for (int r = 0; r < C.rect_h; r += t.match_rows)
             items[Q_MATCH].push_back(make_int4(pi, r, std::min(t.match_rows, C.rect_h - r), 0));
@@ -546,7 +549,7 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         zt::reproj_params(C.Q, C.R1, rcfg, D.rp);
         D.sample_type = p.sample_type;
         D.rows = p.rows; D.cols = p.cols; D.rw = C.rect_w; D.rh = C.rect_h;
-        D.post_smooth = p.decode.post_smooth;
+        D.post_smooth = p.decode.enable_hdr ? (p.decode.post_smooth ? 2 : 3) : (p.decode.post_smooth ? 1 : 0);
         D.pha_f = p.pha_f > 0 ? p.pha_f : zim_decode_max_order(&p.decode);
         D.grad_threshold = (float)rcfg->grad_threshold;
         const size_t src = (size_t)p.rows * p.cols, dst = (size_t)C.rect_w * C.rect_h;

@@ -265,10 +265,11 @@ __global__ void rectify_kernel(const int32_t* __restrict__ order, const float* _
 // Post-smooth once per source pixel (the reference smooths the decoded phase
 // map before setData, JSLAB_PhaseShiftDecoder_V2.cpp:274-295) ...
 __global__ void smooth_kernel(const int32_t* __restrict__ order, const float* __restrict__ res, int rows, int cols,
-                              int32_t* __restrict__ K16, float* __restrict__ R) {
+                              int hdr, int32_t* __restrict__ K16, float* __restrict__ R) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= cols || y >= rows) return;
-    zt::smooth_pixel(order, res, rows, cols, x, y, K16, R);
+    if (hdr) zt::smooth_pixel_hdr(order, res, rows, cols, x, y, K16, R);
+    else zt::smooth_pixel(order, res, rows, cols, x, y, K16, R);
 }
 
 // ... then remap the smoothed taps.
@@ -409,16 +410,17 @@ zim_status zim_rectify_launch(zim_ctx* ctx, int cam, const int32_t* order, const
                               int post_smooth, int32_t* smooth_k16, float* smooth_r, int32_t* rbase, float* rres,
                               int32_t* rorder, cudaStream_t st) {
     dim3 blk(32, 8), grd((ctx->rect_w + 31) / 32, (ctx->rect_h + 7) / 8);
-    if (post_smooth) {
+    if (post_smooth == 1 || post_smooth == 2) {
         dim3 sgrd((cols + 31) / 32, (rows + 7) / 8);
-        smooth_kernel<<<sgrd, blk, 0, st>>>(order, residual, rows, cols, smooth_k16, smooth_r);
+        smooth_kernel<<<sgrd, blk, 0, st>>>(order, residual, rows, cols, post_smooth == 2 ? 1 : 0, smooth_k16,
+                                            smooth_r);
         rectify_smoothed_kernel<<<grd, blk, 0, st>>>(smooth_k16, smooth_r, order, rows, cols, ctx->d_map[cam][0],
                                                      ctx->d_map[cam][1], ctx->rect_h, ctx->rect_w, rbase, rres,
                                                      rorder);
         ctx->launches += 2;
     } else {
         rectify_kernel<<<grd, blk, 0, st>>>(order, residual, rows, cols, ctx->d_map[cam][0], ctx->d_map[cam][1],
-                                            ctx->rect_h, ctx->rect_w, 0, rbase, rres, rorder);
+                                            ctx->rect_h, ctx->rect_w, post_smooth, rbase, rres, rorder);
         ctx->launches += 1;
     }
     ZIM_LAUNCH_CHECK(ctx);
@@ -435,9 +437,10 @@ extern "C" ZIM_API zim_status zim_rectify(zim_ctx* ctx, int cam, const int32_t* 
     if (rows != ctx->src_h || cols != ctx->src_w)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "image size differs from calibration");
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (post_smooth < 0 || post_smooth > 3) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "post_smooth must be 0..3");
     int32_t* sk = nullptr;
     float* sr = nullptr;
-    if (post_smooth) {
+    if (post_smooth == 1 || post_smooth == 2) {
         const size_t src = (size_t)rows * cols;
         zim_status s = zim_scratch_reserve(ctx, 2 * zim_align256(src * 4) + 1024);
         if (s) return s;

@@ -60,8 +60,14 @@ static bool is_int(double v) { return std::isfinite(v) && v == std::floor(v); }
 
 extern "C" ZIM_API zim_status zim_decode_validate(const zim_decode_config* c) {
     if (!c) return ZIM_ERR_INVALID_ARG;
-    if (c->enable_hdr) return ZIM_ERR_UNSUPPORTED;
     if (!(c->modulation_threshold >= 0) || !std::isfinite(c->preblur_sigma)) return ZIM_ERR_INVALID_ARG;
+    if (c->enable_hdr) {
+        // the reference fits HDR phase for its phase-shift frequencies only; Gray bits would threshold saturated frames
+        if (c->encoding != ZIM_ENC_HETERODYNE3 && c->encoding != ZIM_ENC_HIERARCHICAL) return ZIM_ERR_UNSUPPORTED;
+        if (!(c->hdr_saturation_gray > 0) || !(c->hdr_min_amplitude >= 0)) return ZIM_ERR_INVALID_ARG;
+        for (int i = 0; i < (c->encoding == ZIM_ENC_HETERODYNE3 ? 3 : c->n_freq) && i < 4; i++)
+            if (c->shift_num[i] > 12) return ZIM_ERR_INVALID_ARG;  // JSLAB_HDRPhaseFit: 3..12 steps
+    }
     auto steps_ok = [](int n) { return n >= 3 && n <= 32; };
     switch (c->encoding) {
     case ZIM_ENC_HETERODYNE3: {
@@ -276,8 +282,8 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
     for (int c = 0; c < 2; c++) {
         s = zim_decode_launch(ctx, d, frames[c], sample_type, rows, cols, B.order[c], B.res[c], nullptr, nullptr, st);
         if (s) return s;
-        s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->post_smooth, B.sk[c], B.sr[c],
-                               B.rbase[c], B.rres[c], B.rorder[c], st);
+        s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->enable_hdr ? (d->post_smooth ? 2 : 3) : (d->post_smooth ? 1 : 0),
+                               B.sk[c], B.sr[c], B.rbase[c], B.rres[c], B.rorder[c], st);
         if (s) return s;
     }
     const int RH = ctx->rect_h, RW = ctx->rect_w;

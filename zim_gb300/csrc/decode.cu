@@ -31,30 +31,39 @@ __global__ void __launch_bounds__(zt::DX* zt::DY) decode_kernel(const T* __restr
                        mod_out, valid_out);
 }
 
-// Absolute phase as f64 (startCalculate's CV_64F map), optional 3x3 post-smooth
-// (fixed [1/4 1/2 1/4] kernel, BORDER_REPLICATE).
+// Absolute phase as f64 (startCalculate's CV_64F map; 0 where invalid), with
+// the optional 3x3 post-smooth (fixed [1/4 1/2 1/4] kernel, BORDER_REPLICATE):
+// post_smooth 1 blurs the phase map as is; 2 is the HDR form, the blur divided
+// by the blurred validity, 0 at invalid pixels (JSLAB_PhaseShiftDecoder_V2.cpp:280-291);
+// 3 is an HDR decode without smoothing.  An HDR decode marks invalid pixels
+// with order -1 (a plain decode zeroes them, and Gray code can give a valid -1).
 __global__ void phase_f64_kernel(const int32_t* __restrict__ order, const float* __restrict__ res, int rows, int cols,
                                  int post_smooth, double* __restrict__ out) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= cols || y >= rows) return;
-    if (!post_smooth) {
-        size_t o = (size_t)y * cols + x;
-        out[o] = 6.283185307179586 * order[o] + (double)res[o];
+    const size_t oc = (size_t)y * cols + x;
+    const bool hdr = post_smooth >= 2;
+    if (post_smooth == 0 || post_smooth == 3) {
+        out[oc] = hdr && order[oc] < 0 ? 0.0 : 6.283185307179586 * order[oc] + (double)res[oc];
         return;
     }
-    int K = 0;
-    double R = 0;
+    if (hdr && order[oc] < 0) {
+        out[oc] = 0.0;
+        return;
+    }
+    double P = 0, W = 0;
     for (int a = -1; a <= 1; a++) {
         int yy = min(max(y + a, 0), rows - 1);
         for (int b = -1; b <= 1; b++) {
             int xx = min(max(x + b, 0), cols - 1);
             int w = (a == 0 ? 2 : 1) * (b == 0 ? 2 : 1);
             size_t o = (size_t)yy * cols + xx;
-            K += w * order[o];
-            R += w * (double)res[o];
+            if (hdr && order[o] < 0) continue;
+            P += w * (6.283185307179586 * order[o] + (double)res[o]);
+            W += w;
         }
     }
-    out[(size_t)y * cols + x] = 6.283185307179586 * (K / 16.0) + R / 16.0;
+    out[oc] = hdr ? P / W : P / 16.0;
 }
 
 }  // namespace

@@ -38,6 +38,9 @@ struct DecodeParams {
     float fratio[4];
     // Gray code
     int gray_bits, gray_base, complementary;
+    // HDR least squares (JSLAB_HDRPhaseFit.h:10-61)
+    int hdr;
+    float hdr_sat, hdr_min_amp;
 };
 
 inline void decode_params(const zim_decode_config* c, int rows, int cols, DecodeParams& p) {
@@ -88,6 +91,48 @@ inline void decode_params(const zim_decode_config* c, int rows, int cols, Decode
         p.gray_base = c->shift_num[0];
         p.complementary = c->encoding == ZIM_ENC_GRAYCODE_COMPLEMENTARY;
     }
+    p.hdr = c->enable_hdr ? 1 : 0;
+    p.hdr_sat = (float)c->hdr_saturation_gray;
+    p.hdr_min_amp = (float)c->hdr_min_amplitude;
+}
+
+// HDR fit of one frequency at one pixel (JSLAB_HDRPhaseFit.h:10-61 and
+// JSLAB_PhaseShiftDecoder_V2.cpp:73-90): raw samples with 0 <= I < saturation
+// enter an equal-variance least-squares fit of I = A + C cos d - S sin d
+// (solved here from the 3x3 normal equations, the reference's cached
+// pseudo-inverse of the same subset); fewer than three samples, amplitude
+// hypot(C, S) <= min_amp or A <= 1e-3 reject the pixel.  Returns the sums the
+// phase-shift path would have formed: sin_sum = S N/2, cos_sum = C N/2,
+// sum = A N.
+template <typename T>
+__device__ __forceinline__ bool hdr_fit(const T* __restrict__ f0, size_t npx, int N, const float* sv, const float* cv,
+                                        float sat, float min_amp, float& sin_sum, float& cos_sum, float& sum) {
+    float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f, r0 = 0.f, r1 = 0.f, r2 = 0.f;
+    int n = 0;
+    for (int k = 0; k < N; k++) {
+        const float v = (float)__ldg(f0 + (size_t)k * npx);
+        if (!(v >= 0.f && v < sat)) continue;
+        const float c = cv[k], s = -sv[k];
+        m00 += 1.f; m01 += c; m02 += s;
+        m11 = fmaf(c, c, m11); m12 = fmaf(c, s, m12); m22 = fmaf(s, s, m22);
+        r0 += v; r1 = fmaf(c, v, r1); r2 = fmaf(s, v, r2);
+        n++;
+    }
+    if (n < 3) return false;
+    // symmetric 3x3 inverse by cofactors
+    const float c00 = fmaf(m11, m22, -m12 * m12), c01 = fmaf(m02, m12, -m01 * m22), c02 = fmaf(m01, m12, -m02 * m11);
+    const float det = fmaf(m00, c00, fmaf(m01, c01, m02 * c02));
+    if (!(fabsf(det) > 1e-6f * m00 * m00 * m00)) return false;
+    const float c11 = fmaf(m00, m22, -m02 * m02), c12 = fmaf(m01, m02, -m00 * m12), c22 = fmaf(m00, m11, -m01 * m01);
+    const float id = 1.0f / det;
+    const float A = fmaf(c00, r0, fmaf(c01, r1, c02 * r2)) * id;
+    const float C = fmaf(c01, r0, fmaf(c11, r1, c12 * r2)) * id;
+    const float S = fmaf(c02, r0, fmaf(c12, r1, c22 * r2)) * id;
+    if (!(hypotf(C, S) > min_amp) || !(A > 1e-3f)) return false;
+    sin_sum = S * (float)N * 0.5f;
+    cos_sum = C * (float)N * 0.5f;
+    sum = A * (float)N;
+    return true;
 }
 
 // floor(a / b) for b > 0 and |a / b| < 2^21, from the float reciprocal
@@ -124,11 +169,31 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
     float wrap0 = 0.f, wrap1 = 0.f, wrap2 = 0.f, wrap3 = 0.f;  // named, so they stay in registers
     float mod0 = 0.f;
     bool ok = true;
+    const bool inside = x < p.cols && y < p.rows;
     for (int i = 0; i < p.n_ps; i++) {
         const int N = p.shift[i];
         const T* fb = frames + (size_t)p.fbase[i] * npx;
         const float* sv = p.sinv + p.fbase[i];
         const float* cv = p.cosv + p.fbase[i];
+        if (p.hdr) {
+            // raw samples, no pre-blur: saturation is classified before any blur
+            float S = 0.f, C = 0.f, M = 0.f;
+            if (ok && inside && !hdr_fit(fb + (size_t)y * p.cols + x, npx, N, sv, cv, p.hdr_sat, p.hdr_min_amp, S, C, M))
+                ok = false;
+            if (ok) {
+                const float wr = atan2f(S, C);
+                if (i == 0) wrap0 = wr;
+                else if (i == 1) wrap1 = wr;
+                else if (i == 2) wrap2 = wr;
+                else wrap3 = wr;
+                float b = 2.0f * sqrtf(fmaf(S, S, C * C)) / (float)N;
+                float mean = M / (float)N;
+                float nm = mean > 1e-3f ? b / mean : 0.f;
+                if (i == 0) mod0 = nm;
+                if (nm < p.thr) ok = false;
+            }
+            continue;
+        }
         for (int h = tid; h < DHX * DHY; h += DX * DY) {
             int hy = h / DHX, hx = h - hy * DHX;
             int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
@@ -233,7 +298,7 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             r = wrap0;
         }
     }
-    order[pix] = k;
+    order[pix] = ok ? k : (p.hdr ? -1 : 0);  // the HDR decoder marks invalid orders -1
     residual[pix] = r;
     if (valid_out) valid_out[pix] = ok ? 1 : 0;
 }
@@ -244,10 +309,14 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
 // phase_s = 2*pi*K16/16 + R, K16 = sum (1 2 1)x(1 2 1) * order (BORDER_REPLICATE).
 __device__ __forceinline__ void smoothed_tap(const int32_t* __restrict__ order, const float* __restrict__ res, int x,
                                              int y, int rows, int cols, int post_smooth, int& K16, float& R) {
-    if (!post_smooth) {
+    // post_smooth 0: the tap as decoded; 3: the same for HDR decodes, whose
+    // invalid pixels (order -1) have phase 0
+    if (post_smooth == 0 || post_smooth == 3) {
         size_t o = (size_t)y * cols + x;
-        K16 = 16 * __ldg(order + o);
-        R = __ldg(res + o);
+        const int k = __ldg(order + o);
+        const bool zero = post_smooth == 3 && k < 0;
+        K16 = zero ? 0 : 16 * k;
+        R = zero ? 0.f : __ldg(res + o);
         return;
     }
     int k = 0;
@@ -317,6 +386,46 @@ __device__ __forceinline__ void smooth_pixel(const int32_t* __restrict__ order, 
     const size_t o = (size_t)y * cols + x;
     K16[o] = k;
     R[o] = r;
+}
+
+// HDR post-smooth (JSLAB_PhaseShiftDecoder_V2.cpp:280-291): the blurred phase
+// divided by the blurred validity (invalid pixels, order < 0, count as phase
+// 0 with weight 0), 0 at invalid pixels.  With W = sum of the valid [1 2 1]^2
+// weights and Kw = sum w k: phase = 2 pi Kw / W + 16 (sum w r / 16) / W, and
+// Kw / W splits exactly into an integer q and remainder, so the output keeps
+// the (16 x cycles, residual) form: K16 = 16 q, R = (2 pi rem + 16 Rw) / W.
+__device__ __forceinline__ void smooth_pixel_hdr(const int32_t* __restrict__ order, const float* __restrict__ res,
+                                                 int rows, int cols, int x, int y, int32_t* __restrict__ K16,
+                                                 float* __restrict__ R) {
+    const size_t o = (size_t)y * cols + x;
+    if (__ldg(order + o) < 0) {
+        K16[o] = 0;
+        R[o] = 0.f;
+        return;
+    }
+    int kw = 0, wv = 0;
+    float rw = 0.f;
+#pragma unroll
+    for (int a = -1; a <= 1; a++) {
+        const int yy = min(max(y + a, 0), rows - 1);
+        const int ca = a == 0 ? 2 : 1;
+#pragma unroll
+        for (int b = -1; b <= 1; b++) {
+            const int xx = min(max(x + b, 0), cols - 1);
+            const int cw = ca * (b == 0 ? 2 : 1);
+            const size_t q = (size_t)yy * cols + xx;
+            const int kq = __ldg(order + q);
+            if (kq < 0) continue;
+            kw += cw * kq;
+            wv += cw;
+            rw = fmaf((float)cw * 0.0625f, __ldg(res + q), rw);
+        }
+    }
+    int qd = kw / wv;  // wv in [4, 16]
+    int rem = kw - qd * wv;
+    if (rem < 0) { qd--; rem += wv; }
+    K16[o] = 16 * qd;
+    R[o] = fmaf((float)rem, ZIM_TWO_PI_F, 16.0f * rw) / (float)wv;
 }
 
 __device__ __forceinline__ void rectify_pixel_smoothed(const int32_t* __restrict__ K16, const float* __restrict__ Rs_,
