@@ -120,6 +120,11 @@ typedef struct zim_recon_config {
     double sor_std_mul;                      /* 1.0 */
     int use_metric_gaussian;                 /* 0: radius-3-sigma Gaussian in millimetres */
     double metric_gaussian_sigma;            /* 0.5 */
+    /* 0: Q-matrix reprojection (startCalculate, V2.cpp:397-480).
+     * 1: per-pixel polynomial maps set by zim_set_poly_calib (startCalculate_v2,
+     *    V2.cpp:482-593 with evaluateV2CalibPoint :13-76); the rest of the
+     *    chain is unchanged. */
+    int reproject_model;                     /* 0 */
 } zim_recon_config;
 
 /* PCL PointXYZ memory layout: x, y, z, padding (16 bytes). */
@@ -179,6 +184,67 @@ ZIM_API zim_status zim_get_rectification(const zim_ctx* ctx, double R1[9], doubl
 /* Copies the float rectification maps (rect_h*rect_w each) into device buffers. */
 ZIM_API zim_status zim_get_rectify_maps(zim_ctx* ctx, int cam, float* mapx, float* mapy,
                                         void* stream);
+
+/* JSLAB_PhaseEpipolarReconstructor_V2::setCalibrationParamsV2 (V2.cpp:340-366):
+ * the per-pixel coefficient maps xyz_calib_coeffs[0..2] (CV_32FC4, rows*cols
+ * float4 (c0, c1, c2, c3), row-major, HOST memory) of
+ * JSLAB_StereoCalibParams_V2, used when zim_recon_config.reproject_model = 1.
+ * Call after zim_set_calibration; rows x cols must be its rectified size.
+ * cx = cy = cz = NULL drops the maps.  A later zim_set_calibration keeps them
+ * only while the rectified size is unchanged.  Synchronises. */
+ZIM_API zim_status zim_set_poly_calib(zim_ctx* ctx, const float* cx, const float* cy,
+                                      const float* cz, int rows, int cols);
+
+/* ---- ROI-restricted reconstruction (prepareRectifiedROI / startCalculate_v2_roi,
+ * JSLAB_PhaseEpipolarReconstructor_V2.cpp:595-914) ---- */
+typedef struct zim_rotated_rect {            /* cv::RotatedRect in source pixels */
+    float center_x, center_y, width, height;
+    float angle;                             /* degrees */
+} zim_rotated_rect;
+typedef struct zim_rect { int x, y, width, height; } zim_rect;  /* cv::Rect */
+typedef struct zim_rectified_roi {           /* RectifiedROI (V2.h:97-102) without its mask */
+    zim_rect left_rect, right_rect;
+} zim_rectified_roi;
+
+/* prepareRectifiedROI: the rotated rectangle's corners rounded to integers and
+ * filled (closed polygon + 8-connected outline) in the source image, remapped
+ * INTER_LINEAR (8-bit fixed point) into the rectified frame, thresholded > 0
+ * and dilated 5x5 into roi_mask (rect_h*rect_w device bytes, 255 inside).
+ * left_rect = the bounding box of that mask; right_rect = the ROI's rows and
+ * the right columns holding any order 1..pha_f that occurs in the left ROI,
+ * padded by 32 (all columns if none).  l_order / r_order are the rectified
+ * order maps (zim_rectify).  *valid = 0 for an empty ROI (the reference's
+ * false).  Synchronises the stream. */
+ZIM_API zim_status zim_prepare_roi(zim_ctx* ctx, const zim_rotated_rect* roi, const int32_t* l_order,
+                                   const int32_t* r_order, int pha_f, zim_rectified_roi* out,
+                                   uint8_t* roi_mask, int* valid, void* stream);
+
+/* The source-image mask of a rotated rectangle that zim_prepare_roi starts
+ * from, as one column span per row (host memory, rows entries each; lo > hi
+ * for an empty row).  Host only, no context. */
+ZIM_API zim_status zim_roi_source_spans(const zim_rotated_rect* roi, int rows, int cols, int* lo, int* hi);
+
+/* startCalculate_v2_roi on rectified maps (zim_rectify outputs, rect_h*rect_w):
+ * left_rect pixels inside roi_mask matched against right_rect's columns only
+ * (edge rejection and disparity relative to that window), 5x5 median of the
+ * ROI disparity, reprojection of masked pixels (cfg->reproject_model: 1 the
+ * polynomial maps like the reference, 0 Q) at their rectified coordinates,
+ * then the filter chain; the pre-ROR cloud is kept when ROR leaves fewer than
+ * a tenth of the reprojected points.  xyz (x3), mask and disp (may be NULL)
+ * are left_rect.height x left_rect.width. */
+ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_config* cfg,
+                                       const zim_rectified_roi* roi, const uint8_t* roi_mask,
+                                       const int32_t* l_base, const float* l_res, const int32_t* l_order,
+                                       const int32_t* r_base, const float* r_res, const int32_t* r_order,
+                                       int pha_f, float* xyz, uint8_t* mask, float* disp, void* stream);
+
+/* rectifyLeftImage (V2.cpp:920-924) for either camera: cv::remap INTER_LINEAR
+ * of an 8-bit image (src_h x src_w, device) through the camera's rectification
+ * maps with OpenCV's fixed-point bilinear weights (1/32-pixel positions,
+ * weights in 1/32768, rounded shift) and BORDER_CONSTANT 0, into a
+ * rect_h x rect_w image. */
+ZIM_API zim_status zim_rectify_image(zim_ctx* ctx, int cam, const uint8_t* src, int rows, int cols,
+                                     uint8_t* dst, void* stream);
 
 /* setData for one camera (JSLAB_PhaseEpipolarReconstructor_V2.cpp:368-395):
  * post-smooth (optional) + remap INTER_LINEAR of the phase, INTER_NEAREST of
@@ -248,6 +314,17 @@ ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz, const uint
 ZIM_API zim_status zim_compact_points_noalloc(const float* xyz, const uint8_t* mask, int rows,
                                               int cols, zim_point_xyz* points,
                                               uint64_t* count_dev, void* stream);
+
+/* The vertex body of a binary little-endian PLY file, packed on the device:
+ * for each valid point in row order float x, y, z (12 bytes;
+ * savePointCloudToPlyBinary, main.cpp:85-127) or, with with_gray, float x, y,
+ * z then uchar red = green = blue = gray[pixel] (15 bytes, unaligned; gray
+ * NULL writes 255; savePointCloudToPlyBinaryWithGray, main.cpp:132-160).
+ * records holds rows*cols records at most; *count_dev (device) gets the
+ * number written.  The host writes the header and copies the body out. */
+ZIM_API zim_status zim_pack_ply(zim_ctx* ctx, const float* xyz, const uint8_t* mask,
+                                const uint8_t* gray, int with_gray, int rows, int cols,
+                                void* records, uint64_t* count_dev, void* stream);
 
 /* Whole plain per-pair path (decode L+R, rectify, match, median, reproject,
  * filters) on device buffers.  xyz/mask/disp are rect_h*rect_w.  pha_f <= 0

@@ -5,6 +5,7 @@
 // Reference classes mirrored (PhaseShiftGrayCode3D/src/):
 //   JSLAB_PhaseShiftDecoder            JSLAB_PhaseShiftDecoder.h:10-92
 //   JSLAB_StereoCalibParams_V1         JSLAB_StereoCalibParams_V1.h:9-20
+//   JSLAB_StereoCalibParams_V2         JSLAB_StereoCalibParams_V2.h:8-30 (+ the .bin maps)
 //   JSLAB_PhaseEpipolarReconstructor_V2 JSLAB_PhaseEpipolarReconstructor_V2.h:11-171
 //
 // Images are zim::Image<T> (rows x cols x channels, row-major, owning).  When
@@ -22,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -311,6 +313,45 @@ struct JSLAB_StereoCalibParams_V1 {
     }
 };
 
+// V2: per-pixel coefficient maps xyz_calib_coeffs[0..2] (X, Y, Z), each rows x
+// cols x 4 floats (CV_32FC4), read from <base>_rx/_ry/_rz.bin.
+struct JSLAB_StereoCalibParams_V2 : JSLAB_StereoCalibParams_V1 {
+    zim::Image<float> xyz_calib_coeffs[3];
+
+    // loadMatBinary (JSLAB_StereoCalibParams_V2.cpp:4-17): int type, rows, cols,
+    // then the rows.  Float matrices only (CV_32FC1..4); false on a short file.
+    static bool loadMatBinary(const std::string& filename, zim::Image<float>& mat) {
+        std::ifstream fs(filename, std::ios::binary);
+        if (!fs.is_open()) return false;
+        int32_t head[3];
+        if (!fs.read(reinterpret_cast<char*>(head), sizeof head)) return false;
+        const int depth = head[0] & 7, cn = (head[0] >> 3) + 1;
+        if (depth != 5 || head[1] < 0 || head[2] < 0) return false;  // CV_32F
+        zim::Image<float> m(head[1], head[2], cn);
+        if (!fs.read(reinterpret_cast<char*>(m.ptr()), (std::streamsize)(m.size() * sizeof(float)))) return false;
+        mat = std::move(m);
+        return true;
+    }
+    // saveMatBinary (JSLAB_StereoCalib_V2.cpp:22-30).
+    static bool saveMatBinary(const std::string& filename, const zim::Image<float>& mat) {
+        std::ofstream fs(filename, std::ios::binary);
+        if (!fs.is_open()) return false;
+        const int32_t head[3] = {5 + ((mat.channels - 1) << 3), mat.rows, mat.cols};
+        fs.write(reinterpret_cast<const char*>(head), sizeof head);
+        fs.write(reinterpret_cast<const char*>(mat.ptr()), (std::streamsize)(mat.size() * sizeof(float)));
+        return (bool)fs;
+    }
+    // The maps of loadStereoCalibParams_V2 (JSLAB_StereoCalibParams_V2.cpp:34-43) for a
+    // calibration file name (the part up to its last dot is the base).
+    bool loadCoefficientMaps(const std::string& filename) {
+        const std::string base = filename.substr(0, filename.find_last_of('.'));
+        const char* sfx[3] = {"_rx.bin", "_ry.bin", "_rz.bin"};
+        bool ok = true;
+        for (int k = 0; k < 3; k++) ok = loadMatBinary(base + sfx[k], xyz_calib_coeffs[k]) && ok;
+        return ok;
+    }
+};
+
 // -------------------------------------------------------- reconstructor ----
 
 class JSLAB_PhaseEpipolarReconstructor_V2 {
@@ -333,6 +374,24 @@ public:
                    ctx_->get(), "zim_get_rectification");
         src_w_ = params.image_width;
         src_h_ = params.image_height;
+    }
+
+    // setCalibrationParamsV2 (V2.cpp:340-366): the V1 geometry, then the
+    // coefficient maps when all three are present (4 channels each).
+    void setCalibrationParamsV2(const JSLAB_StereoCalibParams_V2& params) {
+        setCalibrationParams(params);
+        const zim::Image<float>* m = params.xyz_calib_coeffs;
+        use_v2_ = !m[0].empty() && !m[1].empty() && !m[2].empty();
+        zim_ctx* c = ctx_->get();
+        if (!use_v2_) {
+            zim::check(zim_set_poly_calib(c, nullptr, nullptr, nullptr, 0, 0), c, "zim_set_poly_calib");
+            return;
+        }
+        for (int k = 0; k < 3; k++)
+            if (m[k].channels != 4 || m[k].rows != m[0].rows || m[k].cols != m[0].cols)
+                throw zim::Error(ZIM_ERR_INVALID_ARG, "coefficient maps are rows x cols x 4");
+        zim::check(zim_set_poly_calib(c, m[0].ptr(), m[1].ptr(), m[2].ptr(), m[0].rows, m[0].cols), c,
+                   "zim_set_poly_calib");
     }
 
     // setData (JSLAB_PhaseEpipolarReconstructor_V2.h:67-69): absolute phase maps
@@ -381,6 +440,16 @@ public:
         mask_.download(P.ptr(), P.size());
     }
 
+    // startCalculate_v2 (…V2.h, V2.cpp:482-593): the same chain with the
+    // per-pixel polynomial reprojection; no point without coefficient maps.
+    void startCalculate_v2(zim::Image<float>& xyz, zim::Image<uint8_t>& P) {
+        run(use_v2_ ? 1 : -1);
+        xyz = zim::Image<float>(rh_, rw_, 3);
+        P = zim::Image<uint8_t>(rh_, rw_);
+        xyz_.download(xyz.ptr(), xyz.size());
+        mask_.download(P.ptr(), P.size());
+    }
+
     // The cloud as PCL PointXYZ records (x, y, z, pad), valid points in row order.
     void startCalculate(std::vector<zim_point_xyz>& cloud) {
         run();
@@ -398,6 +467,22 @@ public:
         disp = zim::Image<float>(rh_, rw_);
         if (disp_.size()) disp_.download(disp.ptr(), disp.size());
     }
+
+    // rectifyLeftImage (V2.cpp:920-924): 8-bit left image into the rectified frame.
+    void rectifyLeftImage(const zim::Image<uint8_t>& image, zim::Image<uint8_t>& rectified) const {
+        if (image.empty()) {
+            rectified = zim::Image<uint8_t>();
+            return;
+        }
+        zim::DeviceBuffer<uint8_t> src(image.size()), dst((size_t)rw_ * rh_);
+        src.upload(image.ptr(), image.size());
+        zim::check(zim_rectify_image(ctx_->get(), 0, src.get(), image.rows, image.cols, dst.get(), nullptr),
+                   ctx_->get(), "zim_rectify_image");
+        rectified = zim::Image<uint8_t>(rh_, rw_);
+        dst.download(rectified.ptr(), rectified.size());
+    }
+
+    std::shared_ptr<zim::Context> context() const { return ctx_; }
 
 #ifdef ZIM_JSLAB_PCL
     void startCalculate(pcl::PointCloud<pcl::PointXYZ>& cloud) {
@@ -430,6 +515,13 @@ public:
         cv::Mat(x.rows, x.cols, CV_32FC3, x.ptr()).copyTo(xyz);
         cv::Mat(m.rows, m.cols, CV_8UC1, m.ptr()).copyTo(P);
     }
+    void startCalculate_v2(cv::Mat& xyz, cv::Mat& P) {
+        zim::Image<float> x;
+        zim::Image<uint8_t> m;
+        startCalculate_v2(x, m);
+        cv::Mat(x.rows, x.cols, CV_32FC3, x.ptr()).copyTo(xyz);
+        cv::Mat(m.rows, m.cols, CV_8UC1, m.ptr()).copyTo(P);
+    }
     void getDisparityMap(cv::Mat& disp) const {
         zim::Image<float> d;
         getDisparityMap(d);
@@ -438,7 +530,8 @@ public:
 #endif
 
 private:
-    void run() {
+    // model: 0 Q matrix, 1 polynomial maps, -1 no point (startCalculate_v2 without maps)
+    void run(int model = 0) {
         if (!order_[0].size()) throw zim::Error(ZIM_ERR_INVALID_ARG, "setData first");
         zim_ctx* c = ctx_->get();
         const size_t r = (size_t)rw_ * rh_;
@@ -459,9 +552,16 @@ private:
         disp_.resize(r);
         xyz_.resize(3 * r);
         mask_.resize(r);
-        zim::check(zim_median_reproject(c, &cfg_, raw.get(), rh_, rw_, disp_.get(), xyz_.get(), mask_.get(), nullptr), c,
+        zim_recon_config rc = cfg_;
+        rc.reproject_model = model > 0 ? model : 0;
+        zim::check(zim_median_reproject(c, &rc, raw.get(), rh_, rw_, disp_.get(), xyz_.get(), mask_.get(), nullptr), c,
                    "zim_median_reproject");
-        filters();
+        if (model < 0) {
+            zim::cuda_check(cudaMemset(xyz_.get(), 0, 12 * r), "clear");
+            zim::cuda_check(cudaMemset(mask_.get(), 0, r), "clear");
+        } else {
+            filters();
+        }
         zim::cuda_check(cudaDeviceSynchronize(), "reconstruct");
     }
 
@@ -517,8 +617,85 @@ private:
     std::shared_ptr<zim::Context> ctx_;
     int src_w_ = 0, src_h_ = 0, rw_ = 0, rh_ = 0, pha_f_ = 0;
     int smooth_mode_ = 0;  // zim_rectify post_smooth mode
+    bool use_v2_ = false;  // coefficient maps set (m_use_v2_coeffs)
     zim::DeviceBuffer<int32_t> order_[2];
     zim::DeviceBuffer<float> res_[2];
     zim::DeviceBuffer<float> disp_, xyz_;
     zim::DeviceBuffer<uint8_t> mask_;
 };
+
+// ----------------------------------------------------------------- outputs ----
+// The reference drivers' writers (main.cpp:85-184, JSLAB_PhaseDisparityExporter.cpp:115-141).
+// The PLY vertex body is packed on the GPU (zim_pack_ply) and copied out once.
+
+namespace zim {
+inline bool write_ply(Context& ctx, const Image<float>& xyz, const Image<uint8_t>& P, const Image<uint8_t>* gray,
+                      const std::string& file_name) {
+    if (xyz.channels != 3 || xyz.rows != P.rows || xyz.cols != P.cols || P.channels != 1) return false;
+    const bool with_gray = gray != nullptr;
+    const size_t n = (size_t)P.rows * P.cols, rec = with_gray ? 15 : 12;
+    DeviceBuffer<float> dx(xyz.size());
+    DeviceBuffer<uint8_t> dm(n), dg(with_gray && !gray->empty() ? n : 0), body(n * rec);
+    DeviceBuffer<uint64_t> cnt(1);
+    dx.upload(xyz.ptr(), xyz.size());
+    dm.upload(P.ptr(), n);
+    if (dg.size()) dg.upload(gray->ptr(), n);
+    check(zim_pack_ply(ctx.get(), dx.get(), dm.get(), dg.size() ? dg.get() : nullptr, with_gray ? 1 : 0, P.rows,
+                       P.cols, body.get(), cnt.get(), nullptr),
+          ctx.get(), "zim_pack_ply");
+    uint64_t count = 0;
+    cnt.download(&count, 1);
+    std::vector<uint8_t> h(count * rec);
+    if (count) body.download(h.data(), h.size());
+    std::ofstream fs(file_name, std::ios::binary);
+    if (!fs.is_open()) return false;
+    fs << "ply\nformat binary_little_endian 1.0\nelement vertex " << count << "\n"
+       << "property float x\nproperty float y\nproperty float z\n";
+    if (with_gray) fs << "property uchar red\nproperty uchar green\nproperty uchar blue\n";
+    fs << "end_header\n";
+    fs.write(reinterpret_cast<const char*>(h.data()), (std::streamsize)h.size());
+    return (bool)fs;
+}
+}  // namespace zim
+
+inline bool savePointCloudToPlyBinary(zim::Context& ctx, const zim::Image<float>& xyz, const zim::Image<uint8_t>& P,
+                                      const std::string& file_name) {
+    return zim::write_ply(ctx, xyz, P, nullptr, file_name);
+}
+
+// gray_image: the rectified left image (same size), or empty for white points.
+inline bool savePointCloudToPlyBinaryWithGray(zim::Context& ctx, const zim::Image<float>& xyz,
+                                              const zim::Image<uint8_t>& P, const zim::Image<uint8_t>& gray_image,
+                                              const std::string& file_name) {
+    if (!gray_image.empty() && (gray_image.rows != P.rows || gray_image.cols != P.cols || gray_image.channels != 1))
+        return false;
+    return zim::write_ply(ctx, xyz, P, &gray_image, file_name);
+}
+
+// "x y z" lines of the points with -10000 < z < 10000 and |z| > 0.0001.
+inline bool saveToTxt(const zim::Image<float>& xyz, const std::string& filename) {
+    std::ofstream out(filename);
+    if (!out.is_open()) return false;
+    for (size_t i = 0; i + 2 < xyz.size(); i += 3) {
+        const float x = xyz.data[i], y = xyz.data[i + 1], z = xyz.data[i + 2];
+        if (z > -10000 && z < 10000 && std::fabs(z) > 0.0001f) out << x << " " << y << " " << z << "\n";
+    }
+    return true;
+}
+
+// Row-major doubles plus the info text of the reference's exporter.
+inline bool saveRaw64F(const zim::Image<double>& data, const std::string& raw_path, const std::string& info_path) {
+    if (data.empty() || data.channels != 1) return false;
+    std::ofstream raw(raw_path, std::ios::binary);
+    if (!raw.is_open()) return false;
+    raw.write(reinterpret_cast<const char*>(data.ptr()), (std::streamsize)(data.size() * sizeof(double)));
+    raw.close();
+    std::ofstream info(info_path);
+    if (info.is_open())
+        info << "rows " << data.rows << "\n"
+             << "cols " << data.cols << "\n"
+             << "type CV_64FC1 (double)\n"
+             << "layout row-major, one double per pixel\n"
+             << "rows/cols written on the FIRST line as 'rows cols' for convenience\n";
+    return true;
+}

@@ -207,6 +207,14 @@ def remap_linear(src, mapx, mapy):
     return dst
 
 
+def remap_u8(src, mapx, mapy):
+    src = _c(src, np.uint8); mapx = _c(mapx, np.float32); mapy = _c(mapy, np.float32)
+    dst = np.empty(mapx.shape, np.uint8)
+    lib().zo_remap_u8(_p(src), C.c_int(src.shape[0]), C.c_int(src.shape[1]), _p(mapx), _p(mapy),
+                      C.c_int(mapx.shape[0]), C.c_int(mapx.shape[1]), _p(dst))
+    return dst
+
+
 def remap_nearest(src, mapx, mapy):
     src = _c(src, np.int32); mapx = _c(mapx, np.float32); mapy = _c(mapy, np.float32)
     dst = np.empty(mapx.shape, np.int32)
@@ -221,6 +229,19 @@ def stereo_match(lph, rph, lk, rk, pha_f, grad_threshold=1.0, eps=1e-5):
     disp = np.empty((H, W)); best = np.empty((H, W), np.int32); near = np.empty((H, W), np.uint8)
     lib().zo_stereo_match(_p(lph), _p(rph), _p(lk), _p(rk), C.c_int(H), C.c_int(W), C.c_int(pha_f),
                           C.c_double(grad_threshold), _p(disp), _p(best), _p(near), C.c_double(eps))
+    return disp, best, near
+
+
+def stereo_match_roi(lph, lk, lmask, rph, rk, dx_off, pha_f, grad_threshold=1.0, eps=1e-5):
+    """startCalculate_v2_roi's matching on cropped windows (same rows)."""
+    lph = _c(lph, np.float64); lk = _c(lk, np.int32); lmask = _c(lmask, np.uint8)
+    rph = _c(rph, np.float64); rk = _c(rk, np.int32)
+    H, LW = lph.shape
+    RW = rph.shape[1]
+    disp = np.empty((H, LW)); best = np.empty((H, LW), np.int32); near = np.empty((H, LW), np.uint8)
+    lib().zo_stereo_match_roi(_p(lph), _p(lk), _p(lmask), C.c_int(LW), _p(rph), _p(rk), C.c_int(RW), C.c_int(H),
+                              C.c_int(dx_off), C.c_int(pha_f), C.c_double(grad_threshold), _p(disp), _p(best),
+                              _p(near), C.c_double(eps))
     return disp, best, near
 
 
@@ -239,6 +260,20 @@ def reproject(disp, Q, R1, min_depth=0.0, max_depth=1000.0, use_rectified=True, 
                        _p(_c(R1, np.float64).reshape(9)), C.c_double(min_depth), C.c_double(max_depth),
                        C.c_int(int(use_rectified)), _p(xyz), _p(mask), _p(near), C.c_double(eps))
     return xyz, mask, near
+
+
+def poly_reproject(disp, maps, R1, min_depth=0.0, max_depth=1000.0, use_rectified=True):
+    """startCalculate_v2's reprojection; maps = (cx, cy, cz), each (H, W, 4) float32."""
+    disp = _c(disp, np.float32)
+    H, W = disp.shape
+    m = [_c(a, np.float32) for a in maps]
+    for a in m:
+        assert a.shape == (H, W, 4)
+    xyz = np.empty((H, W, 3), np.float32); mask = np.empty((H, W), np.uint8)
+    lib().zo_poly_reproject(_p(disp), C.c_int(H), C.c_int(W), _p(m[0]), _p(m[1]), _p(m[2]),
+                            _p(_c(R1, np.float64).reshape(9)), C.c_double(min_depth), C.c_double(max_depth),
+                            C.c_int(int(use_rectified)), _p(xyz), _p(mask))
+    return xyz, mask
 
 
 def px_gaussian(xyz, mask, update_mask=False, eps=1e-5):

@@ -62,7 +62,8 @@ def _filters(xyz, mask, f: Filters):
     return xyz, mask
 
 
-def run_pair(decode_kwargs, pha_f, L, R, rect: Rectification, f: Filters = Filters()):
+def run_pair(decode_kwargs, pha_f, L, R, rect: Rectification, f: Filters = Filters(), poly=None):
+    """poly: (cx, cy, cz) coefficient maps for startCalculate_v2's reprojection."""
     cfg = O.make_decode_cfg(**decode_kwargs)
     r = []
     for cam, fr in enumerate((L, R)):
@@ -72,7 +73,10 @@ def run_pair(decode_kwargs, pha_f, L, R, rect: Rectification, f: Filters = Filte
     disp, _, _ = O.stereo_match(r[0][0], r[1][0], r[0][1], r[1][1], pha_f)
     d32 = disp.astype(np.float32)
     dm = O.median5(d32) if f.use_median else d32
-    xyz, mask, _ = O.reproject(dm, rect.Q, rect.R1, f.min_depth, f.max_depth, True)
+    if poly is not None:
+        xyz, mask = O.poly_reproject(dm, poly, rect.R1, f.min_depth, f.max_depth, True)
+    else:
+        xyz, mask, _ = O.reproject(dm, rect.Q, rect.R1, f.min_depth, f.max_depth, True)
     return _filters(xyz, mask, f)
 
 

@@ -581,6 +581,31 @@ void zo_remap_linear(const double* src, int srows, int scols, const float* mapx,
     }
 }
 
+/* remap INTER_LINEAR of an 8-bit image (rectifyLeftImage, V2.cpp:920-924):
+ * OpenCV's fixed-point path -- 1/32-pixel positions, integer weights
+ * (32 - f or f) x (32 - g or g) x 32 summing to 32768, (sum + 2^14) >> 15,
+ * BORDER_CONSTANT 0. */
+void zo_remap_u8(const uint8_t* src, int srows, int scols, const float* mapx, const float* mapy, int drows,
+                 int dcols, uint8_t* dst) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < drows; i++) {
+        for (int j = 0; j < dcols; j++) {
+            size_t o = (size_t)i * dcols + j;
+            int sx = (int)lrintf(mapx[o] * 32.0f), sy = (int)lrintf(mapy[o] * 32.0f);
+            int x0 = sx >> 5, y0 = sy >> 5, fx = sx & 31, fy = sy & 31;
+            int wx[2] = {32 - fx, fx}, wy[2] = {32 - fy, fy};
+            int acc = 0;
+            for (int t = 0; t < 4; t++) {
+                int xx = x0 + (t & 1), yy = y0 + (t >> 1);
+                int v = (xx >= 0 && yy >= 0 && xx < scols && yy < srows) ? src[(size_t)yy * scols + xx] : 0;
+                acc += v * wy[t >> 1] * wx[t & 1] * 32;
+            }
+            acc = (acc + (1 << 14)) >> 15;
+            dst[o] = (uint8_t)(acc > 255 ? 255 : acc);
+        }
+    }
+}
+
 /* remap INTER_NEAREST: position rounded to nearest (ties to even), BORDER_CONSTANT 0. */
 void zo_remap_nearest(const int32_t* src, int srows, int scols, const float* mapx, const float* mapy,
                       int drows, int dcols, int32_t* dst) {
@@ -596,6 +621,61 @@ void zo_remap_nearest(const int32_t* src, int srows, int scols, const float* map
 
 /* ------------------------------------------------------------------------ */
 /* stereoMatch, src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:933-1006. */
+/* ROI matching, src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:719-778: left window
+ * (lcols wide, masked) against a right column window (rcols wide) of the same
+ * rows; edge rejection relative to the right window; disparity = global left
+ * x - global right x - delta with dx_off = left x - right x. */
+void zo_stereo_match_roi(const double* lph, const int32_t* lk, const uint8_t* lmask, int lcols, const double* rph,
+                         const int32_t* rk, int rcols, int rows, int dx_off, int pha_f, double grad_threshold,
+                         double* disp, int32_t* best, uint8_t* near, double eps) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < rows; i++) {
+        const double* rp = rph + (size_t)i * rcols;
+        const int32_t* rkr = rk + (size_t)i * rcols;
+        for (int j = 0; j < lcols; j++) {
+            size_t o = (size_t)i * lcols + j;
+            disp[o] = 0.0;
+            if (best) best[o] = -1;
+            if (near) near[o] = 0;
+            if (!lmask[o]) continue;
+            int k = lk[o];
+            if (k > pha_f || k <= 0) continue;
+            double min_cost = 1e9, second = 1e9;
+            int best_jR = -1;
+            double l_val = lph[o];
+            for (int c = 0; c < rcols; c++) {
+                if (rkr[c] != k) continue;
+                double diff = fabs(rp[c] - l_val);
+                if (diff < min_cost) {
+                    second = min_cost;
+                    min_cost = diff;
+                    best_jR = c;
+                } else if (diff < second) {
+                    second = diff;
+                }
+            }
+            if (best_jR < 0) continue;
+            if (near) {
+                uint8_t f = 0;
+                if (second - min_cost < eps) f |= 1;
+                if (fabs(min_cost - grad_threshold) < eps) f |= 2;
+                near[o] = f;
+            }
+            if (min_cost >= grad_threshold) continue;
+            if (best_jR < 2 || best_jR >= rcols - 1) continue;
+            double cost0 = rp[best_jR - 1] - l_val;
+            double cost1 = rp[best_jR] - l_val;
+            double cost2 = rp[best_jR + 1] - l_val;
+            double num = cost1 * (cost0 - cost2);
+            double den = 2.0 * (cost0 - cost1) * (cost1 - cost2);
+            double delta = 0.0;
+            if (fabs(den) > 1e-9) delta = num / den;
+            disp[o] = (double)(j + dx_off) - (double)best_jR - delta;
+            if (best) best[o] = best_jR;
+        }
+    }
+}
+
 void zo_stereo_match(const double* lph, const double* rph, const int32_t* lk, const int32_t* rk,
                      int rows, int cols, int pha_f, double grad_threshold, double* disp,
                      int32_t* best, uint8_t* near, double eps) {
@@ -703,6 +783,89 @@ void zo_reproject(const float* disp, int rows, int cols, const double Q[16], con
                 } else {
                     xyz[3 * o] = (float)rx; xyz[3 * o + 1] = (float)ry; xyz[3 * o + 2] = (float)rz;
                 }
+                mask[o] = 1;
+            }
+        }
+    }
+}
+
+/* evaluateV2CalibPoint, src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:13-76: model
+ * tags in c3 of the x map (-1 inverse depth, -2 fitted ray, -3 z-linear x/y) and
+ * of the z map (-1 inverse depth, -4 rational); otherwise cubics in d.  Tag tests
+ * are float arithmetic, the evaluation double (built without contraction). */
+static int zo_poly_point(const float* cx, const float* cy, const float* cz, double d, double* xr, double* yr,
+                         double* zr) {
+    const float inv_tag = -1.0f, ray_tag = -2.0f, lin_tag = -3.0f, rat_tag = -4.0f;
+    if (fabsf(cz[0]) <= 1e-9 && fabsf(cz[1]) <= 1e-9 && fabsf(cz[2]) <= 1e-9 && fabsf(cz[3]) <= 1e-9) return 0;
+    if (fabsf(cx[3] - inv_tag) < 1e-6f) {
+        double d2 = d * d;
+        double inv_z = cz[0] + cz[1] * d + cz[2] * d2 + cz[3] * d2 * d;
+        if (!isfinite(inv_z) || fabs(inv_z) < 1e-12) return 0;
+        *zr = 1.0 / inv_z;
+        *xr = cx[0] * *zr;
+        *yr = cy[0] * *zr;
+    } else if (fabsf(cx[3] - ray_tag) < 1e-6f) {
+        double d2 = d * d;
+        if (fabsf(cz[3] - inv_tag) < 1e-6f) {
+            double inv_z = cz[0] + cz[1] * d + cz[2] * d2;
+            if (!isfinite(inv_z) || fabs(inv_z) < 1e-12) return 0;
+            *zr = 1.0 / inv_z;
+        } else {
+            *zr = cz[0] + cz[1] * d + cz[2] * d2 + cz[3] * d2 * d;
+        }
+        *xr = cx[0] * *zr;
+        *yr = cy[0] * *zr;
+    } else if (fabsf(cx[3] - lin_tag) < 1e-6f) {
+        if (fabsf(cz[3] - rat_tag) < 1e-6f) {
+            double denom = cz[1] * d + 1.0;
+            if (!isfinite(denom) || fabs(denom) < 1e-12) return 0;
+            *zr = cz[0] / denom;
+        } else {
+            double d2 = d * d, d3 = d2 * d;
+            *zr = cz[0] + cz[1] * d + cz[2] * d2 + cz[3] * d3;
+        }
+        *xr = cx[0] * *zr + cx[1];
+        *yr = cy[0] * *zr + cy[1];
+    } else if (fabsf(cz[3] - inv_tag) < 1e-6f) {
+        double inv_z = cz[0] + cz[1] * d + cz[2] * d * d;
+        if (!isfinite(inv_z) || fabs(inv_z) < 1e-12) return 0;
+        *zr = 1.0 / inv_z;
+        *xr = cx[0] * *zr;
+        *yr = cy[0] * *zr;
+    } else {
+        double d2 = d * d, d3 = d2 * d;
+        *xr = cx[0] + cx[1] * d + cx[2] * d2 + cx[3] * d3;
+        *yr = cy[0] + cy[1] * d + cy[2] * d2 + cy[3] * d3;
+        *zr = cz[0] + cz[1] * d + cz[2] * d2 + cz[3] * d3;
+    }
+    return isfinite(*xr) && isfinite(*yr) && isfinite(*zr);
+}
+
+/* startCalculate_v2's reprojection loop, src/JSLAB_PhaseEpipolarReconstructor_V2.cpp:500-566
+ * (maps: rows*cols*4 floats each). */
+void zo_poly_reproject(const float* disp, int rows, int cols, const float* mx, const float* my, const float* mz,
+                       const double R1[9], double min_depth, double max_depth, int use_rectified, float* xyz,
+                       uint8_t* mask) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < rows; i++) {
+        for (int j = 0; j < cols; j++) {
+            size_t o = (size_t)i * cols + j;
+            xyz[3 * o] = xyz[3 * o + 1] = xyz[3 * o + 2] = 0.0f;
+            mask[o] = 0;
+            double d = disp[o];
+            if (fabs(d) < 1e-5) continue;
+            double x, y, z;
+            if (!zo_poly_point(mx + 4 * o, my + 4 * o, mz + 4 * o, d, &x, &y, &z)) continue;
+            double rx = R1[0] * x + R1[3] * y + R1[6] * z;
+            double ry = R1[1] * x + R1[4] * y + R1[7] * z;
+            double rz = R1[2] * x + R1[5] * y + R1[8] * z;
+            if (use_rectified) {
+                if (z > min_depth && z < max_depth) {
+                    xyz[3 * o] = (float)x; xyz[3 * o + 1] = (float)y; xyz[3 * o + 2] = (float)z;
+                    mask[o] = 1;
+                }
+            } else if (rz > min_depth && rz < max_depth) {
+                xyz[3 * o] = (float)rx; xyz[3 * o + 1] = (float)ry; xyz[3 * o + 2] = (float)rz;
                 mask[o] = 1;
             }
         }

@@ -97,6 +97,9 @@ void zo_init_rectify_map(const double K[9], const double D[5], const double R[9]
 /* remap INTER_LINEAR (1/32 quantised, BORDER_CONSTANT 0) of an f64 plane. */
 void zo_remap_linear(const double* src, int srows, int scols, const float* mapx,
                      const float* mapy, int drows, int dcols, double* dst);
+/* remap INTER_LINEAR of an 8-bit image (OpenCV fixed point, BORDER_CONSTANT 0). */
+void zo_remap_u8(const uint8_t* src, int srows, int scols, const float* mapx, const float* mapy, int drows,
+                 int dcols, uint8_t* dst);
 /* remap INTER_NEAREST (BORDER_CONSTANT 0) of an i32 plane. */
 void zo_remap_nearest(const int32_t* src, int srows, int scols, const float* mapx,
                       const float* mapy, int drows, int dcols, int32_t* dst);
@@ -111,6 +114,14 @@ void zo_stereo_match(const double* lph, const double* rph, const int32_t* lk,
 /* medianBlur(5) on f32, BORDER_REPLICATE. */
 void zo_median5(const float* src, float* dst, int rows, int cols);
 
+/* ROI matching (startCalculate_v2_roi): masked left window vs right column window. */
+void zo_stereo_match_roi(const double* lph, const int32_t* lk, const uint8_t* lmask, int lcols, const double* rph,
+                         const int32_t* rk, int rcols, int rows, int dx_off, int pha_f, double grad_threshold,
+                         double* disp, int32_t* best, uint8_t* near, double eps);
+/* Per-pixel polynomial reprojection (startCalculate_v2); maps rows*cols*4 floats. */
+void zo_poly_reproject(const float* disp, int rows, int cols, const float* mx, const float* my, const float* mz,
+                       const double R1[9], double min_depth, double max_depth, int use_rectified, float* xyz,
+                       uint8_t* mask);
 /* Q reprojection.  near: 1 = depth gate within eps. */
 void zo_reproject(const float* disp, int rows, int cols, const double Q[16], const double R1[9],
                   double min_depth, double max_depth, int use_rectified, float* xyz,

@@ -2,7 +2,8 @@
 // reference classes (decoder per camera, then the V2 reconstructor): a
 // fronto-parallel plane seen by an ideal rig, hierarchical 1/8/64 x 4-step
 // fringes rendered analytically.  Exit status 0 when the plane comes back at
-// the expected depth.
+// the expected depth, and when the V2 path (coefficient maps equivalent to Q,
+// written and read back as .bin files under argv[1]) reproduces it.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -10,7 +11,21 @@
 
 #include "zim_jslab.hpp"
 
-int main() {
+// Inverse-depth maps (x-map tag -1) reproducing the Q reprojection.
+static void q_maps(const double Q[16], int rows, int cols, JSLAB_StereoCalibParams_V2& p) {
+    for (int k = 0; k < 3; k++) p.xyz_calib_coeffs[k] = zim::Image<float>(rows, cols, 4);
+    for (int i = 0; i < rows; i++)
+        for (int j = 0; j < cols; j++) {
+            float* cx = p.xyz_calib_coeffs[0].ptr() + 4 * ((size_t)i * cols + j);
+            float* cy = p.xyz_calib_coeffs[1].ptr() + 4 * ((size_t)i * cols + j);
+            float* cz = p.xyz_calib_coeffs[2].ptr() + 4 * ((size_t)i * cols + j);
+            cx[0] = (float)((j + Q[3]) / Q[11]); cx[3] = -1.0f;
+            cy[0] = (float)((i + Q[7]) / Q[11]);
+            cz[0] = (float)(Q[15] / Q[11]); cz[1] = (float)(Q[14] / Q[11]);
+        }
+}
+
+int main(int argc, char** argv) {
     const int W = 640, H = 480;
     const double f = 600.0, B = 100.0, disparity = 80.0;  // Z = f B / d = 750 mm
     const double fr[3] = {1, 8, 64};
@@ -94,5 +109,65 @@ int main() {
                 cloud.size(), frac, zmed);
     const bool ok = std::fabs(zmed - f * B / disparity) < 0.01 * f * B / disparity && frac > 0.5 &&
                     cloud.size() > z.size() / 2;
-    return ok ? 0 : 2;
+    if (!ok) return 2;
+
+    // V2: polynomial maps through the .bin format, then startCalculate_v2
+    double Q[16];
+    int rw = 0, rh = 0;
+    zim::check(zim_get_rectification(ctx->get(), nullptr, nullptr, nullptr, nullptr, Q, &rw, &rh), ctx->get(), "rect");
+    JSLAB_StereoCalibParams_V2 v2;
+    static_cast<JSLAB_StereoCalibParams_V1&>(v2) = calib;
+    q_maps(Q, rh, rw, v2);
+    if (argc > 1) {
+        const std::string fn = std::string(argv[1]) + "/stereo_v2.xml";
+        const char* sfx[3] = {"_rx.bin", "_ry.bin", "_rz.bin"};
+        for (int k = 0; k < 3; k++)
+            if (!JSLAB_StereoCalibParams_V2::saveMatBinary(std::string(argv[1]) + "/stereo_v2" + sfx[k],
+                                                           v2.xyz_calib_coeffs[k]))
+                return 3;
+        JSLAB_StereoCalibParams_V2 back;
+        static_cast<JSLAB_StereoCalibParams_V1&>(back) = calib;
+        if (!back.loadCoefficientMaps(fn)) return 4;
+        for (int k = 0; k < 3; k++)
+            if (back.xyz_calib_coeffs[k].data != v2.xyz_calib_coeffs[k].data) return 5;
+        v2 = back;
+    }
+    rec.setCalibrationParamsV2(v2);
+    rec.setData(*left, *right);
+    zim::Image<float> xq, xp;
+    zim::Image<uint8_t> pq, pp;
+    rec.startCalculate(xq, pq);
+    rec.startCalculate_v2(xp, pp);
+    size_t n = 0, diff = 0;
+    double worst = 0;
+    for (size_t i = 0; i < pq.size(); i++) {
+        diff += pq.data[i] != pp.data[i];
+        if (pq.data[i] && pp.data[i]) {
+            n++;
+            for (int c = 0; c < 3; c++)
+                worst = std::max(worst, (double)std::fabs(xq.data[3 * i + c] - xp.data[3 * i + c]) /
+                                            (1.0 + std::fabs(xq.data[3 * i + c])));
+        }
+    }
+    std::printf("{\"v2_points\": %zu, \"v2_mask_diff\": %zu, \"v2_max_rel\": %.3g}\n", n, diff, worst);
+    if (!(n > z.size() / 2 && diff <= pq.size() / 10000 && worst < 1e-5)) return 6;
+
+    // outputs: grey PLY from the rectified left image, .raw phase dump
+    if (argc > 1) {
+        zim::Image<uint8_t> gray;
+        rec.rectifyLeftImage(frames[0][0], gray);
+        if (gray.rows != rh || gray.cols != rw) return 7;
+        const std::string dir = argv[1];
+        size_t valid = 0;
+        for (uint8_t m : pq.data) valid += m != 0;
+        if (!savePointCloudToPlyBinaryWithGray(*ctx, xq, pq, gray, dir + "/cloud.ply")) return 8;
+        std::ifstream ply(dir + "/cloud.ply", std::ios::binary | std::ios::ate);
+        const std::string head = "ply\nformat binary_little_endian 1.0\nelement vertex " + std::to_string(valid) +
+                                 "\nproperty float x\nproperty float y\nproperty float z\nproperty uchar red\n"
+                                 "property uchar green\nproperty uchar blue\nend_header\n";
+        if ((size_t)ply.tellg() != head.size() + 15 * valid) return 9;
+        if (!saveRaw64F(phL, dir + "/phase_left_global.raw", dir + "/phase_left_global.info.txt")) return 10;
+        std::printf("{\"ply_vertices\": %zu}\n", valid);
+    }
+    return 0;
 }

@@ -28,8 +28,8 @@ def test_adapter_compiles_and_links(native):
 
 
 @pytest.mark.gpu
-def test_adapter_reconstructs_plane(native):
+def test_adapter_reconstructs_plane(native, tmp_path):
     exe = build()
-    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -38,12 +38,29 @@ class ReconConfig(C.Structure):
                 ("use_mls", C.c_int), ("mls_window_size", C.c_int), ("mls_spatial_sigma", C.c_float),
                 ("mls_polynomial_order", C.c_int), ("mls_max_radius", C.c_float), ("mls_iterations", C.c_int),
                 ("use_sor", C.c_int), ("sor_mean_k", C.c_int), ("sor_std_mul", C.c_double),
-                ("use_metric_gaussian", C.c_int), ("metric_gaussian_sigma", C.c_double)]
+                ("use_metric_gaussian", C.c_int), ("metric_gaussian_sigma", C.c_double),
+                ("reproject_model", C.c_int)]
 
 
 class SorStats(C.Structure):
     _fields_ = [("n_valid", C.c_double), ("mean", C.c_double), ("stddev", C.c_double), ("threshold", C.c_double),
                 ("n_far_search", C.c_uint32)]
+
+
+class RotatedRect(C.Structure):
+    _fields_ = [("center_x", C.c_float), ("center_y", C.c_float), ("width", C.c_float), ("height", C.c_float),
+                ("angle", C.c_float)]
+
+
+class Rect(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("width", C.c_int), ("height", C.c_int)]
+
+    def as_tuple(self):
+        return (self.x, self.y, self.width, self.height)
+
+
+class RectifiedROI(C.Structure):
+    _fields_ = [("left_rect", Rect), ("right_rect", Rect)]
 
 
 class PointXYZ(C.Structure):
@@ -103,6 +120,12 @@ PROTOTYPES = {
     "zim_set_calibration": (I, [V, V, I]),
     "zim_get_rectification": (I, [V, V, V, V, V, V, V, V]),
     "zim_get_rectify_maps": (I, [V, I, V, V, V]),
+    "zim_set_poly_calib": (I, [V, V, V, V, I, I]),
+    "zim_rectify_image": (I, [V, I, V, I, I, V, V]),
+    "zim_roi_source_spans": (I, [V, I, I, V, V]),
+    "zim_prepare_roi": (I, [V, V, V, V, I, V, V, V, V]),
+    "zim_reconstruct_roi": (I, [V, V, V, V, V, V, V, V, V, V, I, V, V, V, V]),
+    "zim_pack_ply": (I, [V, V, V, V, I, I, I, V, V, V]),
     "zim_rectify": (I, [V, I, V, V, I, I, I, V, V, V, V]),
     "zim_match": (I, [V, V, V, V, V, V, V, I, I, I, D, V, V, V]),
     "zim_median_reproject": (I, [V, V, V, I, I, V, V, V, V]),

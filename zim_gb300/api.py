@@ -29,8 +29,10 @@ from ._lib import (ENC_GRAYCODE, ENC_GRAYCODE_COMPLEMENTARY, ENC_HETERODYNE3, EN
 
 __all__ = ["Context", "decode_config", "recon_config", "calib_struct", "decode", "decode_phase_f64",
            "rectify", "match", "median_reproject", "filter_px_gaussian", "filter_ror", "filter_mls", "filter_sor",
-           "filter_metric_gaussian", "compact_points", "reconstruct_pair", "reconstruct_pair_host", "DecodedPhase",
+           "filter_metric_gaussian", "compact_points", "pack_ply", "rectify_image", "rotated_rect",
+           "roi_source_spans", "RectifiedROI", "prepare_roi", "reconstruct_roi", "reconstruct_pair", "reconstruct_pair_host", "DecodedPhase",
            "JSLAB_PhaseShiftDecoder", "JSLAB_PhaseShiftDecoderV2_GPU", "JSLAB_StereoCalibParams_V1",
+           "JSLAB_StereoCalibParams_V2",
            "JSLAB_PhaseEpipolarReconstructor_V2", "ZimError", "ENC_HETERODYNE3", "ENC_HIERARCHICAL",
            "ENC_GRAYCODE", "ENC_GRAYCODE_COMPLEMENTARY"]
 
@@ -92,6 +94,20 @@ class Context:
         self.P1, self.P2, self.Q = P1.reshape(3, 4), P2.reshape(3, 4), Q.reshape(4, 4)
         self.rect_w, self.rect_h = w.value, h.value
         self.src_w, self.src_h = cs.width, cs.height
+        return self
+
+    def set_poly_calib(self, cx=None, cy=None, cz=None):
+        """setCalibrationParamsV2's coefficient maps: three (rect_h, rect_w, 4)
+        float32 arrays (X, Y, Z), or None to drop them."""
+        if cx is None and cy is None and cz is None:
+            self.check(self._L.zim_set_poly_calib(self.h, None, None, None, 0, 0))
+            return self
+        maps = [np.ascontiguousarray(m, dtype=np.float32) for m in (cx, cy, cz)]
+        for m in maps:
+            if m.ndim != 3 or m.shape[2] != 4 or m.shape[:2] != maps[0].shape[:2]:
+                raise ZimError(_lib.ERR_INVALID_ARG, "coefficient maps are rows x cols x 4 float32")
+        H, W = maps[0].shape[:2]
+        self.check(self._L.zim_set_poly_calib(self.h, *(_p(m) for m in maps), H, W))
         return self
 
     def rectify_maps(self, cam: int):
@@ -291,6 +307,81 @@ def compact_points(ctx, xyz, mask):
     return pts[: int(cnt.item())]
 
 
+def pack_ply(ctx, xyz, mask, gray=None, with_gray=False):
+    """PLY vertex body of the valid points (row order) as a uint8 device tensor:
+    12 bytes (float x, y, z) per point, or 15 with with_gray (+ grey as r, g, b;
+    255 when gray is None)."""
+    H, W = mask.shape
+    rec = 15 if with_gray else 12
+    body = torch.empty(H * W * rec, dtype=torch.uint8, device=mask.device)
+    cnt = torch.zeros(1, dtype=torch.int64, device=mask.device)
+    ctx.check(_lib.load().zim_pack_ply(ctx.h, _p(xyz), _p(mask), _p(gray) if gray is not None else None,
+                                       int(bool(with_gray)), H, W, _p(body), _p(cnt), _stream()))
+    return body[: int(cnt.item()) * rec]
+
+
+def rectify_image(ctx, cam, image):
+    """rectifyLeftImage (cam 0) or the right camera's: 8-bit image remapped
+    INTER_LINEAR into the rectified frame."""
+    image = image.contiguous()
+    H, W = image.shape
+    out = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device=image.device)
+    ctx.check(_lib.load().zim_rectify_image(ctx.h, int(cam), _p(image), H, W, _p(out), _stream()))
+    return out
+
+
+def rotated_rect(roi) -> _lib.RotatedRect:
+    """cv::RotatedRect from ((cx, cy), (w, h), angle) -- OpenCV's Python form -- or as is."""
+    if isinstance(roi, _lib.RotatedRect):
+        return roi
+    (cx, cy), (w, h), a = roi
+    return _lib.RotatedRect(float(cx), float(cy), float(w), float(h), float(a))
+
+
+def roi_source_spans(roi, rows, cols):
+    """The filled rotated rectangle in the source image: (lo, hi) column per row."""
+    lo = np.empty(rows, np.int32); hi = np.empty(rows, np.int32)
+    check(_lib.load().zim_roi_source_spans(C.byref(rotated_rect(roi)), int(rows), int(cols), _p(lo), _p(hi)))
+    return lo, hi
+
+
+@dataclass
+class RectifiedROI:
+    """RectifiedROI (JSLAB_PhaseEpipolarReconstructor_V2.h:97-102): rectangles as
+    (x, y, width, height); mask is the full rectified-frame ROI mask (device)."""
+    left_rect: tuple
+    right_rect: tuple
+    mask: Optional[torch.Tensor]
+
+
+def prepare_roi(ctx: Context, roi, l_order, r_order, pha_f) -> Optional[RectifiedROI]:
+    """prepareRectifiedROI on rectified order maps; None for an empty ROI."""
+    mask = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device=l_order.device)
+    out = _lib.RectifiedROI()
+    valid = C.c_int(0)
+    ctx.check(_lib.load().zim_prepare_roi(ctx.h, C.byref(rotated_rect(roi)), _p(l_order), _p(r_order), int(pha_f),
+                                          C.byref(out), _p(mask), C.byref(valid), _stream()))
+    if not valid.value:
+        return None
+    return RectifiedROI(out.left_rect.as_tuple(), out.right_rect.as_tuple(), mask)
+
+
+def reconstruct_roi(ctx: Context, rcfg, roi: RectifiedROI, left, right, pha_f, want_disp=False):
+    """startCalculate_v2_roi on rectified (base, res, order) triples; outputs are
+    left_rect-sized (xyz, mask, disp)."""
+    lb, lr, lo = left
+    rb, rr, ro = right
+    x, y, w, h = roi.left_rect
+    xyz = torch.empty((h, w, 3), dtype=torch.float32, device=lo.device)
+    mask = torch.empty((h, w), dtype=torch.uint8, device=lo.device)
+    disp = torch.empty((h, w), dtype=torch.float32, device=lo.device) if want_disp else None
+    rr_ = _lib.RectifiedROI(_lib.Rect(*roi.left_rect), _lib.Rect(*roi.right_rect))
+    ctx.check(_lib.load().zim_reconstruct_roi(ctx.h, C.byref(rcfg), C.byref(rr_), _p(roi.mask), _p(lb), _p(lr),
+                                              _p(lo), _p(rb), _p(rr), _p(ro), int(pha_f), _p(xyz), _p(mask),
+                                              _p(disp), _stream()))
+    return xyz, mask, disp
+
+
 def reconstruct_pair(ctx, dcfg, rcfg, left, right, pha_f=0, out=None, want_disp=False):
     """Whole plain per-pair path on device frames.  Returns (xyz, mask, disp)."""
     F, H, W = left.shape
@@ -447,6 +538,14 @@ class JSLAB_StereoCalibParams_V1:
                             self.image_size[1])
 
 
+@dataclass
+class JSLAB_StereoCalibParams_V2(JSLAB_StereoCalibParams_V1):
+    """Mirror of JSLAB_StereoCalibParams_V2 (JSLAB_StereoCalibParams_V2.h:8-30): the V1
+    fields plus xyz_calib_coeffs[0..2], per-pixel (c0, c1, c2, c3) maps for X, Y
+    and Z as (rows, cols, 4) float32 (CV_32FC4)."""
+    xyz_calib_coeffs: list = field(default_factory=lambda: [np.zeros((0, 0, 4), np.float32) for _ in range(3)])
+
+
 class JSLAB_PhaseEpipolarReconstructor_V2:
     """Mirror of JSLAB_PhaseEpipolarReconstructor_V2 (JSLAB_PhaseEpipolarReconstructor_V2.h:11-171)."""
 
@@ -493,6 +592,7 @@ class JSLAB_PhaseEpipolarReconstructor_V2:
         self._rect = None
         self._pha_f = 0
         self._disp = None
+        self._use_v2 = False
 
     @property
     def context(self) -> Context:
@@ -500,6 +600,17 @@ class JSLAB_PhaseEpipolarReconstructor_V2:
 
     def setCalibrationParams(self, params: JSLAB_StereoCalibParams_V1):
         self._ctx.set_calibration(params.as_struct(), self.m_config.use_full_left_rectification)
+
+    def setCalibrationParamsV2(self, params: JSLAB_StereoCalibParams_V2):
+        """setCalibrationParamsV2 (V2.cpp:340-366): the V1 geometry, then the
+        coefficient maps when all three are non-empty."""
+        self.setCalibrationParams(params)
+        maps = [np.asarray(m) for m in params.xyz_calib_coeffs]
+        self._use_v2 = all(m.size for m in maps)
+        if self._use_v2:
+            self._ctx.set_poly_calib(*maps)
+        else:
+            self._ctx.set_poly_calib()
 
     def setData(self, left, right, left_k=None, right_k=None, left_mod=None, pha_f: int = 0):
         """left/right: DecodedPhase (exact path) or float64 absolute-phase maps with left_k/right_k.
@@ -523,11 +634,25 @@ class JSLAB_PhaseEpipolarReconstructor_V2:
 
     def startCalculate(self):
         """Runs match -> median -> reproject -> filters; returns (xyz, P)."""
+        return self._calculate(0)
+
+    def startCalculate_v2(self):
+        """startCalculate_v2 (V2.cpp:482-593): reprojection through the per-pixel
+        coefficient maps.  Without maps the reference writes no point, so
+        neither does this (the disparity map is still computed)."""
+        return self._calculate(1)
+
+    def _calculate(self, model: int):
         if self._rect is None:
             raise ZimError(_lib.ERR_INVALID_ARG, "setData first")
         c = self.m_config
         rc = c.as_struct()
         disp, _ = match(self._ctx, self._rect[0], self._rect[1], self._pha_f, c.grad_threshold, want_best=False)
+        if model == 1 and not self._use_v2:
+            dmed, xyz, mask = median_reproject(self._ctx, rc, disp)
+            self._disp = dmed
+            return torch.zeros_like(xyz), torch.zeros_like(mask)
+        rc.reproject_model = model
         dmed, xyz, mask = median_reproject(self._ctx, rc, disp)
         self._disp = dmed
         if c.use_px_gaussian:
@@ -547,3 +672,33 @@ class JSLAB_PhaseEpipolarReconstructor_V2:
 
     def getDisparityMap(self) -> torch.Tensor:
         return self._disp.clone()
+
+    def prepareRectifiedROI(self, roi_original) -> Optional[RectifiedROI]:
+        """prepareRectifiedROI (V2.cpp:595-675); None where the reference returns false."""
+        if self._rect is None:
+            return None
+        return prepare_roi(self._ctx, roi_original, self._rect[0][2], self._rect[1][2], self._pha_f)
+
+    def startCalculate_v2_roi(self, roi):
+        """startCalculate_v2_roi (V2.cpp:677-913) for a rotated rectangle or a
+        prepared RectifiedROI: a left_rect-sized (xyz, P), or (None, None) where
+        the reference releases its outputs.  Without coefficient maps it runs
+        startCalculate_v2 on the whole frame, like the reference."""
+        if self._rect is None:
+            raise ZimError(_lib.ERR_INVALID_ARG, "setData first")
+        if not self._use_v2:
+            return self.startCalculate_v2()
+        if not isinstance(roi, RectifiedROI):
+            roi = self.prepareRectifiedROI(roi)
+            if roi is None:
+                return None, None
+        rc = self.m_config.as_struct()
+        rc.reproject_model = 1
+        xyz, mask, disp = reconstruct_roi(self._ctx, rc, roi, self._rect[0], self._rect[1], self._pha_f,
+                                          want_disp=True)
+        self._disp = disp
+        return xyz, mask
+
+    def rectifyLeftImage(self, image) -> torch.Tensor:
+        """rectifyLeftImage (V2.cpp:920-924): the left 8-bit image in the rectified frame."""
+        return rectify_image(self._ctx, 0, torch.as_tensor(image).to("cuda", torch.uint8))

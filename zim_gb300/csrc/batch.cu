@@ -468,6 +468,8 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     if (!b) return ZIM_ERR_INVALID_ARG;
     zim_ctx* ctx = b->ctx;
     if (!pairs || n_pairs < 1 || !rcfg) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad argument");
+    if (rcfg->reproject_model != 0)
+        return zim_fail(ctx, ZIM_ERR_UNSUPPORTED, "the batch reprojects through each calibration's Q matrix");
     if (rcfg->use_sor || rcfg->use_mls || rcfg->use_metric_gaussian)
         return zim_fail(ctx, ZIM_ERR_UNSUPPORTED,
                         "the batch runs the pixel-domain stages; run SOR / MLS / metric Gaussian per cloud after it");

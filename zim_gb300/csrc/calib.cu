@@ -285,7 +285,48 @@ __global__ void rectify_smoothed_kernel(const int32_t* __restrict__ K16, const f
     zt::rectify_pixel_smoothed(K16, R, order, srows, scols, mapx[o], mapy[o], rbase[o], rres[o], rorder[o]);
 }
 
+// rectifyLeftImage: cv::remap INTER_LINEAR of an 8-bit image.  OpenCV rounds
+// the map to 1/32 pixel and weights the four taps with (32 - fx or fx) x
+// (32 - fy or fy) x 32, which sum to 32768 exactly; the result is
+// (sum + 16384) >> 15, taps outside the image read 0 (BORDER_CONSTANT).
+__global__ void rectify_image_kernel(const uint8_t* __restrict__ src, int srows, int scols,
+                                     const float* __restrict__ mapx, const float* __restrict__ mapy, int drows,
+                                     int dcols, uint8_t* __restrict__ dst) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= dcols || i >= drows) return;
+    size_t o = (size_t)i * dcols + j;
+    int sx = __float2int_rn(mapx[o] * 32.0f), sy = __float2int_rn(mapy[o] * 32.0f);
+    int x0 = sx >> 5, y0 = sy >> 5, fx = sx & 31, fy = sy & 31;
+    int acc = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        int xx = x0 + (t & 1), yy = y0 + (t >> 1);
+        if (xx < 0 || yy < 0 || xx >= scols || yy >= srows) continue;
+        int w = ((t >> 1) ? fy : 32 - fy) * ((t & 1) ? fx : 32 - fx) * 32;
+        acc += w * (int)__ldg(src + (size_t)yy * scols + xx);
+    }
+    dst[o] = (uint8_t)min((acc + (1 << 14)) >> 15, 255);
+}
+
 }  // namespace
+
+extern "C" ZIM_API zim_status zim_rectify_image(zim_ctx* ctx, int cam, const uint8_t* src, int rows, int cols,
+                                                uint8_t* dst, void* stream) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    if (!ctx->calibrated) return zim_fail(ctx, ZIM_ERR_NOT_CALIBRATED, "not calibrated");
+    if ((cam != 0 && cam != 1) || !src || !dst) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad argument");
+    if (rows != ctx->src_h || cols != ctx->src_w)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "image %dx%d differs from calibration %dx%d", cols, rows,
+                        ctx->src_w, ctx->src_h);
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    dim3 blk(32, 8), grd((ctx->rect_w + 31) / 32, (ctx->rect_h + 7) / 8);
+    rectify_image_kernel<<<grd, blk, 0, zim_stream(stream)>>>(src, rows, cols, ctx->d_map[cam][0], ctx->d_map[cam][1],
+                                                               ctx->rect_h, ctx->rect_w, dst);
+    ctx->launches += 1;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
 
 void zim_rect_free(zim_rect_state& st) {
     for (int k = 0; k < 2; k++)
@@ -378,6 +419,38 @@ extern "C" ZIM_API zim_status zim_set_calibration(zim_ctx* ctx, const zim_stereo
     ctx->rect_w = st.rect_w;
     ctx->rect_h = st.rect_h;
     ctx->calibrated = true;
+    if (ctx->poly_w != ctx->rect_w || ctx->poly_h != ctx->rect_h) zim_set_poly_calib(ctx, nullptr, nullptr, nullptr, 0, 0);
+    return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_set_poly_calib(zim_ctx* ctx, const float* cx, const float* cy, const float* cz,
+                                                 int rows, int cols) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const bool drop = !cx && !cy && !cz;
+    if (!drop) {
+        if (!cx || !cy || !cz) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "all three coefficient maps or none");
+        if (!ctx->calibrated) return zim_fail(ctx, ZIM_ERR_NOT_CALIBRATED, "zim_set_calibration first");
+        if (rows != ctx->rect_h || cols != ctx->rect_w)
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "coefficient maps %dx%d differ from the rectified size %dx%d",
+                            cols, rows, ctx->rect_w, ctx->rect_h);
+    }
+    ZIM_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    const size_t n = drop ? 0 : (size_t)rows * cols;
+    if (n != (size_t)ctx->poly_w * ctx->poly_h) {
+        for (int k = 0; k < 3; k++) {
+            cudaFree(ctx->d_poly[k]);
+            ctx->d_poly[k] = nullptr;
+        }
+        ctx->poly_w = ctx->poly_h = 0;
+        for (int k = 0; k < 3 && n; k++) ZIM_CUDA_TRY(ctx, cudaMalloc(&ctx->d_poly[k], n * sizeof(float4)));
+    }
+    if (drop) return ZIM_OK;
+    const float* src[3] = {cx, cy, cz};
+    for (int k = 0; k < 3; k++)
+        ZIM_CUDA_TRY(ctx, cudaMemcpy(ctx->d_poly[k], src[k], n * sizeof(float4), cudaMemcpyHostToDevice));
+    ctx->poly_w = cols;
+    ctx->poly_h = rows;
     return ZIM_OK;
 }
 

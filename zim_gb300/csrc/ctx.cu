@@ -160,6 +160,7 @@ extern "C" ZIM_API void zim_destroy(zim_ctx* ctx) {
     cudaDeviceSynchronize();
     for (int c = 0; c < 2; c++)
         for (int m = 0; m < 2; m++) cudaFree(ctx->d_map[c][m]);
+    for (int k = 0; k < 3; k++) cudaFree(ctx->d_poly[k]);
     cudaFree(ctx->scratch);
     cudaFree(ctx->d_error);
     cudaFree(ctx->d_sor_stats);
@@ -271,7 +272,7 @@ static zim_status check_pair_args(zim_ctx* ctx, const zim_decode_config* d, cons
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "mls_window_size out of range");
     if (r->use_ror && (r->radius_window_size < 0 || r->radius_window_size > ZIM_MAX_ROR_WINDOW))
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, %d]", ZIM_MAX_ROR_WINDOW);
-    return ZIM_OK;
+    return zim_check_reproject(ctx, r);
 }
 
 static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_recon_config* r, const void* lf,

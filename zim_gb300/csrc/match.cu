@@ -20,11 +20,24 @@ namespace {
 
 constexpr int MATCH_THREADS = 256;
 
-__global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
-    const int32_t* __restrict__ l_base, const float* __restrict__ l_res, const int32_t* __restrict__ l_order,
-    const int32_t* __restrict__ r_base, const float* __restrict__ r_res, const int32_t* __restrict__ r_order,
-    int cols, int pha_f, float grad_threshold, float* __restrict__ disp, int32_t* __restrict__ best_col) {
+// Left and right windows of one launch.  The whole-frame match uses the full
+// rows of both images; the ROI match a left rectangle and a right column
+// window over the same rectified rows, and an optional left mask.
+struct MatchWin {
+    const int32_t* l_base; const float* l_res; const int32_t* l_order;  // at the left window's origin
+    const int32_t* r_base; const float* r_res; const int32_t* r_order;  // at the right window's origin
+    const uint8_t* l_mask;  // at the left window's origin, or null
+    size_t stride;          // elements per image row
+    int l_cols, r_cols;     // window widths
+    int dx_off;             // left window x - right window x
+    float* disp;            // l_cols per row, row pitch out_stride
+    int32_t* best_col;
+    size_t out_stride;
+};
+
+__global__ void __launch_bounds__(MATCH_THREADS) match_kernel(MatchWin w, int pha_f, float grad_threshold) {
     extern __shared__ int4 smem_raw[];
+    const int cols = w.r_cols;
     int* s_ord = reinterpret_cast<int*>(smem_raw);
     int* s_base = s_ord + cols;
     float* s_res = reinterpret_cast<float*>(s_base + cols);
@@ -32,27 +45,40 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
     int* s_hi = s_lo + (pha_f + 1);
 
     const int row = blockIdx.x;
-    const size_t ro = (size_t)row * cols;
+    const size_t ro = (size_t)row * w.stride;
     for (int k = threadIdx.x; k <= pha_f; k += blockDim.x) {
         s_lo[k] = INT_MAX;
         s_hi[k] = -1;
     }
     for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-        s_ord[j] = r_order[ro + j];
-        s_base[j] = r_base[ro + j];
-        s_res[j] = r_res[ro + j];
+        s_ord[j] = w.r_order[ro + j];
+        s_base[j] = w.r_base[ro + j];
+        s_res[j] = w.r_res[ro + j];
     }
     __syncthreads();
     zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, threadIdx.x, blockDim.x);
     __syncthreads();
-    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
-        float d;
-        int best;
-        zt::match_pixel(j, l_order[ro + j], l_base[ro + j], l_res[ro + j], s_ord, s_base, s_res, s_lo, s_hi, cols,
-                        pha_f, grad_threshold, d, best);
-        disp[ro + j] = d;
-        if (best_col) best_col[ro + j] = best;
+    const size_t oo = (size_t)row * w.out_stride;
+    for (int j = threadIdx.x; j < w.l_cols; j += blockDim.x) {
+        float d = 0.f;
+        int best = -1;
+        if (!w.l_mask || w.l_mask[ro + j])
+            zt::match_pixel(j, w.l_order[ro + j], w.l_base[ro + j], w.l_res[ro + j], s_ord, s_base, s_res, s_lo,
+                            s_hi, cols, pha_f, grad_threshold, d, best, w.dx_off);
+        w.disp[oo + j] = d;
+        if (w.best_col) w.best_col[oo + j] = best;
     }
+}
+
+zim_status launch_match(zim_ctx* ctx, const MatchWin& w, int rows, int pha_f, double grad_threshold,
+                        cudaStream_t st) {
+    size_t smem = (size_t)w.r_cols * 12 + (size_t)(pha_f + 1) * 8;
+    // the attribute is per device and per function: set it on every call
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    match_kernel<<<rows, MATCH_THREADS, smem, st>>>(w, pha_f, (float)grad_threshold);
+    ctx->launches += 1;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
 }
 
 }  // namespace
@@ -60,14 +86,22 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(
 zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_res, const int32_t* l_order,
                             const int32_t* r_base, const float* r_res, const int32_t* r_order, int rows, int cols,
                             int pha_f, double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st) {
-    size_t smem = (size_t)cols * 12 + (size_t)(pha_f + 1) * 8;
-    // the attribute is per device and per function: set it on every call
-    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    match_kernel<<<rows, MATCH_THREADS, smem, st>>>(l_base, l_res, l_order, r_base, r_res, r_order, cols, pha_f,
-                                                    (float)grad_threshold, disp, best_col);
-    ctx->launches += 1;
-    ZIM_LAUNCH_CHECK(ctx);
-    return ZIM_OK;
+    MatchWin w{l_base, l_res, l_order, r_base, r_res, r_order, nullptr, (size_t)cols, cols, cols, 0, disp,
+               best_col, (size_t)cols};
+    return launch_match(ctx, w, rows, pha_f, grad_threshold, st);
+}
+
+// ROI matching (startCalculate_v2_roi, V2.cpp:719-778): left rectangle lx, ly,
+// lw, lh with the left mask, right columns [rx, rx + rw) of the same rows;
+// disp / best_col are lw x lh.
+zim_status zim_match_roi_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_res, const int32_t* l_order,
+                                const int32_t* r_base, const float* r_res, const int32_t* r_order,
+                                const uint8_t* l_mask, int cols, int lx, int ly, int lw, int lh, int rx, int rw,
+                                int pha_f, double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st) {
+    const size_t lo = (size_t)ly * cols + lx, ro = (size_t)ly * cols + rx;
+    MatchWin w{l_base + lo, l_res + lo, l_order + lo, r_base + ro, r_res + ro, r_order + ro,
+               l_mask ? l_mask + lo : nullptr, (size_t)cols, lw, rw, lx - rx, disp, best_col, (size_t)lw};
+    return launch_match(ctx, w, lh, pha_f, grad_threshold, st);
 }
 
 extern "C" ZIM_API zim_status zim_match(zim_ctx* ctx, const int32_t* l_base, const float* l_res,

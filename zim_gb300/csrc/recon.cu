@@ -90,8 +90,39 @@ __global__ void compact_scan_kernel(uint32_t* __restrict__ counts, int nb, uint6
     if (threadIdx.x == 0) *count_dev = carry_s;
 }
 
+// Record layouts the compaction can emit for each valid point, in row order.
+enum Emit { EMIT_POINTXYZ, EMIT_PLY_XYZ, EMIT_PLY_XYZ_GRAY };
+
+// Binary little-endian PLY vertex bodies (savePointCloudToPlyBinary and
+// savePointCloudToPlyBinaryWithGray, main.cpp:85-160): float x, y, z, then for
+// the grey variant the grey value three times as uchar red, green, blue.
+template <int E>
+__device__ __forceinline__ void emit(const float* __restrict__ xyz, const uint8_t* __restrict__ gray, size_t i,
+                                     uint32_t pos, void* __restrict__ out) {
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    if (E == EMIT_POINTXYZ) {
+        zim_point_xyz p;
+        p.x = x; p.y = y; p.z = z;
+        p.pad = 1.0f;
+        static_cast<zim_point_xyz*>(out)[pos] = p;
+    } else if (E == EMIT_PLY_XYZ) {
+        float* r = static_cast<float*>(out) + 3 * (size_t)pos;
+        r[0] = x; r[1] = y; r[2] = z;
+    } else {
+        uint8_t* r = static_cast<uint8_t*>(out) + 15 * (size_t)pos;  // byte-aligned records
+        const float v[3] = {x, y, z};
+        const uint8_t* b = reinterpret_cast<const uint8_t*>(v);
+#pragma unroll
+        for (int k = 0; k < 12; k++) r[k] = b[k];
+        const uint8_t g = gray ? gray[i] : (uint8_t)255;
+        r[12] = g; r[13] = g; r[14] = g;
+    }
+}
+
+template <int E>
 __global__ void compact_write_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
-                                     const uint32_t* __restrict__ offsets, zim_point_xyz* __restrict__ pts) {
+                                     const uint32_t* __restrict__ offsets, const uint8_t* __restrict__ gray,
+                                     void* __restrict__ out) {
     __shared__ uint32_t warp_off[CB / 32];
     size_t i = (size_t)blockIdx.x * CB + threadIdx.x;
     bool v = i < n && mask[i];
@@ -108,15 +139,7 @@ __global__ void compact_write_kernel(const float* __restrict__ xyz, const uint8_
         warp_off[threadIdx.x] = x - s;
     }
     __syncthreads();
-    if (v) {
-        uint32_t pos = offsets[blockIdx.x] + warp_off[w] + __popc(b & ((1u << lane) - 1u));
-        zim_point_xyz p;
-        p.x = xyz[3 * i];
-        p.y = xyz[3 * i + 1];
-        p.z = xyz[3 * i + 2];
-        p.pad = 1.0f;
-        pts[pos] = p;
-    }
+    if (v) emit<E>(xyz, gray, i, offsets[blockIdx.x] + warp_off[w] + __popc(b & ((1u << lane) - 1u)), out);
 }
 
 }  // namespace
@@ -125,6 +148,7 @@ zim_status zim_median_reproject_launch(zim_ctx* ctx, const zim_recon_config* cfg
                                        int cols, float* disp_out, float* xyz, uint8_t* mask, cudaStream_t st) {
     ReprojParams p;
     zt::reproj_params(ctx->Q, ctx->R1, cfg, p);
+    for (int k = 0; k < 3; k++) p.poly[k] = ctx->d_poly[k];
     dim3 blk(RX, RY), grd((cols + RX - 1) / RX, (rows + RY - 1) / RY);
     median_reproject_kernel<<<grd, blk, 0, st>>>(disp, rows, cols, p, disp_out, xyz, mask);
     ctx->launches += 1;
@@ -163,9 +187,36 @@ zim_status zim_compact_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mas
     if (!counts) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "compaction scratch");
     compact_count_kernel<<<nb, CB, 0, st>>>(mask, n, counts);
     compact_scan_kernel<<<1, 1024, 0, st>>>(counts, nb, count_dev);
-    compact_write_kernel<<<nb, CB, 0, st>>>(xyz, mask, n, counts, points);
+    compact_write_kernel<EMIT_POINTXYZ><<<nb, CB, 0, st>>>(xyz, mask, n, counts, nullptr, points);
     ctx->launches += 3;
     ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
+
+static zim_status pack_ply_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, const uint8_t* gray,
+                                  int with_gray, int rows, int cols, void* records, uint64_t* count_dev,
+                                  cudaStream_t st) {
+    size_t n = (size_t)rows * cols;
+    int nb = (int)((n + CB - 1) / CB);
+    uint32_t* counts = (uint32_t*)zim_scratch_take(ctx, (size_t)nb * 4);
+    if (!counts) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "compaction scratch");
+    compact_count_kernel<<<nb, CB, 0, st>>>(mask, n, counts);
+    compact_scan_kernel<<<1, 1024, 0, st>>>(counts, nb, count_dev);
+    if (with_gray)
+        compact_write_kernel<EMIT_PLY_XYZ_GRAY><<<nb, CB, 0, st>>>(xyz, mask, n, counts, gray, records);
+    else
+        compact_write_kernel<EMIT_PLY_XYZ><<<nb, CB, 0, st>>>(xyz, mask, n, counts, nullptr, records);
+    ctx->launches += 3;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
+
+zim_status zim_check_reproject(zim_ctx* ctx, const zim_recon_config* cfg) {
+    if (cfg->reproject_model != 0 && cfg->reproject_model != 1)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "reproject_model must be 0 (Q) or 1 (polynomial maps)");
+    // startCalculate_v2 writes no point without V2 coefficients (V2.cpp:505-548)
+    if (cfg->reproject_model == 1 && !ctx->d_poly[0])
+        return zim_fail(ctx, ZIM_ERR_NOT_CALIBRATED, "reproject_model 1 needs zim_set_poly_calib");
     return ZIM_OK;
 }
 
@@ -184,6 +235,11 @@ extern "C" ZIM_API zim_status zim_median_reproject(zim_ctx* ctx, const zim_recon
     if (s) return s;
     if (!cfg) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "null config");
     if (!ctx->calibrated) return zim_fail(ctx, ZIM_ERR_NOT_CALIBRATED, "not calibrated");
+    s = zim_check_reproject(ctx, cfg);
+    if (s) return s;
+    if (cfg->reproject_model == 1 && (rows != ctx->poly_h || cols != ctx->poly_w))
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "disparity %dx%d differs from the coefficient maps %dx%d", cols, rows,
+                        ctx->poly_w, ctx->poly_h);
     return zim_median_reproject_launch(ctx, cfg, disp, rows, cols, disp_out, xyz, mask, zim_stream(stream));
 }
 
@@ -215,4 +271,17 @@ extern "C" ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz,
     if (s) return s;
     zim_scratch_reset(ctx);
     return zim_compact_launch(ctx, xyz, mask, rows, cols, points, count_dev, zim_stream(stream));
+}
+
+extern "C" ZIM_API zim_status zim_pack_ply(zim_ctx* ctx, const float* xyz, const uint8_t* mask, const uint8_t* gray,
+                                           int with_gray, int rows, int cols, void* records, uint64_t* count_dev,
+                                           void* stream) {
+    zim_status s = check_cloud(ctx, xyz, mask, records, rows, cols);
+    if (s) return s;
+    if (!count_dev) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "null count");
+    size_t nb = ((size_t)rows * cols + CB - 1) / CB;
+    s = zim_scratch_reserve(ctx, nb * 4 + 256);
+    if (s) return s;
+    zim_scratch_reset(ctx);
+    return pack_ply_launch(ctx, xyz, mask, gray, with_gray, rows, cols, records, count_dev, zim_stream(stream));
 }

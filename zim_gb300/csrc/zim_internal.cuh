@@ -32,6 +32,9 @@ struct zim_ctx {
     double ir[2][9];  // (P_c[:, :3] R_c)^-1: rectified pixel -> camera ray
     int src_w = 0, src_h = 0, rect_w = 0, rect_h = 0;
     float* d_map[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    // per-pixel polynomial calibration maps (setCalibrationParamsV2), rect size
+    float4* d_poly[3] = {nullptr, nullptr, nullptr};
+    int poly_w = 0, poly_h = 0;
 
     // persistent scratch arena (per context, grown on demand)
     char* scratch = nullptr;
@@ -87,6 +90,9 @@ zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_
                             const int32_t* l_order, const int32_t* r_base, const float* r_res,
                             const int32_t* r_order, int rows, int cols, int pha_f,
                             double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st);
+// Checks that a reconstruction config can run on this context (reprojection
+// model and its maps).
+zim_status zim_check_reproject(zim_ctx* ctx, const zim_recon_config* cfg);
 zim_status zim_median_reproject_launch(zim_ctx* ctx, const zim_recon_config* cfg, const float* disp,
                                        int rows, int cols, float* disp_out, float* xyz,
                                        uint8_t* mask, cudaStream_t st);

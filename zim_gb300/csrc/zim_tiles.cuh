@@ -465,13 +465,15 @@ __device__ __forceinline__ float phase_diff(int bR, float rR, int bL, float rL) 
 }
 
 // One left pixel against a right row staged in shared memory (s_ord, s_base,
-// s_res) with the per-order column spans [s_lo, s_hi]: the first column of
-// minimum |phase_R - phase_L| among right pixels of the same order (strict <),
-// rejected if min >= grad_threshold or the column is < 2 or >= cols - 1, then
-// the reference's three-point sub-pixel refinement.
+// s_res; cols columns) with the per-order column spans [s_lo, s_hi]: the first
+// column of minimum |phase_R - phase_L| among right pixels of the same order
+// (strict <), rejected if min >= grad_threshold or the column is < 2 or
+// >= cols - 1, then the reference's three-point sub-pixel refinement.
+// dx_off is (left window x) - (right window x) for the ROI path
+// (startCalculate_v2_roi, V2.cpp:719-778: global left x - global right x - delta).
 __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, const int* s_ord, const int* s_base,
                                             const float* s_res, const int* s_lo, const int* s_hi, int cols, int pha_f,
-                                            float grad_threshold, float& d, int& best) {
+                                            float grad_threshold, float& d, int& best, int dx_off = 0) {
     d = 0.f;
     best = -1;
     if (k < 1 || k > pha_f) return;
@@ -494,7 +496,7 @@ __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, cons
         float num = c1 * (c0 - c2);
         float den = 2.0f * (c0 - c1) * (c1 - c2);
         float delta = fabsf(den) > 1e-9f ? num / den : 0.f;
-        d = (float)(j - bj) - delta;
+        d = (float)(j - bj + dx_off) - delta;
         best = bj;
     }
 }
@@ -523,6 +525,14 @@ struct ReprojParams {
     float min_depth, max_depth;
     double dmin_depth, dmax_depth;
     int use_rectified, use_median;
+    int model;                 // 0: Q matrix; 1: per-pixel polynomial maps
+    double dr1[9];
+    const float4* poly[3];     // x, y, z coefficient maps (c0, c1, c2, c3) per rectified pixel
+    // ROI tiles (startCalculate_v2_roi): the disparity tile starts at rectified
+    // pixel (ox, oy); points are made only where roi_mask (rectified frame,
+    // gstride pixels per row) is non-zero.  Whole frames: 0, 0, null.
+    int ox, oy, gstride;
+    const uint8_t* roi_mask;
 };
 
 inline void reproj_params(const double Q[16], const double R1[9], const zim_recon_config* cfg, ReprojParams& p) {
@@ -536,6 +546,82 @@ inline void reproj_params(const double Q[16], const double R1[9], const zim_reco
     p.dmax_depth = cfg->max_depth;
     p.use_rectified = cfg->use_rectified_coords != 0;
     p.use_median = cfg->use_disp_median_filter != 0;
+    p.model = cfg->reproject_model;
+    for (int i = 0; i < 9; i++) p.dr1[i] = R1[i];
+    p.poly[0] = p.poly[1] = p.poly[2] = nullptr;
+    p.ox = p.oy = p.gstride = 0;
+    p.roi_mask = nullptr;
+}
+
+// Per-pixel polynomial calibration, evaluateV2CalibPoint
+// (JSLAB_PhaseEpipolarReconstructor_V2.cpp:13-76): the coefficient maps carry
+// a model tag in c3 of the x map (-1 inverse depth, -2 fitted ray, -3 z-linear
+// x/y) and of the z map (-1 inverse depth, -4 rational depth); untagged maps
+// are cubics in d.  Evaluated in FP64 in the reference's operation order with
+// every product and sum rounded separately (no contraction), so the result is
+// the same bit pattern as a strict IEEE evaluation on the host.
+__device__ __forceinline__ double pm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double pa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ bool poly_tag(float c, float tag) { return fabsf(c - tag) < 1e-6f; }
+
+__device__ __forceinline__ bool poly_point(const float4& cx, const float4& cy, const float4& cz, double d, double& X,
+                                           double& Y, double& Z) {
+    if (fabsf(cz.x) <= 1e-9 && fabsf(cz.y) <= 1e-9 && fabsf(cz.z) <= 1e-9 && fabsf(cz.w) <= 1e-9) return false;
+    const double z0 = cz.x, z1 = cz.y, z2 = cz.z, z3 = cz.w;
+    if (poly_tag(cx.w, -1.0f) || poly_tag(cx.w, -2.0f)) {
+        const double d2 = pm(d, d);
+        if (poly_tag(cx.w, -1.0f) || poly_tag(cz.w, -1.0f)) {
+            // inverse depth: cubic (x-map tag -1) or quadratic (x-map tag -2, z-map tag -1)
+            double iz = pa(pa(z0, pm(z1, d)), pm(z2, d2));
+            if (poly_tag(cx.w, -1.0f)) iz = pa(iz, pm(pm(z3, d2), d));
+            if (!isfinite(iz) || fabs(iz) < 1e-12) return false;
+            Z = 1.0 / iz;
+        } else {
+            Z = pa(pa(pa(z0, pm(z1, d)), pm(z2, d2)), pm(pm(z3, d2), d));
+        }
+        X = pm((double)cx.x, Z);
+        Y = pm((double)cy.x, Z);
+    } else if (poly_tag(cx.w, -3.0f)) {
+        if (poly_tag(cz.w, -4.0f)) {
+            const double den = pa(pm(z1, d), 1.0);
+            if (!isfinite(den) || fabs(den) < 1e-12) return false;
+            Z = z0 / den;
+        } else {
+            const double d2 = pm(d, d), d3 = pm(d2, d);
+            Z = pa(pa(pa(z0, pm(z1, d)), pm(z2, d2)), pm(z3, d3));
+        }
+        X = pa(pm((double)cx.x, Z), (double)cx.y);
+        Y = pa(pm((double)cy.x, Z), (double)cy.y);
+    } else if (poly_tag(cz.w, -1.0f)) {
+        const double iz = pa(pa(z0, pm(z1, d)), pm(pm(z2, d), d));
+        if (!isfinite(iz) || fabs(iz) < 1e-12) return false;
+        Z = 1.0 / iz;
+        X = pm((double)cx.x, Z);
+        Y = pm((double)cy.x, Z);
+    } else {
+        const double d2 = pm(d, d), d3 = pm(d2, d);
+        X = pa(pa(pa((double)cx.x, pm((double)cx.y, d)), pm((double)cx.z, d2)), pm((double)cx.w, d3));
+        Y = pa(pa(pa((double)cy.x, pm((double)cy.y, d)), pm((double)cy.z, d2)), pm((double)cy.w, d3));
+        Z = pa(pa(pa(z0, pm(z1, d)), pm(z2, d2)), pm(z3, d3));
+    }
+    return isfinite(X) && isfinite(Y) && isfinite(Z);
+}
+
+// startCalculate_v2's per-pixel body (:505-547): polynomial point, optional
+// R1^T rotation, depth gate on the reported z.
+__device__ __forceinline__ void poly_reproject_point(const ReprojParams& p, size_t o, float d, float& ox, float& oy,
+                                                     float& oz, uint8_t& m) {
+    const float4 cz = __ldg(p.poly[2] + o);
+    double X, Y, Z;
+    if (!poly_point(__ldg(p.poly[0] + o), __ldg(p.poly[1] + o), cz, (double)d, X, Y, Z)) return;
+    if (p.use_rectified) {
+        if (Z > p.dmin_depth && Z < p.dmax_depth) { ox = (float)X; oy = (float)Y; oz = (float)Z; m = 1; }
+        return;
+    }
+    const double rx = pa(pa(pm(p.dr1[0], X), pm(p.dr1[3], Y)), pm(p.dr1[6], Z));
+    const double ry = pa(pa(pm(p.dr1[1], X), pm(p.dr1[4], Y)), pm(p.dr1[7], Z));
+    const double rz = pa(pa(pm(p.dr1[2], X), pm(p.dr1[5], Y)), pm(p.dr1[8], Z));
+    if (rz > p.dmin_depth && rz < p.dmax_depth) { ox = (float)rx; oy = (float)ry; oz = (float)rz; m = 1; }
 }
 
 __device__ __forceinline__ void cswap(float& a, float& b) {
@@ -607,21 +693,28 @@ __device__ __forceinline__ void median_reproject_tile(const float* __restrict__ 
     if (disp_out) disp_out[o] = d;
     float ox = 0.f, oy = 0.f, oz = 0.f;
     uint8_t m = 0;
-    if (fabsf(d) >= 1e-5f) {
+    // rectified-frame pixel (ROI tiles are offset) and its index in the maps
+    const int gx = x + p.ox, gy = y + p.oy;
+    const size_t go = p.gstride ? (size_t)gy * p.gstride + gx : o;
+    // the reference gates |d| < 1e-5 on the disparity widened to double
+    const bool has_d = fabs((double)d) >= 1e-5 && (!p.roi_mask || p.roi_mask[go]);
+    if (p.model == 1) {
+        if (has_d) poly_reproject_point(p, go, d, ox, oy, oz, m);
+    } else if (has_d) {
         float X, Y, Z;
         float w = fmaf(p.q32, d, p.q33);
         if (fabsf(w) < 1e-2f * (fabsf(p.q32 * d) + fabsf(p.q33))) {
             // near-zero disparity denominator: FP64 divide
             double wd = fma(p.dq32, (double)d, p.dq33);
             double iw = 1.0 / wd;
-            X = (float)(((double)x + p.dq03) * iw);
-            Y = (float)(((double)y + p.dq13) * iw);
+            X = (float)(((double)gx + p.dq03) * iw);
+            Y = (float)(((double)gy + p.dq13) * iw);
             Z = (float)(p.dq23 * iw);
             double zz = p.dq23 * iw;
             if (p.use_rectified) {
                 if (zz > p.dmin_depth && zz < p.dmax_depth) { ox = X; oy = Y; oz = Z; m = 1; }
             } else {
-                double xx = ((double)x + p.dq03) * iw, yy = ((double)y + p.dq13) * iw;
+                double xx = ((double)gx + p.dq03) * iw, yy = ((double)gy + p.dq13) * iw;
                 double rx = fma((double)p.r1[0], xx, fma((double)p.r1[3], yy, (double)p.r1[6] * zz));
                 double ry = fma((double)p.r1[1], xx, fma((double)p.r1[4], yy, (double)p.r1[7] * zz));
                 double rz = fma((double)p.r1[2], xx, fma((double)p.r1[5], yy, (double)p.r1[8] * zz));
@@ -629,8 +722,8 @@ __device__ __forceinline__ void median_reproject_tile(const float* __restrict__ 
             }
         } else {
             float iw = 1.0f / w;
-            X = ((float)x + p.q03) * iw;
-            Y = ((float)y + p.q13) * iw;
+            X = ((float)gx + p.q03) * iw;
+            Y = ((float)gy + p.q13) * iw;
             Z = p.q23 * iw;
             if (p.use_rectified) {
                 if (Z > p.min_depth && Z < p.max_depth) { ox = X; oy = Y; oz = Z; m = 1; }
