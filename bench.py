@@ -10,6 +10,7 @@ rectify -> match -> 5x5 median -> Q reprojection -> SOR (k = 30) -> MLS
 exceed the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--width W --height H]   (the same workload scaled; profiling runs)
 
 N > 1 runs under torchrun: independent replicas, one pair per rank per step
 (weak scaling, no collective on the data path); the time is the max over ranks.
@@ -35,6 +36,12 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mpoints/s at 5 MP (plain per-pair GPU path)"
 UNIT = "Mpoints/s"
 WORKLOAD = "5MP pair: 2448x2048 x2 cams, hierarchical 1/8/64 x 4 steps, u16 12-bit; decode+rectify+match+median+reproject+SOR(k30)+MLS(r2mm,o2)+Gaussian(0.5mm)"
+
+
+def workload_name(W, H):
+    if (W, H) == (2448, 2048):
+        return WORKLOAD
+    return WORKLOAD.replace("5MP pair: 2448x2048", f"{W}x{H} pair (5 MP workload scaled)")
 
 
 def env_rank():
@@ -154,7 +161,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    spec = synth.config1(seed=1 + rank)
+    spec = synth.config1(seed=1 + rank, width=args.width, height=args.height)
     L, R = spec.render(0), spec.render(1)
     F, H, W = L.shape
     ctx = api.Context(local)
@@ -246,9 +253,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (u16 samples; FP64 only for near-zero-disparity divides)",
             "data": "synthetic (seeded scene renderer, zim_gb300/synth)",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "rect": [ctx.rect_w, ctx.rect_h],
+            "config": {"workload": workload_name(W, H), "width": W, "height": H, "rect": [ctx.rect_w, ctx.rect_h],
                        "frames_per_camera": F, "points_per_pair": n_pts, "parallelism": f"replicas x{world}",
-                       "l2": "inputs 240 MB per pair > 129 MB L2 (no flush)"},
+                       "l2": (f"inputs {2 * L.nbytes / 1e6:.0f} MB per pair > 129 MB L2 (no flush)"
+                              if 2 * L.nbytes > 129e6 else "inputs smaller than L2: profiling size only")},
             "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms, 4)},
             "gpu_launches": int(launches),
@@ -571,6 +579,8 @@ def main():
     ap.add_argument("--refine", action="store_true", help="also run calibration refinement (32 poses)")
     ap.add_argument("--refine-poses", type=int, default=32)
     ap.add_argument("--refine-iters", type=int, default=200)
+    ap.add_argument("--width", type=int, default=2448, help="camera width (default: the 5 MP workload)")
+    ap.add_argument("--height", type=int, default=2048)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
