@@ -238,6 +238,20 @@ ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_config* cfg
                                        const int32_t* r_base, const float* r_res, const int32_t* r_order,
                                        int pha_f, float* xyz, uint8_t* mask, float* disp, void* stream);
 
+/* JSLAB_StereoCalib_V2::computePixelwiseDepthCalibration (JSLAB_StereoCalib_V2.cpp:113-240):
+ * n_planes reference planes (disps[k] / masks[k]: DEVICE rows*cols float
+ * disparity and 8-bit mask, passed as a host array of device pointers; a
+ * sample needs mask != 0 and d > 0), reprojected through Q (row-major 4x4, the
+ * rectification the disparities were measured in).  Each plane is fitted by
+ * PCA (plane_eqs[4k..4k+3] = A, B, C, D with unit normal; host, may be NULL);
+ * each pixel with >= 4 samples gets least-squares cubics in d for X, Y and Z
+ * of the samples projected onto their planes, written as float4
+ * (c0, c1, c2, c3) into cx / cy / cz (DEVICE, rows*cols each; zeros where
+ * fewer than 4 samples).  1 <= n_planes <= 64.  Synchronises the stream. */
+ZIM_API zim_status zim_fit_poly_calib(zim_ctx* ctx, const double Q[16], const float* const* disps,
+                                      const uint8_t* const* masks, int n_planes, int rows, int cols,
+                                      float* cx, float* cy, float* cz, double* plane_eqs, void* stream);
+
 /* rectifyLeftImage (V2.cpp:920-924) for either camera: cv::remap INTER_LINEAR
  * of an 8-bit image (src_h x src_w, device) through the camera's rectification
  * maps with OpenCV's fixed-point bilinear weights (1/32-pixel positions,

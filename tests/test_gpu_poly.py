@@ -120,3 +120,90 @@ def test_poly_errors(calibrated):
     with pytest.raises(_lib.ZimError) as e:
         ctx.set_poly_calib(m, m, m)
     assert e.value.status == _lib.ERR_INVALID_ARG
+
+
+# ------------------------------------------------- cubic calibration fit ----
+
+def _fit_case(ctx, n_planes=6, seed=3, noise=0.02):
+    from oracle import calib_fit as F
+    spec, *_ = scene_data("config0")
+    ctx.set_calibration(spec.rig.as_dict(), False)
+    H, W = 48, 64  # a corner of the rectified frame keeps the FP64 oracle fast
+    disps, masks = F.synthetic_planes(ctx.Q, H, W, n_planes=n_planes, seed=seed, noise=noise, dropout=0.1)
+    return F, disps, masks, H, W
+
+
+@pytest.mark.gpu
+def test_fit_poly_calib_matches_oracle(ctx):
+    from zim_gb300 import api
+    F, disps, masks, H, W = _fit_case(ctx)
+    g = api.fit_poly_calib(ctx, ctx.Q, [torch.from_numpy(d).cuda() for d in disps],
+                           [torch.from_numpy(m).cuda() for m in masks])
+    gx, gy, gz = (t.cpu().numpy() for t in g[:3])
+    ox, oy, oz, oeq = F.fit(ctx.Q, disps, masks)
+    # planes: the same up to the eigenvector's sign
+    for a, b in zip(g[3], oeq):
+        s = 1.0 if a[:3] @ b[:3] > 0 else -1.0
+        assert np.allclose(a, s * b, rtol=0, atol=1e-9 * max(1.0, abs(b[3])))
+    fitted = np.count_nonzero(np.stack([(m > 0) & (d > 0) for d, m in zip(disps, masks)]).sum(0) >= 4)
+    assert np.count_nonzero(gz.any(-1)) == np.count_nonzero(oz.any(-1)) == fitted
+    # the two least-squares cubics agree at every sample disparity to the
+    # float32 rounding of their coefficients
+    for d, m in zip(disps, masks):
+        r, c = np.nonzero((m > 0) & (d > 0))
+        dv = d[r, c].astype(np.float64)
+        for gc, oc in ((gx, ox), (gy, oy), (gz, oz)):
+            a, b = F.evaluate(gc[r, c], dv), F.evaluate(oc[r, c], dv)
+            scale = sum(np.abs(oc[r, c, k].astype(np.float64) * dv ** k) for k in range(4))
+            live = oc[r, c].any(-1)
+            assert np.all(np.abs(a - b)[live] <= 4e-7 * scale[live] + 1e-6)
+
+
+@pytest.mark.gpu
+def test_fitted_maps_reconstruct_the_planes(ctx):
+    """Fit on the whole rectified frame, then reproject one plane's disparity
+    through the maps (reproject_model 1): the points lie on that plane."""
+    from oracle import calib_fit as F
+    from zim_gb300 import api
+    spec, *_ = scene_data("config0")
+    ctx.set_calibration(spec.rig.as_dict(), False)
+    H, W = ctx.rect_h, ctx.rect_w
+    # 800-1000 mm: over a 1.25:1 depth range a cubic in d follows z = Q23 / (Q32 d + Q33)
+    # to ~1e-4 relative
+    disps, masks = F.synthetic_planes(ctx.Q, H, W, n_planes=6, seed=4, noise=0.0, dropout=0.0, z0=800.0, z1=1000.0)
+    cx, cy, cz, eqs = api.fit_poly_calib(ctx, ctx.Q, [torch.from_numpy(d).cuda() for d in disps],
+                                         [torch.from_numpy(m).cuda() for m in masks])
+    ctx.set_poly_calib(cx.cpu().numpy(), cy.cpu().numpy(), cz.cpu().numpy())
+    try:
+        rc = api.recon_config(reproject_model=1, use_disp_median_filter=0, max_depth=1e4)
+        _, xyz, mask = api.median_reproject(ctx, rc, torch.from_numpy(disps[2]).cuda())
+        p = xyz.cpu().numpy()[mask.cpu().numpy() > 0].astype(np.float64)
+        assert p.shape[0] > 0.9 * H * W
+        dist = p @ eqs[2, :3] + eqs[2, 3]
+        assert np.abs(dist).max() < 5e-4 * np.abs(p[:, 2]).max()
+    finally:
+        ctx.set_poly_calib()
+        ctx.set_calibration(spec.rig.as_dict(), True)
+
+
+@pytest.mark.gpu
+def test_stereo_calib_v2_class_roundtrip(ctx, tmp_path):
+    from oracle import calib_fit as F
+    from zim_gb300 import api, calib_io
+    spec, *_ = scene_data("config0")
+    rig = spec.rig.as_dict()
+    base = api.JSLAB_StereoCalibParams_V1(rig["K"], rig["D"], rig["R"], rig["t"], (rig["width"], rig["height"]))
+    cal = api.JSLAB_StereoCalib_V2((rig["width"], rig["height"]), base, ctx=api.Context(0))
+    cal._ctx.set_calibration(rig, False)
+    disps, masks = F.synthetic_planes(cal._ctx.Q, rig["height"], rig["width"], n_planes=5, seed=6)
+    for d, m in zip(disps, masks):
+        cal.addPlaneReferenceData(d, m)
+    cal.computePixelwiseDepthCalibration()
+    fn = str(tmp_path / "stereo_v2.xml")
+    assert cal.saveCalibResult(fn)
+    back = api.JSLAB_StereoCalibParams_V2()
+    assert calib_io.loadStereoCalibParams_V2(fn, back)
+    for a, b in zip(cal.getParams().xyz_calib_coeffs, back.xyz_calib_coeffs):
+        assert np.array_equal(a, b) and a.shape == (rig["height"], rig["width"], 4)
+    cal.clearPlaneReferenceData()
+    assert cal._disps == []

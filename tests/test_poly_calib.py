@@ -246,3 +246,43 @@ def test_file_storage_yaml_and_opencv_xml_text(tmp_path):
 def test_recon_config_reproject_model_default(native):
     from zim_gb300 import api
     assert api.recon_config().reproject_model == 0
+
+
+# ------------------------------------------------- cubic calibration fit ----
+
+def _small_rig_q():
+    f, B = 600.0, 150.0
+    K0 = np.array([[f, 0, 47.5], [0, f, 31.5], [0, 0, 1]])
+    K1 = np.array([[f, 0, 45.0], [0, f, 31.5], [0, 0, 1]])
+    c = O.make_calib([K0, K1], [np.zeros(5)] * 2, np.eye(3), [-B, 0, 0], 96, 64)
+    return O.rectification(c, False)
+
+
+def test_fit_oracle_recovers_planes_and_points():
+    from oracle import calib_fit as F
+    R1, R2, P1, P2, Q, w, h = _small_rig_q()
+    disps, masks = F.synthetic_planes(Q, h, w, n_planes=6, seed=1, noise=0.0, dropout=0.0)
+    cx, cy, cz, eqs = F.fit(Q, disps, masks)
+    # the PCA plane of noise-free samples holds every sample
+    for k, (d, m) in enumerate(zip(disps, masks)):
+        r, c = np.nonzero(m)
+        x, y, z = F.q_points(Q, d[r, c].astype(np.float64), r, c)
+        dist = eqs[k, 0] * x + eqs[k, 1] * y + eqs[k, 2] * z + eqs[k, 3]
+        assert np.abs(dist).max() < 1e-6 * np.abs(z).max()
+    # a cubic in d approximates z = Q23 / (Q32 d + Q33) over a 2:1 depth range
+    # (600-1200 mm) to about 0.2 % -- the model's own limit
+    for d, m in zip(disps, masks):
+        r, c = np.nonzero(m)
+        dv = d[r, c].astype(np.float64)
+        x, y, z = F.q_points(Q, dv, r, c)
+        zf = F.evaluate(cz[r, c], dv)
+        assert np.max(np.abs(zf - z) / z) < 3e-3
+
+
+def test_fit_oracle_needs_four_samples():
+    from oracle import calib_fit as F
+    R1, R2, P1, P2, Q, w, h = _small_rig_q()
+    disps, masks = F.synthetic_planes(Q, h, w, n_planes=4, seed=2, noise=0.0, dropout=0.0)
+    masks[0][10, 20] = 0
+    cx, cy, cz, _ = F.fit(Q, disps, masks)
+    assert not cz[10, 20].any() and cz[11, 20].any()

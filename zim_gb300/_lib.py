@@ -123,6 +123,7 @@ PROTOTYPES = {
     "zim_set_poly_calib": (I, [V, V, V, V, I, I]),
     "zim_rectify_image": (I, [V, I, V, I, I, V, V]),
     "zim_roi_source_spans": (I, [V, I, I, V, V]),
+    "zim_fit_poly_calib": (I, [V, V, V, V, I, I, I, V, V, V, V, V]),
     "zim_prepare_roi": (I, [V, V, V, V, I, V, V, V, V]),
     "zim_reconstruct_roi": (I, [V, V, V, V, V, V, V, V, V, V, I, V, V, V, V]),
     "zim_pack_ply": (I, [V, V, V, V, I, I, I, V, V, V]),

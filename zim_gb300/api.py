@@ -30,7 +30,8 @@ from ._lib import (ENC_GRAYCODE, ENC_GRAYCODE_COMPLEMENTARY, ENC_HETERODYNE3, EN
 __all__ = ["Context", "decode_config", "recon_config", "calib_struct", "decode", "decode_phase_f64",
            "rectify", "match", "median_reproject", "filter_px_gaussian", "filter_ror", "filter_mls", "filter_sor",
            "filter_metric_gaussian", "compact_points", "pack_ply", "rectify_image", "rotated_rect",
-           "roi_source_spans", "RectifiedROI", "prepare_roi", "reconstruct_roi", "reconstruct_pair", "reconstruct_pair_host", "DecodedPhase",
+           "roi_source_spans", "RectifiedROI", "prepare_roi", "reconstruct_roi", "fit_poly_calib",
+           "JSLAB_StereoCalib_V2", "reconstruct_pair", "reconstruct_pair_host", "DecodedPhase",
            "JSLAB_PhaseShiftDecoder", "JSLAB_PhaseShiftDecoderV2_GPU", "JSLAB_StereoCalibParams_V1",
            "JSLAB_StereoCalibParams_V2",
            "JSLAB_PhaseEpipolarReconstructor_V2", "ZimError", "ENC_HETERODYNE3", "ENC_HIERARCHICAL",
@@ -380,6 +381,81 @@ def reconstruct_roi(ctx: Context, rcfg, roi: RectifiedROI, left, right, pha_f, w
                                               _p(lo), _p(rb), _p(rr), _p(ro), int(pha_f), _p(xyz), _p(mask),
                                               _p(disp), _stream()))
     return xyz, mask, disp
+
+
+def fit_poly_calib(ctx: Context, Q, disps, masks):
+    """computePixelwiseDepthCalibration on device disparity maps (float32) and
+    masks (uint8) of the reference planes: returns (cx, cy, cz) as
+    (rows, cols, 4) float32 device tensors and the plane equations (n, 4)."""
+    disps = [d.contiguous() for d in disps]
+    masks = [m.contiguous() for m in masks]
+    n = len(disps)
+    H, W = disps[0].shape
+    for d, m in zip(disps, masks):
+        if d.shape != (H, W) or m.shape != (H, W) or d.dtype != torch.float32 or m.dtype != torch.uint8:
+            raise ZimError(_lib.ERR_INVALID_ARG, "disparities float32 and masks uint8 of one size")
+    out = [torch.empty((H, W, 4), dtype=torch.float32, device=disps[0].device) for _ in range(3)]
+    dp = (C.c_void_p * n)(*[d.data_ptr() for d in disps])
+    mp = (C.c_void_p * n)(*[m.data_ptr() for m in masks])
+    eqs = np.zeros((n, 4))
+    Qa = np.ascontiguousarray(np.asarray(Q, np.float64).reshape(16))
+    ctx.check(_lib.load().zim_fit_poly_calib(ctx.h, _p(Qa), dp, mp, n, H, W, *(_p(o) for o in out), _p(eqs),
+                                             _stream()))
+    return out[0], out[1], out[2], eqs
+
+
+class JSLAB_StereoCalib_V2:
+    """The V2 depth-calibration part of JSLAB_StereoCalib_V2 (JSLAB_StereoCalib_V2.h):
+    loadBaseCalibration, addPlaneReferenceData, clearPlaneReferenceData,
+    computePixelwiseDepthCalibration, getParams, saveCalibResult.  The base
+    stereo calibration (calibrateCamera / stereoCalibrate on target images) is
+    taken as given: a JSLAB_StereoCalibParams_V1 or a V1 file."""
+
+    def __init__(self, img_size, base: Optional[JSLAB_StereoCalibParams_V1] = None, ctx: Optional[Context] = None):
+        self.m_img_size = tuple(img_size)
+        self._base = base
+        self._ctx = ctx or Context(torch.cuda.current_device())
+        self._disps, self._masks = [], []
+        self._coeffs = None
+
+    def loadBaseCalibration(self, filename: str) -> bool:
+        from . import calib_io
+        p = JSLAB_StereoCalibParams_V1()
+        if not calib_io.loadStereoCalibParams_V1(filename, p):
+            return False
+        self._base = p
+        self.m_img_size = tuple(p.image_size)
+        return True
+
+    def addPlaneReferenceData(self, disp_map, mask):
+        self._disps.append(torch.as_tensor(disp_map).to("cuda", torch.float32).contiguous())
+        self._masks.append(torch.as_tensor(mask).to("cuda", torch.uint8).contiguous())
+
+    def clearPlaneReferenceData(self):
+        self._disps, self._masks = [], []
+
+    def computePixelwiseDepthCalibration(self):
+        """stereoRectify(flags 0, alpha -1, new size = the image size), then the fit."""
+        if self._base is None:
+            raise ZimError(_lib.ERR_NOT_CALIBRATED, "no base calibration")
+        b = self._base
+        self._ctx.set_calibration(calib_struct(b.camera_matrix, b.dist_coeffs, b.R, b.t, *self.m_img_size), False)
+        cx, cy, cz, eqs = fit_poly_calib(self._ctx, self._ctx.Q, self._disps, self._masks)
+        self._coeffs = [t.cpu().numpy() for t in (cx, cy, cz)]
+        self.plane_eqs = eqs
+
+    def getParams(self) -> "JSLAB_StereoCalibParams_V2":
+        b = self._base
+        p = JSLAB_StereoCalibParams_V2([np.array(k, float) for k in b.camera_matrix],
+                                       [np.array(d, float) for d in b.dist_coeffs], np.array(b.R, float),
+                                       np.array(b.t, float), tuple(self.m_img_size))
+        if self._coeffs is not None:
+            p.xyz_calib_coeffs = [c.copy() for c in self._coeffs]
+        return p
+
+    def saveCalibResult(self, filename: str) -> bool:
+        from . import calib_io
+        return calib_io.saveStereoCalibParams(filename, self.getParams())
 
 
 def reconstruct_pair(ctx, dcfg, rcfg, left, right, pha_f=0, out=None, want_disp=False):

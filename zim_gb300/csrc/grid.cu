@@ -425,60 +425,7 @@ __constant__ signed char c_spiral[WIN_N][2] = {
 static_assert(WIN_W * WIN_H <= TILE_MAX_CAND, "pixel window staged in the candidate buffer");
 static_assert(TILE_MAX_CELLS <= 8 * TILE_T, "cell scan: eight cells per thread");
 
-// Per-thread buffered selection of the K1 smallest squared distances, in
-// column tid of a [cap][TILE_T] shared array.  Values within the current bound
-// are appended unsorted; a full buffer is sorted, cut back to K1 entries and
-// the bound tightened to its K1-th value.  Appending keeps the lanes of a warp
-// in step; each lane sorts its own short list once at the end.
-constexpr int SEL_SLACK = 17;  // cap = K1 + SEL_SLACK
-struct KSel {
-    float* L;  // entry j at L[j * TILE_T]
-    int cnt, K1, cap;
-    float thr;
-    __device__ __forceinline__ float at(int j) const { return L[j * TILE_T]; }
-    __device__ __forceinline__ void sort() {
-        for (int a = 1; a < cnt; a++) {
-            const float v = L[a * TILE_T];
-            int b = a;
-            while (b > 0 && L[(b - 1) * TILE_T] > v) {
-                L[b * TILE_T] = L[(b - 1) * TILE_T];
-                b--;
-            }
-            L[b * TILE_T] = v;
-        }
-    }
-    __device__ __forceinline__ void push(float d2) {
-        if (d2 > thr) return;
-        L[cnt * TILE_T] = d2;
-        if (++cnt == cap) {
-            sort();
-            cnt = K1;
-            thr = L[(K1 - 1) * TILE_T];
-        }
-    }
-    // Mean distance to the k = K1 - 1 neighbours (needs cnt >= K1): drops the
-    // cnt - K1 largest entries, then sums the roots of the K1 smallest (the
-    // query's own zero among them) in fixed point.
-    __device__ __forceinline__ float mean_dist(int k) {
-        while (cnt > K1) {
-            int jm = 0;
-            float vm = L[0];
-            for (int j = 1; j < cnt; j++) {
-                const float v = L[j * TILE_T];
-                if (v > vm) { vm = v; jm = j; }
-            }
-            cnt--;
-            L[jm * TILE_T] = L[cnt * TILE_T];
-        }
-        float vmax = 0.f;
-        for (int j = 0; j < cnt; j++) vmax = fmaxf(vmax, L[j * TILE_T]);
-        const int e = root_exponent(vmax);
-        const float sc = root_scale(e);
-        long long sum = 0;
-        for (int j = 0; j < cnt; j++) sum += root_fixed(L[j * TILE_T], sc);
-        return fixed_mean(sum, e, k);
-    }
-};
+constexpr int SV_CAP = 128;  // survivors per warp query (k + 1 <= 64 of them kept)
 
 // Phase 1: one CTA per 16 x 8 pixel tile on the finest level.
 //  - Window bound: the query and its k nearest valid pixels (in pixel
@@ -491,17 +438,19 @@ struct KSel {
 //    distance to the box boundary.
 //  - Each in-box query scans only the cells its ball of squared radius
 //    min(tau0, g^2) touches; holding k + 1 candidates within that ball, it is
-//    exact.
-// Out-of-box points run a per-thread ring search.  Unresolved queries are
+//    exact.  The warp does this one query at a time, lanes over candidates.
+// Queries the box cannot settle search the finest-level cells that hold the
+// ball of radius sqrt(tau0) (up to FINE_RINGS rings).  Unresolved queries are
 // appended to the deferred list with md = -1.
 __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __restrict__ xyz,
                                                               const uint8_t* __restrict__ mask, int rows, int cols,
                                                               int k, Level g, GridStats* s, float* __restrict__ md_out,
                                                               unsigned* __restrict__ deferred) {
     extern __shared__ float4 tile_smem[];
-    float4* cand = tile_smem;                                         // TILE_MAX_CAND
-    float* Ls = reinterpret_cast<float*>(tile_smem + TILE_MAX_CAND);  // (k + 1) x TILE_T
+    float4* cand = tile_smem;                  // TILE_MAX_CAND
     __shared__ int s_off[TILE_MAX_CELLS + 1];  // candidate offset of each box cell
+    __shared__ float s_sv[TILE_T / 32 * SV_CAP];  // per-warp survivor lists
+    __shared__ int s_nsv[TILE_T / 32];
     __shared__ unsigned s_ws[32];
     __shared__ int s_box[6];
     __shared__ float s_zc;
@@ -641,63 +590,120 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
         by0 = max(lo1, __float2int_rd((qy - R) * ic)); by1 = min(lo1 + (int)ey - 1, __float2int_rd((qy + R) * ic));
         bz0 = max(lo2, __float2int_rd((qz - R) * ic)); bz1 = min(lo2 + (int)ez - 1, __float2int_rd((qz + R) * ic));
     }
-    // The warp scans the union of its queries' cell ranges in step: every lane
-    // reads the same candidate (a shared-memory broadcast) and keeps it when it
-    // lies within the lane's own bound.
+    // Warp-cooperative selection, one query at a time: the lanes split the
+    // query's candidate cells, keep the squared distances within its bound in
+    // the warp's survivor list, then drop the largest until k + 1 remain and
+    // sum their roots in fixed point (the same bits on every path).
+    //  - fast queries read the cell-sorted box in shared memory (consecutive
+    //    lanes, consecutive candidates);
+    //  - the others (and fast queries the box could not settle) search the
+    //    rings of finest cells that hold the ball of their window bound tau0,
+    //    one cell per lane from the global table;
+    //  - what neither settles is deferred to the far search with md = -1.
     const unsigned full = 0xffffffffu;
-    const int ux0 = __reduce_min_sync(full, bx0), ux1 = __reduce_max_sync(full, bx1);
-    const int uy0 = __reduce_min_sync(full, by0), uy1 = __reduce_max_sync(full, by1);
-    const int uz0 = __reduce_min_sync(full, bz0), uz1 = __reduce_max_sync(full, bz1);
-    if (ux0 != INT_MAX) {  // some lane of the warp is on the fast path
-        KSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, thr};
-        for (int iz = uz0; iz <= uz1; iz++)
-            for (int iy = uy0; iy <= uy1; iy++) {
-                const int row = (int)(((long long)(iz - lo2) * ey + (iy - lo1)) * ex) - lo0;
-                const int j1 = s_off[row + ux1 + 1];
-                for (int j = s_off[row + ux0]; j < j1; j++) {
-                    const float4 p = cand[j];
-                    const float d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
-                    if (fq) sel.push(d2);
-                }
-            }
-        if (fq && sel.cnt >= K1) {
-            md_out[i] = sel.mean_dist(k);
-            return;
-        }
-    }
-    if (!active) return;
-    if (!fq) {
-        // per-thread ring search on the finest level
-        KSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, INFINITY};
-        for (int r = 0; r <= FINE_RINGS; r++) {
-            // cells at Chebyshev distance exactly r
-            for (int dz = -r; dz <= r; dz++)
-                for (int dy = -r; dy <= r; dy++) {
-                    const int step = (r == 0 || dz == -r || dz == r || dy == -r || dy == r) ? 1 : 2 * r;
-                    for (int dx = -r; dx <= r; dx += step) {
-                        const int cx = c[0] + dx, cy = c[1] + dy, cz = c[2] + dz;
-                        const uint2 b = bucket(g, cx, cy, cz);
-                        for (unsigned u = b.x; u < b.x + b.y; u++) {
-                            const float4 p = __ldg(g.pts + u);
-                            int px, py, pz;
-                            cell_of(p.x, p.y, p.z, ic, px, py, pz);
-                            if (px == cx && py == cy && pz == cz) sel.push(sqdist(p.x - qx, p.y - qy, p.z - qz));
+    const int lane = tid & 31, wid = tid >> 5;
+    float* sv = s_sv + wid * SV_CAP;
+    bool done = false;
+    // rings that hold every point within sqrt(tau0) of the query (|floor a - floor b| <= ceil |a - b|)
+    int rr = INT_MAX;
+    if (active && tau0 < INFINITY) rr = (int)ceilf((sqrtf(tau0) + margin) * ic);
+    for (int pass = 0; pass < 2; pass++) {
+        unsigned todo = __ballot_sync(full, pass == 0 ? fq : (active && !done && rr <= FINE_RINGS));
+        while (todo) {
+            const int q = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const float Qx = __shfl_sync(full, qx, q), Qy = __shfl_sync(full, qy, q), Qz = __shfl_sync(full, qz, q);
+            const float T = __shfl_sync(full, pass == 0 ? thr : tau0, q);
+            int nsv = 0;
+            if (pass == 0) {
+                const int X0 = __shfl_sync(full, bx0, q), X1 = __shfl_sync(full, bx1, q);
+                const int Y0 = __shfl_sync(full, by0, q), Y1 = __shfl_sync(full, by1, q);
+                const int Z0 = __shfl_sync(full, bz0, q), Z1 = __shfl_sync(full, bz1, q);
+                for (int iz = Z0; iz <= Z1; iz++)
+                    for (int iy = Y0; iy <= Y1; iy++) {
+                        const int row = (int)(((long long)(iz - lo2) * ey + (iy - lo1)) * ex) - lo0;
+                        const int j0 = s_off[row + X0], j1 = s_off[row + X1 + 1];
+                        for (int jb = j0; jb < j1; jb += 32) {
+                            const int j = jb + lane;
+                            float d2 = INFINITY;
+                            if (j < j1) {
+                                const float4 p = cand[j];
+                                d2 = sqdist(p.x - Qx, p.y - Qy, p.z - Qz);
+                            }
+                            const bool keep = d2 <= T;
+                            const unsigned b = __ballot_sync(full, keep);
+                            const int pos = nsv + __popc(b & ((1u << lane) - 1u));
+                            if (keep && pos < SV_CAP) sv[pos] = d2;
+                            nsv += __popc(b);
                         }
                     }
+            } else {
+                const int C0 = __shfl_sync(full, c[0], q), C1 = __shfl_sync(full, c[1], q);
+                const int C2 = __shfl_sync(full, c[2], q), R = __shfl_sync(full, rr, q);
+                const int side = 2 * R + 1, ncell = side * side * side;
+                if (lane == 0) s_nsv[wid] = 0;
+                __syncwarp();
+                for (int t = lane; t < ncell; t += 32) {
+                    const int cx = C0 - R + t % side, cy = C1 - R + (t / side) % side, cz = C2 - R + t / (side * side);
+                    const uint2 b = bucket(g, cx, cy, cz);
+                    for (unsigned u = b.x; u < b.x + b.y; u++) {
+                        const float4 p = __ldg(g.pts + u);
+                        int px, py, pz;
+                        cell_of(p.x, p.y, p.z, ic, px, py, pz);
+                        if (px != cx || py != cy || pz != cz) continue;
+                        const float d2 = sqdist(p.x - Qx, p.y - Qy, p.z - Qz);
+                        if (d2 > T) continue;
+                        const int pos = atomicAdd(&s_nsv[wid], 1);
+                        if (pos < SV_CAP) sv[pos] = d2;
+                    }
                 }
-            float gr = fmaxf(r * cell - margin, 0.f);
-            if (sel.cnt >= K1) {
-                sel.sort();
-                if (sel.at(K1 - 1) <= gr * gr) {
-                    md_out[i] = sel.mean_dist(k);
-                    return;
+                __syncwarp();
+                nsv = s_nsv[wid];
+            }
+            __syncwarp();
+            if (nsv < K1 || nsv > SV_CAP) continue;  // warp-uniform: not settled here
+            // keys: squared-distance bits + 1 (non-negative floats order as unsigned); 0 = empty
+            unsigned key[SV_CAP / 32];
+#pragma unroll
+            for (int r = 0; r < SV_CAP / 32; r++) {
+                const int idx = lane + 32 * r;
+                key[r] = idx < nsv ? __float_as_uint(sv[idx]) + 1u : 0u;
+            }
+            for (int m = nsv - K1; m > 0; m--) {
+                unsigned lm = 0;
+#pragma unroll
+                for (int r = 0; r < SV_CAP / 32; r++) lm = max(lm, key[r]);
+                const unsigned wm = __reduce_max_sync(full, lm);
+                const unsigned own = __ballot_sync(full, lm == wm);
+                if (lane == __ffs(own) - 1) {
+                    bool gone = false;
+#pragma unroll
+                    for (int r = 0; r < SV_CAP / 32; r++)
+                        if (!gone && key[r] == wm) { key[r] = 0u; gone = true; }
                 }
+            }
+            unsigned lm = 0;
+#pragma unroll
+            for (int r = 0; r < SV_CAP / 32; r++) lm = max(lm, key[r]);
+            const float vmax = __uint_as_float(__reduce_max_sync(full, lm) - 1u);
+            const int e = root_exponent(vmax);
+            const float sc = root_scale(e);
+            long long part = 0;
+#pragma unroll
+            for (int r = 0; r < SV_CAP / 32; r++)
+                if (key[r]) part += root_fixed(__uint_as_float(key[r] - 1u), sc);
+            for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(full, part, off);
+            if (lane == q) {
+                md_out[i] = fixed_mean(part, e, k);
+                done = true;
             }
         }
     }
-    md_out[i] = -1.f;
-    unsigned slot = atomicAdd(&s->n_deferred, 1u);
-    deferred[slot] = (unsigned)i;
+    if (active && !done) {
+        md_out[i] = -1.f;
+        const unsigned slot = atomicAdd(&s->n_deferred, 1u);
+        deferred[slot] = (unsigned)i;
+    }
 }
 
 // Occupied cells of the coarse (dense) level: (cell index, offset, count).
@@ -1060,8 +1066,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     float* md = mean_dist ? mean_dist : G.md;
     occupied_cells_kernel<<<(unsigned)((DENSE_MAX + GB - 1) / GB), GB, 0, st>>>(G.tab[1], G.stats, G.occ);
     dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
-    const size_t tsm =
-        (size_t)TILE_MAX_CAND * sizeof(float4) + (size_t)(mean_k + 1 + SEL_SLACK) * TILE_T * sizeof(float);
+    const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
     // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
