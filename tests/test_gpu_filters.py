@@ -121,6 +121,49 @@ def test_sor_parity(ctx, oracle_lib, k):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("k", [30, 50])
+def test_sor_window_path_equals_grid_path(ctx, oracle_lib, k):
+    """The window fast path (certified by the ray bound) gives the same bits as
+    the grid search: the same cloud padded by one invalid column has no pixel
+    rays (its size is not the calibrated one), so every query takes the grid."""
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    H, W = mask.shape
+    xp = torch.zeros((H, W + 1, 3), dtype=torch.float32, device="cuda")
+    mp = torch.zeros((H, W + 1), dtype=torch.uint8, device="cuda")
+    xp[:, :W] = xyz
+    mp[:, :W] = mask
+    m1, md1 = api.filter_sor(ctx, xyz, mask, k, 1.0, want_mean_dist=True)
+    s1 = api.sor_stats(ctx)
+    m2, md2 = api.filter_sor(ctx, xp.contiguous(), mp.contiguous(), k, 1.0, want_mean_dist=True)
+    s2 = api.sor_stats(ctx)
+    assert torch.equal(md1, md2[:, :W].contiguous()) and torch.equal(m1, m2[:, :W].contiguous())
+    assert s1["threshold"] == s2["threshold"]
+    print("sor k", k, "far searches: window path", s1["n_far_search"], "grid path", s2["n_far_search"])
+
+
+@pytest.mark.gpu
+def test_metric_gaussian_window_path_matches_grid_path(ctx, oracle_lib):
+    """Window-certified points against the grid path (the padded cloud has no
+    pixel rays): the same neighbours, summed in another order, so equal to a
+    few float ulps."""
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    H, W = mask.shape
+    xp = torch.zeros((H, W + 1, 3), dtype=torch.float32, device="cuda")
+    mp = torch.zeros((H, W + 1), dtype=torch.uint8, device="cuda")
+    xp[:, :W] = xyz
+    mp[:, :W] = mask
+    a = api.filter_metric_gaussian(ctx, xyz, mask, 0.5).cpu().numpy()
+    b = api.filter_metric_gaussian(ctx, xp.contiguous(), mp.contiguous(), 0.5)[:, :W].cpu().numpy()
+    m = mask.cpu().numpy() > 0
+    assert np.array_equal(a[~m], b[~m])
+    err = np.abs(a[m].astype(np.float64) - b[m]).max(axis=1)
+    scale = np.abs(b[m]).max(axis=1)
+    assert (err <= 4 * np.spacing(scale.astype(np.float32))).all(), float(err.max())
+
+
+@pytest.mark.gpu
 def test_metric_gaussian_parity(ctx, oracle_lib):
     from zim_gb300 import api
     xyz, mask = cloud(ctx, oracle_lib)

@@ -350,7 +350,8 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
         uint8_t* om = next_m(ST_SOR);
         float* ox = next_x(ST_SOR);
         // removed points read as zero in the organised output
-        s = zim_sor_launch(ctx, cx, cm, RH, RW, r->sor_mean_k, r->sor_std_mul, ox, om, nullptr, st);
+        s = zim_sor_launch(ctx, cx, cm, RH, RW, r->sor_mean_k, r->sor_std_mul, ox, om, nullptr,
+                           zim_rays_of(ctx, r->use_rectified_coords != 0, 0, 0), st);
         if (s) return s;
         ctx->scratch_used = grid_mark;
         cx = ox; cm = om;
@@ -364,7 +365,8 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
     }
     if (on[ST_MG]) {
         float* ox = next_x(ST_MG);
-        s = zim_metric_gaussian_launch(ctx, cx, cm, RH, RW, r->metric_gaussian_sigma, ox, st);
+        s = zim_metric_gaussian_launch(ctx, cx, cm, RH, RW, r->metric_gaussian_sigma, ox,
+                                       zim_rays_of(ctx, r->use_rectified_coords != 0, 0, 0), st);
         if (s) return s;
         ctx->scratch_used = grid_mark;
         cx = ox;

@@ -61,6 +61,7 @@ struct GridStats {
     double thr;                    // SOR threshold, and the largest float <= it
     float thr_f;
     int keep_all;
+    unsigned ray_dev_bits;         // largest distance of a point from its pixel ray (float bits)
     unsigned n_deferred, n_occ, p2_next;
 };
 
@@ -98,6 +99,7 @@ __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
     s->n_deferred = s->n_occ = s->p2_next = 0;
+    s->ray_dev_bits = 0u;
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
 
@@ -426,6 +428,7 @@ static_assert(WIN_W * WIN_H <= TILE_MAX_CAND, "pixel window staged in the candid
 static_assert(TILE_MAX_CELLS <= 8 * TILE_T, "cell scan: eight cells per thread");
 
 constexpr int SV_CAP = 128;  // survivors per warp query (k + 1 <= 64 of them kept)
+constexpr int SEL_SLACK = 17;  // per-thread selection lists hold k + 1 + SEL_SLACK
 
 // Phase 1: one CTA per 16 x 8 pixel tile on the finest level.
 //  - Window bound: the query and its k nearest valid pixels (in pixel
@@ -445,7 +448,7 @@ constexpr int SV_CAP = 128;  // survivors per warp query (k + 1 <= 64 of them ke
 __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __restrict__ xyz,
                                                               const uint8_t* __restrict__ mask, int rows, int cols,
                                                               int k, Level g, GridStats* s, float* __restrict__ md_out,
-                                                              unsigned* __restrict__ deferred) {
+                                                              unsigned* __restrict__ deferred, int unresolved_only) {
     extern __shared__ float4 tile_smem[];
     float4* cand = tile_smem;                  // TILE_MAX_CAND
     __shared__ int s_off[TILE_MAX_CELLS + 1];  // candidate offset of each box cell
@@ -460,7 +463,10 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
     const int x = x0 + (tid % TILE_X), y = y0 + (tid / TILE_X);
     const bool in = x < cols && y < rows;
     const size_t i = in ? (size_t)y * cols + x : 0;
-    const bool active = in && mask[i] && s->n_valid > k;
+    // after the window pass only the queries it left (md = -2) are searched here
+    const bool active = in && mask[i] && s->n_valid > k && (!unresolved_only || md_out[i] == -2.f);
+    if (in && !active && !unresolved_only) md_out[i] = 0.f;
+    if (!__syncthreads_or(active)) return;  // the whole CTA leaves together
     const float ic = s->inv_cell[0], cell = s->cell[0];
     float qx = 0.f, qy = 0.f, qz = 0.f;
     int c[3] = {0, 0, 0};
@@ -468,7 +474,6 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
         qx = xyz[3 * i]; qy = xyz[3 * i + 1]; qz = xyz[3 * i + 2];
         cell_of(qx, qy, qz, ic, c[0], c[1], c[2]);
     }
-    if (in && !active) md_out[i] = 0.f;
     // window bound tau0 from the pixel neighbourhood (staged in cand; w = 0 marks invalid)
     for (int t = tid; t < WIN_W * WIN_H; t += TILE_T) {
         const int wx = x0 - WIN_R + t % WIN_W, wy = y0 - WIN_R + t / WIN_W;
@@ -706,6 +711,185 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
     }
 }
 
+// ------------------------------------------------ window fast path (SOR) ----
+//
+// An organised cloud from one camera keeps its neighbours close in the image:
+// a point p seen along the ray of pixel b, and a query q near the ray of pixel
+// a, satisfy |p - q| >= |q| sin(angle(a, b)) - dev(q) - dev(p), where dev is a
+// point's distance from its own pixel ray.  For every pixel b outside the
+// (2 WR + 1)^2 window around a, |b - a| >= WR + 1 pixels, and with the pinhole
+// rays a = (u - cx, v - cy, f), |a x b| >= f |b - a| and |b| <= |a| + |b - a|,
+// so sin(angle) >= f (WR + 1) / (|a| (|a| + WR + 1)).  A query whose k + 1
+// nearest points inside its window lie within
+//     |q| f (WR + 1) / (|a| (|a| + WR + 1)) - dev(q) - max dev
+// has the same k + 1 nearest points in the whole cloud: its mean distance is
+// exact from the window alone.  Queries the bound does not certify are left
+// to the grid search (md = -2).
+
+struct RayParams {
+    float cx, cy, f, R[9];
+    int ox, oy;
+};
+
+__device__ __forceinline__ void ray_dir(const RayParams& r, int u, int v, float& ax, float& ay, float& az) {
+    const float x = (float)(u + r.ox) - r.cx, y = (float)(v + r.oy) - r.cy;
+    ax = fmaf(r.R[0], x, fmaf(r.R[1], y, r.R[2] * r.f));
+    ay = fmaf(r.R[3], x, fmaf(r.R[4], y, r.R[5] * r.f));
+    az = fmaf(r.R[6], x, fmaf(r.R[7], y, r.R[8] * r.f));
+}
+
+// Distance of p from the line through the origin along a: |p x a| / |a|.
+__device__ __forceinline__ float ray_dev(float px, float py, float pz, float ax, float ay, float az) {
+    const float cx = fmaf(py, az, -pz * ay), cy = fmaf(pz, ax, -px * az), cz = fmaf(px, ay, -py * ax);
+    return sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz))) * rsqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+}
+
+__global__ void ray_dev_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
+                               RayParams rp, GridStats* s) {
+    const size_t n = (size_t)rows * cols;
+    float m = 0.f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!mask[i]) continue;
+        float ax, ay, az;
+        ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
+        const float d = ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
+        m = fmaxf(m, d == d ? d : INFINITY);  // NaN counts as unbounded
+    }
+    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+    if ((threadIdx.x & 31) == 0 && b) atomicMax(&s->ray_dev_bits, b);
+}
+
+constexpr int WR = 7;  // window half-size of the fast path
+constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
+constexpr int WN = (2 * WR + 1) * (2 * WR + 1) - 1;
+// pixel offsets of the window ordered by length, then row, then column
+__constant__ signed char c_spiral7[WN][2] = {
+    {0, -1}, {-1, 0}, {1, 0}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0}, {2, 0}, {0, 2},
+    {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
+    {0, -3}, {-3, 0}, {3, 0}, {0, 3}, {-1, -3}, {1, -3}, {-3, -1}, {3, -1}, {-3, 1}, {3, 1}, {-1, 3}, {1, 3},
+    {-2, -3}, {2, -3}, {-3, -2}, {3, -2}, {-3, 2}, {3, 2}, {-2, 3}, {2, 3}, {0, -4}, {-4, 0}, {4, 0}, {0, 4},
+    {-1, -4}, {1, -4}, {-4, -1}, {4, -1}, {-4, 1}, {4, 1}, {-1, 4}, {1, 4}, {-3, -3}, {3, -3}, {-3, 3}, {3, 3},
+    {-2, -4}, {2, -4}, {-4, -2}, {4, -2}, {-4, 2}, {4, 2}, {-2, 4}, {2, 4}, {0, -5}, {-3, -4}, {3, -4}, {-4, -3},
+    {4, -3}, {-5, 0}, {5, 0}, {-4, 3}, {4, 3}, {-3, 4}, {3, 4}, {0, 5}, {-1, -5}, {1, -5}, {-5, -1}, {5, -1},
+    {-5, 1}, {5, 1}, {-1, 5}, {1, 5}, {-2, -5}, {2, -5}, {-5, -2}, {5, -2}, {-5, 2}, {5, 2}, {-2, 5}, {2, 5},
+    {-4, -4}, {4, -4}, {-4, 4}, {4, 4}, {-3, -5}, {3, -5}, {-5, -3}, {5, -3}, {-5, 3}, {5, 3}, {-3, 5}, {3, 5},
+    {0, -6}, {-6, 0}, {6, 0}, {0, 6}, {-1, -6}, {1, -6}, {-6, -1}, {6, -1}, {-6, 1}, {6, 1}, {-1, 6}, {1, 6},
+    {-2, -6}, {2, -6}, {-6, -2}, {6, -2}, {-6, 2}, {6, 2}, {-2, 6}, {2, 6}, {-4, -5}, {4, -5}, {-5, -4}, {5, -4},
+    {-5, 4}, {5, 4}, {-4, 5}, {4, 5}, {-3, -6}, {3, -6}, {-6, -3}, {6, -3}, {-6, 3}, {6, 3}, {-3, 6}, {3, 6},
+    {0, -7}, {-7, 0}, {7, 0}, {0, 7}, {-1, -7}, {1, -7}, {-5, -5}, {5, -5}, {-7, -1}, {7, -1}, {-7, 1}, {7, 1},
+    {-5, 5}, {5, 5}, {-1, 7}, {1, 7}, {-4, -6}, {4, -6}, {-6, -4}, {6, -4}, {-6, 4}, {6, 4}, {-4, 6}, {4, 6},
+    {-2, -7}, {2, -7}, {-7, -2}, {7, -2}, {-7, 2}, {7, 2}, {-2, 7}, {2, 7}, {-3, -7}, {3, -7}, {-7, -3}, {7, -3},
+    {-7, 3}, {7, 3}, {-3, 7}, {3, 7}, {-5, -6}, {5, -6}, {-6, -5}, {6, -5}, {-6, 5}, {6, 5}, {-5, 6}, {5, 6},
+    {-4, -7}, {4, -7}, {-7, -4}, {7, -4}, {-7, 4}, {7, 4}, {-4, 7}, {4, 7}, {-6, -6}, {6, -6}, {-6, 6}, {6, 6},
+    {-5, -7}, {5, -7}, {-7, -5}, {7, -5}, {-7, 5}, {7, 5}, {-5, 7}, {5, 7}, {-6, -7}, {6, -7}, {-7, -6}, {7, -6},
+    {-7, 6}, {7, 6}, {-6, 7}, {6, 7}, {-7, -7}, {7, -7}, {-7, 7}, {7, 7},
+};
+
+// Per-thread selection of the K1 smallest squared distances in column tid of
+// a [cap][TILE_T] shared array: values within the bound are appended; a full
+// list is sorted, cut to K1 and the bound tightened to its K1-th value.
+struct WinSel {
+    float* L;
+    int cnt, K1, cap;
+    float thr;
+    __device__ __forceinline__ void sort() {
+        for (int a = 1; a < cnt; a++) {
+            const float v = L[a * TILE_T];
+            int b = a;
+            while (b > 0 && L[(b - 1) * TILE_T] > v) {
+                L[b * TILE_T] = L[(b - 1) * TILE_T];
+                b--;
+            }
+            L[b * TILE_T] = v;
+        }
+    }
+    __device__ __forceinline__ void push(float d2) {
+        if (d2 > thr) return;
+        L[cnt * TILE_T] = d2;
+        if (++cnt == cap) {
+            sort();
+            cnt = K1;
+            thr = L[(K1 - 1) * TILE_T];
+        }
+    }
+};
+
+__global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restrict__ xyz,
+                                                            const uint8_t* __restrict__ mask, int rows, int cols,
+                                                            int k, RayParams rp, const GridStats* __restrict__ s,
+                                                            float* __restrict__ md_out) {
+    extern __shared__ float4 win_smem[];
+    float4* W = win_smem;                                      // WW x WH window, w = 1 valid
+    float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1 + SEL_SLACK) x TILE_T
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+    for (int t = tid; t < WW * WH; t += TILE_T) {
+        const int wx = x0 - WR + t % WW, wy = y0 - WR + t / WW;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
+            const size_t j = (size_t)wy * cols + wx;
+            if (mask[j]) v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
+        }
+        W[t] = v;
+    }
+    __syncthreads();
+    const int tx = tid % TILE_X, ty = tid / TILE_X;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= cols || y >= rows) return;  // no block-wide synchronisation below
+    const size_t i = (size_t)y * cols + x;
+    if (!mask[i] || !(s->n_valid > k)) {
+        md_out[i] = 0.f;
+        return;
+    }
+    const int wc = (ty + WR) * WW + tx + WR;
+    const float4 q = W[wc];
+    // window bound: the query and its first k valid window pixels
+    float tau0 = INFINITY;
+    {
+        int found = 0;
+        float m = 0.f;
+        for (int o = 0; o < WN && found < k; o++) {
+            const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
+            if (p.w == 0.f) continue;
+            m = fmaxf(m, sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
+            found++;
+        }
+        if (found == k) tau0 = m;
+    }
+    if (!(tau0 < INFINITY)) {
+        md_out[i] = -2.f;
+        return;
+    }
+    const int K1 = k + 1;
+    WinSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, tau0};
+    sel.push(0.f);  // the query itself
+    for (int o = 0; o < WN; o++) {
+        const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
+        if (p.w == 0.f) continue;
+        sel.push(sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
+    }
+    sel.sort();
+    const float kth = sel.L[(K1 - 1) * TILE_T];
+    // certificate
+    float ax, ay, az;
+    ray_dir(rp, x, y, ax, ay, az);
+    const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
+    const float bound = qn * rp.f * (float)(WR + 1) / (an * (an + (float)(WR + 1)));
+    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits);
+    // slack for the float rounding of every term (relative 1e-5 of |q|)
+    const bool ok = bound - dev - 1e-5f * qn > sqrtf(kth);
+    if (!ok) {
+        md_out[i] = -2.f;
+        return;
+    }
+    const int e = root_exponent(kth);
+    const float sc = root_scale(e);
+    long long sum = 0;
+    for (int j = 0; j < K1; j++) sum += root_fixed(sel.L[j * TILE_T], sc);
+    md_out[i] = fixed_mean(sum, e, k);
+}
+
 // Occupied cells of the coarse (dense) level: (cell index, offset, count).
 __global__ void occupied_cells_kernel(const uint2* __restrict__ tab, GridStats* s, uint4* __restrict__ occ) {
     const unsigned used = (unsigned)s->dims[0] * (unsigned)s->dims[1] * (unsigned)s->dims[2];
@@ -921,11 +1105,79 @@ __global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t
 // Radius-3-sigma Gaussian: out = p + sum w (q - p) / sum w over the 27 cells of
 // side 3 sigma around p; buckets are index-sorted, so the FP32 sums are
 // deterministic.
+// Metric Gaussian by the window fast path: the points within r of a query,
+// summed over its (2 WRG + 1)^2 window, whenever the ray bound puts every
+// point outside the window farther than r (see sor_window_kernel); the others
+// are marked -2 in `pending` for metric_gaussian_kernel.
+constexpr int WRG = 6;
+constexpr int GW = TILE_X + 2 * WRG, GH = TILE_Y + 2 * WRG;
+
+__global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restrict__ xyz,
+                                                           const uint8_t* __restrict__ mask, int rows, int cols,
+                                                           float r, float inv2s2, RayParams rp,
+                                                           const GridStats* __restrict__ s,
+                                                           float* __restrict__ pending, float* __restrict__ out) {
+    __shared__ float4 W[GW * GH];
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+    for (int t = tid; t < GW * GH; t += TILE_T) {
+        const int wx = x0 - WRG + t % GW, wy = y0 - WRG + t / GW;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
+            const size_t j = (size_t)wy * cols + wx;
+            if (mask[j]) v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
+        }
+        W[t] = v;
+    }
+    __syncthreads();
+    const int tx = tid % TILE_X, ty = tid / TILE_X;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= cols || y >= rows) return;
+    const size_t i = (size_t)y * cols + x;
+    const float4 q = W[(ty + WRG) * GW + tx + WRG];
+    if (!mask[i]) {  // invalid points pass through
+        out[3 * i] = xyz[3 * i];
+        out[3 * i + 1] = xyz[3 * i + 1];
+        out[3 * i + 2] = xyz[3 * i + 2];
+        pending[i] = 0.f;
+        return;
+    }
+    float ax, ay, az;
+    ray_dir(rp, x, y, ax, ay, az);
+    const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+    const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
+    const float bound = qn * rp.f * (float)(WRG + 1) / (an * (an + (float)(WRG + 1)));
+    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits);
+    if (!(bound - dev - 1e-5f * qn > r)) {
+        pending[i] = -2.f;
+        return;
+    }
+    const float r2 = r * r;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+    for (int dy = -WRG; dy <= WRG; dy++)
+        for (int dx = -WRG; dx <= WRG; dx++) {
+            const float4 p = W[(ty + WRG + dy) * GW + tx + WRG + dx];
+            if (p.w == 0.f) continue;
+            const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
+            const float d2 = sqdist(ex, ey, ez);
+            if (d2 > r2) continue;
+            const float w = __expf(-d2 * inv2s2);
+            sx = fmaf(w, ex, sx); sy = fmaf(w, ey, sy); sz = fmaf(w, ez, sz);
+            sw += w;
+        }
+    const float iw = 1.0f / sw;
+    out[3 * i] = q.x + sx * iw;
+    out[3 * i + 1] = q.y + sy * iw;
+    out[3 * i + 2] = q.z + sz * iw;
+    pending[i] = 0.f;
+}
+
 __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                        float r2, float inv2s2, Level g, const GridStats* __restrict__ s,
-                                       float* __restrict__ out) {
+                                       const float* __restrict__ pending, float* __restrict__ out) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (pending && pending[i] != -2.f) return;  // settled by the window pass
     const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
     if (!mask[i]) {
         out[3 * i] = qx; out[3 * i + 1] = qy; out[3 * i + 2] = qz;
@@ -937,7 +1189,7 @@ __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint
     float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
     auto acc = [&](const float4& p) {
         float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-        float d2 = dx * dx + dy * dy + dz * dz;
+        float d2 = sqdist(dx, dy, dz);
         if (d2 > r2) return;
         float w = __expf(-d2 * inv2s2);
         sx = fmaf(w, dx, sx); sy = fmaf(w, dy, sy); sz = fmaf(w, dz, sz);
@@ -1052,7 +1304,8 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
 size_t zim_grid_scratch_bytes(size_t n) { return grid_bytes(n, MAX_LEVELS); }
 
 zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, int mean_k,
-                          double std_mul, float* xyz_out, uint8_t* mask_out, float* mean_dist, cudaStream_t st) {
+                          double std_mul, float* xyz_out, uint8_t* mask_out, float* mean_dist,
+                          const zim_ray_model& rays, cudaStream_t st) {
     size_t n = (size_t)rows * cols;
     GridScratch G;
     zim_status s = carve_grid(ctx, n, MAX_LEVELS, G);
@@ -1066,10 +1319,24 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     float* md = mean_dist ? mean_dist : G.md;
     occupied_cells_kernel<<<(unsigned)((DENSE_MAX + GB - 1) / GB), GB, 0, st>>>(G.tab[1], G.stats, G.occ);
     dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
+    const int window = rays.valid ? 1 : 0;
+    if (window) {
+        RayParams rp;
+        rp.cx = rays.cx; rp.cy = rays.cy; rp.f = rays.f;
+        for (int a = 0; a < 9; a++) rp.R[a] = rays.R[a];
+        rp.ox = rays.ox; rp.oy = rays.oy;
+        ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
+                                                                                     G.stats);
+        const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1 + SEL_SLACK) * TILE_T * 4;
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+        sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md);
+        ctx->launches += 2;
+    }
     const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
     // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-    sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
+    sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
+                                                    window);
     sor_knn_far_kernel<<<(unsigned)(4 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
         xyz, mean_k, G.stats, G.occ, G.pts[1], G.deferred, md, ctx->d_error);
     ctx->launches += 3;
@@ -1088,7 +1355,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
 }
 
 zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
-                                      double sigma, float* out, cudaStream_t st) {
+                                      double sigma, float* out, const zim_ray_model& rays, cudaStream_t st) {
     size_t n = (size_t)rows * cols;
     GridScratch G;
     zim_status s = carve_grid(ctx, n, 1, G);
@@ -1097,8 +1364,22 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, true, G, st);
     if (s) return s;
     Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
-    metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(
-        xyz, mask, n, rad * rad, (float)(1.0 / (2.0 * sigma * sigma)), g, G.stats, out);
+    const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
+    float* pending = nullptr;
+    if (rays.valid) {
+        RayParams rp;
+        rp.cx = rays.cx; rp.cy = rays.cy; rp.f = rays.f;
+        for (int a = 0; a < 9; a++) rp.R[a] = rays.R[a];
+        rp.ox = rays.ox; rp.oy = rays.oy;
+        ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
+                                                                                     G.stats);
+        dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
+        pending = G.md;
+        mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);
+        ctx->launches += 2;
+    }
+    metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
+                                                                        pending, out);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
@@ -1114,7 +1395,11 @@ extern "C" ZIM_API zim_status zim_filter_sor(zim_ctx* ctx, const float* xyz, con
     zim_status s = zim_scratch_reserve(ctx, zim_grid_scratch_bytes((size_t)rows * cols));
     if (s) return s;
     zim_scratch_reset(ctx);
-    return zim_sor_launch(ctx, xyz, mask, rows, cols, mean_k, std_mul, nullptr, mask_out, mean_dist, zim_stream(stream));
+    // a cloud of the calibrated rectified size: its pixels' rays as the window hint
+    const zim_ray_model rays = rows == ctx->rect_h && cols == ctx->rect_w ? zim_rays_of(ctx, true, 0, 0)
+                                                                          : zim_ray_model{};
+    return zim_sor_launch(ctx, xyz, mask, rows, cols, mean_k, std_mul, nullptr, mask_out, mean_dist, rays,
+                          zim_stream(stream));
 }
 
 extern "C" ZIM_API zim_status zim_filter_sor_stats(zim_ctx* ctx, zim_sor_stats* out) {
@@ -1141,5 +1426,7 @@ extern "C" ZIM_API zim_status zim_filter_metric_gaussian(zim_ctx* ctx, const flo
     zim_status s = zim_scratch_reserve(ctx, zim_grid_scratch_bytes((size_t)rows * cols));
     if (s) return s;
     zim_scratch_reset(ctx);
-    return zim_metric_gaussian_launch(ctx, xyz, mask, rows, cols, sigma, out, zim_stream(stream));
+    const zim_ray_model rays = rows == ctx->rect_h && cols == ctx->rect_w ? zim_rays_of(ctx, true, 0, 0)
+                                                                          : zim_ray_model{};
+    return zim_metric_gaussian_launch(ctx, xyz, mask, rows, cols, sigma, out, rays, zim_stream(stream));
 }

@@ -211,6 +211,22 @@ static zim_status pack_ply_launch(zim_ctx* ctx, const float* xyz, const uint8_t*
     return ZIM_OK;
 }
 
+zim_ray_model zim_rays_of(const zim_ctx* ctx, bool rectified_coords, int ox, int oy) {
+    zim_ray_model r;
+    if (!ctx->calibrated || !(ctx->Q[11] != 0.0)) return r;
+    // Q reprojects pixel (u, v) along (u + Q03, v + Q13, Q23)
+    r.cx = (float)-ctx->Q[3];
+    r.cy = (float)-ctx->Q[7];
+    r.f = (float)ctx->Q[11];
+    if (!rectified_coords)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) r.R[3 * a + b] = (float)ctx->R1[3 * b + a];  // R1^T
+    r.ox = ox;
+    r.oy = oy;
+    r.valid = 1;
+    return r;
+}
+
 zim_status zim_check_reproject(zim_ctx* ctx, const zim_recon_config* cfg) {
     if (cfg->reproject_model != 0 && cfg->reproject_model != 1)
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "reproject_model must be 0 (Q) or 1 (polynomial maps)");

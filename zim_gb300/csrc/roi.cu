@@ -422,7 +422,8 @@ extern "C" ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_
     if (r->use_sor) {
         float* xo = (xb[0] != cx) ? xb[0] : xb[1];
         uint8_t* mo = (mb[0] != cm) ? mb[0] : mb[1];
-        s = zim_sor_launch(ctx, cx, cm, H, W, r->sor_mean_k, r->sor_std_mul, xo, mo, nullptr, st);
+        s = zim_sor_launch(ctx, cx, cm, H, W, r->sor_mean_k, r->sor_std_mul, xo, mo, nullptr,
+                           zim_rays_of(ctx, r->use_rectified_coords != 0, L.x, L.y), st);
         if (s) return s;
         ctx->scratch_used = grid_mark;
         cx = xo;
@@ -437,7 +438,8 @@ extern "C" ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_
     }
     if (r->use_metric_gaussian) {
         float* xo = (xb[0] != cx) ? xb[0] : xb[1];
-        s = zim_metric_gaussian_launch(ctx, cx, cm, H, W, r->metric_gaussian_sigma, xo, st);
+        s = zim_metric_gaussian_launch(ctx, cx, cm, H, W, r->metric_gaussian_sigma, xo,
+                                       zim_rays_of(ctx, r->use_rectified_coords != 0, L.x, L.y), st);
         if (s) return s;
         ctx->scratch_used = grid_mark;
         cx = xo;

@@ -90,6 +90,20 @@ zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_
                             const int32_t* l_order, const int32_t* r_base, const float* r_res,
                             const int32_t* r_order, int rows, int cols, int pha_f,
                             double grad_threshold, float* disp, int32_t* best_col, cudaStream_t st);
+// Pixel rays of an organised cloud: cloud pixel (u, v) looks from the origin
+// along R (u + ox - cx, v + oy - cy, f).  The window fast paths of the grid
+// filters use it only as a hint: they measure how far every point lies from
+// its ray and fall back to the exact grid search where the bound does not hold.
+struct zim_ray_model {
+    float cx = 0.f, cy = 0.f, f = 0.f;
+    float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    int ox = 0, oy = 0;
+    int valid = 0;
+};
+// The rays of the context's rectified left camera (rotated by R1^T for clouds
+// in camera coordinates); invalid when the context is not calibrated.
+zim_ray_model zim_rays_of(const zim_ctx* ctx, bool rectified_coords, int ox, int oy);
+
 // Checks that a reconstruction config can run on this context (reprojection
 // model and its maps).
 zim_status zim_check_reproject(zim_ctx* ctx, const zim_recon_config* cfg);
@@ -106,9 +120,10 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
                           float* out, float* tmp, cudaStream_t st);
 zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
                           int mean_k, double std_mul, float* xyz_out, uint8_t* mask_out,
-                          float* mean_dist, cudaStream_t st);
+                          float* mean_dist, const zim_ray_model& rays, cudaStream_t st);
 zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
-                                      int cols, double sigma, float* out, cudaStream_t st);
+                                      int cols, double sigma, float* out, const zim_ray_model& rays,
+                                      cudaStream_t st);
 zim_status zim_compact_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows,
                               int cols, zim_point_xyz* points, uint64_t* count_dev, cudaStream_t st);
 
