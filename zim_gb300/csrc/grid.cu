@@ -24,8 +24,13 @@
 //            (k + 1)-th distance.
 // A visited point's finest cell is re-derived from its coordinates, so hash
 // collisions never count a point twice.  Both filters are deterministic: the
-// SOR statistics are summed in a fixed order, and the Gaussian's buckets are
-// sorted by pixel index before they are summed.
+// SOR statistics are summed in a fixed order, and the Gaussian's grid path sums
+// in 64-bit fixed point (independent of bucket order).
+//
+// Window fast paths (sor_window_kernel, mg_window_kernel): on an organised
+// cloud most queries are settled from their pixel window alone, certified
+// exact by a bound on the distance to every point seen along another pixel's
+// ray; only the queries the bound does not certify reach the grid searches.
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -861,24 +866,47 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
         return;
     }
     const int K1 = k + 1;
-    WinSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, tau0};
-    sel.push(0.f);  // the query itself
-    for (int o = 0; o < WN; o++) {
-        const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
-        if (p.w == 0.f) continue;
-        sel.push(sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
-    }
-    sel.sort();
-    const float kth = sel.L[(K1 - 1) * TILE_T];
-    // certificate
+    // bound(r) = C r / (an + r): no point of a pixel at distance >= r from the
+    // query's lies nearer than bound(r) - dev (slack: float rounding, 1e-5 |q|)
     float ax, ay, az;
     ray_dir(rp, x, y, ax, ay, az);
     const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
     const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
-    const float bound = qn * rp.f * (float)(WR + 1) / (an * (an + (float)(WR + 1)));
-    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits);
-    // slack for the float rounding of every term (relative 1e-5 of |q|)
-    const bool ok = bound - dev - 1e-5f * qn > sqrtf(kth);
+    const float C = qn * rp.f / an;
+    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits) + 1e-5f * qn;
+    // squared pixel distance beyond which every point is farther than sqrt(thr):
+    // C r / (an + r) > sqrt(thr) + dev  <=>  r > (sqrt(thr) + dev) an / (C - sqrt(thr) - dev)
+    auto stop_r2 = [&](float thr) {
+        const float sd = sqrtf(thr) + dev;
+        if (!(C > sd)) return INFINITY;
+        const float r = sd * an / (C - sd);
+        return r * r;
+    };
+    WinSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, tau0};
+    sel.push(0.f);  // the query itself
+    float last = sel.thr, rs2 = stop_r2(last), rbreak = (float)(WR + 1);
+    // the spiral runs by increasing length: once past the stop distance, the
+    // rest of the window (and everything outside it) is provably farther
+    for (int o = 0; o < WN; o++) {
+        const int dx = c_spiral7[o][0], dy = c_spiral7[o][1];
+        const float r2o = (float)(dx * dx + dy * dy);
+        if (r2o > rs2) {
+            rbreak = fminf(sqrtf(r2o), rbreak);
+            break;
+        }
+        const float4 p = W[wc + dy * WW + dx];
+        if (p.w == 0.f) continue;
+        sel.push(sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
+        if (sel.thr != last) {
+            last = sel.thr;
+            rs2 = stop_r2(last);
+        }
+    }
+    sel.sort();
+    const float kth = sel.L[(K1 - 1) * TILE_T];
+    // certificate: every pixel not visited is at least rbreak away (the
+    // unvisited window entries) or WR + 1 away (outside the window)
+    const bool ok = C * rbreak / (an + rbreak) - dev > sqrtf(kth);
     if (!ok) {
         md_out[i] = -2.f;
         return;
@@ -1106,10 +1134,10 @@ __global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t
 // side 3 sigma around p; buckets are index-sorted, so the FP32 sums are
 // deterministic.
 // Metric Gaussian by the window fast path: the points within r of a query,
-// summed over its (2 WRG + 1)^2 window, whenever the ray bound puts every
-// point outside the window farther than r (see sor_window_kernel); the others
-// are marked -2 in `pending` for metric_gaussian_kernel.
-constexpr int WRG = 6;
+// summed in spiral order over its window up to the pixel distance beyond which
+// the ray bound puts every point farther than r (see sor_window_kernel); the
+// others are marked -2 in `pending` for metric_gaussian_kernel.
+constexpr int WRG = WR;
 constexpr int GW = TILE_X + 2 * WRG, GH = TILE_Y + 2 * WRG;
 
 __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restrict__ xyz,
@@ -1146,25 +1174,30 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     ray_dir(rp, x, y, ax, ay, az);
     const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
     const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
-    const float bound = qn * rp.f * (float)(WRG + 1) / (an * (an + (float)(WRG + 1)));
-    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits);
-    if (!(bound - dev - 1e-5f * qn > r)) {
+    const float C = qn * rp.f / an;
+    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits) + 1e-5f * qn;
+    // pixels farther than rs from the query hold no point within r
+    const float sd = r + dev;
+    const float rs = C > sd ? sd * an / (C - sd) : INFINITY;
+    if (!(rs < (float)(WRG + 1))) {
         pending[i] = -2.f;
         return;
     }
-    const float r2 = r * r;
-    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
-    for (int dy = -WRG; dy <= WRG; dy++)
-        for (int dx = -WRG; dx <= WRG; dx++) {
-            const float4 p = W[(ty + WRG + dy) * GW + tx + WRG + dx];
-            if (p.w == 0.f) continue;
-            const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-            const float d2 = sqdist(ex, ey, ez);
-            if (d2 > r2) continue;
-            const float w = __expf(-d2 * inv2s2);
-            sx = fmaf(w, ex, sx); sy = fmaf(w, ey, sy); sz = fmaf(w, ez, sz);
-            sw += w;
-        }
+    const float rs2 = rs * rs, r2 = r * r;
+    const int wc = (ty + WRG) * GW + tx + WRG;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 1.f;  // the query itself: weight 1, offset 0
+    for (int o = 0; o < WN; o++) {
+        const int dx = c_spiral7[o][0], dy = c_spiral7[o][1];
+        if ((float)(dx * dx + dy * dy) > rs2) break;
+        const float4 p = W[wc + dy * GW + dx];
+        if (p.w == 0.f) continue;
+        const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
+        const float d2 = sqdist(ex, ey, ez);
+        if (d2 > r2) continue;
+        const float w = __expf(-d2 * inv2s2);
+        sx = fmaf(w, ex, sx); sy = fmaf(w, ey, sy); sz = fmaf(w, ez, sz);
+        sw += w;
+    }
     const float iw = 1.0f / sw;
     out[3 * i] = q.x + sx * iw;
     out[3 * i + 1] = q.y + sy * iw;
@@ -1186,21 +1219,26 @@ __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint
     const float ic = s->inv_cell[0];
     int cx, cy, cz;
     cell_of(qx, qy, qz, ic, cx, cy, cz);
-    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+    // fixed-point sums (each term rounded on its own): the result does not
+    // depend on the order the buckets list their points in
+    const float r = sqrtf(r2), sc = 1099511627776.0f / r;  // 2^40 / r
+    long long sx = 0, sy = 0, sz = 0, sw = 0;
     auto acc = [&](const float4& p) {
         float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
         float d2 = sqdist(dx, dy, dz);
         if (d2 > r2) return;
         float w = __expf(-d2 * inv2s2);
-        sx = fmaf(w, dx, sx); sy = fmaf(w, dy, sy); sz = fmaf(w, dz, sz);
-        sw += w;
+        sx += __float2ll_rn(w * dx * sc);
+        sy += __float2ll_rn(w * dy * sc);
+        sz += __float2ll_rn(w * dz * sc);
+        sw += __float2ll_rn(w * 1099511627776.0f);
     };
     visit_ring(g, ic, cx, cy, cz, 0, acc);
     visit_ring(g, ic, cx, cy, cz, 1, acc);
-    float iw = 1.0f / sw;
-    out[3 * i] = qx + sx * iw;
-    out[3 * i + 1] = qy + sy * iw;
-    out[3 * i + 2] = qz + sz * iw;
+    const double k = (double)r / (double)sw;  // (S / 2^40 * r) / (W / 2^40)
+    out[3 * i] = (float)((double)qx + (double)sx * k);
+    out[3 * i + 1] = (float)((double)qy + (double)sy * k);
+    out[3 * i + 2] = (float)((double)qz + (double)sz * k);
 }
 
 unsigned table_size(size_t want) {
@@ -1361,7 +1399,7 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     zim_status s = carve_grid(ctx, n, 1, G);
     if (s) return s;
     const float rad = (float)(3.0 * sigma);
-    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, true, G, st);
+    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, false, G, st);
     if (s) return s;
     Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
     const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
