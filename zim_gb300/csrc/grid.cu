@@ -35,7 +35,7 @@
 #include <climits>
 #include <cmath>
 
-#include "zim_internal.cuh"
+#include "zim_tiles.cuh"
 
 namespace {
 
@@ -731,64 +731,14 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
 // exact from the window alone.  Queries the bound does not certify are left
 // to the grid search (md = -2).
 
-struct RayParams {
-    float cx, cy, f, R[9];
-    int ox, oy;
-};
-
-__device__ __forceinline__ void ray_dir(const RayParams& r, int u, int v, float& ax, float& ay, float& az) {
-    const float x = (float)(u + r.ox) - r.cx, y = (float)(v + r.oy) - r.cy;
-    ax = fmaf(r.R[0], x, fmaf(r.R[1], y, r.R[2] * r.f));
-    ay = fmaf(r.R[3], x, fmaf(r.R[4], y, r.R[5] * r.f));
-    az = fmaf(r.R[6], x, fmaf(r.R[7], y, r.R[8] * r.f));
-}
-
-// Distance of p from the line through the origin along a: |p x a| / |a|.
-__device__ __forceinline__ float ray_dev(float px, float py, float pz, float ax, float ay, float az) {
-    const float cx = fmaf(py, az, -pz * ay), cy = fmaf(pz, ax, -px * az), cz = fmaf(px, ay, -py * ax);
-    return sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz))) * rsqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-}
-
-__global__ void ray_dev_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                               RayParams rp, GridStats* s) {
-    const size_t n = (size_t)rows * cols;
-    float m = 0.f;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (!mask[i]) continue;
-        float ax, ay, az;
-        ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
-        const float d = ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
-        m = fmaxf(m, d == d ? d : INFINITY);  // NaN counts as unbounded
-    }
-    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
-    if ((threadIdx.x & 31) == 0 && b) atomicMax(&s->ray_dev_bits, b);
-}
-
-constexpr int WR = 7;  // window half-size of the fast path
+using zt::RayParams;
+using zt::ray_dir;
+using zt::ray_dev;
+using zt::ray_dev_kernel;
+using zt::c_spiral7;
+constexpr int WR = zt::SPIRAL_R;  // window half-size of the fast path
 constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
-constexpr int WN = (2 * WR + 1) * (2 * WR + 1) - 1;
-// pixel offsets of the window ordered by length, then row, then column
-__constant__ signed char c_spiral7[WN][2] = {
-    {0, -1}, {-1, 0}, {1, 0}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0}, {2, 0}, {0, 2},
-    {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
-    {0, -3}, {-3, 0}, {3, 0}, {0, 3}, {-1, -3}, {1, -3}, {-3, -1}, {3, -1}, {-3, 1}, {3, 1}, {-1, 3}, {1, 3},
-    {-2, -3}, {2, -3}, {-3, -2}, {3, -2}, {-3, 2}, {3, 2}, {-2, 3}, {2, 3}, {0, -4}, {-4, 0}, {4, 0}, {0, 4},
-    {-1, -4}, {1, -4}, {-4, -1}, {4, -1}, {-4, 1}, {4, 1}, {-1, 4}, {1, 4}, {-3, -3}, {3, -3}, {-3, 3}, {3, 3},
-    {-2, -4}, {2, -4}, {-4, -2}, {4, -2}, {-4, 2}, {4, 2}, {-2, 4}, {2, 4}, {0, -5}, {-3, -4}, {3, -4}, {-4, -3},
-    {4, -3}, {-5, 0}, {5, 0}, {-4, 3}, {4, 3}, {-3, 4}, {3, 4}, {0, 5}, {-1, -5}, {1, -5}, {-5, -1}, {5, -1},
-    {-5, 1}, {5, 1}, {-1, 5}, {1, 5}, {-2, -5}, {2, -5}, {-5, -2}, {5, -2}, {-5, 2}, {5, 2}, {-2, 5}, {2, 5},
-    {-4, -4}, {4, -4}, {-4, 4}, {4, 4}, {-3, -5}, {3, -5}, {-5, -3}, {5, -3}, {-5, 3}, {5, 3}, {-3, 5}, {3, 5},
-    {0, -6}, {-6, 0}, {6, 0}, {0, 6}, {-1, -6}, {1, -6}, {-6, -1}, {6, -1}, {-6, 1}, {6, 1}, {-1, 6}, {1, 6},
-    {-2, -6}, {2, -6}, {-6, -2}, {6, -2}, {-6, 2}, {6, 2}, {-2, 6}, {2, 6}, {-4, -5}, {4, -5}, {-5, -4}, {5, -4},
-    {-5, 4}, {5, 4}, {-4, 5}, {4, 5}, {-3, -6}, {3, -6}, {-6, -3}, {6, -3}, {-6, 3}, {6, 3}, {-3, 6}, {3, 6},
-    {0, -7}, {-7, 0}, {7, 0}, {0, 7}, {-1, -7}, {1, -7}, {-5, -5}, {5, -5}, {-7, -1}, {7, -1}, {-7, 1}, {7, 1},
-    {-5, 5}, {5, 5}, {-1, 7}, {1, 7}, {-4, -6}, {4, -6}, {-6, -4}, {6, -4}, {-6, 4}, {6, 4}, {-4, 6}, {4, 6},
-    {-2, -7}, {2, -7}, {-7, -2}, {7, -2}, {-7, 2}, {7, 2}, {-2, 7}, {2, 7}, {-3, -7}, {3, -7}, {-7, -3}, {7, -3},
-    {-7, 3}, {7, 3}, {-3, 7}, {3, 7}, {-5, -6}, {5, -6}, {-6, -5}, {6, -5}, {-6, 5}, {6, 5}, {-5, 6}, {5, 6},
-    {-4, -7}, {4, -7}, {-7, -4}, {7, -4}, {-7, 4}, {7, 4}, {-4, 7}, {4, 7}, {-6, -6}, {6, -6}, {-6, 6}, {6, 6},
-    {-5, -7}, {5, -7}, {-7, -5}, {7, -5}, {-7, 5}, {7, 5}, {-5, 7}, {5, 7}, {-6, -7}, {6, -7}, {-7, -6}, {7, -6},
-    {-7, 6}, {7, 6}, {-6, 7}, {6, 7}, {-7, -7}, {7, -7}, {-7, 7}, {7, 7},
-};
+constexpr int WN = zt::SPIRAL_N;
 
 // Per-thread selection of the K1 smallest squared distances in column tid of
 // a [cap][TILE_T] shared array: values within the bound are appended; a full
@@ -1359,12 +1309,9 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
     const int window = rays.valid ? 1 : 0;
     if (window) {
-        RayParams rp;
-        rp.cx = rays.cx; rp.cy = rays.cy; rp.f = rays.f;
-        for (int a = 0; a < 9; a++) rp.R[a] = rays.R[a];
-        rp.ox = rays.ox; rp.oy = rays.oy;
+        const RayParams rp = zt::ray_params(rays);
         ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
-                                                                                     G.stats);
+                                                                                     &G.stats->ray_dev_bits);
         const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1 + SEL_SLACK) * TILE_T * 4;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
         sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md);
@@ -1405,12 +1352,9 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
     float* pending = nullptr;
     if (rays.valid) {
-        RayParams rp;
-        rp.cx = rays.cx; rp.cy = rays.cy; rp.f = rays.f;
-        for (int a = 0; a < 9; a++) rp.R[a] = rays.R[a];
-        rp.ox = rays.ox; rp.oy = rays.oy;
+        const RayParams rp = zt::ray_params(rays);
         ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
-                                                                                     G.stats);
+                                                                                     &G.stats->ray_dev_bits);
         dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
         pending = G.md;
         mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);

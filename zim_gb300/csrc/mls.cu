@@ -12,7 +12,7 @@
 // query point, which keeps FP32 sums at millimetre scale.
 #include <cmath>
 
-#include "zim_internal.cuh"
+#include "zim_tiles.cuh"
 
 namespace {
 
@@ -71,73 +71,114 @@ __device__ void sym_eigen3(const float C[3][3], float ev[3], float E[3][3]) {
     }
 }
 
-// Cholesky solve; thr[i] is the singular-pivot threshold of row i (the
-// reference's 1e-12 expressed in the scaled basis).
-__device__ bool cholesky_solve(float A[6][6], const float b[6], float x[6], int nc, const float thr[6]) {
-    float L[6][6];
-    for (int i = 0; i < nc; i++)
+// Cholesky solve of an N x N system held in registers (every index is a
+// compile-time constant after unrolling); thr[i] is the singular-pivot
+// threshold of row i (the reference's 1e-12 expressed in the scaled basis).
+template <int N>
+__device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const float (&b)[N], float (&x)[N],
+                                               const float (&thr)[6]) {
+    float L[N][N];
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
         for (int j = 0; j <= i; j++) {
             float s = A[i][j];
+#pragma unroll
             for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
             if (i == j) {
-                if (s <= thr[i]) return false;
-                L[i][j] = sqrtf(s);
+                ok = ok && s > thr[i];
+                L[i][j] = sqrtf(fmaxf(s, 1e-30f));
             } else {
                 L[i][j] = s / L[j][j];
             }
         }
-    float y[6];
-    for (int i = 0; i < nc; i++) {
+    float y[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
         float s = b[i];
+#pragma unroll
         for (int k = 0; k < i; k++) s -= L[i][k] * y[k];
         y[i] = s / L[i][i];
     }
-    for (int i = nc - 1; i >= 0; i--) {
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
         float s = y[i];
-        for (int k = i + 1; k < nc; k++) s -= L[k][i] * x[k];
+#pragma unroll
+        for (int k = i + 1; k < N; k++) s -= L[k][i] * x[k];
         x[i] = s / L[i][i];
     }
-    return true;
+    return ok;
 }
 
-// MLS of one valid point at pixel (x, y).  nb(i, j, dx, dy, dz) yields the
-// offset of the neighbour at pixel (i, j) from the query point and whether it
-// is a valid point; the window runs row-major over the pixels of the image.
-template <typename Nb>
-__device__ __forceinline__ void mls_point(int x, int y, int rows, int cols, int hw, float inv_2s2, int order,
-                                          float r2c, Nb nb, float& ox, float& oy, float& oz, bool& moved) {
-    moved = false;
-    const int r0 = max(0, y - hw), r1 = min(rows, y + hw + 1), c0 = max(0, x - hw), c1 = min(cols, x + hw + 1);
-    // 1. weighted centroid (relative to p)
-    float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
-    int nv = 0;
-    for (int i = r0; i < r1; i++)
-        for (int j = c0; j < c1; j++) {
-            float dx, dy, dz;
-            if (!nb(i, j, dx, dy, dz)) continue;
-            float d2 = dx * dx + dy * dy + dz * dz;
-            if (!(d2 <= r2c)) continue;
-            float w = __expf(-d2 * inv_2s2);
-            cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
-            ws += w;
-            nv++;
+// Normal equations of the order-N polynomial fit (N = 3: 1, u, v; N = 6: also
+// u^2, uv, v^2), accumulated in registers.
+template <int N, typename Visit>
+__device__ __forceinline__ void fit_accumulate(Visit& visit, float inv_2s2, float r2c, float is, float cx, float cy,
+                                               float cz, float t1x, float t1y, float t1z, float t2x, float t2y,
+                                               float t2z, float nx, float ny, float nz, float (&A)[N][N],
+                                               float (&bv)[N]) {
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+        bv[a] = 0.f;
+#pragma unroll
+        for (int b = 0; b < N; b++) A[a][b] = 0.f;
+    }
+    visit([&](float dx, float dy, float dz) {
+        float d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 <= r2c)) return;
+        float w = __expf(-d2 * inv_2s2);
+        float ex = dx - cx, ey = dy - cy, ez = dz - cz;
+        float u = (ex * t1x + ey * t1y + ez * t1z) * is;
+        float v = (ex * t2x + ey * t2y + ez * t2z) * is;
+        float f = ex * nx + ey * ny + ez * nz;
+        float bs[6] = {1.f, u, v, u * u, u * v, v * v};
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+            float wa = w * bs[a];
+            bv[a] = fmaf(wa, f, bv[a]);
+#pragma unroll
+            for (int b = a; b < N; b++) A[a][b] = fmaf(wa, bs[b], A[a][b]);
         }
+    });
+#pragma unroll
+    for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int b = 0; b < a; b++) A[a][b] = A[b][a];
+}
+
+// MLS of one valid point.  visit(fn) calls fn(dx, dy, dz) with the offset from
+// the query point of every valid neighbour of its window (in a fixed order);
+// the distance test against the cut-off is made here.
+template <typename Visit>
+__device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, Visit visit, float& ox, float& oy,
+                                          float& oz, bool& moved) {
+    moved = false;
+    // 1. weighted centroid and covariance in one sweep, from the moments about
+    // the query point (offsets of at most the cut-off radius, so the FP32
+    // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
+    // ~1e-7 rad, far below the 1e-5 mm the points are held to)
+    float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
+    float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f;
+    int nv = 0;
+    visit([&](float dx, float dy, float dz) {
+        float d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 <= r2c)) return;
+        float w = __expf(-d2 * inv_2s2);
+        cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
+        const float wx = w * dx, wy = w * dy;
+        m00 = fmaf(wx, dx, m00); m01 = fmaf(wx, dy, m01); m02 = fmaf(wx, dz, m02);
+        m11 = fmaf(wy, dy, m11); m12 = fmaf(wy, dz, m12); m22 = fmaf(w * dz, dz, m22);
+        ws += w;
+        nv++;
+    });
     if (nv < 3 || ws < 1e-12f) return;
     const float iw = 1.0f / ws;
     cx *= iw; cy *= iw; cz *= iw;
-    // 2. weighted covariance
-    float C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    for (int i = r0; i < r1; i++)
-        for (int j = c0; j < c1; j++) {
-            float dx, dy, dz;
-            if (!nb(i, j, dx, dy, dz)) continue;
-            float d2 = dx * dx + dy * dy + dz * dz;
-            if (!(d2 <= r2c)) continue;
-            float w = __expf(-d2 * inv_2s2);
-            float ex = dx - cx, ey = dy - cy, ez = dz - cz;
-            C[0][0] = fmaf(w * ex, ex, C[0][0]); C[0][1] = fmaf(w * ex, ey, C[0][1]); C[0][2] = fmaf(w * ex, ez, C[0][2]);
-            C[1][1] = fmaf(w * ey, ey, C[1][1]); C[1][2] = fmaf(w * ey, ez, C[1][2]); C[2][2] = fmaf(w * ez, ez, C[2][2]);
-        }
+    // 2. weighted covariance about the centroid: sum w d d^T - ws c c^T
+    float C[3][3];
+    C[0][0] = fmaf(-ws * cx, cx, m00); C[0][1] = fmaf(-ws * cx, cy, m01); C[0][2] = fmaf(-ws * cx, cz, m02);
+    C[1][1] = fmaf(-ws * cy, cy, m11); C[1][2] = fmaf(-ws * cy, cz, m12); C[2][2] = fmaf(-ws * cz, cz, m22);
     C[1][0] = C[0][1]; C[2][0] = C[0][2]; C[2][1] = C[1][2];
     float ev[3], E[3][3];
     sym_eigen3(C, ev, E);
@@ -179,50 +220,36 @@ __device__ __forceinline__ void mls_point(int x, int y, int rows, int cols, int 
         const float s2 = is * is, s4 = s2 * s2;  // pivot of degree-d row scales by h^(-2d)
         thr[0] = 1e-12f; thr[1] = thr[2] = 1e-12f * s2; thr[3] = thr[4] = thr[5] = 1e-12f * s4;
     }
-    if (cur > 0) {
-        const int nc = cur == 1 ? 3 : 6;
-        float A[6][6], bv[6];
+    if (cur == 2) {
+        float A[6][6], bv[6], x6[6];
+        fit_accumulate<6>(visit, inv_2s2, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
+        solved = cholesky_fixed<6>(A, bv, x6, thr);
+        if (solved) {
 #pragma unroll
-        for (int a = 0; a < 6; a++) {
-            bv[a] = 0.f;
+            for (int a = 0; a < 6; a++) co[a] = x6[a];
+        } else {
+            // order 1 on the leading block of the same normal equations
+            float A3[3][3], b3[3], x3[3];
 #pragma unroll
-            for (int b = 0; b < 6; b++) A[a][b] = 0.f;
-        }
-        for (int i = r0; i < r1; i++)
-            for (int j = c0; j < c1; j++) {
-                float dx, dy, dz;
-                if (!nb(i, j, dx, dy, dz)) continue;
-                float d2 = dx * dx + dy * dy + dz * dz;
-                if (!(d2 <= r2c)) continue;
-                float w = __expf(-d2 * inv_2s2);
-                float ex = dx - cx, ey = dy - cy, ez = dz - cz;
-                float u = (ex * t1x + ey * t1y + ez * t1z) * is;
-                float v = (ex * t2x + ey * t2y + ez * t2z) * is;
-                float f = ex * nx + ey * ny + ez * nz;
-                float bs[6] = {1.f, u, v, u * u, u * v, v * v};
-#pragma unroll
-                for (int a = 0; a < 6; a++) {
-                    if (a < nc) {
-                        float wa = w * bs[a];
-                        bv[a] = fmaf(wa, f, bv[a]);
-#pragma unroll
-                        for (int b = 0; b < 6; b++)
-                            if (b >= a && b < nc) A[a][b] = fmaf(wa, bs[b], A[a][b]);
-                    }
-                }
-            }
-        for (int a = 0; a < nc; a++)
-            for (int b = 0; b < a; b++) A[a][b] = A[b][a];
-        solved = cholesky_solve(A, bv, co, nc, thr);
-        if (!solved && cur == 2) {
-            float A1[6][6], b1[6];
             for (int a = 0; a < 3; a++) {
-                b1[a] = bv[a];
-                for (int b = 0; b < 3; b++) A1[a][b] = A[a][b];
+                b3[a] = bv[a];
+#pragma unroll
+                for (int b = 0; b < 3; b++) A3[a][b] = A[a][b];
             }
-            solved = cholesky_solve(A1, b1, co, 3, thr);
-            if (solved) cur = 1;
+            solved = cholesky_fixed<3>(A3, b3, x3, thr);
+            if (solved) {
+                cur = 1;
+#pragma unroll
+                for (int a = 0; a < 3; a++) co[a] = x3[a];
+            }
         }
+    } else if (cur == 1) {
+        float A[3][3], bv[3], x3[3];
+        fit_accumulate<3>(visit, inv_2s2, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
+        solved = cholesky_fixed<3>(A, bv, x3, thr);
+        if (solved)
+#pragma unroll
+            for (int a = 0; a < 3; a++) co[a] = x3[a];
     }
     if (!solved) {
         float dot = ex0 * nx + ey0 * ny + ez0 * nz;
@@ -252,13 +279,16 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
     float ox = 0.f, oy = 0.f, oz = 0.f;
     bool moved = false;
     if (mask[o]) {
-        auto nb = [&](int i, int j, float& dx, float& dy, float& dz) {
-            const size_t q = (size_t)i * cols + j;
-            if (!__ldg(mask + q)) return false;
-            dx = __ldg(src + 3 * q) - px; dy = __ldg(src + 3 * q + 1) - py; dz = __ldg(src + 3 * q + 2) - pz;
-            return true;
+        const int r0 = max(0, y - hw), r1 = min(rows, y + hw + 1), c0 = max(0, x - hw), c1 = min(cols, x + hw + 1);
+        auto visit = [&](auto&& fn) {
+            for (int i = r0; i < r1; i++)
+                for (int j = c0; j < c1; j++) {
+                    const size_t q = (size_t)i * cols + j;
+                    if (!__ldg(mask + q)) continue;
+                    fn(__ldg(src + 3 * q) - px, __ldg(src + 3 * q + 1) - py, __ldg(src + 3 * q + 2) - pz);
+                }
         };
-        mls_point(x, y, rows, cols, hw, inv_2s2, order, r2c, nb, ox, oy, oz, moved);
+        mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
     }
     dst[3 * o] = moved ? px + ox : px;
     dst[3 * o + 1] = moved ? py + oy : py;
@@ -289,19 +319,24 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     }
     __syncthreads();
     const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
-    if (x >= cols || y >= rows) return;
+    const bool inside = x < cols && y < rows;
+    const int cc = (threadIdx.y + hw) * TW + threadIdx.x + hw;
+    const float4 c = mls_sp[cc];
+    if (!inside) return;
     const size_t o = (size_t)y * cols + x;
-    const float4 c = mls_sp[(threadIdx.y + hw) * TW + threadIdx.x + hw];
     const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
     float ox = 0.f, oy = 0.f, oz = 0.f;
     bool moved = false;
     if (c.w != 0.f) {
-        auto nb = [&](int i, int j, float& dx, float& dy, float& dz) {
-            const float4 q = mls_sp[(i - gy0) * TW + (j - gx0)];
-            dx = q.x - px; dy = q.y - py; dz = q.z - pz;
-            return true;  // invalid neighbours are NaN and fail the distance test
+        // invalid and off-image neighbours are NaN and fail the distance test
+        auto visit = [&](auto&& fn) {
+            for (int i = -hw; i <= hw; i++)
+                for (int j = -hw; j <= hw; j++) {
+                    const float4 q = mls_sp[cc + i * TW + j];
+                    fn(q.x - px, q.y - py, q.z - pz);
+                }
         };
-        mls_point(x, y, rows, cols, hw, inv_2s2, order, r2c, nb, ox, oy, oz, moved);
+        mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
     }
     dst[3 * o] = moved ? px + ox : px;
     dst[3 * o + 1] = moved ? py + oy : py;

@@ -514,6 +514,83 @@ __device__ __forceinline__ void match_spans(const int* s_ord, int cols, int pha_
     }
 }
 
+// -------------------------------------------------------- pixel rays ----
+// An organised cloud from one camera: cloud pixel (u, v) looks from the origin
+// along R (u + ox - cx, v + oy - cy, f).  A point p seen along the ray of
+// pixel b and a query q near the ray of pixel a satisfy
+// |p - q| >= |q| sin(angle(a, b)) - dev(q) - dev(p) (dev: distance from the own
+// ray), and with |a x b| >= f |b - a|, |b| <= |a| + |b - a|:
+// sin(angle) >= f |b - a| / (|a| (|a| + |b - a|)), increasing in |b - a|.
+// The window paths of the filters use this to stop scanning a pixel window.
+
+struct RayParams {
+    float cx, cy, f, R[9];
+    int ox, oy;
+};
+
+__device__ __forceinline__ void ray_dir(const RayParams& r, int u, int v, float& ax, float& ay, float& az) {
+    const float x = (float)(u + r.ox) - r.cx, y = (float)(v + r.oy) - r.cy;
+    ax = fmaf(r.R[0], x, fmaf(r.R[1], y, r.R[2] * r.f));
+    ay = fmaf(r.R[3], x, fmaf(r.R[4], y, r.R[5] * r.f));
+    az = fmaf(r.R[6], x, fmaf(r.R[7], y, r.R[8] * r.f));
+}
+
+// Distance of p from the line through the origin along a: |p x a| / |a|.
+__device__ __forceinline__ float ray_dev(float px, float py, float pz, float ax, float ay, float az) {
+    const float cx = fmaf(py, az, -pz * ay), cy = fmaf(pz, ax, -px * az), cz = fmaf(px, ay, -py * ax);
+    return sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz))) * rsqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+}
+
+// Largest distance of a valid point from its pixel ray, as float bits into
+// *dev (atomicMax; *dev starts at 0).
+static __global__ void ray_dev_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
+                               RayParams rp, unsigned* __restrict__ dev) {
+    const size_t n = (size_t)rows * cols;
+    float m = 0.f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!mask[i]) continue;
+        float ax, ay, az;
+        ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
+        const float d = ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
+        m = fmaxf(m, d == d ? d : INFINITY);  // NaN counts as unbounded
+    }
+    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+    if ((threadIdx.x & 31) == 0 && b) atomicMax(dev, b);
+}
+
+inline RayParams ray_params(const zim_ray_model& r) {
+    RayParams p;
+    p.cx = r.cx; p.cy = r.cy; p.f = r.f;
+    for (int a = 0; a < 9; a++) p.R[a] = r.R[a];
+    p.ox = r.ox; p.oy = r.oy;
+    return p;
+}
+
+// pixel offsets of the window ordered by length, then row, then column
+constexpr int SPIRAL_R = 7;
+constexpr int SPIRAL_N = (2 * SPIRAL_R + 1) * (2 * SPIRAL_R + 1) - 1;
+__constant__ signed char c_spiral7[SPIRAL_N][2] = {
+    {0, -1}, {-1, 0}, {1, 0}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0}, {2, 0}, {0, 2},
+    {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
+    {0, -3}, {-3, 0}, {3, 0}, {0, 3}, {-1, -3}, {1, -3}, {-3, -1}, {3, -1}, {-3, 1}, {3, 1}, {-1, 3}, {1, 3},
+    {-2, -3}, {2, -3}, {-3, -2}, {3, -2}, {-3, 2}, {3, 2}, {-2, 3}, {2, 3}, {0, -4}, {-4, 0}, {4, 0}, {0, 4},
+    {-1, -4}, {1, -4}, {-4, -1}, {4, -1}, {-4, 1}, {4, 1}, {-1, 4}, {1, 4}, {-3, -3}, {3, -3}, {-3, 3}, {3, 3},
+    {-2, -4}, {2, -4}, {-4, -2}, {4, -2}, {-4, 2}, {4, 2}, {-2, 4}, {2, 4}, {0, -5}, {-3, -4}, {3, -4}, {-4, -3},
+    {4, -3}, {-5, 0}, {5, 0}, {-4, 3}, {4, 3}, {-3, 4}, {3, 4}, {0, 5}, {-1, -5}, {1, -5}, {-5, -1}, {5, -1},
+    {-5, 1}, {5, 1}, {-1, 5}, {1, 5}, {-2, -5}, {2, -5}, {-5, -2}, {5, -2}, {-5, 2}, {5, 2}, {-2, 5}, {2, 5},
+    {-4, -4}, {4, -4}, {-4, 4}, {4, 4}, {-3, -5}, {3, -5}, {-5, -3}, {5, -3}, {-5, 3}, {5, 3}, {-3, 5}, {3, 5},
+    {0, -6}, {-6, 0}, {6, 0}, {0, 6}, {-1, -6}, {1, -6}, {-6, -1}, {6, -1}, {-6, 1}, {6, 1}, {-1, 6}, {1, 6},
+    {-2, -6}, {2, -6}, {-6, -2}, {6, -2}, {-6, 2}, {6, 2}, {-2, 6}, {2, 6}, {-4, -5}, {4, -5}, {-5, -4}, {5, -4},
+    {-5, 4}, {5, 4}, {-4, 5}, {4, 5}, {-3, -6}, {3, -6}, {-6, -3}, {6, -3}, {-6, 3}, {6, 3}, {-3, 6}, {3, 6},
+    {0, -7}, {-7, 0}, {7, 0}, {0, 7}, {-1, -7}, {1, -7}, {-5, -5}, {5, -5}, {-7, -1}, {7, -1}, {-7, 1}, {7, 1},
+    {-5, 5}, {5, 5}, {-1, 7}, {1, 7}, {-4, -6}, {4, -6}, {-6, -4}, {6, -4}, {-6, 4}, {6, 4}, {-4, 6}, {4, 6},
+    {-2, -7}, {2, -7}, {-7, -2}, {7, -2}, {-7, 2}, {7, 2}, {-2, 7}, {2, 7}, {-3, -7}, {3, -7}, {-7, -3}, {7, -3},
+    {-7, 3}, {7, 3}, {-3, 7}, {3, 7}, {-5, -6}, {5, -6}, {-6, -5}, {6, -5}, {-6, 5}, {6, 5}, {-5, 6}, {5, 6},
+    {-4, -7}, {4, -7}, {-7, -4}, {7, -4}, {-7, 4}, {7, 4}, {-4, 7}, {4, 7}, {-6, -6}, {6, -6}, {-6, 6}, {6, 6},
+    {-5, -7}, {5, -7}, {-7, -5}, {7, -5}, {-7, 5}, {7, 5}, {-5, 7}, {5, 7}, {-6, -7}, {6, -7}, {-7, -6}, {7, -6},
+    {-7, 6}, {7, 6}, {-6, 7}, {6, 7}, {-7, -7}, {7, -7}, {-7, 7}, {7, 7},
+};
+
 // -------------------------------------------------- median + reprojection ----
 
 constexpr int RX = 32, RY = 8;  // median/reprojection tile
