@@ -907,10 +907,12 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                                                                      const unsigned* __restrict__ deferred,
                                                                      float* __restrict__ md_out,
                                                                      uint32_t* __restrict__ err) {
-    __shared__ float L[P2_WARPS][KNN_MAX_K1][32];
-    __shared__ float M[P2_WARPS][KNN_MAX_K1];  // merged K1 smallest, ascending
+    // per warp: K1 sorted entries per lane, then the merged K1 smallest
+    extern __shared__ float far_smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int K1 = k + 1;
+    float* Lw = far_smem + (size_t)w * K1 * 33;  // Lw[j * 32 + lane]: lane's j-th smallest
+    float* Mw = Lw + (size_t)K1 * 32;            // K1 merged
     const unsigned nd = s->n_deferred, nocc = s->n_occ;
     for (;;) {
         unsigned item = 0;
@@ -926,18 +928,29 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         // the lanes split a cell's points; each keeps its K1 smallest, sorted
         auto scan_cell = [&](unsigned j) {
             const uint4 o = occ[j];
-            for (unsigned u = o.y + lane; u < o.y + o.z; u += 32) {
-                const float4 p = __ldg(pts + u);
-                const float d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
-                int jj;
-                if (cnt < K1) jj = cnt++;
-                else if (d2 < L[w][K1 - 1][lane]) jj = K1 - 1;
-                else continue;
-                while (jj > 0 && L[w][jj - 1][lane] > d2) {
-                    L[w][jj][lane] = L[w][jj - 1][lane];
-                    jj--;
+            const unsigned end = o.y + o.z;
+            // four loads in flight per lane, then the insertions
+            for (unsigned u0 = o.y + lane; u0 < end; u0 += 128) {
+                float4 p[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const unsigned u = u0 + 32u * r;
+                    p[r] = u < end ? __ldg(pts + u) : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
-                L[w][jj][lane] = d2;
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    if (u0 + 32u * r >= end) break;
+                    const float d2 = sqdist(p[r].x - qx, p[r].y - qy, p[r].z - qz);
+                    int jj;
+                    if (cnt < K1) jj = cnt++;
+                    else if (d2 < Lw[(K1 - 1) * 32 + lane]) jj = K1 - 1;
+                    else continue;
+                    while (jj > 0 && Lw[(jj - 1) * 32 + lane] > d2) {
+                        Lw[jj * 32 + lane] = Lw[(jj - 1) * 32 + lane];
+                        jj--;
+                    }
+                    Lw[jj * 32 + lane] = d2;
+                }
             }
             __syncwarp();
         };
@@ -946,7 +959,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
             int head = 0;
             float kk = INFINITY;
             for (int round = 0; round < K1; round++) {
-                float v = head < cnt ? L[w][head][lane] : INFINITY;
+                float v = head < cnt ? Lw[head * 32 + lane] : INFINITY;
                 int who = lane;
                 for (int off = 16; off; off >>= 1) {
                     float ov = __shfl_xor_sync(0xffffffffu, v, off);
@@ -954,7 +967,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                     if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
                 }
                 if (lane == who) head++;
-                if (lane == 0) M[w][round] = v;
+                if (lane == 0) Mw[round] = v;
                 if (round == K1 - 1) kk = v;
             }
             __syncwarp();
@@ -1012,7 +1025,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
             const int e = root_exponent(kth);
             const float sc = root_scale(e);
             long long part = 0;
-            for (int j = lane; j < K1; j += 32) part += root_fixed(M[w][j], sc);
+            for (int j = lane; j < K1; j += 32) part += root_fixed(Mw[j], sc);
             for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
             md = fixed_mean(part, e, k);
         }
@@ -1322,7 +1335,9 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
                                                     window);
-    sor_knn_far_kernel<<<(unsigned)(4 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
+    // enough warps in flight to cover the latency of the long point scans
+    const size_t fsm = (size_t)P2_WARPS * (mean_k + 1) * 33 * sizeof(float);
+    sor_knn_far_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, fsm, st>>>(
         xyz, mean_k, G.stats, G.occ, G.pts[1], G.deferred, md, ctx->d_error);
     ctx->launches += 3;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
