@@ -146,7 +146,9 @@ extern "C" ZIM_API zim_status zim_create(int device, zim_ctx** out) {
     if (cudaFree(0) != cudaSuccess || cudaMalloc(&ctx->d_error, sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->d_error, 0, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->d_sor_stats, 256) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess) {
+        cudaMallocHost(&ctx->h_pinned, 4096) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->aux_event, cudaEventDisableTiming) != cudaSuccess) {
         delete ctx;
         return ZIM_ERR_CUDA;
     }
@@ -165,6 +167,8 @@ extern "C" ZIM_API void zim_destroy(zim_ctx* ctx) {
     cudaFree(ctx->d_error);
     cudaFree(ctx->d_sor_stats);
     cudaFreeHost(ctx->h_pinned);
+    if (ctx->aux_event) cudaEventDestroy(ctx->aux_event);
+    if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     delete ctx;
 }
 
@@ -275,12 +279,16 @@ static zim_status check_pair_args(zim_ctx* ctx, const zim_decode_config* d, cons
     return zim_check_reproject(ctx, r);
 }
 
+// right_ready (may be null): an event the right camera's frames wait for, so
+// that their upload overlaps the left camera's decode.
 static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_recon_config* r, const void* lf,
                            const void* rf, int sample_type, int rows, int cols, int pha_f, float* xyz_out,
-                           uint8_t* mask_out, float* disp_out, PairBuffers& B, cudaStream_t st) {
+                           uint8_t* mask_out, float* disp_out, PairBuffers& B, cudaStream_t st,
+                           cudaEvent_t right_ready = nullptr) {
     zim_status s;
     const void* frames[2] = {lf, rf};
     for (int c = 0; c < 2; c++) {
+        if (c == 1 && right_ready) ZIM_CUDA_TRY(ctx, cudaStreamWaitEvent(st, right_ready, 0));
         s = zim_decode_launch(ctx, d, frames[c], sample_type, rows, cols, B.order[c], B.res[c], nullptr, nullptr, st);
         if (s) return s;
         s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->enable_hdr ? (d->post_smooth ? 2 : 3) : (d->post_smooth ? 1 : 0),
@@ -443,12 +451,17 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     float* ddisp = (float*)zim_scratch_take(ctx, dst * 4);
     if (!dl || !dr || !dxyz || !dmask || !ddisp) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "scratch carve failed");
     cudaStream_t st = zim_stream(stream);
+    // the right frames travel on the second queue while the left camera decodes
+    // (the second queue starts after everything already on st)
     ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(dl, lf, fbytes, cudaMemcpyHostToDevice, st));
-    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(dr, rf, fbytes, cudaMemcpyHostToDevice, st));
+    ZIM_CUDA_TRY(ctx, cudaEventRecord(ctx->aux_event, st));
+    ZIM_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_event, 0));
+    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(dr, rf, fbytes, cudaMemcpyHostToDevice, ctx->aux_stream));
+    ZIM_CUDA_TRY(ctx, cudaEventRecord(ctx->aux_event, ctx->aux_stream));
     PairBuffers B;
     s = carve_pair(ctx, r, rows, cols, ddisp, B);
     if (s) return s;
-    s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, dxyz, dmask, ddisp, B, st);
+    s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, dxyz, dmask, ddisp, B, st, ctx->aux_event);
     if (s) return s;
     ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st));
     ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st));

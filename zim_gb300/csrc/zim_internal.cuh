@@ -45,6 +45,8 @@ struct zim_ctx {
     void* h_pinned = nullptr;     // small pinned staging (counts)
     unsigned long long launches = 0;  // kernels this context has launched
     void* d_sor_stats = nullptr;      // device copy of the last SOR run's statistics (256 B)
+    cudaStream_t aux_stream = nullptr; // second copy engine queue for the host entry points
+    cudaEvent_t aux_event = nullptr;
     bool have_sor_stats = false;
     double last_sor_std_mul = 1.0;
 };

@@ -199,7 +199,18 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
             const T* src = fb + (size_t)gy * p.cols + gx;
             float s = 0.f, c = 0.f, m = 0.f;
-            for (int k = 0; k < N; k++) {
+            int k = 0;
+            // four frames' loads in flight before their sums (the same
+            // accumulation order as one frame at a time)
+            for (; k + 4 <= N; k += 4) {
+                const float v0 = (float)__ldg(src + (size_t)k * npx), v1 = (float)__ldg(src + (size_t)(k + 1) * npx);
+                const float v2 = (float)__ldg(src + (size_t)(k + 2) * npx), v3 = (float)__ldg(src + (size_t)(k + 3) * npx);
+                s = fmaf(-sv[k], v0, s); c = fmaf(cv[k], v0, c); m += v0;
+                s = fmaf(-sv[k + 1], v1, s); c = fmaf(cv[k + 1], v1, c); m += v1;
+                s = fmaf(-sv[k + 2], v2, s); c = fmaf(cv[k + 2], v2, c); m += v2;
+                s = fmaf(-sv[k + 3], v3, s); c = fmaf(cv[k + 3], v3, c); m += v3;
+            }
+            for (; k < N; k++) {
                 float v = (float)__ldg(src + (size_t)k * npx);
                 s = fmaf(-sv[k], v, s);
                 c = fmaf(cv[k], v, c);
