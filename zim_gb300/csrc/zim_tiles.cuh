@@ -146,9 +146,33 @@ __device__ __forceinline__ int floor_div(int a, int b, float inv_b) {
 }
 
 // Shared memory of one decode tile: the raw per-pixel sums of the tile + halo.
+constexpr int DEC_MAX_PS = 4;  // phase-shift frequencies staged together
 struct DecodeSmem {
-    float S[DHY][DHX + 1], C[DHY][DHX + 1], M[DHY][DHX + 1];
+    float S[DEC_MAX_PS][DHY][DHX + 1], C[DEC_MAX_PS][DHY][DHX + 1], M[DEC_MAX_PS][DHY][DHX + 1];
 };
+
+// Raw sums of one halo pixel over the N frames of one frequency, four frames'
+// loads in flight at a time (the same accumulation order as one at a time).
+template <typename T>
+__device__ __forceinline__ void frame_sums(const T* __restrict__ src, size_t npx, int N, const float* sv,
+                                           const float* cv, float& s, float& c, float& m) {
+    s = 0.f; c = 0.f; m = 0.f;
+    int k = 0;
+    for (; k + 4 <= N; k += 4) {
+        const float v0 = (float)__ldg(src + (size_t)k * npx), v1 = (float)__ldg(src + (size_t)(k + 1) * npx);
+        const float v2 = (float)__ldg(src + (size_t)(k + 2) * npx), v3 = (float)__ldg(src + (size_t)(k + 3) * npx);
+        s = fmaf(-sv[k], v0, s); c = fmaf(cv[k], v0, c); m += v0;
+        s = fmaf(-sv[k + 1], v1, s); c = fmaf(cv[k + 1], v1, c); m += v1;
+        s = fmaf(-sv[k + 2], v2, s); c = fmaf(cv[k + 2], v2, c); m += v2;
+        s = fmaf(-sv[k + 3], v3, s); c = fmaf(cv[k + 3], v3, c); m += v3;
+    }
+    for (; k < N; k++) {
+        float v = (float)__ldg(src + (size_t)k * npx);
+        s = fmaf(-sv[k], v, s);
+        c = fmaf(cv[k], v, c);
+        m += v;
+    }
+}
 
 // Decodes tile (bx, by) of DX x DY pixels with the DX * DY threads of a block
 // (tid = ty * DX + tx).  The pre-blur is linear, so the blurred sums
@@ -170,6 +194,26 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
     float mod0 = 0.f;
     bool ok = true;
     const bool inside = x < p.cols && y < p.rows;
+    if (!p.hdr) {
+        // every frequency's halo sums in one pass: all of a pixel's frame loads
+        // are issued before the tile waits
+        for (int h = tid; h < DHX * DHY; h += DX * DY) {
+            const int hy = h / DHX, hx = h - hy * DHX;
+            const int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
+            const size_t pix = (size_t)gy * p.cols + gx;
+#pragma unroll
+            for (int i = 0; i < DEC_MAX_PS; i++) {
+                if (i >= p.n_ps) break;
+                float s, c, m;
+                frame_sums(frames + (size_t)p.fbase[i] * npx + pix, npx, p.shift[i], p.sinv + p.fbase[i],
+                           p.cosv + p.fbase[i], s, c, m);
+                sm.S[i][hy][hx] = s;
+                sm.C[i][hy][hx] = c;
+                sm.M[i][hy][hx] = m;
+            }
+        }
+        __syncthreads();
+    }
     for (int i = 0; i < p.n_ps; i++) {
         const int N = p.shift[i];
         const T* fb = frames + (size_t)p.fbase[i] * npx;
@@ -194,44 +238,16 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             }
             continue;
         }
-        for (int h = tid; h < DHX * DHY; h += DX * DY) {
-            int hy = h / DHX, hx = h - hy * DHX;
-            int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
-            const T* src = fb + (size_t)gy * p.cols + gx;
-            float s = 0.f, c = 0.f, m = 0.f;
-            int k = 0;
-            // four frames' loads in flight before their sums (the same
-            // accumulation order as one frame at a time)
-            for (; k + 4 <= N; k += 4) {
-                const float v0 = (float)__ldg(src + (size_t)k * npx), v1 = (float)__ldg(src + (size_t)(k + 1) * npx);
-                const float v2 = (float)__ldg(src + (size_t)(k + 2) * npx), v3 = (float)__ldg(src + (size_t)(k + 3) * npx);
-                s = fmaf(-sv[k], v0, s); c = fmaf(cv[k], v0, c); m += v0;
-                s = fmaf(-sv[k + 1], v1, s); c = fmaf(cv[k + 1], v1, c); m += v1;
-                s = fmaf(-sv[k + 2], v2, s); c = fmaf(cv[k + 2], v2, c); m += v2;
-                s = fmaf(-sv[k + 3], v3, s); c = fmaf(cv[k + 3], v3, c); m += v3;
-            }
-            for (; k < N; k++) {
-                float v = (float)__ldg(src + (size_t)k * npx);
-                s = fmaf(-sv[k], v, s);
-                c = fmaf(cv[k], v, c);
-                m += v;
-            }
-            sm.S[hy][hx] = s;
-            sm.C[hy][hx] = c;
-            sm.M[hy][hx] = m;
-        }
-        __syncthreads();
         float S = 0.f, C = 0.f, M = 0.f;
 #pragma unroll
         for (int a = 0; a < 3; a++)
 #pragma unroll
             for (int b = 0; b < 3; b++) {
                 float w = p.w2d[a * 3 + b];
-                S = fmaf(w, sm.S[ty + a][tx + b], S);
-                C = fmaf(w, sm.C[ty + a][tx + b], C);
-                M = fmaf(w, sm.M[ty + a][tx + b], M);
+                S = fmaf(w, sm.S[i][ty + a][tx + b], S);
+                C = fmaf(w, sm.C[i][ty + a][tx + b], C);
+                M = fmaf(w, sm.M[i][ty + a][tx + b], M);
             }
-        __syncthreads();
         if (ok) {
             const float wr = atan2f(S, C);
             if (i == 0) wrap0 = wr;
@@ -245,6 +261,8 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
             if (nm < p.thr) ok = false;
         }
     }
+    // every thread is past its last shared read before the block's next tile
+    if (!p.hdr) __syncthreads();
     if (x >= p.cols || y >= p.rows) return;
     const size_t pix = (size_t)y * p.cols + x;
     if (mod_out) mod_out[pix] = mod0;
