@@ -45,6 +45,7 @@ constexpr int SCAN_B = 1024;
 constexpr int MAX_LEVELS = 2;    // finest + one coarse level
 constexpr int FINE_RINGS = 2;    // phase-1 fallback rings on the finest level
 constexpr int P2_WARPS = 4;      // phase-2 warps per CTA
+constexpr int RING_MAX = 6;      // phase-2 rings of dense cells before the best-first search
 constexpr int TILE_X = 16, TILE_Y = 8, TILE_T = TILE_X * TILE_Y;
 constexpr int TILE_DILATE = 2;        // cells added around a tile's box
 constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
@@ -903,6 +904,7 @@ __device__ __forceinline__ float cell_box_d2(unsigned idx, const GridStats* __re
 __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float* __restrict__ xyz, int k,
                                                                      GridStats* s,
                                                                      const uint4* __restrict__ occ,
+                                                                     const uint2* __restrict__ tab1,
                                                                      const float4* __restrict__ pts,
                                                                      const unsigned* __restrict__ deferred,
                                                                      float* __restrict__ md_out,
@@ -926,11 +928,10 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
         int cnt = 0;
         // the lanes split a cell's points; each keeps its K1 smallest, sorted
-        auto scan_cell = [&](unsigned j) {
-            const uint4 o = occ[j];
-            const unsigned end = o.y + o.z;
+        auto scan_range = [&](unsigned first, unsigned count) {
+            const unsigned end = first + count;
             // four loads in flight per lane, then the insertions
-            for (unsigned u0 = o.y + lane; u0 < end; u0 += 128) {
+            for (unsigned u0 = first + lane; u0 < end; u0 += 128) {
                 float4 p[4];
 #pragma unroll
                 for (int r = 0; r < 4; r++) {
@@ -953,6 +954,10 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                 }
             }
             __syncwarp();
+        };
+        auto scan_cell = [&](unsigned j) {
+            const uint4 o = occ[j];
+            scan_range(o.y, o.z);
         };
         // the K1 smallest over all lanes, in order, into M; returns the K1-th
         auto merge = [&]() {
@@ -977,8 +982,57 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         float last_d = -1.f;
         int last_j = -1;
         bool done = false;
+        // Rings of dense cells around the query's cell: ring r holds every cell
+        // at Chebyshev distance r, all at least (r - 1) cells away; after each
+        // ring the K1 smallest so far bound the rest.  Far-isolated points
+        // (more than RING_MAX rings) take the best-first search below.
+        {
+            const float c1 = s->cell[1], ic1 = s->inv_cell[1];
+            const int nx = s->dims[0], ny = s->dims[1], nz = s->dims[2];
+            const int qcx = min(max(__float2int_rd((qx - s->org[0]) * ic1), 0), nx - 1);
+            const int qcy = min(max(__float2int_rd((qy - s->org[1]) * ic1), 0), ny - 1);
+            const int qcz = min(max(__float2int_rd((qz - s->org[2]) * ic1), 0), nz - 1);
+            for (int r = 0; r <= RING_MAX; r++) {
+                if (r >= 1 && kth < INFINITY) {
+                    const float gap = (float)(r - 1) * c1 - margin;
+                    if (gap > 0.f && gap * gap > kth) {
+                        done = true;
+                        break;
+                    }
+                }
+                const int side = 2 * r + 1, ncell = side * side * side;
+                for (int t0 = 0; t0 < ncell; t0 += 32) {
+                    const int t = t0 + lane;
+                    bool take = false;
+                    uint2 e = make_uint2(0u, 0u);
+                    if (t < ncell) {
+                        const int dx = t % side - r, dy = (t / side) % side - r, dz = t / (side * side) - r;
+                        const int cheb = max(abs(dx), max(abs(dy), abs(dz)));
+                        const int ix = qcx + dx, iy = qcy + dy, iz = qcz + dz;
+                        if (cheb == r && ix >= 0 && ix < nx && iy >= 0 && iy < ny && iz >= 0 && iz < nz) {
+                            const unsigned idx = ((unsigned)iz * (unsigned)ny + (unsigned)iy) * (unsigned)nx + (unsigned)ix;
+                            e = __ldg(tab1 + idx);
+                            take = e.y > 0u && cell_box_d2(idx, s, qx, qy, qz, margin) <= kth;
+                        }
+                    }
+                    unsigned m = __ballot_sync(0xffffffffu, take);
+                    while (m) {
+                        const int b = __ffs(m) - 1;
+                        m &= m - 1;
+                        scan_range(__shfl_sync(0xffffffffu, e.x, b), __shfl_sync(0xffffffffu, e.y, b));
+                    }
+                }
+                kth = merge();
+            }
+        }
+        if (!done) {
+            // restart from nothing: best-first over the occupied cells
+            cnt = 0;
+            kth = INFINITY;
+            __syncwarp();
+        }
         // best-first until k + 1 points are held
-        for (unsigned iter = 0; iter <= nocc; iter++) {
+        for (unsigned iter = 0; !done && iter <= nocc; iter++) {
             // nearest cell after (last_d, last_j) in (distance, index) order
             float bd = INFINITY;
             int bj = INT_MAX;
@@ -999,7 +1053,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
             last_j = bj;
             if (kth < INFINITY) break;
         }
-        if (kth < INFINITY) {
+        if (!done && kth < INFINITY) {
             // every cell not yet visited whose cube lies within the current
             // (k + 1)-th distance, in index order, then one merge
             for (unsigned j0 = 0; j0 < nocc; j0 += 32) {
@@ -1338,7 +1392,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     // enough warps in flight to cover the latency of the long point scans
     const size_t fsm = (size_t)P2_WARPS * (mean_k + 1) * 33 * sizeof(float);
     sor_knn_far_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, fsm, st>>>(
-        xyz, mean_k, G.stats, G.occ, G.pts[1], G.deferred, md, ctx->d_error);
+        xyz, mean_k, G.stats, G.occ, G.tab[1], G.pts[1], G.deferred, md, ctx->d_error);
     ctx->launches += 3;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
     const unsigned pblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
