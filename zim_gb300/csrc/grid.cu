@@ -743,29 +743,48 @@ constexpr int WN = zt::SPIRAL_N;
 
 // Per-thread selection of the K1 smallest squared distances in column tid of
 // a [cap][TILE_T] shared array: values within the bound are appended; a full
-// list is sorted, cut to K1 and the bound tightened to its K1-th value.
+// list is cut to its K1 smallest (quickselect) and the bound tightened to the
+// K1-th value.
 struct WinSel {
     float* L;
     int cnt, K1, cap;
     float thr;
-    __device__ __forceinline__ void sort() {
-        for (int a = 1; a < cnt; a++) {
-            const float v = L[a * TILE_T];
-            int b = a;
-            while (b > 0 && L[(b - 1) * TILE_T] > v) {
-                L[b * TILE_T] = L[(b - 1) * TILE_T];
-                b--;
+    __device__ __forceinline__ float& at(int j) { return L[j * TILE_T]; }
+    // Rearranges entries [0, cnt) so that [0, K1) hold the K1 smallest;
+    // returns the K1-th smallest (Hoare partitions, median-of-three pivots).
+    __device__ __forceinline__ float select() {
+        int lo = 0, hi = cnt - 1;
+        const int t = K1 - 1;
+        while (lo < hi) {
+            const float a = at(lo), b = at((lo + hi) >> 1), c = at(hi);
+            const float pv = fmaxf(fminf(a, b), fminf(fmaxf(a, b), c));
+            int i = lo, j = hi;
+            while (i <= j) {
+                while (at(i) < pv) i++;
+                while (at(j) > pv) j--;
+                if (i <= j) {
+                    const float v = at(i);
+                    at(i) = at(j);
+                    at(j) = v;
+                    i++;
+                    j--;
+                }
             }
-            L[b * TILE_T] = v;
+            if (t <= j) hi = j;
+            else if (t >= i) lo = i;
+            else break;  // t lies among entries equal to the pivot
         }
+        // [0, K1) now holds the K1 smallest; the K1-th is their maximum
+        float m = at(0);
+        for (int j = 1; j < K1; j++) m = fmaxf(m, at(j));
+        return m;
     }
     __device__ __forceinline__ void push(float d2) {
         if (d2 > thr) return;
-        L[cnt * TILE_T] = d2;
+        at(cnt) = d2;
         if (++cnt == cap) {
-            sort();
+            thr = select();
             cnt = K1;
-            thr = L[(K1 - 1) * TILE_T];
         }
     }
 };
@@ -853,8 +872,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
             rs2 = stop_r2(last);
         }
     }
-    sel.sort();
-    const float kth = sel.L[(K1 - 1) * TILE_T];
+    const float kth = sel.select();
     // certificate: every pixel not visited is at least rbreak away (the
     // unvisited window entries) or WR + 1 away (outside the window)
     const bool ok = C * rbreak / (an + rbreak) - dev > sqrtf(kth);
