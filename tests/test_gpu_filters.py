@@ -143,6 +143,25 @@ def test_sor_window_path_equals_grid_path(ctx, oracle_lib, k):
 
 
 @pytest.mark.gpu
+def test_mls_ray_disk_equals_full_window(ctx, oracle_lib):
+    """The ray bound only skips window pixels beyond the cut-off: with pixel
+    rays (the calibrated size) and without (the cloud padded by one invalid
+    column) the MLS output is bit-identical."""
+    import math
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    H, W = mask.shape
+    xp = torch.zeros((H, W + 1, 3), dtype=torch.float32, device="cuda")
+    mp = torch.zeros((H, W + 1), dtype=torch.uint8, device="cuda")
+    xp[:, :W] = xyz
+    mp[:, :W] = mask
+    args = (7, 2.0 / math.sqrt(2.0), 2, 2.0, 2)
+    a = api.filter_mls(ctx, xyz, mask, *args)
+    b = api.filter_mls(ctx, xp.contiguous(), mp.contiguous(), *args)[:, :W].contiguous()
+    assert torch.equal(a, b)
+
+
+@pytest.mark.gpu
 def test_metric_gaussian_window_path_matches_grid_path(ctx, oracle_lib):
     """Window-certified points against the grid path (the padded cloud has no
     pixel rays): the same neighbours, summed in another order, so equal to a

@@ -367,7 +367,8 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
     if (on[ST_MLS]) {
         float* ox = next_x(ST_MLS);
         s = zim_mls_launch(ctx, cx, cm, RH, RW, r->mls_window_size, r->mls_spatial_sigma, r->mls_polynomial_order,
-                           r->mls_max_radius, r->mls_iterations, ox, B.mls_tmp, st);
+                           r->mls_max_radius, r->mls_iterations, ox, B.mls_tmp,
+                           zim_rays_of(ctx, r->use_rectified_coords != 0, 0, 0), st);
         if (s) return s;
         cx = ox;
     }

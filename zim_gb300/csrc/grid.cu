@@ -1349,10 +1349,13 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     const unsigned sblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
     spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
     spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats);
-    spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
-    spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats);
+    if (!(fixed_cell > 0.f)) {  // the trimmed spacing sets the cell
+        spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
+        spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats);
+        ctx->launches += 2;
+    }
     cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
-    ctx->launches += 6;
+    ctx->launches += 4;
     for (int l = 0; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
         ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));

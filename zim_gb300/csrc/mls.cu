@@ -299,9 +299,14 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
 // and off-image pixels (their distance test fails).
 inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * hw) * sizeof(float4); }
 
+// With pixel rays (rays != 0) each row of the window is cut to the disk beyond
+// which the ray bound puts every point outside the cut-off: the pixels left out
+// would fail the distance test, so the neighbours and their order are those
+// of the full window.  The disk is the largest of the warp's (one loop bound).
 __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restrict__ src,
                                                           const uint8_t* __restrict__ mask, int rows, int cols, int hw,
-                                                          float inv_2s2, int order, float r2c,
+                                                          float inv_2s2, int order, float r2c, int rays,
+                                                          zt::RayParams rp, const unsigned* __restrict__ dev_max,
                                                           float* __restrict__ dst) {
     extern __shared__ float4 mls_sp[];
     const int TW = MX + 2 * hw, TH = MY + 2 * hw;
@@ -322,6 +327,24 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     const bool inside = x < cols && y < rows;
     const int cc = (threadIdx.y + hw) * TW + threadIdx.x + hw;
     const float4 c = mls_sp[cc];
+    float wr2 = INFINITY;  // squared pixel radius of the warp's disk
+    if (rays) {
+        float rs2 = 0.f;
+        if (inside && c.w != 0.f) {
+            float ax, ay, az;
+            zt::ray_dir(rp, x, y, ax, ay, az);
+            const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+            const float qn = sqrtf(fmaf(c.x, c.x, fmaf(c.y, c.y, c.z * c.z)));
+            const float C = qn * rp.f / an;
+            const float sd = sqrtf(r2c) + zt::ray_dev(c.x, c.y, c.z, ax, ay, az) + __uint_as_float(*dev_max) + 1e-5f * qn;
+            rs2 = INFINITY;
+            if (C > sd) {
+                const float r = sd * an / (C - sd);
+                rs2 = r * r;
+            }
+        }
+        wr2 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(rs2)));
+    }
     if (!inside) return;
     const size_t o = (size_t)y * cols + x;
     const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
@@ -330,11 +353,15 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     if (c.w != 0.f) {
         // invalid and off-image neighbours are NaN and fail the distance test
         auto visit = [&](auto&& fn) {
-            for (int i = -hw; i <= hw; i++)
-                for (int j = -hw; j <= hw; j++) {
+            for (int i = -hw; i <= hw; i++) {
+                const float rem = wr2 - (float)(i * i);
+                if (rem < 0.f) continue;
+                const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
+                for (int j = -w; j <= w; j++) {
                     const float4 q = mls_sp[cc + i * TW + j];
                     fn(q.x - px, q.y - py, q.z - pz);
                 }
+            }
         };
         mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
     }
@@ -349,7 +376,7 @@ size_t zim_mls_scratch_bytes(size_t n_points) { return zim_align256(n_points * 1
 
 zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, int window,
                           float sigma, int order, float max_radius, int iterations, float* out, float* tmp,
-                          cudaStream_t st) {
+                          const zim_ray_model& rays, cudaStream_t st) {
     const float r2c = max_radius > 0.f ? max_radius * max_radius : 9.0f * sigma * sigma;
     const float inv_2s2 = 1.0f / (2.0f * sigma * sigma);
     const int ord = order < 0 ? 0 : (order > 2 ? 2 : order);
@@ -359,13 +386,27 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const bool use_smem = smem <= 96 * 1024;
     if (use_smem)
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(mls_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int use_rays = use_smem && rays.valid;
+    unsigned* dev_max = nullptr;
+    if (use_rays) {
+        dev_max = (unsigned*)zim_scratch_take(ctx, 256);
+        if (!dev_max) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "MLS scratch");
+    }
+    const zt::RayParams rp = zt::ray_params(rays);
     // ping-pong so that the last pass lands in `out`
     const float* in = xyz;
     for (int it = 0; it < n_iter; it++) {
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
+        if (use_rays) {
+            ZIM_CUDA_TRY(ctx, cudaMemsetAsync(dev_max, 0, 4, st));
+            zt::ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), 256, 0, st>>>(in, mask, rows, cols,
+                                                                                              rp, dev_max);
+            ctx->launches += 1;
+        }
         if (use_smem)
-            mls_smem_kernel<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
+            mls_smem_kernel<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp,
+                                                    dev_max, dst);
         else
             mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;
@@ -384,12 +425,13 @@ extern "C" ZIM_API zim_status zim_filter_mls(zim_ctx* ctx, const float* xyz, con
     if (out == xyz) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     float* tmp = nullptr;
-    if (iterations > 1) {
-        zim_status s = zim_scratch_reserve(ctx, zim_mls_scratch_bytes((size_t)rows * cols));
-        if (s) return s;
-        zim_scratch_reset(ctx);
-        tmp = (float*)zim_scratch_take(ctx, (size_t)rows * cols * 12);
-    }
-    return zim_mls_launch(ctx, xyz, mask, rows, cols, window, sigma, order, max_radius, iterations, out, tmp,
+    zim_status s = zim_scratch_reserve(ctx, zim_mls_scratch_bytes((size_t)rows * cols) + 512);
+    if (s) return s;
+    zim_scratch_reset(ctx);
+    if (iterations > 1) tmp = (float*)zim_scratch_take(ctx, (size_t)rows * cols * 12);
+    // a cloud of the calibrated rectified size: its pixels' rays bound the window
+    const zim_ray_model rays = rows == ctx->rect_h && cols == ctx->rect_w ? zim_rays_of(ctx, true, 0, 0)
+                                                                          : zim_ray_model{};
+    return zim_mls_launch(ctx, xyz, mask, rows, cols, window, sigma, order, max_radius, iterations, out, tmp, rays,
                           zim_stream(stream));
 }

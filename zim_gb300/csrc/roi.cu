@@ -432,7 +432,8 @@ extern "C" ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_
     if (r->use_mls) {
         float* xo = (xb[0] != cx) ? xb[0] : xb[1];
         s = zim_mls_launch(ctx, cx, cm, H, W, r->mls_window_size, r->mls_spatial_sigma, r->mls_polynomial_order,
-                           r->mls_max_radius, r->mls_iterations, xo, mls_tmp, st);
+                           r->mls_max_radius, r->mls_iterations, xo, mls_tmp,
+                           zim_rays_of(ctx, r->use_rectified_coords != 0, L.x, L.y), st);
         if (s) return s;
         cx = xo;
     }

@@ -119,7 +119,7 @@ zim_status zim_ror_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
                           uint8_t* mask_out, cudaStream_t st);
 zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
                           int window, float sigma, int order, float max_radius, int iterations,
-                          float* out, float* tmp, cudaStream_t st);
+                          float* out, float* tmp, const zim_ray_model& rays, cudaStream_t st);
 zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
                           int mean_k, double std_mul, float* xyz_out, uint8_t* mask_out,
                           float* mean_dist, const zim_ray_model& rays, cudaStream_t st);
