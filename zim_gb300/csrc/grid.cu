@@ -243,18 +243,24 @@ __global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int le
 __device__ __forceinline__ float sqdist(float dx, float dy, float dz) { return fmaf(dz, dz, fmaf(dy, dy, dx * dx)); }
 
 // Order-independent sum of the k + 1 nearest distances: each root, scaled by
-// 2^(56 - e) with sqrt(largest squared distance) < 2^e, is truncated to an
-// integer and the integers are added exactly, so every search path and every
-// visiting order gives the same bits.  (Roots below 2^(e - 56) count as 0.)
+// 2^(23 - e) with sqrt(largest squared distance) < 2^e, is truncated to an
+// integer below 2^23 and the integers are added exactly (at most 64 of them:
+// below 2^29), so every search path and every visiting order gives the same
+// bits.  The truncation is one FMA rounded toward zero onto 2^23, whose
+// mantissa then holds the integer: no 64-bit conversion (FP64 pipe) per root.
+// Roots below 2^(e - 23), a 2^-22 fraction of the largest, count as 0.
 __device__ __forceinline__ int root_exponent(float d2max) {
     int e;
     frexpf(sqrtf(d2max), &e);
-    return max(e, -60);  // keeps the scale 2^(56 - e) finite
+    return min(max(e, -60), 100);  // keeps 2^(23 - e) and 2^(e - 23) normal
 }
-__device__ __forceinline__ float root_scale(int e) { return ldexpf(1.0f, 56 - e); }
-__device__ __forceinline__ long long root_fixed(float d2, float scale) { return __float2ll_rz(sqrtf(d2) * scale); }
-__device__ __forceinline__ float fixed_mean(long long sum, int e, int k) {
-    return (float)(ldexp((double)sum, e - 56) / (double)k);
+__device__ __forceinline__ float root_scale(int e) { return __uint_as_float((unsigned)(150 - e) << 23); }
+__device__ __forceinline__ unsigned root_fixed(float d2, float scale) {
+    return __float_as_uint(__fmaf_rz(sqrtf(d2), scale, 8388608.f)) - 0x4B000000u;
+}
+// (sum / k) 2^(e - 23), one float division
+__device__ __forceinline__ float fixed_mean(unsigned sum, int e, int k) {
+    return __fdiv_rn(__uint2float_rn(sum), (float)k) * __uint_as_float((unsigned)(104 + e) << 23);
 }
 
 __device__ __forceinline__ void cell_of(float x, float y, float z, float ic, int& cx, int& cy, int& cz) {
@@ -699,11 +705,11 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
             const float vmax = __uint_as_float(__reduce_max_sync(full, lm) - 1u);
             const int e = root_exponent(vmax);
             const float sc = root_scale(e);
-            long long part = 0;
+            unsigned part = 0;
 #pragma unroll
             for (int r = 0; r < SV_CAP / 32; r++)
                 if (key[r]) part += root_fixed(__uint_as_float(key[r] - 1u), sc);
-            for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(full, part, off);
+            part = __reduce_add_sync(full, part);
             if (lane == q) {
                 md_out[i] = fixed_mean(part, e, k);
                 done = true;
@@ -729,8 +735,12 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
 // nearest points inside its window lie within
 //     |q| f (WR + 1) / (|a| (|a| + WR + 1)) - dev(q) - max dev
 // has the same k + 1 nearest points in the whole cloud: its mean distance is
-// exact from the window alone.  Queries the bound does not certify are left
-// to the grid search (md = -2).
+// exact from the window alone.  Inside the window the same bound holds with the
+// largest dev of the block's staged points in place of the cloud's (points
+// averaged across a depth edge lie far off their rays, but only near it), so
+// the spiral stops at the radius that local bound gives and the cloud-wide
+// maximum only has to clear the window's edge.  Queries the bounds do not
+// certify are left to the grid search (md = -2).
 
 using zt::RayParams;
 using zt::ray_dir;
@@ -798,16 +808,27 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1 + SEL_SLACK) x TILE_T
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+    __shared__ unsigned warp_dev[TILE_T / 32];
+    unsigned tdev = 0u;  // largest dev of this thread's staged points (float bits, >= 0)
     for (int t = tid; t < WW * WH; t += TILE_T) {
         const int wx = x0 - WR + t % WW, wy = y0 - WR + t / WW;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
             const size_t j = (size_t)wy * cols + wx;
-            if (mask[j]) v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
+            if (mask[j]) {
+                v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
+                float ax, ay, az;
+                ray_dir(rp, wx, wy, ax, ay, az);
+                tdev = max(tdev, __float_as_uint(ray_dev(v.x, v.y, v.z, ax, ay, az)));
+            }
         }
         W[t] = v;
     }
+    tdev = __reduce_max_sync(0xffffffffu, tdev);
+    if ((tid & 31) == 0) warp_dev[tid >> 5] = tdev;
     __syncthreads();
+#pragma unroll
+    for (int j = 0; j < TILE_T / 32; j++) tdev = max(tdev, warp_dev[j]);
     const int tx = tid % TILE_X, ty = tid / TILE_X;
     const int x = x0 + tx, y = y0 + ty;
     if (x >= cols || y >= rows) return;  // no block-wide synchronisation below
@@ -818,24 +839,23 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     }
     const int wc = (ty + WR) * WW + tx + WR;
     const float4 q = W[wc];
-    // window bound: the query and its first k valid window pixels
-    float tau0 = INFINITY;
-    {
-        int found = 0;
-        float m = 0.f;
-        for (int o = 0; o < WN && found < k; o++) {
-            const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
-            if (p.w == 0.f) continue;
-            m = fmaxf(m, sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
-            found++;
-        }
-        if (found == k) tau0 = m;
+    const int K1 = k + 1;
+    // the query and its first k valid window pixels in spiral order fill the
+    // list; their largest distance is the first bound
+    WinSel sel{Ls + tid, 1, K1, K1 + SEL_SLACK, 0.f};
+    sel.at(0) = 0.f;
+    int o = 0;
+    for (; o < WN && sel.cnt < K1; o++) {
+        const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
+        if (p.w == 0.f) continue;
+        const float d2 = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
+        sel.at(sel.cnt++) = d2;
+        sel.thr = fmaxf(sel.thr, d2);
     }
-    if (!(tau0 < INFINITY)) {
+    if (sel.cnt < K1) {
         md_out[i] = -2.f;
         return;
     }
-    const int K1 = k + 1;
     // bound(r) = C r / (an + r): no point of a pixel at distance >= r from the
     // query's lies nearer than bound(r) - dev (slack: float rounding, 1e-5 |q|)
     float ax, ay, az;
@@ -843,21 +863,21 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
     const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
     const float C = qn * rp.f / an;
-    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits) + 1e-5f * qn;
-    // squared pixel distance beyond which every point is farther than sqrt(thr):
-    // C r / (an + r) > sqrt(thr) + dev  <=>  r > (sqrt(thr) + dev) an / (C - sqrt(thr) - dev)
+    const float dev_q = ray_dev(q.x, q.y, q.z, ax, ay, az) + 1e-5f * qn;
+    const float dev = dev_q + __uint_as_float(tdev);                    // window pixels
+    const float dev_out = dev_q + __uint_as_float(s->ray_dev_bits);     // pixels outside it
+    // squared pixel distance beyond which every window point is farther than
+    // sqrt(thr): C r / (an + r) > sqrt(thr) + dev  <=>  r > (sqrt(thr) + dev) an / (C - sqrt(thr) - dev)
     auto stop_r2 = [&](float thr) {
         const float sd = sqrtf(thr) + dev;
         if (!(C > sd)) return INFINITY;
         const float r = sd * an / (C - sd);
         return r * r;
     };
-    WinSel sel{Ls + tid, 0, K1, K1 + SEL_SLACK, tau0};
-    sel.push(0.f);  // the query itself
     float last = sel.thr, rs2 = stop_r2(last), rbreak = (float)(WR + 1);
     // the spiral runs by increasing length: once past the stop distance, the
     // rest of the window (and everything outside it) is provably farther
-    for (int o = 0; o < WN; o++) {
+    for (; o < WN; o++) {
         const int dx = c_spiral7[o][0], dy = c_spiral7[o][1];
         const float r2o = (float)(dx * dx + dy * dy);
         if (r2o > rs2) {
@@ -872,19 +892,172 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
             rs2 = stop_r2(last);
         }
     }
-    const float kth = sel.select();
-    // certificate: every pixel not visited is at least rbreak away (the
-    // unvisited window entries) or WR + 1 away (outside the window)
-    const bool ok = C * rbreak / (an + rbreak) - dev > sqrtf(kth);
+    // a list of exactly K1 entries is the K1 smallest, its bound their largest
+    const float kth = sel.cnt == K1 ? sel.thr : sel.select();
+    // certificate: every window pixel not visited is at least rbreak away, and
+    // every pixel outside the window at least WR + 1
+    const float rk = sqrtf(kth), ro = (float)(WR + 1);
+    const bool ok = C * rbreak / (an + rbreak) - dev > rk && C * ro / (an + ro) - dev_out > rk;
     if (!ok) {
         md_out[i] = -2.f;
         return;
     }
     const int e = root_exponent(kth);
     const float sc = root_scale(e);
-    long long sum = 0;
+    unsigned sum = 0;
     for (int j = 0; j < K1; j++) sum += root_fixed(sel.L[j * TILE_T], sc);
     md_out[i] = fixed_mean(sum, e, k);
+}
+
+// Second window pass for the deferred queries: one warp per query walks square
+// pixel rings r = 1, 2, ... (lanes over a ring's 8 r pixels) straight from the
+// cloud, keeping the squared distances within the current bound in the warp's
+// list, until the ray bound puts every farther pixel beyond the bound
+// (certified: md written, the query leaves the far search) or FAR_WR rings
+// pass (left to the far search).  The bound starts at the query's window
+// bound tau0 and tightens to the (k + 1)-th smallest whenever the list fills.
+constexpr int FAR_WR = 24;
+constexpr int FW_CAP = 256;  // list entries per warp (8 per lane)
+
+// Smallest list value v with at least K entries <= v (entries: lane j holds
+// keys[r] for r < 8, 0xffffffff = empty; keys are non-negative float bits).
+__device__ __forceinline__ unsigned warp_kth_key(const unsigned (&keys)[FW_CAP / 32], int K) {
+    unsigned lo = 0u, hi = 0x7f800000u;  // +inf bits
+    while (lo < hi) {
+        const unsigned mid = lo + ((hi - lo) >> 1);
+        int c = 0;
+#pragma unroll
+        for (int r = 0; r < FW_CAP / 32; r++) c += keys[r] <= mid;
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (c >= K) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(P2_WARPS * 32) sor_far_window_kernel(const float* __restrict__ xyz,
+                                                                       const uint8_t* __restrict__ mask, int rows,
+                                                                       int cols, int k, RayParams rp,
+                                                                       GridStats* s, unsigned* __restrict__ deferred,
+                                                                       float* __restrict__ md_out) {
+    __shared__ float lst[P2_WARPS][FW_CAP];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned nd = s->n_deferred;
+    const int K1 = k + 1;
+    const float devmax = __uint_as_float(s->ray_dev_bits);
+    for (unsigned item = blockIdx.x * P2_WARPS + w; item < nd; item += gridDim.x * P2_WARPS) {
+        const unsigned i = deferred[item];
+        const int x = (int)(i % (unsigned)cols), y = (int)(i / (unsigned)cols);
+        const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
+        float ax, ay, az;
+        ray_dir(rp, x, y, ax, ay, az);
+        const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+        const float qn = sqrtf(fmaf(qx, qx, fmaf(qy, qy, qz * qz)));
+        const float C = qn * rp.f / an;
+        const float dev = ray_dev(qx, qy, qz, ax, ay, az) + devmax + 1e-5f * qn;
+        float thr = INFINITY;
+        if (lane == 0) lst[w][0] = 0.f;  // the query itself
+        int n = 1;                        // list entries (warp-uniform)
+        // keep only the entries <= the K1-th smallest (ties kept); the K1-th
+        // smallest of real points bounds the (k + 1)-th nearest distance
+        auto tighten = [&]() {
+            __syncwarp();
+            unsigned keys[FW_CAP / 32];
+#pragma unroll
+            for (int q = 0; q < FW_CAP / 32; q++) {
+                const int e = lane + 32 * q;
+                keys[q] = e < n ? __float_as_uint(lst[w][e]) : 0xffffffffu;
+            }
+            const unsigned kk = warp_kth_key(keys, K1);
+            thr = __uint_as_float(kk);
+            __syncwarp();
+            int m = 0;
+#pragma unroll
+            for (int q = 0; q < FW_CAP / 32; q++) {
+                const bool kp = keys[q] <= kk;
+                const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                if (kp) lst[w][m + __popc(bb & ((1u << lane) - 1u))] = __uint_as_float(keys[q]);
+                m += __popc(bb);
+            }
+            n = m;
+            __syncwarp();
+        };
+        bool certified = false, overflow = false;
+        for (int r = 1; r <= FAR_WR && !certified && !overflow; r++) {
+            // every pixel of ring r and beyond is at least r pixels away
+            if (thr < INFINITY && C * (float)r / (an + (float)r) > sqrtf(thr) + dev) {
+                certified = true;
+                break;
+            }
+            for (int t0 = 0; t0 < 8 * r; t0 += 32) {
+                if (n > FW_CAP - 32) {
+                    tighten();
+                    if (n > FW_CAP - 32) {  // too many ties to hold
+                        overflow = true;
+                        break;
+                    }
+                }
+                const int t = t0 + lane;
+                float d2 = INFINITY;
+                if (t < 8 * r) {
+                    int dx, dy;
+                    const int side = t / (2 * r), o = t % (2 * r);
+                    if (side == 0) { dx = -r + o; dy = -r; }
+                    else if (side == 1) { dx = r; dy = -r + o; }
+                    else if (side == 2) { dx = r - o; dy = r; }
+                    else { dx = -r; dy = r - o; }
+                    const int px = x + dx, py = y + dy;
+                    if (px >= 0 && px < cols && py >= 0 && py < rows) {
+                        const size_t j = (size_t)py * cols + px;
+                        if (mask[j]) d2 = sqdist(xyz[3 * j] - qx, xyz[3 * j + 1] - qy, xyz[3 * j + 2] - qz);
+                    }
+                }
+                const bool keep = d2 < INFINITY && d2 <= thr;
+                const unsigned b = __ballot_sync(0xffffffffu, keep);
+                if (keep) lst[w][n + __popc(b & ((1u << lane) - 1u))] = d2;
+                n += __popc(b);
+                if (thr == INFINITY && n >= 2 * K1) tighten();
+            }
+        }
+        if (!certified && !overflow && thr < INFINITY) {
+            const float r = (float)(FAR_WR + 1);  // everything the rings did not reach
+            certified = C * r / (an + r) > sqrtf(thr) + dev;
+        }
+        if (!certified) {
+            // left to the far search, with the bound found so far: md = -1 - bound
+            if (lane == 0 && thr < INFINITY) md_out[i] = -1.f - thr;
+            __syncwarp();
+            continue;
+        }
+        // the K1 smallest of the list: values below the K1-th plus its ties
+        __syncwarp();
+        unsigned keys[FW_CAP / 32];
+#pragma unroll
+        for (int q = 0; q < FW_CAP / 32; q++) {
+            const int e = lane + 32 * q;
+            keys[q] = e < n ? __float_as_uint(lst[w][e]) : 0xffffffffu;
+        }
+        const unsigned kk = warp_kth_key(keys, K1);
+        const float kth = __uint_as_float(kk);
+        const int e = root_exponent(kth);
+        const float sc = root_scale(e);
+        unsigned part = 0;
+        int below = 0;
+#pragma unroll
+        for (int q = 0; q < FW_CAP / 32; q++)
+            if (keys[q] < kk) {
+                part += root_fixed(__uint_as_float(keys[q]), sc);
+                below++;
+            }
+        part = __reduce_add_sync(0xffffffffu, part);
+        below = __reduce_add_sync(0xffffffffu, below);
+        part += (unsigned)(K1 - below) * root_fixed(kth, sc);
+        if (lane == 0) {
+            md_out[i] = fixed_mean(part, e, k);
+            deferred[item] = 0xffffffffu;  // settled: the far search skips it
+        }
+        __syncwarp();
+    }
 }
 
 // Occupied cells of the coarse (dense) level: (cell index, offset, count).
@@ -933,6 +1106,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
     const int K1 = k + 1;
     float* Lw = far_smem + (size_t)w * K1 * 33;  // Lw[j * 32 + lane]: lane's j-th smallest
     float* Mw = Lw + (size_t)K1 * 32;            // K1 merged
+    float* lw = far_smem + (size_t)P2_WARPS * K1 * 33 + (size_t)w * FW_CAP;  // ring phase list
     const unsigned nd = s->n_deferred, nocc = s->n_occ;
     for (;;) {
         unsigned item = 0;
@@ -940,6 +1114,7 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nd) break;
         const unsigned i = deferred[item];
+        if (i == 0xffffffffu) continue;  // settled by the second window pass
         const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
         // the cell mapping (x - org) * inv_cell and the cube corners org + i * cell
         // round by a few ulps of the largest coordinate
@@ -1001,25 +1176,54 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         int last_j = -1;
         bool done = false;
         // Rings of dense cells around the query's cell: ring r holds every cell
-        // at Chebyshev distance r, all at least (r - 1) cells away; after each
-        // ring the K1 smallest so far bound the rest.  Far-isolated points
-        // (more than RING_MAX rings) take the best-first search below.
+        // at Chebyshev distance r, all at least (r - 1) cells away.  The warp
+        // keeps the squared distances within the bound (the second window
+        // pass's, else the (k + 1)-th smallest held) in its list and stops once
+        // the next ring lies beyond the bound.  Far-isolated points (more than
+        // RING_MAX rings) take the best-first search below.
+        float thr = md_out[i] < -1.f ? -1.f - md_out[i] : INFINITY;
+        float fmd = 0.f;
+        bool ring_done = false;
         {
+            int n = 0;
+            bool overflow = false;
+            auto tighten = [&]() {
+                __syncwarp();
+                unsigned keys[FW_CAP / 32];
+#pragma unroll
+                for (int q = 0; q < FW_CAP / 32; q++) {
+                    const int e = lane + 32 * q;
+                    keys[q] = e < n ? __float_as_uint(lw[e]) : 0xffffffffu;
+                }
+                const unsigned kk = warp_kth_key(keys, K1);
+                thr = fminf(thr, __uint_as_float(kk));
+                __syncwarp();
+                int m = 0;
+#pragma unroll
+                for (int q = 0; q < FW_CAP / 32; q++) {
+                    const bool kp = keys[q] <= __float_as_uint(thr);
+                    const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                    if (kp) lw[m + __popc(bb & ((1u << lane) - 1u))] = __uint_as_float(keys[q]);
+                    m += __popc(bb);
+                }
+                n = m;
+                __syncwarp();
+            };
             const float c1 = s->cell[1], ic1 = s->inv_cell[1];
             const int nx = s->dims[0], ny = s->dims[1], nz = s->dims[2];
             const int qcx = min(max(__float2int_rd((qx - s->org[0]) * ic1), 0), nx - 1);
             const int qcy = min(max(__float2int_rd((qy - s->org[1]) * ic1), 0), ny - 1);
             const int qcz = min(max(__float2int_rd((qz - s->org[2]) * ic1), 0), nz - 1);
-            for (int r = 0; r <= RING_MAX; r++) {
-                if (r >= 1 && kth < INFINITY) {
+            for (int r = 0; r <= RING_MAX && !overflow; r++) {
+                if (r >= 1 && thr < INFINITY) {
                     const float gap = (float)(r - 1) * c1 - margin;
-                    if (gap > 0.f && gap * gap > kth) {
-                        done = true;
+                    if (gap > 0.f && gap * gap > thr) {
+                        done = n >= K1;
                         break;
                     }
                 }
                 const int side = 2 * r + 1, ncell = side * side * side;
-                for (int t0 = 0; t0 < ncell; t0 += 32) {
+                for (int t0 = 0; t0 < ncell && !overflow; t0 += 32) {
                     const int t = t0 + lane;
                     bool take = false;
                     uint2 e = make_uint2(0u, 0u);
@@ -1030,17 +1234,63 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                         if (cheb == r && ix >= 0 && ix < nx && iy >= 0 && iy < ny && iz >= 0 && iz < nz) {
                             const unsigned idx = ((unsigned)iz * (unsigned)ny + (unsigned)iy) * (unsigned)nx + (unsigned)ix;
                             e = __ldg(tab1 + idx);
-                            take = e.y > 0u && cell_box_d2(idx, s, qx, qy, qz, margin) <= kth;
+                            take = e.y > 0u && cell_box_d2(idx, s, qx, qy, qz, margin) <= thr;
                         }
                     }
                     unsigned m = __ballot_sync(0xffffffffu, take);
-                    while (m) {
+                    while (m && !overflow) {
                         const int b = __ffs(m) - 1;
                         m &= m - 1;
-                        scan_range(__shfl_sync(0xffffffffu, e.x, b), __shfl_sync(0xffffffffu, e.y, b));
+                        const unsigned first = __shfl_sync(0xffffffffu, e.x, b);
+                        const unsigned end = first + __shfl_sync(0xffffffffu, e.y, b);
+                        for (unsigned u0 = first; u0 < end; u0 += 32) {
+                            if (n > FW_CAP - 32) {
+                                tighten();
+                                if (n > FW_CAP - 32) {  // too many ties to hold
+                                    overflow = true;
+                                    break;
+                                }
+                            }
+                            const unsigned u = u0 + lane;
+                            float d2 = INFINITY;
+                            if (u < end) {
+                                const float4 p = __ldg(pts + u);
+                                d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
+                            }
+                            const bool keep = d2 < INFINITY && d2 <= thr;
+                            const unsigned bb = __ballot_sync(0xffffffffu, keep);
+                            if (keep) lw[n + __popc(bb & ((1u << lane) - 1u))] = d2;
+                            n += __popc(bb);
+                            if (thr == INFINITY && n >= 2 * K1) tighten();
+                        }
                     }
                 }
-                kth = merge();
+            }
+            if (done) {
+                __syncwarp();
+                unsigned keys[FW_CAP / 32];
+#pragma unroll
+                for (int q = 0; q < FW_CAP / 32; q++) {
+                    const int e2 = lane + 32 * q;
+                    keys[q] = e2 < n ? __float_as_uint(lw[e2]) : 0xffffffffu;
+                }
+                const unsigned kk = warp_kth_key(keys, K1);
+                const float kv = __uint_as_float(kk);
+                const int ee = root_exponent(kv);
+                const float sc = root_scale(ee);
+                unsigned part = 0;
+                int below = 0;
+#pragma unroll
+                for (int q = 0; q < FW_CAP / 32; q++)
+                    if (keys[q] < kk) {
+                        part += root_fixed(__uint_as_float(keys[q]), sc);
+                        below++;
+                    }
+                part = __reduce_add_sync(0xffffffffu, part);
+                below = __reduce_add_sync(0xffffffffu, below);
+                part += (unsigned)(K1 - below) * root_fixed(kv, sc);
+                fmd = fixed_mean(part, ee, k);
+                ring_done = true;
             }
         }
         if (!done) {
@@ -1092,13 +1342,13 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
             done = true;
         }
         if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
-        float md = 0.f;
-        if (kth < INFINITY) {
+        float md = fmd;
+        if (!ring_done && kth < INFINITY) {
             const int e = root_exponent(kth);
             const float sc = root_scale(e);
-            long long part = 0;
+            unsigned part = 0;
             for (int j = lane; j < K1; j += 32) part += root_fixed(Mw[j], sc);
-            for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+            part = __reduce_add_sync(0xffffffffu, part);
             md = fixed_mean(part, e, k);
         }
         if (lane == 0) md_out[i] = md;
@@ -1410,8 +1660,15 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
                                                     window);
+    if (window) {
+        const RayParams rp = zt::ray_params(rays);
+        sor_far_window_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
+            xyz, mask, rows, cols, mean_k, rp, G.stats, G.deferred, md);
+        ctx->launches += 1;
+    }
     // enough warps in flight to cover the latency of the long point scans
-    const size_t fsm = (size_t)P2_WARPS * (mean_k + 1) * 33 * sizeof(float);
+    const size_t fsm = (size_t)P2_WARPS * ((mean_k + 1) * 33 + FW_CAP) * sizeof(float);
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
     sor_knn_far_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, fsm, st>>>(
         xyz, mean_k, G.stats, G.occ, G.tab[1], G.pts[1], G.deferred, md, ctx->d_error);
     ctx->launches += 3;
