@@ -143,6 +143,49 @@ def test_sor_window_path_equals_grid_path(ctx, oracle_lib, k):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("k", [30, 63])
+def test_sor_isolated_and_duplicate_points(ctx, oracle_lib, k):
+    """Far-isolated points (their k + 1 nearest lie hundreds of mm away: the
+    CTA-per-query coarse search) and a pile of 150 identical points (ties at
+    distance 0 beyond any list's room) against the oracle, on both search
+    paths."""
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    H, W = mask.shape
+    x = xyz.cpu().numpy().copy()
+    m = mask.cpu().numpy().copy()
+    rng = np.random.default_rng(7)
+    idx = np.flatnonzero(m.reshape(-1))
+    pick = rng.choice(idx, 190, replace=False)
+    flat = x.reshape(-1, 3)
+    # 40 outliers pushed 150-600 mm along random directions
+    d = rng.normal(size=(40, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    flat[pick[:40]] += (d * rng.uniform(150, 600, (40, 1))).astype(np.float32)
+    # 150 copies of one surface point
+    flat[pick[40:]] = flat[pick[40]]
+    xt = torch.from_numpy(x).cuda()
+    mt = torch.from_numpy(m).cuda()
+    mo, md = api.filter_sor(ctx, xt, mt, k, 1.0, want_mean_dist=True)
+    om, omd, thr, near = oracle_lib.sor(x, m, k, 1.0, eps=EPS)
+    gmd = md.cpu().numpy()
+    v = m > 0
+    rel = np.abs(gmd[v] - omd[v]) / np.maximum(omd[v], 1e-6)
+    assert rel.max() <= 1e-5, float(rel.max())
+    assert (gmd.reshape(-1)[pick[40:]] == 0).all()
+    assert ((mo.cpu().numpy() != om) & (near == 0)).sum() == 0
+    assert ctx.check_device() == 0
+    # the grid-only path (no pixel rays) gives the same bits
+    xp = torch.zeros((H, W + 1, 3), dtype=torch.float32, device="cuda")
+    mp = torch.zeros((H, W + 1), dtype=torch.uint8, device="cuda")
+    xp[:, :W] = xt
+    mp[:, :W] = mt
+    m2, md2 = api.filter_sor(ctx, xp.contiguous(), mp.contiguous(), k, 1.0, want_mean_dist=True)
+    assert torch.equal(md, md2[:, :W].contiguous()) and torch.equal(mo, m2[:, :W].contiguous())
+    assert ctx.check_device() == 0
+
+
+@pytest.mark.gpu
 def test_mls_ray_disk_equals_full_window(ctx, oracle_lib):
     """The ray bound only skips window pixels beyond the cut-off: with pixel
     rays (the calibrated size) and without (the cloud padded by one invalid

@@ -18,10 +18,11 @@
 //            memory; every thread scans the same candidate list and is exact
 //            once it holds k + 1 candidates within its distance to the box
 //            boundary;
-//   phase 2: one warp per remaining point (isolated outliers) searches the
-//            coarse level best-first: occupied cells in order of the distance
-//            to their cube, until the next cube is farther than the current
-//            (k + 1)-th distance.
+//   phase 2: one warp per remaining point searches rings of coarse cells
+//            around its own until the next ring lies beyond the (k + 1)-th
+//            distance held;
+//   phase 3: the few points still open (far-isolated outliers) take one CTA
+//            each over the coarse level's occupied cells.
 // A visited point's finest cell is re-derived from its coordinates, so hash
 // collisions never count a point twice.  Both filters are deterministic: the
 // SOR statistics are summed in a fixed order, and the Gaussian's grid path sums
@@ -45,7 +46,10 @@ constexpr int SCAN_B = 1024;
 constexpr int MAX_LEVELS = 2;    // finest + one coarse level
 constexpr int FINE_RINGS = 2;    // phase-1 fallback rings on the finest level
 constexpr int P2_WARPS = 4;      // phase-2 warps per CTA
-constexpr int RING_MAX = 6;      // phase-2 rings of dense cells before the best-first search
+constexpr int RING_MAX = 6;      // phase-2 rings of dense cells before the hard list
+// md marker of a deferred query whose bound on the (k + 1)-th squared distance
+// is handed on in the bound array (md = -1: no bound)
+constexpr float MD_BOUND = -3.f;
 constexpr int TILE_X = 16, TILE_Y = 8, TILE_T = TILE_X * TILE_Y;
 constexpr int TILE_DILATE = 2;        // cells added around a tile's box
 constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
@@ -68,7 +72,7 @@ struct GridStats {
     float thr_f;
     int keep_all;
     unsigned ray_dev_bits;         // largest distance of a point from its pixel ray (float bits)
-    unsigned n_deferred, n_occ, p2_next;
+    unsigned n_deferred, n_occ, p2_next, n_hard;
 };
 
 __device__ __forceinline__ int fbits(float f) {
@@ -104,7 +108,7 @@ struct Max { __device__ int operator()(int a, int b) const { return a > b ? a : 
 __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
-    s->n_deferred = s->n_occ = s->p2_next = 0;
+    s->n_deferred = s->n_occ = s->p2_next = s->n_hard = 0;
     s->ray_dev_bits = 0u;
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
@@ -939,7 +943,8 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_far_window_kernel(const flo
                                                                        const uint8_t* __restrict__ mask, int rows,
                                                                        int cols, int k, RayParams rp,
                                                                        GridStats* s, unsigned* __restrict__ deferred,
-                                                                       float* __restrict__ md_out) {
+                                                                       float* __restrict__ md_out,
+                                                                       float* __restrict__ bound) {
     __shared__ float lst[P2_WARPS][FW_CAP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned nd = s->n_deferred;
@@ -1024,8 +1029,11 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_far_window_kernel(const flo
             certified = C * r / (an + r) > sqrtf(thr) + dev;
         }
         if (!certified) {
-            // left to the far search, with the bound found so far: md = -1 - bound
-            if (lane == 0 && thr < INFINITY) md_out[i] = -1.f - thr;
+            // left to the far search, with the bound found so far
+            if (lane == 0 && thr < INFINITY) {
+                md_out[i] = MD_BOUND;
+                bound[i] = thr;
+            }
             __syncwarp();
             continue;
         }
@@ -1086,28 +1094,27 @@ __device__ __forceinline__ float cell_box_d2(unsigned idx, const GridStats* __re
     return ex * ex + ey * ey + ez * ez;
 }
 
-// Phase 2: one warp per deferred point over the coarse level's occupied cells.
-// Best-first (nearest cube first, lanes splitting each cell's points, lane
-// lists merged after each cell) until k + 1 points are held; the (k + 1)-th
-// distance then bounds the search, so one pass over the cells scans every
-// unvisited cell whose cube lies within it, and one merge ends the query.
-// Work is handed out through an atomic counter.
+// Phase 2: one warp per deferred point on the coarse (dense) level, ring by
+// ring of cells around the query's cell: ring r holds every cell at Chebyshev
+// distance r, all at least (r - 1) cells away.  The warp keeps the squared
+// distances within the bound (the second window pass's, else the (k + 1)-th
+// smallest held) in its list and stops once the next ring lies beyond the
+// bound.  Queries still open after RING_MAX rings, or whose ties overflow the
+// list, go to the hard list (md = MD_BOUND with a valid bound in the bound
+// array, or -1).  Work is handed out through an atomic counter.
 __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float* __restrict__ xyz, int k,
                                                                      GridStats* s,
-                                                                     const uint4* __restrict__ occ,
                                                                      const uint2* __restrict__ tab1,
                                                                      const float4* __restrict__ pts,
                                                                      const unsigned* __restrict__ deferred,
                                                                      float* __restrict__ md_out,
-                                                                     uint32_t* __restrict__ err) {
-    // per warp: K1 sorted entries per lane, then the merged K1 smallest
-    extern __shared__ float far_smem[];
+                                                                     float* __restrict__ bound,
+                                                                     unsigned* __restrict__ hard) {
+    __shared__ float lst[P2_WARPS][FW_CAP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int K1 = k + 1;
-    float* Lw = far_smem + (size_t)w * K1 * 33;  // Lw[j * 32 + lane]: lane's j-th smallest
-    float* Mw = Lw + (size_t)K1 * 32;            // K1 merged
-    float* lw = far_smem + (size_t)P2_WARPS * K1 * 33 + (size_t)w * FW_CAP;  // ring phase list
-    const unsigned nd = s->n_deferred, nocc = s->n_occ;
+    float* lw = lst[w];
+    const unsigned nd = s->n_deferred;
     for (;;) {
         unsigned item = 0;
         if (lane == 0) item = atomicAdd(&s->p2_next, 1u);
@@ -1119,69 +1126,8 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         // the cell mapping (x - org) * inv_cell and the cube corners org + i * cell
         // round by a few ulps of the largest coordinate
         const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
-        int cnt = 0;
-        // the lanes split a cell's points; each keeps its K1 smallest, sorted
-        auto scan_range = [&](unsigned first, unsigned count) {
-            const unsigned end = first + count;
-            // four loads in flight per lane, then the insertions
-            for (unsigned u0 = first + lane; u0 < end; u0 += 128) {
-                float4 p[4];
-#pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    const unsigned u = u0 + 32u * r;
-                    p[r] = u < end ? __ldg(pts + u) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    if (u0 + 32u * r >= end) break;
-                    const float d2 = sqdist(p[r].x - qx, p[r].y - qy, p[r].z - qz);
-                    int jj;
-                    if (cnt < K1) jj = cnt++;
-                    else if (d2 < Lw[(K1 - 1) * 32 + lane]) jj = K1 - 1;
-                    else continue;
-                    while (jj > 0 && Lw[(jj - 1) * 32 + lane] > d2) {
-                        Lw[jj * 32 + lane] = Lw[(jj - 1) * 32 + lane];
-                        jj--;
-                    }
-                    Lw[jj * 32 + lane] = d2;
-                }
-            }
-            __syncwarp();
-        };
-        auto scan_cell = [&](unsigned j) {
-            const uint4 o = occ[j];
-            scan_range(o.y, o.z);
-        };
-        // the K1 smallest over all lanes, in order, into M; returns the K1-th
-        auto merge = [&]() {
-            int head = 0;
-            float kk = INFINITY;
-            for (int round = 0; round < K1; round++) {
-                float v = head < cnt ? Lw[head * 32 + lane] : INFINITY;
-                int who = lane;
-                for (int off = 16; off; off >>= 1) {
-                    float ov = __shfl_xor_sync(0xffffffffu, v, off);
-                    int ow = __shfl_xor_sync(0xffffffffu, who, off);
-                    if (ov < v || (ov == v && ow < who)) { v = ov; who = ow; }
-                }
-                if (lane == who) head++;
-                if (lane == 0) Mw[round] = v;
-                if (round == K1 - 1) kk = v;
-            }
-            __syncwarp();
-            return kk;
-        };
-        float kth = INFINITY;
-        float last_d = -1.f;
-        int last_j = -1;
         bool done = false;
-        // Rings of dense cells around the query's cell: ring r holds every cell
-        // at Chebyshev distance r, all at least (r - 1) cells away.  The warp
-        // keeps the squared distances within the bound (the second window
-        // pass's, else the (k + 1)-th smallest held) in its list and stops once
-        // the next ring lies beyond the bound.  Far-isolated points (more than
-        // RING_MAX rings) take the best-first search below.
-        float thr = md_out[i] < -1.f ? -1.f - md_out[i] : INFINITY;
+        float thr = md_out[i] == MD_BOUND ? bound[i] : INFINITY;
         float fmd = 0.f;
         bool ring_done = false;
         {
@@ -1243,24 +1189,32 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                         m &= m - 1;
                         const unsigned first = __shfl_sync(0xffffffffu, e.x, b);
                         const unsigned end = first + __shfl_sync(0xffffffffu, e.y, b);
-                        for (unsigned u0 = first; u0 < end; u0 += 32) {
-                            if (n > FW_CAP - 32) {
+                        // 128 points a step: four loads in flight per lane
+                        for (unsigned u0 = first; u0 < end; u0 += 128) {
+                            if (n > FW_CAP - 128) {
                                 tighten();
-                                if (n > FW_CAP - 32) {  // too many ties to hold
+                                if (n > FW_CAP - 128) {  // too many ties to hold
                                     overflow = true;
                                     break;
                                 }
                             }
-                            const unsigned u = u0 + lane;
-                            float d2 = INFINITY;
-                            if (u < end) {
-                                const float4 p = __ldg(pts + u);
-                                d2 = sqdist(p.x - qx, p.y - qy, p.z - qz);
+                            float d2[4];
+#pragma unroll
+                            for (int r = 0; r < 4; r++) {
+                                const unsigned u = u0 + 32u * r + lane;
+                                d2[r] = INFINITY;
+                                if (u < end) {
+                                    const float4 p = __ldg(pts + u);
+                                    d2[r] = sqdist(p.x - qx, p.y - qy, p.z - qz);
+                                }
                             }
-                            const bool keep = d2 < INFINITY && d2 <= thr;
-                            const unsigned bb = __ballot_sync(0xffffffffu, keep);
-                            if (keep) lw[n + __popc(bb & ((1u << lane) - 1u))] = d2;
-                            n += __popc(bb);
+#pragma unroll
+                            for (int r = 0; r < 4; r++) {
+                                const bool keep = d2[r] < INFINITY && d2[r] <= thr;
+                                const unsigned bb = __ballot_sync(0xffffffffu, keep);
+                                if (keep) lw[n + __popc(bb & ((1u << lane) - 1u))] = d2[r];
+                                n += __popc(bb);
+                            }
                             if (thr == INFINITY && n >= 2 * K1) tighten();
                         }
                     }
@@ -1293,66 +1247,233 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
                 ring_done = true;
             }
         }
-        if (!done) {
-            // restart from nothing: best-first over the occupied cells
-            cnt = 0;
-            kth = INFINITY;
-            __syncwarp();
-        }
-        // best-first until k + 1 points are held
-        for (unsigned iter = 0; !done && iter <= nocc; iter++) {
-            // nearest cell after (last_d, last_j) in (distance, index) order
-            float bd = INFINITY;
-            int bj = INT_MAX;
-            for (unsigned j = lane; j < nocc; j += 32) {
-                float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
-                bool after = d > last_d || (d == last_d && (int)j > last_j);
-                if (after && (d < bd || (d == bd && (int)j < bj))) { bd = d; bj = (int)j; }
+        if (lane == 0) {
+            if (ring_done) {
+                md_out[i] = fmd;
+            } else {
+                // a finite bound is valid: the second pass's, or a (k + 1)-th smallest held
+                hard[atomicAdd(&s->n_hard, 1u)] = i;
+                md_out[i] = thr < INFINITY ? MD_BOUND : -1.f;
+                bound[i] = thr;
             }
-            for (int off = 16; off; off >>= 1) {
-                float od = __shfl_xor_sync(0xffffffffu, bd, off);
-                int oj = __shfl_xor_sync(0xffffffffu, bj, off);
-                if (od < bd || (od == bd && oj < bj)) { bd = od; bj = oj; }
-            }
-            if (bj == INT_MAX) break;
-            scan_cell((unsigned)bj);
-            kth = merge();
-            last_d = bd;
-            last_j = bj;
-            if (kth < INFINITY) break;
         }
-        if (!done && kth < INFINITY) {
-            // every cell not yet visited whose cube lies within the current
-            // (k + 1)-th distance, in index order, then one merge
-            for (unsigned j0 = 0; j0 < nocc; j0 += 32) {
-                const unsigned j = j0 + lane;
-                bool take = false;
-                if (j < nocc) {
-                    const float d = cell_box_d2(__ldg(&occ[j].x), s, qx, qy, qz, margin);
-                    take = d <= kth && (d > last_d || (d == last_d && (int)j > last_j));
-                }
-                unsigned m = __ballot_sync(0xffffffffu, take);
-                while (m) {
-                    const int b = __ffs(m) - 1;
-                    m &= m - 1;
-                    scan_cell(j0 + (unsigned)b);
-                }
-            }
-            kth = merge();
-            done = true;
-        }
-        if (!done && lane == 0) atomicOr(err, 0x10u);  // fewer than k+1 points reachable
-        float md = fmd;
-        if (!ring_done && kth < INFINITY) {
-            const int e = root_exponent(kth);
-            const float sc = root_scale(e);
-            unsigned part = 0;
-            for (int j = lane; j < K1; j += 32) part += root_fixed(Mw[j], sc);
-            part = __reduce_add_sync(0xffffffffu, part);
-            md = fixed_mean(part, e, k);
-        }
-        if (lane == 0) md_out[i] = md;
         __syncwarp();
+    }
+}
+
+// Farthest point of a coarse cell's cube (grown by the margin) from q, squared.
+__device__ __forceinline__ float cell_far_d2(unsigned idx, const GridStats* __restrict__ s, float qx, float qy,
+                                             float qz, float margin) {
+    const unsigned nx = (unsigned)s->dims[0], ny = (unsigned)s->dims[1];
+    const float c = s->cell[1];
+    const float lx = s->org[0] + (float)(idx % nx) * c - margin;
+    const float ly = s->org[1] + (float)((idx / nx) % ny) * c - margin;
+    const float lz = s->org[2] + (float)(idx / (nx * ny)) * c - margin;
+    const float w = c + 2.f * margin;
+    const float ex = fmaxf(fabsf(qx - lx), fabsf(lx + w - qx));
+    const float ey = fmaxf(fabsf(qy - ly), fabsf(ly + w - qy));
+    const float ez = fmaxf(fabsf(qz - lz), fabsf(lz + w - qz));
+    return ex * ex + ey * ey + ez * ez;
+}
+
+// Phase 3: one CTA per hard query over the coarse level's occupied cells.  The
+// bound starts at the farthest corner of the nearest-cornered cell holding
+// K1 points (or the query's own bound).  Warps take cells one at a time and
+// skip those whose cube lies beyond the CTA's bound; each keeps in its list
+// the distances below its bound and counts those equal to it, and a list of K1
+// or more entries tightens the bound to their K1-th smallest, shared through
+// an atomic minimum.  Lists then hold every point below the final bound, plus
+// the counted ties: one warp selects the K1 smallest from them.
+constexpr int HARD_T = 1024, HARD_W = HARD_T / 32;
+__global__ void __launch_bounds__(HARD_T) sor_hard_kernel(const float* __restrict__ xyz, int k,
+                                                          const GridStats* __restrict__ s,
+                                                          const uint4* __restrict__ occ,
+                                                          const float4* __restrict__ pts,
+                                                          const unsigned* __restrict__ hard,
+                                                          float* __restrict__ md_out,
+                                                          const float* __restrict__ bound,
+                                                          uint32_t* __restrict__ err) {
+    __shared__ float hl[HARD_W][FW_CAP];
+    __shared__ unsigned s_thr, s_next, s_ties;
+    __shared__ unsigned s_wmin[HARD_W];
+    __shared__ int s_n[HARD_W];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int K1 = k + 1;
+    const unsigned nh = s->n_hard, nocc = s->n_occ;
+    const float margin = 1e-4f * s->cell[1] + 4e-6f * s->amax;
+    float* lw = hl[w];
+    for (unsigned item = blockIdx.x; item < nh; item += gridDim.x) {
+        const unsigned i = hard[item];
+        const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
+        const float own = md_out[i] == MD_BOUND ? bound[i] : INFINITY;
+        // a cell of K1 points lies wholly within its farthest corner
+        unsigned fb = 0x7f800000u;  // +inf bits; non-negative floats order as unsigned
+        for (unsigned j = tid; j < nocc; j += HARD_T) {
+            const uint4 o = __ldg(occ + j);
+            if (o.z >= (unsigned)K1) fb = min(fb, __float_as_uint(cell_far_d2(o.x, s, qx, qy, qz, margin) * 1.00001f));
+        }
+        fb = __reduce_min_sync(0xffffffffu, fb);
+        if (lane == 0) s_wmin[w] = fb;
+        if (tid == 0) {
+            s_next = 0u;
+            s_ties = 0u;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            unsigned m = __float_as_uint(own);
+            for (int j = 0; j < HARD_W; j++) m = min(m, s_wmin[j]);
+            s_thr = m;
+        }
+        __syncthreads();
+        float thr = __uint_as_float(s_thr);
+        int n = 0;      // list entries (all below thr)
+        unsigned tie = 0u;  // points at exactly thr
+        auto tighten = [&]() {
+            __syncwarp();
+            unsigned keys[FW_CAP / 32];
+#pragma unroll
+            for (int q = 0; q < FW_CAP / 32; q++) {
+                const int e = lane + 32 * q;
+                keys[q] = e < n ? __float_as_uint(lw[e]) : 0xffffffffu;
+            }
+            if (n < K1) return;  // warp-uniform; the K1-th is thr itself or unknown
+            const unsigned kk = warp_kth_key(keys, K1);  // below thr
+            thr = __uint_as_float(kk);
+            int m = 0;
+            unsigned t = 0u;
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < FW_CAP / 32; q++) {
+                const bool kp = keys[q] < kk;
+                const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                if (kp) lw[m + __popc(bb & ((1u << lane) - 1u))] = __uint_as_float(keys[q]);
+                m += __popc(bb);
+                t += __popc(__ballot_sync(0xffffffffu, keys[q] == kk));
+            }
+            n = m;
+            tie = t;
+            if (lane == 0) atomicMin(&s_thr, kk);
+            __syncwarp();
+        };
+        for (;;) {
+            unsigned j = 0;
+            if (lane == 0) j = atomicAdd(&s_next, 1u);
+            j = __shfl_sync(0xffffffffu, j, 0);
+            if (j >= nocc) break;
+            const float shared_thr = __uint_as_float(*(volatile unsigned*)&s_thr);
+            if (shared_thr < thr) {  // another warp's bound: entries at or above it go
+                thr = shared_thr;
+                int m = 0;
+                __syncwarp();
+                for (int q0 = 0; q0 < n; q0 += 32) {
+                    const int e = q0 + lane;
+                    const float v = e < n ? lw[e] : INFINITY;
+                    const bool kp = v < thr;
+                    const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                    __syncwarp();
+                    if (kp) lw[m + __popc(bb & ((1u << lane) - 1u))] = v;
+                    m += __popc(bb);
+                }
+                n = m;
+                tie = 0u;
+                __syncwarp();
+            }
+            const uint4 o = __ldg(occ + j);
+            if (cell_box_d2(o.x, s, qx, qy, qz, margin) > thr) continue;
+            const unsigned end = o.y + o.z;
+            for (unsigned u0 = o.y; u0 < end; u0 += 128) {
+                if (n > FW_CAP - 128) tighten();  // n < K1 after it: room for 128
+                float d2[4];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const unsigned u = u0 + 32u * r + lane;
+                    d2[r] = __int_as_float(0x7fffffff);  // NaN: neither below nor equal to the bound
+                    if (u < end) {
+                        const float4 p = __ldg(pts + u);
+                        d2[r] = sqdist(p.x - qx, p.y - qy, p.z - qz);
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const bool kp = d2[r] < thr;
+                    const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                    if (kp) lw[n + __popc(bb & ((1u << lane) - 1u))] = d2[r];
+                    n += __popc(bb);
+                    tie += __popc(__ballot_sync(0xffffffffu, d2[r] == thr));
+                }
+                if (n >= 2 * K1 && !(thr < INFINITY)) tighten();
+            }
+            if (n >= K1) tighten();
+        }
+        __syncthreads();
+        // final bound: entries below it stay; entries equal to it and the
+        // ties of the warps that hold it are counted
+        const float fin = __uint_as_float(s_thr);
+        {
+            unsigned t = thr == fin ? tie : 0u;
+            int m = 0;
+            __syncwarp();
+            for (int q0 = 0; q0 < n; q0 += 32) {
+                const int e = q0 + lane;
+                const float v = e < n ? lw[e] : __int_as_float(0x7fffffff);
+                const bool kp = v < fin;
+                const unsigned bb = __ballot_sync(0xffffffffu, kp);
+                t += __popc(__ballot_sync(0xffffffffu, v == fin));
+                __syncwarp();
+                if (kp) lw[m + __popc(bb & ((1u << lane) - 1u))] = v;
+                m += __popc(bb);
+            }
+            if (lane == 0) {
+                s_n[w] = m;
+                atomicAdd(&s_ties, t);
+            }
+        }
+        __syncthreads();
+        if (w == 0) {
+            // the K1-th smallest of the lists' entries and the ties (at fin):
+            // binary search on the key bits
+            const unsigned ties = s_ties;
+            int total = 0;
+            for (int v = 0; v < HARD_W; v++) total += s_n[v];
+            unsigned lo = 0u, hi = __float_as_uint(fin);
+            if (!(fin < INFINITY) || total + (int)ties < K1) {
+                if (lane == 0) {
+                    atomicOr(err, 0x10u);  // fewer than k + 1 points reachable
+                    md_out[i] = 0.f;
+                }
+            } else {
+                if (total >= K1) {
+                    while (lo < hi) {
+                        const unsigned mid = lo + ((hi - lo) >> 1);
+                        int c = 0;
+                        for (int v = 0; v < HARD_W; v++)
+                            for (int e = lane; e < s_n[v]; e += 32) c += __float_as_uint(hl[v][e]) <= mid;
+                        c = __reduce_add_sync(0xffffffffu, c);
+                        if (c >= K1) hi = mid;
+                        else lo = mid + 1u;
+                    }
+                }
+                const unsigned kk = hi;  // the K1-th (fin when fewer than K1 entries lie below it)
+                const float kv = __uint_as_float(kk);
+                const int ee = root_exponent(kv);
+                const float sc = root_scale(ee);
+                unsigned part = 0u;
+                int below = 0;
+                for (int v = 0; v < HARD_W; v++)
+                    for (int e = lane; e < s_n[v]; e += 32) {
+                        const unsigned key = __float_as_uint(hl[v][e]);
+                        if (key < kk) {
+                            part += root_fixed(hl[v][e], sc);
+                            below++;
+                        }
+                    }
+                part = __reduce_add_sync(0xffffffffu, part);
+                below = __reduce_add_sync(0xffffffffu, below);
+                part += (unsigned)(K1 - below) * root_fixed(kv, sc);
+                if (lane == 0) md_out[i] = fixed_mean(part, ee, k);
+            }
+        }
+        __syncthreads();  // the lists are reused by the next query
     }
 }
 
@@ -1546,6 +1667,8 @@ struct GridScratch {
     unsigned* tot;
     float* md;
     unsigned* deferred;
+    unsigned* hard;  // phase-3 queries
+    float* bound;    // per pixel: a deferred query's bound (md = MD_BOUND)
     double* part;
     uint4* occ;  // occupied coarse cells: (cell index, offset, count, 0)
 };
@@ -1557,7 +1680,7 @@ size_t part_bytes(size_t n) {
 }
 
 size_t grid_bytes(size_t n, int levels) {
-    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 2 + zim_align256(part_bytes(n)) +
+    size_t b = zim_align256(sizeof(GridStats)) + zim_align256(n * 4) * 4 + zim_align256(part_bytes(n)) +
                zim_align256((size_t)level_table(n, levels - 1) * sizeof(uint4));
     unsigned tmax = 1024;
     for (int l = 0; l < levels; l++) {
@@ -1584,9 +1707,11 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     G.tot = (unsigned*)zim_scratch_take(ctx, ((tmax + SCAN_B - 1) / SCAN_B) * 4);
     G.md = (float*)zim_scratch_take(ctx, n * 4);
     G.deferred = (unsigned*)zim_scratch_take(ctx, n * 4);
+    G.hard = (unsigned*)zim_scratch_take(ctx, n * 4);
+    G.bound = (float*)zim_scratch_take(ctx, n * 4);
     G.part = (double*)zim_scratch_take(ctx, part_bytes(n));
     G.occ = (uint4*)zim_scratch_take(ctx, (size_t)G.tsize[levels - 1] * sizeof(uint4));
-    if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.part || !G.occ)
+    if (!G.stats || !G.counts || !G.tot || !G.md || !G.deferred || !G.hard || !G.bound || !G.part || !G.occ)
         return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "grid scratch carve");
     return ZIM_OK;
 }
@@ -1663,15 +1788,17 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     if (window) {
         const RayParams rp = zt::ray_params(rays);
         sor_far_window_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
-            xyz, mask, rows, cols, mean_k, rp, G.stats, G.deferred, md);
+            xyz, mask, rows, cols, mean_k, rp, G.stats, G.deferred, md, G.bound);
         ctx->launches += 1;
     }
-    // enough warps in flight to cover the latency of the long point scans
-    const size_t fsm = (size_t)P2_WARPS * ((mean_k + 1) * 33 + FW_CAP) * sizeof(float);
-    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-    sor_knn_far_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, fsm, st>>>(
-        xyz, mean_k, G.stats, G.occ, G.tab[1], G.pts[1], G.deferred, md, ctx->d_error);
-    ctx->launches += 3;
+    // enough warps in flight to cover the latency of the point scans
+    const unsigned sms = (unsigned)(ctx->sm_count > 0 ? ctx->sm_count : 152);
+    sor_knn_far_kernel<<<8 * sms, P2_WARPS * 32, 0, st>>>(xyz, mean_k, G.stats, G.tab[1], G.pts[1], G.deferred, md,
+                                                          G.bound, G.hard);
+    // a few hard queries per cloud: one CTA each
+    sor_hard_kernel<<<2 * sms, HARD_T, 0, st>>>(xyz, mean_k, G.stats, G.occ, G.pts[1], G.hard, md, G.bound,
+                                                ctx->d_error);
+    ctx->launches += 4;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
     const unsigned pblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
     sor_partial_kernel<<<pblk, GB, 0, st>>>(mask, md, n, G.part);
