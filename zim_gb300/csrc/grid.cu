@@ -444,7 +444,6 @@ static_assert(WIN_W * WIN_H <= TILE_MAX_CAND, "pixel window staged in the candid
 static_assert(TILE_MAX_CELLS <= 8 * TILE_T, "cell scan: eight cells per thread");
 
 constexpr int SV_CAP = 128;  // survivors per warp query (k + 1 <= 64 of them kept)
-constexpr int SEL_SLACK = 17;  // per-thread selection lists hold k + 1 + SEL_SLACK
 
 // Phase 1: one CTA per 16 x 8 pixel tile on the finest level.
 //  - Window bound: the query and its k nearest valid pixels (in pixel
@@ -755,51 +754,34 @@ constexpr int WR = zt::SPIRAL_R;  // window half-size of the fast path
 constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
 constexpr int WN = zt::SPIRAL_N;
 
-// Per-thread selection of the K1 smallest squared distances in column tid of
-// a [cap][TILE_T] shared array: values within the bound are appended; a full
-// list is cut to its K1 smallest (quickselect) and the bound tightened to the
-// K1-th value.
-struct WinSel {
+// Per-thread max-heap of the K1 smallest squared distances seen so far, in
+// column tid of a [K1][TILE_T] shared array (conflict-free): the root is the
+// current K1-th smallest, and a nearer point replaces it with one sift-down.
+struct WinHeap {
     float* L;
-    int cnt, K1, cap;
-    float thr;
+    int K1;
     __device__ __forceinline__ float& at(int j) { return L[j * TILE_T]; }
-    // Rearranges entries [0, cnt) so that [0, K1) hold the K1 smallest;
-    // returns the K1-th smallest (Hoare partitions, median-of-three pivots).
-    __device__ __forceinline__ float select() {
-        int lo = 0, hi = cnt - 1;
-        const int t = K1 - 1;
-        while (lo < hi) {
-            const float a = at(lo), b = at((lo + hi) >> 1), c = at(hi);
-            const float pv = fmaxf(fminf(a, b), fminf(fmaxf(a, b), c));
-            int i = lo, j = hi;
-            while (i <= j) {
-                while (at(i) < pv) i++;
-                while (at(j) > pv) j--;
-                if (i <= j) {
-                    const float v = at(i);
-                    at(i) = at(j);
-                    at(j) = v;
-                    i++;
-                    j--;
+    // places v at j, moving larger children up
+    __device__ __forceinline__ void sift(int j, float v) {
+        for (;;) {
+            int c = 2 * j + 1;
+            if (c >= K1) break;
+            float cv = at(c);
+            if (c + 1 < K1) {
+                const float c2 = at(c + 1);
+                if (c2 > cv) {
+                    cv = c2;
+                    c++;
                 }
             }
-            if (t <= j) hi = j;
-            else if (t >= i) lo = i;
-            else break;  // t lies among entries equal to the pivot
+            if (!(cv > v)) break;
+            at(j) = cv;
+            j = c;
         }
-        // [0, K1) now holds the K1 smallest; the K1-th is their maximum
-        float m = at(0);
-        for (int j = 1; j < K1; j++) m = fmaxf(m, at(j));
-        return m;
+        at(j) = v;
     }
-    __device__ __forceinline__ void push(float d2) {
-        if (d2 > thr) return;
-        at(cnt) = d2;
-        if (++cnt == cap) {
-            thr = select();
-            cnt = K1;
-        }
+    __device__ __forceinline__ void build() {
+        for (int j = K1 / 2 - 1; j >= 0; j--) sift(j, at(j));
     }
 };
 
@@ -809,7 +791,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
                                                             float* __restrict__ md_out) {
     extern __shared__ float4 win_smem[];
     float4* W = win_smem;                                      // WW x WH window, w = 1 valid
-    float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1 + SEL_SLACK) x TILE_T
+    float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1) x TILE_T heaps
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
     __shared__ unsigned warp_dev[TILE_T / 32];
@@ -845,21 +827,21 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float4 q = W[wc];
     const int K1 = k + 1;
     // the query and its first k valid window pixels in spiral order fill the
-    // list; their largest distance is the first bound
-    WinSel sel{Ls + tid, 1, K1, K1 + SEL_SLACK, 0.f};
-    sel.at(0) = 0.f;
-    int o = 0;
-    for (; o < WN && sel.cnt < K1; o++) {
+    // heap; its root (their largest distance) is the first bound
+    WinHeap heap{Ls + tid, K1};
+    heap.at(0) = 0.f;
+    int cnt = 1, o = 0;
+    for (; o < WN && cnt < K1; o++) {
         const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
         if (p.w == 0.f) continue;
-        const float d2 = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
-        sel.at(sel.cnt++) = d2;
-        sel.thr = fmaxf(sel.thr, d2);
+        heap.at(cnt++) = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
     }
-    if (sel.cnt < K1) {
+    if (cnt < K1) {
         md_out[i] = -2.f;
         return;
     }
+    heap.build();
+    float thr = heap.at(0);
     // bound(r) = C r / (an + r): no point of a pixel at distance >= r from the
     // query's lies nearer than bound(r) - dev (slack: float rounding, 1e-5 |q|)
     float ax, ay, az;
@@ -878,7 +860,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
         const float r = sd * an / (C - sd);
         return r * r;
     };
-    float last = sel.thr, rs2 = stop_r2(last), rbreak = (float)(WR + 1);
+    float rs2 = stop_r2(thr), rbreak = (float)(WR + 1);
     // the spiral runs by increasing length: once past the stop distance, the
     // rest of the window (and everything outside it) is provably farther
     for (; o < WN; o++) {
@@ -890,14 +872,14 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
         }
         const float4 p = W[wc + dy * WW + dx];
         if (p.w == 0.f) continue;
-        sel.push(sqdist(p.x - q.x, p.y - q.y, p.z - q.z));
-        if (sel.thr != last) {
-            last = sel.thr;
-            rs2 = stop_r2(last);
+        const float d2 = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
+        if (d2 < thr) {
+            heap.sift(0, d2);
+            thr = heap.at(0);
+            rs2 = stop_r2(thr);
         }
     }
-    // a list of exactly K1 entries is the K1 smallest, its bound their largest
-    const float kth = sel.cnt == K1 ? sel.thr : sel.select();
+    const float kth = thr;
     // certificate: every window pixel not visited is at least rbreak away, and
     // every pixel outside the window at least WR + 1
     const float rk = sqrtf(kth), ro = (float)(WR + 1);
@@ -909,7 +891,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const int e = root_exponent(kth);
     const float sc = root_scale(e);
     unsigned sum = 0;
-    for (int j = 0; j < K1; j++) sum += root_fixed(sel.L[j * TILE_T], sc);
+    for (int j = 0; j < K1; j++) sum += root_fixed(heap.at(j), sc);
     md_out[i] = fixed_mean(sum, e, k);
 }
 
@@ -1775,7 +1757,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         const RayParams rp = zt::ray_params(rays);
         ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
                                                                                      &G.stats->ray_dev_bits);
-        const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1 + SEL_SLACK) * TILE_T * 4;
+        const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
         sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md);
         ctx->launches += 2;
