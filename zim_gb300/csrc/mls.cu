@@ -303,26 +303,41 @@ inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * 
 // which the ray bound puts every point outside the cut-off: the pixels left out
 // would fail the distance test, so the neighbours and their order are those
 // of the full window.  The disk is the largest of the warp's (one loop bound).
+// Every neighbour is a staged pixel, so the bound takes the largest distance of
+// a staged point from its own ray (points smoothed across a depth edge lie far
+// off their rays, but only near the edge).
 __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restrict__ src,
                                                           const uint8_t* __restrict__ mask, int rows, int cols, int hw,
                                                           float inv_2s2, int order, float r2c, int rays,
-                                                          zt::RayParams rp, const unsigned* __restrict__ dev_max,
-                                                          float* __restrict__ dst) {
+                                                          zt::RayParams rp, float* __restrict__ dst) {
     extern __shared__ float4 mls_sp[];
+    __shared__ unsigned warp_dev[MX * MY / 32];
     const int TW = MX + 2 * hw, TH = MY + 2 * hw;
     const int gx0 = blockIdx.x * MX - hw, gy0 = blockIdx.y * MY - hw;
     const int tid = threadIdx.y * MX + threadIdx.x;
+    unsigned tdev = 0u;  // largest ray distance of this thread's staged points (float bits, >= 0)
     for (int t = tid; t < TW * TH; t += MX * MY) {
         const int ty = t / TW, tx = t - ty * TW;
         const int gx = gx0 + tx, gy = gy0 + ty;
         float4 v = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
         if (gx >= 0 && gy >= 0 && gx < cols && gy < rows) {
             const size_t q = (size_t)gy * cols + gx;
-            if (__ldg(mask + q)) v = make_float4(__ldg(src + 3 * q), __ldg(src + 3 * q + 1), __ldg(src + 3 * q + 2), 1.f);
+            if (__ldg(mask + q)) {
+                v = make_float4(__ldg(src + 3 * q), __ldg(src + 3 * q + 1), __ldg(src + 3 * q + 2), 1.f);
+                if (rays) {
+                    float ax, ay, az;
+                    zt::ray_dir(rp, gx, gy, ax, ay, az);
+                    tdev = max(tdev, __float_as_uint(zt::ray_dev(v.x, v.y, v.z, ax, ay, az)));
+                }
+            }
         }
         mls_sp[t] = v;
     }
+    tdev = __reduce_max_sync(0xffffffffu, tdev);
+    if ((tid & 31) == 0) warp_dev[tid >> 5] = tdev;
     __syncthreads();
+#pragma unroll
+    for (int j = 0; j < MX * MY / 32; j++) tdev = max(tdev, warp_dev[j]);
     const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
     const bool inside = x < cols && y < rows;
     const int cc = (threadIdx.y + hw) * TW + threadIdx.x + hw;
@@ -336,7 +351,7 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
             const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
             const float qn = sqrtf(fmaf(c.x, c.x, fmaf(c.y, c.y, c.z * c.z)));
             const float C = qn * rp.f / an;
-            const float sd = sqrtf(r2c) + zt::ray_dev(c.x, c.y, c.z, ax, ay, az) + __uint_as_float(*dev_max) + 1e-5f * qn;
+            const float sd = sqrtf(r2c) + zt::ray_dev(c.x, c.y, c.z, ax, ay, az) + __uint_as_float(tdev) + 1e-5f * qn;
             rs2 = INFINITY;
             if (C > sd) {
                 const float r = sd * an / (C - sd);
@@ -387,26 +402,15 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     if (use_smem)
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(mls_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int use_rays = use_smem && rays.valid;
-    unsigned* dev_max = nullptr;
-    if (use_rays) {
-        dev_max = (unsigned*)zim_scratch_take(ctx, 256);
-        if (!dev_max) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "MLS scratch");
-    }
     const zt::RayParams rp = zt::ray_params(rays);
     // ping-pong so that the last pass lands in `out`
     const float* in = xyz;
     for (int it = 0; it < n_iter; it++) {
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
-        if (use_rays) {
-            ZIM_CUDA_TRY(ctx, cudaMemsetAsync(dev_max, 0, 4, st));
-            zt::ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), 256, 0, st>>>(in, mask, rows, cols,
-                                                                                              rp, dev_max);
-            ctx->launches += 1;
-        }
         if (use_smem)
             mls_smem_kernel<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp,
-                                                    dev_max, dst);
+                                                    dst);
         else
             mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;
