@@ -246,21 +246,31 @@ __global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int le
 // points gives the same value at every call site of the kNN search.
 __device__ __forceinline__ float sqdist(float dx, float dy, float dz) { return fmaf(dz, dz, fmaf(dy, dy, dx * dx)); }
 
+// Hardware square root (PTX sqrt.approx.f32, relative error below 2^-22): one
+// instruction, the same at every call site, so every search path rounds alike.
+__device__ __forceinline__ float root_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Order-independent sum of the k + 1 nearest distances: each root, scaled by
-// 2^(23 - e) with sqrt(largest squared distance) < 2^e, is truncated to an
+// 2^(23 - e) with root(largest squared distance) < 2^e, is truncated to an
 // integer below 2^23 and the integers are added exactly (at most 64 of them:
 // below 2^29), so every search path and every visiting order gives the same
 // bits.  The truncation is one FMA rounded toward zero onto 2^23, whose
 // mantissa then holds the integer: no 64-bit conversion (FP64 pipe) per root.
+// The roots are root_approx's; e leaves 2^-19 of room above the largest, more
+// than the approximation's error, so no smaller entry's root reaches 2^e.
 // Roots below 2^(e - 23), a 2^-22 fraction of the largest, count as 0.
 __device__ __forceinline__ int root_exponent(float d2max) {
     int e;
-    frexpf(sqrtf(d2max), &e);
+    frexpf(root_approx(d2max) * 1.000002f, &e);
     return min(max(e, -60), 100);  // keeps 2^(23 - e) and 2^(e - 23) normal
 }
 __device__ __forceinline__ float root_scale(int e) { return __uint_as_float((unsigned)(150 - e) << 23); }
 __device__ __forceinline__ unsigned root_fixed(float d2, float scale) {
-    return __float_as_uint(__fmaf_rz(sqrtf(d2), scale, 8388608.f)) - 0x4B000000u;
+    return __float_as_uint(__fmaf_rz(root_approx(d2), scale, 8388608.f)) - 0x4B000000u;
 }
 // (sum / k) 2^(e - 23), one float division
 __device__ __forceinline__ float fixed_mean(unsigned sum, int e, int k) {
@@ -853,11 +863,13 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float dev = dev_q + __uint_as_float(tdev);                    // window pixels
     const float dev_out = dev_q + __uint_as_float(s->ray_dev_bits);     // pixels outside it
     // squared pixel distance beyond which every window point is farther than
-    // sqrt(thr): C r / (an + r) > sqrt(thr) + dev  <=>  r > (sqrt(thr) + dev) an / (C - sqrt(thr) - dev)
+    // sqrt(thr): C r / (an + r) > sqrt(thr) + dev  <=>  r > (sqrt(thr) + dev) an / (C - sqrt(thr) - dev).
+    // Approximate arithmetic: the stop only ends the walk; the exact
+    // certificate below decides whether the window result stands.
     auto stop_r2 = [&](float thr) {
-        const float sd = sqrtf(thr) + dev;
+        const float sd = root_approx(thr) + dev;
         if (!(C > sd)) return INFINITY;
-        const float r = sd * an / (C - sd);
+        const float r = __fdividef(sd * an, C - sd);
         return r * r;
     };
     float rs2 = stop_r2(thr), rbreak = (float)(WR + 1);
