@@ -111,36 +111,66 @@ __device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const flo
     return ok;
 }
 
+// Gaussian weight exp(-d2 / (2 s^2)) = 2^(d2 * kw) with kw = -log2(e) / (2 s^2):
+// one multiply and the hardware base-2 exponential (PTX ex2.approx).
+__device__ __forceinline__ float mls_weight(float d2, float kw) {
+    float w;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(d2 * kw));
+    return w;
+}
+
 // Normal equations of the order-N polynomial fit (N = 3: 1, u, v; N = 6: also
-// u^2, uv, v^2), accumulated in registers.
+// u^2, uv, v^2) in tangent coordinates u, v (scaled by is) and height f about
+// the centroid c.  Entry (a, b) is the weighted moment of u^i v^j whose
+// exponents are those of basis terms a and b added: the 15 moments with
+// i + j <= 4 (6 for N = 3) and the right-hand side's 6 (3) are accumulated,
+// then the symmetric matrix is filled.
 template <int N, typename Visit>
-__device__ __forceinline__ void fit_accumulate(Visit& visit, float inv_2s2, float r2c, float is, float cx, float cy,
+__device__ __forceinline__ void fit_accumulate(Visit& visit, float kw, float r2c, float is, float cx, float cy,
                                                float cz, float t1x, float t1y, float t1z, float t2x, float t2y,
                                                float t2z, float nx, float ny, float nz, float (&A)[N][N],
                                                float (&bv)[N]) {
-#pragma unroll
-    for (int a = 0; a < N; a++) {
-        bv[a] = 0.f;
-#pragma unroll
-        for (int b = 0; b < N; b++) A[a][b] = 0.f;
-    }
+    // u = (d - c) . t1 is as one FMA chain on d (likewise v, f)
+    const float ax = t1x * is, ay = t1y * is, az = t1z * is;
+    const float bx = t2x * is, by = t2y * is, bz = t2z * is;
+    const float uc = fmaf(cx, ax, fmaf(cy, ay, cz * az));
+    const float vc = fmaf(cx, bx, fmaf(cy, by, cz * bz));
+    const float fc = fmaf(cx, nx, fmaf(cy, ny, cz * nz));
+    float m00 = 0.f, m10 = 0.f, m01 = 0.f, m20 = 0.f, m11 = 0.f, m02 = 0.f;
+    float m30 = 0.f, m21 = 0.f, m12 = 0.f, m03 = 0.f, m40 = 0.f, m31 = 0.f, m22 = 0.f, m13 = 0.f, m04 = 0.f;
+    float b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f, b4 = 0.f, b5 = 0.f;
     visit([&](float dx, float dy, float dz) {
-        float d2 = dx * dx + dy * dy + dz * dz;
+        const float d2 = dx * dx + dy * dy + dz * dz;
         if (!(d2 <= r2c)) return;
-        float w = __expf(-d2 * inv_2s2);
-        float ex = dx - cx, ey = dy - cy, ez = dz - cz;
-        float u = (ex * t1x + ey * t1y + ez * t1z) * is;
-        float v = (ex * t2x + ey * t2y + ez * t2z) * is;
-        float f = ex * nx + ey * ny + ez * nz;
-        float bs[6] = {1.f, u, v, u * u, u * v, v * v};
-#pragma unroll
-        for (int a = 0; a < N; a++) {
-            float wa = w * bs[a];
-            bv[a] = fmaf(wa, f, bv[a]);
-#pragma unroll
-            for (int b = a; b < N; b++) A[a][b] = fmaf(wa, bs[b], A[a][b]);
+        const float w = mls_weight(d2, kw);
+        const float u = fmaf(dx, ax, fmaf(dy, ay, fmaf(dz, az, -uc)));
+        const float v = fmaf(dx, bx, fmaf(dy, by, fmaf(dz, bz, -vc)));
+        const float f = fmaf(dx, nx, fmaf(dy, ny, fmaf(dz, nz, -fc)));
+        const float wu = w * u, wv = w * v, wf = w * f;
+        m00 += w; m10 += wu; m01 += wv;
+        m20 = fmaf(wu, u, m20); m11 = fmaf(wu, v, m11); m02 = fmaf(wv, v, m02);
+        b0 += wf; b1 = fmaf(wf, u, b1); b2 = fmaf(wf, v, b2);
+        if (N == 6) {
+            const float uu = u * u, uv = u * v, vv = v * v;
+            m30 = fmaf(wu, uu, m30); m21 = fmaf(wu, uv, m21); m12 = fmaf(wu, vv, m12); m03 = fmaf(wv, vv, m03);
+            const float wuu = wu * u, wvv = wv * v;
+            m40 = fmaf(wuu, uu, m40); m31 = fmaf(wuu, uv, m31); m22 = fmaf(wuu, vv, m22);
+            m13 = fmaf(wvv, uv, m13); m04 = fmaf(wvv, vv, m04);
+            b3 = fmaf(wf, uu, b3); b4 = fmaf(wf, uv, b4); b5 = fmaf(wf, vv, b5);
         }
     });
+    // basis exponents: 1 (0,0), u (1,0), v (0,1), u^2 (2,0), uv (1,1), v^2 (0,2)
+    A[0][0] = m00; A[0][1] = m10; A[0][2] = m01;
+    A[1][1] = m20; A[1][2] = m11; A[2][2] = m02;
+    bv[0] = b0; bv[1] = b1; bv[2] = b2;
+    if constexpr (N == 6) {
+        A[0][3] = m20; A[0][4] = m11; A[0][5] = m02;
+        A[1][3] = m30; A[1][4] = m21; A[1][5] = m12;
+        A[2][3] = m21; A[2][4] = m12; A[2][5] = m03;
+        A[3][3] = m40; A[3][4] = m31; A[3][5] = m22;
+        A[4][4] = m22; A[4][5] = m13; A[5][5] = m04;
+        bv[3] = b3; bv[4] = b4; bv[5] = b5;
+    }
 #pragma unroll
     for (int a = 0; a < N; a++)
 #pragma unroll
@@ -154,6 +184,7 @@ template <typename Visit>
 __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, Visit visit, float& ox, float& oy,
                                           float& oz, bool& moved) {
     moved = false;
+    const float kw = -1.44269504088896341f * inv_2s2;  // -log2(e) / (2 s^2)
     // 1. weighted centroid and covariance in one sweep, from the moments about
     // the query point (offsets of at most the cut-off radius, so the FP32
     // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
@@ -164,7 +195,7 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
     visit([&](float dx, float dy, float dz) {
         float d2 = dx * dx + dy * dy + dz * dz;
         if (!(d2 <= r2c)) return;
-        float w = __expf(-d2 * inv_2s2);
+        float w = mls_weight(d2, kw);
         cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
         const float wx = w * dx, wy = w * dy;
         m00 = fmaf(wx, dx, m00); m01 = fmaf(wx, dy, m01); m02 = fmaf(wx, dz, m02);
@@ -222,7 +253,7 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
     }
     if (cur == 2) {
         float A[6][6], bv[6], x6[6];
-        fit_accumulate<6>(visit, inv_2s2, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
+        fit_accumulate<6>(visit, kw, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
         solved = cholesky_fixed<6>(A, bv, x6, thr);
         if (solved) {
 #pragma unroll
@@ -245,7 +276,7 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
         }
     } else if (cur == 1) {
         float A[3][3], bv[3], x3[3];
-        fit_accumulate<3>(visit, inv_2s2, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
+        fit_accumulate<3>(visit, kw, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
         solved = cholesky_fixed<3>(A, bv, x3, thr);
         if (solved)
 #pragma unroll
