@@ -759,10 +759,35 @@ using zt::RayParams;
 using zt::ray_dir;
 using zt::ray_dev;
 using zt::ray_dev_kernel;
-using zt::c_spiral7;
 constexpr int WR = zt::SPIRAL_R;  // window half-size of the fast path
 constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
 constexpr int WN = zt::SPIRAL_N;
+constexpr int WR2MAX = 2 * WR * WR;
+
+// The window's pixel offsets ordered by length, then row, then column, as
+// staged-tile offsets with their squared length, and per squared radius the
+// number of offsets within it: a walk's stop radius becomes a loop limit.
+struct WinSpiral {
+    int ent[WN];             // (dy * WW + dx) & 0xffff | (dx^2 + dy^2) << 16
+    short upto[WR2MAX + 1];  // offsets of squared length <= i
+    constexpr WinSpiral() : ent(), upto() {
+        int n = 0;
+        for (int l = 1; l <= WR2MAX; l++)
+            for (int dy = -WR; dy <= WR; dy++)
+                for (int dx = -WR; dx <= WR; dx++)
+                    if (dx * dx + dy * dy == l) ent[n++] = ((dy * WW + dx) & 0xffff) | (l << 16);
+        int c = 0;
+        for (int i = 0; i <= WR2MAX; i++) {
+            while (c < WN && (ent[c] >> 16) <= i) c++;
+            upto[i] = (short)c;
+        }
+    }
+};
+__constant__ WinSpiral c_win = WinSpiral();
+__device__ __forceinline__ int win_off(int o) { return (int)(short)(c_win.ent[o] & 0xffff); }
+__device__ __forceinline__ int win_len2(int o) { return c_win.ent[o] >> 16; }
+// offsets whose squared length is at most r2 (r2 >= 0 or +inf)
+__device__ __forceinline__ int win_upto(float r2) { return r2 < (float)WR2MAX ? c_win.upto[(int)r2] : WN; }
 
 // Per-thread max-heap of the K1 smallest squared distances seen so far, in
 // column tid of a [K1][TILE_T] shared array (conflict-free): the root is the
@@ -842,7 +867,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     heap.at(0) = 0.f;
     int cnt = 1, o = 0;
     for (; o < WN && cnt < K1; o++) {
-        const float4 p = W[wc + c_spiral7[o][1] * WW + c_spiral7[o][0]];
+        const float4 p = W[wc + win_off(o)];
         if (p.w == 0.f) continue;
         heap.at(cnt++) = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
     }
@@ -872,25 +897,21 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
         const float r = __fdividef(sd * an, C - sd);
         return r * r;
     };
-    float rs2 = stop_r2(thr), rbreak = (float)(WR + 1);
     // the spiral runs by increasing length: once past the stop distance, the
     // rest of the window (and everything outside it) is provably farther
-    for (; o < WN; o++) {
-        const int dx = c_spiral7[o][0], dy = c_spiral7[o][1];
-        const float r2o = (float)(dx * dx + dy * dy);
-        if (r2o > rs2) {
-            rbreak = fminf(sqrtf(r2o), rbreak);
-            break;
-        }
-        const float4 p = W[wc + dy * WW + dx];
+    int lim = win_upto(stop_r2(thr));
+    for (; o < lim; o++) {
+        const float4 p = W[wc + win_off(o)];
         if (p.w == 0.f) continue;
         const float d2 = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
         if (d2 < thr) {
             heap.sift(0, d2);
             thr = heap.at(0);
-            rs2 = stop_r2(thr);
+            lim = win_upto(stop_r2(thr));
         }
     }
+    // every window offset not visited is at least as long as offset o
+    const float rbreak = o < WN ? fminf(sqrtf((float)win_len2(o)), (float)(WR + 1)) : (float)(WR + 1);
     const float kth = thr;
     // certificate: every window pixel not visited is at least rbreak away, and
     // every pixel outside the window at least WR + 1
@@ -1583,13 +1604,13 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
         pending[i] = -2.f;
         return;
     }
-    const float rs2 = rs * rs, r2 = r * r;
+    const float r2 = r * r;
     const int wc = (ty + WRG) * GW + tx + WRG;
     float sx = 0.f, sy = 0.f, sz = 0.f, sw = 1.f;  // the query itself: weight 1, offset 0
-    for (int o = 0; o < WN; o++) {
-        const int dx = c_spiral7[o][0], dy = c_spiral7[o][1];
-        if ((float)(dx * dx + dy * dy) > rs2) break;
-        const float4 p = W[wc + dy * GW + dx];
+    const int lim = win_upto(rs * rs);
+    static_assert(GW == WW && WRG == WR, "the window table's tile");
+    for (int o = 0; o < lim; o++) {
+        const float4 p = W[wc + win_off(o)];
         if (p.w == 0.f) continue;
         const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
         const float d2 = sqdist(ex, ey, ez);
