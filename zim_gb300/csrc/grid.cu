@@ -118,15 +118,18 @@ __global__ void stats_init_kernel(GridStats* s) {
 // not depend on the order blocks finish in.
 constexpr int SPACING_BLOCKS = 1024;
 
-// pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count
+// pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count.
+// Counts are integers (exact); a thread's spacings add in FP32 (they only set
+// the cell size) and go to FP64 once, for the fixed-order totals.
 __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
                                 GridStats* s, double* __restrict__ part) {
     const size_t n = (size_t)rows * cols;
-    double d = 0, c = 0, nv = 0;
+    float df = 0.f;
+    unsigned ci = 0u, nvi = 0u;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (!mask[i]) continue;
-        nv += 1;
+        nvi++;
         const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
         for (int a = 0; a < 3; a++) {
             mn[a] = min(mn[a], fbits(p[a]));
@@ -134,13 +137,13 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
         }
         if ((i % cols) + 1 < (size_t)cols && mask[i + 1]) {
             float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
-            d += sqrtf(dx * dx + dy * dy + dz * dz);
-            c += 1;
+            df += sqrtf(dx * dx + dy * dy + dz * dz);
+            ci++;
         }
     }
-    d = block_reduce(d, Add(), 0.0);
-    c = block_reduce(c, Add(), 0.0);
-    nv = block_reduce(nv, Add(), 0.0);
+    double d = block_reduce((double)df, Add(), 0.0);
+    double c = block_reduce((double)ci, Add(), 0.0);
+    double nv = block_reduce((double)nvi, Add(), 0.0);
     for (int a = 0; a < 3; a++) {
         mn[a] = block_reduce(mn[a], Min(), INT_MAX);
         mx[a] = block_reduce(mx[a], Max(), INT_MIN);
@@ -161,15 +164,17 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
                                 const GridStats* __restrict__ s, double* __restrict__ part) {
     const size_t n = (size_t)rows * cols;
     const double m1 = s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 0.0;
-    double d = 0, c = 0;
+    const float cut = (float)(3.0 * m1);  // the pass only sets the cell size
+    float df = 0.f;
+    unsigned ci = 0u;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (!(mask[i] && (i % cols) + 1 < (size_t)cols && mask[i + 1])) continue;
         float dx = xyz[3 * i + 3] - xyz[3 * i], dy = xyz[3 * i + 4] - xyz[3 * i + 1], dz = xyz[3 * i + 5] - xyz[3 * i + 2];
         float v = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (v <= 3.0 * m1) { d += v; c += 1; }
+        if (v <= cut) { df += v; ci++; }
     }
-    d = block_reduce(d, Add(), 0.0);
-    c = block_reduce(c, Add(), 0.0);
+    double d = block_reduce((double)df, Add(), 0.0);
+    double c = block_reduce((double)ci, Add(), 0.0);
     if (threadIdx.x == 0) {
         part[3 * blockIdx.x] = d;
         part[3 * blockIdx.x + 1] = c;
@@ -1495,17 +1500,26 @@ __global__ void __launch_bounds__(HARD_T) sor_hard_kernel(const float* __restric
 // Per-block sums of the mean distances (valid pixels, grid-stride over a fixed
 // number of blocks, so each thread's share is fixed), then a fixed-order total.
 // FP64 runs at a small fraction of the FP32 rate: two double adds per point.
+// A thread's terms add in FP32 with a compensation term (Neumaier: the sum is
+// exact to ~2^-24 of its size, like a double sum of these few terms) and go to
+// FP64 once; no FP64 operation per point.
+__device__ __forceinline__ void comp_add(float& sum, float& comp, float x) {
+    const float t = sum + x;
+    comp += fabsf(sum) >= fabsf(x) ? (sum - t) + x : (x - t) + sum;
+    sum = t;
+}
+
 __global__ void sor_partial_kernel(const uint8_t* __restrict__ mask, const float* __restrict__ md, size_t n,
                                    double* __restrict__ part) {
-    double a = 0, b = 0;
+    float as = 0.f, ac = 0.f, bs = 0.f, bc = 0.f;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (!mask[i]) continue;
         const float m = md[i];
-        a += m;
-        b += (double)(m * m);  // PCL: float square, double sum
+        comp_add(as, ac, m);
+        comp_add(bs, bc, m * m);  // PCL: float square, double sum
     }
-    a = block_reduce(a, Add(), 0.0);
-    b = block_reduce(b, Add(), 0.0);
+    double a = block_reduce((double)as + (double)ac, Add(), 0.0);
+    double b = block_reduce((double)bs + (double)bc, Add(), 0.0);
     if (threadIdx.x == 0) {
         part[2 * blockIdx.x] = a;
         part[2 * blockIdx.x + 1] = b;
