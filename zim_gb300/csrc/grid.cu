@@ -118,14 +118,15 @@ __global__ void stats_init_kernel(GridStats* s) {
 // not depend on the order blocks finish in.
 constexpr int SPACING_BLOCKS = 1024;
 
-// pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count.
-// Counts are integers (exact); a thread's spacings add in FP32 (they only set
-// the cell size) and go to FP64 once, for the fixed-order totals.
+// pass 1: mean spacing of horizontally adjacent valid pixels, bbox, count, and
+// (rays != 0) the largest distance of a point from its pixel ray.  Counts are
+// integers (exact); a thread's spacings add in FP32 (they only set the cell
+// size) and go to FP64 once, for the fixed-order totals.
 __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                                GridStats* s, double* __restrict__ part) {
+                                int rays, zt::RayParams rp, GridStats* s, double* __restrict__ part) {
     const size_t n = (size_t)rows * cols;
     float df = 0.f;
-    unsigned ci = 0u, nvi = 0u;
+    unsigned ci = 0u, nvi = 0u, dev = 0u;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         if (!mask[i]) continue;
@@ -134,6 +135,12 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
         for (int a = 0; a < 3; a++) {
             mn[a] = min(mn[a], fbits(p[a]));
             mx[a] = max(mx[a], fbits(p[a]));
+        }
+        if (rays) {
+            float ax, ay, az;
+            zt::ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
+            const float d = zt::ray_dev(p[0], p[1], p[2], ax, ay, az);
+            dev = max(dev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
         }
         if ((i % cols) + 1 < (size_t)cols && mask[i + 1]) {
             float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
@@ -144,6 +151,10 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
     double d = block_reduce((double)df, Add(), 0.0);
     double c = block_reduce((double)ci, Add(), 0.0);
     double nv = block_reduce((double)nvi, Add(), 0.0);
+    if (rays) {  // uniform
+        dev = __reduce_max_sync(0xffffffffu, dev);
+        if ((threadIdx.x & 31) == 0 && dev) atomicMax(&s->ray_dev_bits, dev);
+    }
     for (int a = 0; a < 3; a++) {
         mn[a] = block_reduce(mn[a], Min(), INT_MAX);
         mx[a] = block_reduce(mx[a], Max(), INT_MIN);
@@ -763,7 +774,6 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
 using zt::RayParams;
 using zt::ray_dir;
 using zt::ray_dev;
-using zt::ray_dev_kernel;
 constexpr int WR = zt::SPIRAL_R;  // window half-size of the fast path
 constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
 constexpr int WN = zt::SPIRAL_N;
@@ -845,7 +855,8 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
                 v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
                 float ax, ay, az;
                 ray_dir(rp, wx, wy, ax, ay, az);
-                tdev = max(tdev, __float_as_uint(ray_dev(v.x, v.y, v.z, ax, ay, az)));
+                const float d = ray_dev(v.x, v.y, v.z, ax, ay, az);
+                tdev = max(tdev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
             }
         }
         W[t] = v;
@@ -1745,13 +1756,16 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     return ZIM_OK;
 }
 
+// rays: pixel rays of the organised cloud, or null; with them the stats also
+// get the largest distance of a point from its ray (ray_dev_bits).
 zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
-                      float factor, bool sort_buckets, GridScratch& G, cudaStream_t st) {
+                      float factor, bool sort_buckets, const RayParams* rays, GridScratch& G, cudaStream_t st) {
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
     const unsigned sblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
-    spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
+    spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, rays ? 1 : 0, rays ? *rays : RayParams{}, G.stats,
+                                         G.part);
     spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats);
     if (!(fixed_cell > 0.f)) {  // the trimmed spacing sets the cell
         spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
@@ -1793,7 +1807,8 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     // finest cell ~ 3.5 x spacing: the (k+1)-th neighbour of a surface point
     // lies within one ring for ~98% of points at k = 30
     float factor = 3.5f * sqrtf(fmaxf(1.0f, (float)mean_k / 30.0f));
-    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, G, st);
+    const RayParams rpw = zt::ray_params(rays);
+    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, rays.valid ? &rpw : nullptr, G, st);
     if (s) return s;
     const Level fine{G.tab[0], G.pts[0], G.tsize[0] - 1};
     float* md = mean_dist ? mean_dist : G.md;
@@ -1801,13 +1816,11 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
     const int window = rays.valid ? 1 : 0;
     if (window) {
-        const RayParams rp = zt::ray_params(rays);
-        ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
-                                                                                     &G.stats->ray_dev_bits);
+        const RayParams rp = rpw;
         const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
         sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md);
-        ctx->launches += 2;
+        ctx->launches += 1;
     }
     const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
     // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
@@ -1849,19 +1862,18 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     zim_status s = carve_grid(ctx, n, 1, G);
     if (s) return s;
     const float rad = (float)(3.0 * sigma);
-    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, false, G, st);
+    const RayParams rpw = zt::ray_params(rays);
+    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, false, rays.valid ? &rpw : nullptr, G, st);
     if (s) return s;
     Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
     const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
     float* pending = nullptr;
     if (rays.valid) {
-        const RayParams rp = zt::ray_params(rays);
-        ray_dev_kernel<<<4 * (ctx->sm_count > 0 ? ctx->sm_count : 152), GB, 0, st>>>(xyz, mask, rows, cols, rp,
-                                                                                     &G.stats->ray_dev_bits);
+        const RayParams rp = rpw;
         dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
         pending = G.md;
         mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);
-        ctx->launches += 2;
+        ctx->launches += 1;
     }
     metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
                                                                         pending, out);

@@ -358,7 +358,8 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
                 if (rays) {
                     float ax, ay, az;
                     zt::ray_dir(rp, gx, gy, ax, ay, az);
-                    tdev = max(tdev, __float_as_uint(zt::ray_dev(v.x, v.y, v.z, ax, ay, az)));
+                    const float d = zt::ray_dev(v.x, v.y, v.z, ax, ay, az);
+                    tdev = max(tdev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
                 }
             }
         }

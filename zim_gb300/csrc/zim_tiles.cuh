@@ -570,23 +570,6 @@ __device__ __forceinline__ float ray_dev(float px, float py, float pz, float ax,
     return sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz))) * rsqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
 }
 
-// Largest distance of a valid point from its pixel ray, as float bits into
-// *dev (atomicMax; *dev starts at 0).
-static __global__ void ray_dev_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                               RayParams rp, unsigned* __restrict__ dev) {
-    const size_t n = (size_t)rows * cols;
-    float m = 0.f;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (!mask[i]) continue;
-        float ax, ay, az;
-        ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
-        const float d = ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
-        m = fmaxf(m, d == d ? d : INFINITY);  // NaN counts as unbounded
-    }
-    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
-    if ((threadIdx.x & 31) == 0 && b) atomicMax(dev, b);
-}
-
 inline RayParams ray_params(const zim_ray_model& r) {
     RayParams p;
     p.cx = r.cx; p.cy = r.cy; p.f = r.f;
