@@ -174,46 +174,52 @@ __device__ __forceinline__ void frame_sums(const T* __restrict__ src, size_t npx
     }
 }
 
+// Raw per-pixel sums of the tile (bx, by) and its 1-pixel halo (clamped to the
+// image) into shared memory, every frequency in one pass: all of a pixel's
+// frame loads are issued before the tile waits.  Ends with a block barrier.
+template <typename T>
+__device__ __forceinline__ void decode_stage_sums(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
+                                                  int tid, DecodeSmem& sm) {
+    const int gx0 = bx * DX - 1, gy0 = by * DY - 1;
+    const size_t npx = (size_t)p.rows * p.cols;
+    for (int h = tid; h < DHX * DHY; h += DX * DY) {
+        const int hy = h / DHX, hx = h - hy * DHX;
+        const int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
+        const size_t pix = (size_t)gy * p.cols + gx;
+#pragma unroll
+        for (int i = 0; i < DEC_MAX_PS; i++) {
+            if (i >= p.n_ps) break;
+            float s, c, m;
+            frame_sums(frames + (size_t)p.fbase[i] * npx + pix, npx, p.shift[i], p.sinv + p.fbase[i],
+                       p.cosv + p.fbase[i], s, c, m);
+            sm.S[i][hy][hx] = s;
+            sm.C[i][hy][hx] = c;
+            sm.M[i][hy][hx] = m;
+        }
+    }
+    __syncthreads();
+}
+
 // Decodes tile (bx, by) of DX x DY pixels with the DX * DY threads of a block
 // (tid = ty * DX + tx).  The pre-blur is linear, so the blurred sums
 // S = -sum sin_k I_k, C = sum cos_k I_k, sum I_k are the 3x3 blur of the raw
-// per-pixel sums: the tile computes them over its 1-pixel halo into shared
-// memory once per frequency.  Ends with every thread past its last shared
-// read, so the caller may start the next tile at once.
+// per-pixel sums, staged over the tile's 1-pixel halo in shared memory (by
+// decode_stage_sums or the caller, before this is called; not with HDR).
+// Ends with every thread past its last shared read, so the caller may start
+// the next tile at once.
 template <typename T>
-__device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
-                                            int tid, DecodeSmem& sm, int32_t* __restrict__ order,
-                                            float* __restrict__ residual, float* __restrict__ mod_out,
-                                            uint8_t* __restrict__ valid_out) {
+__device__ __forceinline__ void decode_finish(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
+                                              int tid, DecodeSmem& sm, int32_t* __restrict__ order,
+                                              float* __restrict__ residual, float* __restrict__ mod_out,
+                                              uint8_t* __restrict__ valid_out) {
     const int tx = tid % DX, ty = tid / DX;
     const int x = bx * DX + tx, y = by * DY + ty;
-    const int gx0 = bx * DX - 1, gy0 = by * DY - 1;
     const size_t npx = (size_t)p.rows * p.cols;
 
     float wrap0 = 0.f, wrap1 = 0.f, wrap2 = 0.f, wrap3 = 0.f;  // named, so they stay in registers
     float mod0 = 0.f;
     bool ok = true;
     const bool inside = x < p.cols && y < p.rows;
-    if (!p.hdr) {
-        // every frequency's halo sums in one pass: all of a pixel's frame loads
-        // are issued before the tile waits
-        for (int h = tid; h < DHX * DHY; h += DX * DY) {
-            const int hy = h / DHX, hx = h - hy * DHX;
-            const int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
-            const size_t pix = (size_t)gy * p.cols + gx;
-#pragma unroll
-            for (int i = 0; i < DEC_MAX_PS; i++) {
-                if (i >= p.n_ps) break;
-                float s, c, m;
-                frame_sums(frames + (size_t)p.fbase[i] * npx + pix, npx, p.shift[i], p.sinv + p.fbase[i],
-                           p.cosv + p.fbase[i], s, c, m);
-                sm.S[i][hy][hx] = s;
-                sm.C[i][hy][hx] = c;
-                sm.M[i][hy][hx] = m;
-            }
-        }
-        __syncthreads();
-    }
     for (int i = 0; i < p.n_ps; i++) {
         const int N = p.shift[i];
         const T* fb = frames + (size_t)p.fbase[i] * npx;
@@ -330,6 +336,16 @@ __device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const 
     order[pix] = ok ? k : (p.hdr ? -1 : 0);  // the HDR decoder marks invalid orders -1
     residual[pix] = r;
     if (valid_out) valid_out[pix] = ok ? 1 : 0;
+}
+
+// One decode tile with its sums staged from global memory.
+template <typename T>
+__device__ __forceinline__ void decode_tile(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
+                                            int tid, DecodeSmem& sm, int32_t* __restrict__ order,
+                                            float* __restrict__ residual, float* __restrict__ mod_out,
+                                            uint8_t* __restrict__ valid_out) {
+    if (!p.hdr) decode_stage_sums(frames, p, bx, by, tid, sm);
+    decode_finish(frames, p, bx, by, tid, sm, order, residual, mod_out, valid_out);
 }
 
 // --------------------------------------------------------------- rectify ----
