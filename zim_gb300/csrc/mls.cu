@@ -3,10 +3,11 @@
 // Reference: PhaseShiftGrayCode3D/src/JSLAB_MLS_Filter.cpp:11-441 (CPU) and
 // JSLAB_MLS_Filter.cu:14-466 (GPU).  Per valid pixel, over the (2hw+1)^2
 // window of valid neighbours within the 3-D cut-off: weights
-// w = exp(-d^2 / 2 sigma^2), weighted centroid, weighted covariance, closed-form
-// symmetric 3x3 eigen-decomposition (normal = smallest eigenvector), then an
-// order-0/1/2 polynomial fit f(u, v) in the tangent frame by Cholesky with the
-// 2 -> 1 -> 0 fallback, and projection of the point onto the fitted surface.
+// w = exp(-d^2 / 2 sigma^2), weighted centroid, weighted covariance, its
+// smallest eigenvector in closed form (the normal), then an order-0/1/2
+// polynomial fit f(u, v) in a tangent frame about the normal by Cholesky with
+// the 2 -> 1 -> 0 fallback, and projection of the point onto the fitted
+// surface.
 // Order selection follows the CPU reference: order drops to 0 when fewer than
 // {3, 5, 8}[order] neighbours.  Coordinates are accumulated relative to the
 // query point, which keeps FP32 sums at millimetre scale.
@@ -18,19 +19,18 @@ namespace {
 
 constexpr int MX = 16, MY = 8;
 
-__device__ void sym_eigen3(const float C[3][3], float ev[3], float E[3][3]) {
+// Unit eigenvector of the smallest eigenvalue of a symmetric 3x3 matrix (the
+// surface normal of a weighted covariance): the eigenvalue in closed form
+// (trigonometric solution of the characteristic cubic), the vector as the
+// longest cross product of two rows of C - lambda I.  Zero when that
+// eigenvalue is not simple enough to give a direction.
+__device__ void sym_normal3(const float C[3][3], float n[3]) {
     const float p1 = C[0][1] * C[0][1] + C[0][2] * C[0][2] + C[1][2] * C[1][2];
-    if (p1 < 1e-20f) {
-        ev[0] = C[0][0]; ev[1] = C[1][1]; ev[2] = C[2][2];
-        int id[3] = {0, 1, 2};
-        for (int i = 0; i < 2; i++)
-            for (int j = i + 1; j < 3; j++)
-                if (ev[i] > ev[j]) {
-                    float t = ev[i]; ev[i] = ev[j]; ev[j] = t;
-                    int ti = id[i]; id[i] = id[j]; id[j] = ti;
-                }
-        for (int i = 0; i < 3; i++)
-            for (int c = 0; c < 3; c++) E[i][c] = (c == id[i]) ? 1.f : 0.f;
+    if (p1 < 1e-20f) {  // diagonal: the axis of the smallest entry
+        int m = 0;
+        if (C[1][1] < C[m][m]) m = 1;
+        if (C[2][2] < C[m][m]) m = 2;
+        n[0] = m == 0 ? 1.f : 0.f; n[1] = m == 1 ? 1.f : 0.f; n[2] = m == 2 ? 1.f : 0.f;
         return;
     }
     const float tr = C[0][0] + C[1][1] + C[2][2];
@@ -47,28 +47,24 @@ __device__ void sym_eigen3(const float C[3][3], float ev[3], float E[3][3]) {
                 B[0][2] * (B[1][0] * B[2][1] - B[1][1] * B[2][0]);
     float r = fminf(1.f, fmaxf(-1.f, det * 0.5f));
     float phi = acosf(r) / 3.0f;
-    ev[0] = q + 2.0f * p * cosf(phi + 2.0f * ZIM_PI_F / 3.0f);
-    ev[2] = q + 2.0f * p * cosf(phi);
-    ev[1] = tr - ev[0] - ev[2];
-    for (int idx = 0; idx < 3; idx++) {
-        float A[3][3];
-        for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) A[i][j] = C[i][j] - (i == j ? ev[idx] : 0.f);
-        float c01[3] = {A[0][1] * A[1][2] - A[0][2] * A[1][1], A[0][2] * A[1][0] - A[0][0] * A[1][2],
-                        A[0][0] * A[1][1] - A[0][1] * A[1][0]};
-        float c02[3] = {A[0][1] * A[2][2] - A[0][2] * A[2][1], A[0][2] * A[2][0] - A[0][0] * A[2][2],
-                        A[0][0] * A[2][1] - A[0][1] * A[2][0]};
-        float c12[3] = {A[1][1] * A[2][2] - A[1][2] * A[2][1], A[1][2] * A[2][0] - A[1][0] * A[2][2],
-                        A[1][0] * A[2][1] - A[1][1] * A[2][0]};
-        float l01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
-        float l02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
-        float l12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
-        float b0 = c12[0], b1 = c12[1], b2 = c12[2], bl = l12;
-        if (l01 > bl) { b0 = c01[0]; b1 = c01[1]; b2 = c01[2]; bl = l01; }
-        if (l02 > bl) { b0 = c02[0]; b1 = c02[1]; b2 = c02[2]; bl = l02; }
-        float il = bl > 1e-20f ? rsqrtf(bl) : 0.f;
-        E[idx][0] = b0 * il; E[idx][1] = b1 * il; E[idx][2] = b2 * il;
-    }
+    const float ev = q + 2.0f * p * cosf(phi + 2.0f * ZIM_PI_F / 3.0f);
+    float A[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) A[i][j] = C[i][j] - (i == j ? ev : 0.f);
+    float c01[3] = {A[0][1] * A[1][2] - A[0][2] * A[1][1], A[0][2] * A[1][0] - A[0][0] * A[1][2],
+                    A[0][0] * A[1][1] - A[0][1] * A[1][0]};
+    float c02[3] = {A[0][1] * A[2][2] - A[0][2] * A[2][1], A[0][2] * A[2][0] - A[0][0] * A[2][2],
+                    A[0][0] * A[2][1] - A[0][1] * A[2][0]};
+    float c12[3] = {A[1][1] * A[2][2] - A[1][2] * A[2][1], A[1][2] * A[2][0] - A[1][0] * A[2][2],
+                    A[1][0] * A[2][1] - A[1][1] * A[2][0]};
+    float l01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
+    float l02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
+    float l12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
+    float b0 = c12[0], b1 = c12[1], b2 = c12[2], bl = l12;
+    if (l01 > bl) { b0 = c01[0]; b1 = c01[1]; b2 = c01[2]; bl = l01; }
+    if (l02 > bl) { b0 = c02[0]; b1 = c02[1]; b2 = c02[2]; bl = l02; }
+    float il = bl > 1e-20f ? rsqrtf(bl) : 0.f;
+    n[0] = b0 * il; n[1] = b1 * il; n[2] = b2 * il;
 }
 
 // Cholesky solve of an N x N system held in registers (every index is a
@@ -77,7 +73,7 @@ __device__ void sym_eigen3(const float C[3][3], float ev[3], float E[3][3]) {
 template <int N>
 __device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const float (&b)[N], float (&x)[N],
                                                const float (&thr)[6]) {
-    float L[N][N];
+    float L[N][N], iL[N];
     bool ok = true;
 #pragma unroll
     for (int i = 0; i < N; i++)
@@ -88,9 +84,11 @@ __device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const flo
             for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
             if (i == j) {
                 ok = ok && s > thr[i];
-                L[i][j] = sqrtf(fmaxf(s, 1e-30f));
+                const float g = fmaxf(s, 1e-30f);
+                iL[i] = rsqrtf(g);  // 1 / L[i][i]: the solves multiply
+                L[i][j] = g * iL[i];
             } else {
-                L[i][j] = s / L[j][j];
+                L[i][j] = s * iL[j];
             }
         }
     float y[N];
@@ -99,14 +97,14 @@ __device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const flo
         float s = b[i];
 #pragma unroll
         for (int k = 0; k < i; k++) s -= L[i][k] * y[k];
-        y[i] = s / L[i][i];
+        y[i] = s * iL[i];
     }
 #pragma unroll
     for (int i = N - 1; i >= 0; i--) {
         float s = y[i];
 #pragma unroll
         for (int k = i + 1; k < N; k++) s -= L[k][i] * x[k];
-        x[i] = s / L[i][i];
+        x[i] = s * iL[i];
     }
     return ok;
 }
@@ -211,30 +209,31 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
     C[0][0] = fmaf(-ws * cx, cx, m00); C[0][1] = fmaf(-ws * cx, cy, m01); C[0][2] = fmaf(-ws * cx, cz, m02);
     C[1][1] = fmaf(-ws * cy, cy, m11); C[1][2] = fmaf(-ws * cy, cz, m12); C[2][2] = fmaf(-ws * cz, cz, m22);
     C[1][0] = C[0][1]; C[2][0] = C[0][2]; C[2][1] = C[1][2];
-    float ev[3], E[3][3];
-    sym_eigen3(C, ev, E);
-    // Orthonormal tangent frame: t1 is re-orthogonalised against the normal and
-    // t2 = n x t1.  Exact eigenvectors already satisfy this (up to sign, which
-    // the projection is invariant to); in FP32 it keeps the polynomial basis
-    // from degenerating when the two in-plane eigenvalues nearly coincide.
-    float nx = E[0][0], ny = E[0][1], nz = E[0][2];
-    float t1x = E[1][0], t1y = E[1][1], t1z = E[1][2];
-    float t2x = E[2][0], t2y = E[2][1], t2z = E[2][2];
+    float nv3[3];
+    sym_normal3(C, nv3);
+    // Orthonormal tangent frame about the normal: the polynomial spaces of
+    // orders 0-2 are unchanged by a rotation of (u, v), so any orthonormal pair
+    // fits the same surface; t1 is the coordinate axis least aligned with the
+    // normal, orthogonalised against it, and t2 = n x t1.  (A zero normal gives
+    // a zero frame: the fit fails and the point stays.)
+    float nx = nv3[0], ny = nv3[1], nz = nv3[2];
+    float t1x = 0.f, t1y = 0.f, t1z = 0.f, t2x = 0.f, t2y = 0.f, t2z = 0.f;
     {
         float nn = nx * nx + ny * ny + nz * nz;
         if (nn > 1e-30f) {
             float in = rsqrtf(nn);
             nx *= in; ny *= in; nz *= in;
-            float d = t1x * nx + t1y * ny + t1z * nz;
-            float ax = t1x - d * nx, ay = t1y - d * ny, az = t1z - d * nz;
-            float aa = ax * ax + ay * ay + az * az;
-            if (aa > 1e-30f) {
-                float ia = rsqrtf(aa);
-                t1x = ax * ia; t1y = ay * ia; t1z = az * ia;
-                t2x = ny * t1z - nz * t1y;
-                t2y = nz * t1x - nx * t1z;
-                t2z = nx * t1y - ny * t1x;
-            }
+            const float ux = fabsf(nx), uy = fabsf(ny), uz = fabsf(nz);
+            const int a = ux <= uy && ux <= uz ? 0 : (uy <= uz ? 1 : 2);
+            const float d = a == 0 ? nx : (a == 1 ? ny : nz);
+            float ax = (a == 0 ? 1.f : 0.f) - d * nx, ay = (a == 1 ? 1.f : 0.f) - d * ny, az = (a == 2 ? 1.f : 0.f) - d * nz;
+            float ia = rsqrtf(ax * ax + ay * ay + az * az);  // >= 2/3: the axis is at least 54.7 deg off the normal
+            t1x = ax * ia; t1y = ay * ia; t1z = az * ia;
+            t2x = ny * t1z - nz * t1y;
+            t2y = nz * t1x - nx * t1z;
+            t2z = nx * t1y - ny * t1x;
+        } else {
+            nx = ny = nz = 0.f;
         }
     }
     const int min_nb = order == 2 ? 8 : (order == 1 ? 5 : 3);
