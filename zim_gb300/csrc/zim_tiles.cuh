@@ -236,9 +236,8 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
                 else if (i == 1) wrap1 = wr;
                 else if (i == 2) wrap2 = wr;
                 else wrap3 = wr;
-                float b = 2.0f * sqrtf(fmaf(S, S, C * C)) / (float)N;
-                float mean = M / (float)N;
-                float nm = mean > 1e-3f ? b / mean : 0.f;
+                // (2 |S, C| / N) / (M / N), one division
+                float nm = M > 1e-3f * (float)N ? 2.0f * sqrtf(fmaf(S, S, C * C)) / M : 0.f;
                 if (i == 0) mod0 = nm;
                 if (nm < p.thr) ok = false;
             }
@@ -260,9 +259,8 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
             else if (i == 1) wrap1 = wr;
             else if (i == 2) wrap2 = wr;
             else wrap3 = wr;
-            float b = 2.0f * sqrtf(fmaf(S, S, C * C)) / (float)N;
-            float mean = M / (float)N;
-            float nm = mean > 1e-3f ? b / mean : 0.f;
+            // normalised modulation (2 |S, C| / N) / (M / N), one division
+            float nm = M > 1e-3f * (float)N ? 2.0f * sqrtf(fmaf(S, S, C * C)) / M : 0.f;
             if (i == 0) mod0 = nm;
             if (nm < p.thr) ok = false;
         }
