@@ -835,10 +835,18 @@ struct WinHeap {
     }
 };
 
+// A query the window pass cannot settle goes straight to the deferred list
+// (md = -1) for the second window pass and the grid searches.
+__device__ __forceinline__ void defer_query(GridStats* s, unsigned* deferred, float* md_out, size_t i) {
+    md_out[i] = -1.f;
+    deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
+}
+
 __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restrict__ xyz,
                                                             const uint8_t* __restrict__ mask, int rows, int cols,
-                                                            int k, RayParams rp, const GridStats* __restrict__ s,
-                                                            float* __restrict__ md_out) {
+                                                            int k, RayParams rp, GridStats* __restrict__ s,
+                                                            float* __restrict__ md_out,
+                                                            unsigned* __restrict__ deferred) {
     extern __shared__ float4 win_smem[];
     float4* W = win_smem;                                      // WW x WH window, w = 1 valid
     float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1) x TILE_T heaps
@@ -888,7 +896,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
         heap.at(cnt++) = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
     }
     if (cnt < K1) {
-        md_out[i] = -2.f;
+        defer_query(s, deferred, md_out, i);
         return;
     }
     heap.build();
@@ -934,7 +942,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float rk = sqrtf(kth), ro = (float)(WR + 1);
     const bool ok = C * rbreak / (an + rbreak) - dev > rk && C * ro / (an + ro) - dev_out > rk;
     if (!ok) {
-        md_out[i] = -2.f;
+        defer_query(s, deferred, md_out, i);
         return;
     }
     const int e = root_exponent(kth);
@@ -1757,9 +1765,11 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
 }
 
 // rays: pixel rays of the organised cloud, or null; with them the stats also
-// get the largest distance of a point from its ray (ray_dev_bits).
+// get the largest distance of a point from its ray (ray_dev_bits).  Levels
+// below first_level get their cell sizes but no tables.
 zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
-                      float factor, bool sort_buckets, const RayParams* rays, GridScratch& G, cudaStream_t st) {
+                      float factor, bool sort_buckets, const RayParams* rays, GridScratch& G, cudaStream_t st,
+                      int first_level = 0) {
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
@@ -1774,7 +1784,7 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     }
     cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
     ctx->launches += 4;
-    for (int l = 0; l < G.levels; l++) {
+    for (int l = first_level; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
         ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
         hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts);
@@ -1808,7 +1818,10 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     // lies within one ring for ~98% of points at k = 30
     float factor = 3.5f * sqrtf(fmaxf(1.0f, (float)mean_k / 30.0f));
     const RayParams rpw = zt::ray_params(rays);
-    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, rays.valid ? &rpw : nullptr, G, st);
+    // with pixel rays the window passes and the coarse level settle every
+    // query: the finest level (the tile search's) is not built
+    s = build_grid(ctx, xyz, mask, rows, cols, 0.f, factor, false, rays.valid ? &rpw : nullptr, G, st,
+                   rays.valid ? 1 : 0);
     if (s) return s;
     const Level fine{G.tab[0], G.pts[0], G.tsize[0] - 1};
     float* md = mean_dist ? mean_dist : G.md;
@@ -1819,14 +1832,17 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         const RayParams rp = rpw;
         const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md);
+        sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred);
+        ctx->launches += 1;
+    } else {
+        // without pixel rays every query starts on the finest grid level
+        const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
+        // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+        sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
+                                                        0);
         ctx->launches += 1;
     }
-    const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
-    // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
-    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-    sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
-                                                    window);
     if (window) {
         const RayParams rp = zt::ray_params(rays);
         sor_far_window_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
@@ -1840,7 +1856,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     // a few hard queries per cloud: one CTA each
     sor_hard_kernel<<<2 * sms, HARD_T, 0, st>>>(xyz, mean_k, G.stats, G.occ, G.pts[1], G.hard, md, G.bound,
                                                 ctx->d_error);
-    ctx->launches += 4;
+    ctx->launches += 3;
     const unsigned nblk = (unsigned)((n + GB - 1) / GB);
     const unsigned pblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
     sor_partial_kernel<<<pblk, GB, 0, st>>>(mask, md, n, G.part);
