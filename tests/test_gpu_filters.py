@@ -226,6 +226,35 @@ def test_metric_gaussian_window_path_matches_grid_path(ctx, oracle_lib):
 
 
 @pytest.mark.gpu
+def test_metric_gaussian_pending_queries_take_the_grid(ctx, oracle_lib):
+    """Points moved 30 mm off their pixel rays make the ray bound useless for
+    every query, so with pixel rays the window pass leaves them all to the
+    grid (built on demand): the same bits as the grid-only path (the cloud
+    padded by an invalid column has no rays), and the oracle's values."""
+    from zim_gb300 import api
+    xyz, mask = cloud(ctx, oracle_lib)
+    H, W = mask.shape
+    x = xyz.cpu().numpy().copy()
+    m = mask.cpu().numpy()
+    idx = np.flatnonzero(m.reshape(-1))[::9973][:20]
+    x.reshape(-1, 3)[idx, 0] += 30.0
+    xt = torch.from_numpy(x).cuda()
+    out = api.filter_metric_gaussian(ctx, xt, mask, 0.5)
+    xp = torch.zeros((H, W + 1, 3), dtype=torch.float32, device="cuda")
+    mp = torch.zeros((H, W + 1), dtype=torch.uint8, device="cuda")
+    xp[:, :W] = xt
+    mp[:, :W] = mask
+    out2 = api.filter_metric_gaussian(ctx, xp.contiguous(), mp.contiguous(), 0.5)
+    assert torch.equal(out, out2[:, :W].contiguous())
+    ox, near = oracle_lib.metric_gaussian(x, m, 0.5, eps=EPS)
+    g = out.cpu().numpy()
+    sel = (m > 0) & (near == 0)
+    err = report("metric_gaussian pending", g, ox, sel)
+    assert ((err > point_tol(ox[sel])).any(axis=1)).mean() <= 1e-3
+    assert ctx.check_device() == 0
+
+
+@pytest.mark.gpu
 def test_metric_gaussian_parity(ctx, oracle_lib):
     from zim_gb300 import api
     xyz, mask = cloud(ctx, oracle_lib)

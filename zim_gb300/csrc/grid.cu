@@ -73,6 +73,7 @@ struct GridStats {
     int keep_all;
     unsigned ray_dev_bits;         // largest distance of a point from its pixel ray (float bits)
     unsigned n_deferred, n_occ, p2_next, n_hard;
+    unsigned n_pending;            // metric Gaussian: queries the window pass left to the grid
 };
 
 __device__ __forceinline__ int fbits(float f) {
@@ -108,7 +109,7 @@ struct Max { __device__ int operator()(int a, int b) const { return a > b ? a : 
 __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
-    s->n_deferred = s->n_occ = s->p2_next = s->n_hard = 0;
+    s->n_deferred = s->n_occ = s->p2_next = s->n_hard = s->n_pending = 0;
     s->ray_dev_bits = 0u;
     for (int a = 0; a < 3; a++) { s->bbox_min[a] = INT_MAX; s->bbox_max[a] = INT_MIN; }
 }
@@ -315,11 +316,16 @@ __device__ __forceinline__ unsigned grid_slot(const GridStats* __restrict__ s, i
     return ((unsigned)iz * (unsigned)s->dims[1] + (unsigned)iy) * (unsigned)s->dims[0] + (unsigned)ix;
 }
 
+// The table-build kernels take a gate: when it points to 0 the tables are not
+// needed (no query is left for the grid) and every block returns at once.
+__device__ __forceinline__ bool gated_off(const unsigned* gate) { return gate && *gate == 0u; }
+
 // Neighbouring pixels mostly share a cell, so the lanes of a warp that hit the
 // same slot add to it once (the lowest such lane).
 __global__ void hash_count_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                   const GridStats* __restrict__ s, int level, unsigned tmask,
-                                  unsigned* __restrict__ counts) {
+                                  unsigned* __restrict__ counts, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool v = i < n && mask[i];
     const unsigned h = v ? grid_slot(s, level, tmask, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) : 0xffffffffu;
@@ -350,7 +356,8 @@ __device__ __forceinline__ unsigned block_scan_incl(unsigned v, unsigned* ws) {
 
 // exclusive scan of the counts into tab[].x (per-block part), block totals
 __global__ void scan_blocks_kernel(const unsigned* __restrict__ counts, uint2* __restrict__ tab, size_t n,
-                                   unsigned* __restrict__ block_tot) {
+                                   unsigned* __restrict__ block_tot, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     __shared__ unsigned ws[32];
     size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
     unsigned v = i < n ? counts[i] : 0u;
@@ -359,7 +366,8 @@ __global__ void scan_blocks_kernel(const unsigned* __restrict__ counts, uint2* _
     if (threadIdx.x == SCAN_B - 1) block_tot[blockIdx.x] = incl;
 }
 
-__global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb) {
+__global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     __shared__ unsigned carry;
     __shared__ unsigned ws[32];
     if (threadIdx.x == 0) carry = 0;
@@ -376,7 +384,9 @@ __global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb) {
     }
 }
 
-__global__ void scan_add_kernel(uint2* __restrict__ tab, size_t n, const unsigned* __restrict__ tot) {
+__global__ void scan_add_kernel(uint2* __restrict__ tab, size_t n, const unsigned* __restrict__ tot,
+                                const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
     if (i < n) tab[i].x += tot[blockIdx.x];
 }
@@ -384,7 +394,8 @@ __global__ void scan_add_kernel(uint2* __restrict__ tab, size_t n, const unsigne
 __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                     const GridStats* __restrict__ s, int level, unsigned tmask,
                                     const uint2* __restrict__ tab, unsigned* __restrict__ fill,
-                                    float4* __restrict__ pts) {
+                                    float4* __restrict__ pts, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool v = i < n && mask[i];
     float x = 0.f, y = 0.f, z = 0.f;
@@ -1597,7 +1608,7 @@ constexpr int GW = TILE_X + 2 * WRG, GH = TILE_Y + 2 * WRG;
 __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restrict__ xyz,
                                                            const uint8_t* __restrict__ mask, int rows, int cols,
                                                            float r, float inv2s2, RayParams rp,
-                                                           const GridStats* __restrict__ s,
+                                                           GridStats* __restrict__ s,
                                                            float* __restrict__ pending, float* __restrict__ out) {
     __shared__ float4 W[GW * GH];
     const int tid = threadIdx.x;
@@ -1635,6 +1646,7 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     const float rs = C > sd ? sd * an / (C - sd) : INFINITY;
     if (!(rs < (float)(WRG + 1))) {
         pending[i] = -2.f;
+        atomicAdd(&s->n_pending, 1u);  // the grid gets built
         return;
     }
     const float r2 = r * r;
@@ -1662,6 +1674,7 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
 __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                        float r2, float inv2s2, Level g, const GridStats* __restrict__ s,
                                        const float* __restrict__ pending, float* __restrict__ out) {
+    if (pending && s->n_pending == 0u) return;  // the window pass settled every query
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (pending && pending[i] != -2.f) return;  // settled by the window pass
@@ -1764,12 +1777,10 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     return ZIM_OK;
 }
 
-// rays: pixel rays of the organised cloud, or null; with them the stats also
-// get the largest distance of a point from its ray (ray_dev_bits).  Levels
-// below first_level get their cell sizes but no tables.
-zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
-                      float factor, bool sort_buckets, const RayParams* rays, GridScratch& G, cudaStream_t st,
-                      int first_level = 0) {
+// The grid's statistics (spacing, bounding box, cell sizes; with pixel rays
+// also the largest distance of a point from its ray, ray_dev_bits).
+zim_status grid_stats(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
+                      float factor, const RayParams* rays, GridScratch& G, cudaStream_t st) {
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
     stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
@@ -1784,15 +1795,25 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     }
     cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
     ctx->launches += 4;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
+
+// The levels' tables from first_level up (counting sort of the points by
+// slot); gate as for the table kernels (null: always built).
+zim_status grid_tables(zim_ctx* ctx, const float* xyz, const uint8_t* mask, size_t n, bool sort_buckets,
+                       GridScratch& G, cudaStream_t st, int first_level = 0, const unsigned* gate = nullptr) {
+    const unsigned nblk = (unsigned)((n + GB - 1) / GB);
     for (int l = first_level; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
         ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
-        hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts);
-        scan_blocks_kernel<<<nb, SCAN_B, 0, st>>>(G.counts, G.tab[l], T, G.tot);
-        scan_totals_kernel<<<1, SCAN_B, 0, st>>>(G.tot, (int)nb);
-        scan_add_kernel<<<nb, SCAN_B, 0, st>>>(G.tab[l], T, G.tot);
+        hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts, gate);
+        scan_blocks_kernel<<<nb, SCAN_B, 0, st>>>(G.counts, G.tab[l], T, G.tot, gate);
+        scan_totals_kernel<<<1, SCAN_B, 0, st>>>(G.tot, (int)nb, gate);
+        scan_add_kernel<<<nb, SCAN_B, 0, st>>>(G.tab[l], T, G.tot, gate);
         ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
-        hash_scatter_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.tab[l], G.counts, G.pts[l]);
+        hash_scatter_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.tab[l], G.counts, G.pts[l],
+                                                  gate);
         ctx->launches += 5;
         if (sort_buckets) {
             bucket_sort_kernel<<<(T + GB - 1) / GB, GB, 0, st>>>(G.tab[l], T, G.pts[l]);
@@ -1801,6 +1822,15 @@ zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     }
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
+}
+
+// Statistics and tables (levels from first_level up).
+zim_status build_grid(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
+                      float factor, bool sort_buckets, const RayParams* rays, GridScratch& G, cudaStream_t st,
+                      int first_level = 0) {
+    zim_status s = grid_stats(ctx, xyz, mask, rows, cols, fixed_cell, factor, rays, G, st);
+    if (s) return s;
+    return grid_tables(ctx, xyz, mask, (size_t)rows * cols, sort_buckets, G, st, first_level);
 }
 
 }  // namespace
@@ -1879,7 +1909,7 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     if (s) return s;
     const float rad = (float)(3.0 * sigma);
     const RayParams rpw = zt::ray_params(rays);
-    s = build_grid(ctx, xyz, mask, rows, cols, rad, 1.0f, false, rays.valid ? &rpw : nullptr, G, st);
+    s = grid_stats(ctx, xyz, mask, rows, cols, rad, 1.0f, rays.valid ? &rpw : nullptr, G, st);
     if (s) return s;
     Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
     const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
@@ -1891,6 +1921,10 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);
         ctx->launches += 1;
     }
+    // the grid only for the queries the window pass left (built, then skipped
+    // on the device when there are none)
+    s = grid_tables(ctx, xyz, mask, n, false, G, st, 0, pending ? &G.stats->n_pending : nullptr);
+    if (s) return s;
     metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
                                                                         pending, out);
     ctx->launches += 1;
