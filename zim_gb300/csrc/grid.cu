@@ -32,6 +32,7 @@
 // cloud most queries are settled from their pixel window alone, certified
 // exact by a bound on the distance to every point seen along another pixel's
 // ray; only the queries the bound does not certify reach the grid searches.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -106,6 +107,10 @@ struct Add { template <typename T> __device__ T operator()(T a, T b) const { ret
 struct Min { __device__ int operator()(int a, int b) const { return a < b ? a : b; } };
 struct Max { __device__ int operator()(int a, int b) const { return a > b ? a : b; } };
 
+// The build kernels take a gate: when it points to 0 the grid is not needed
+// (no query is left for it) and every block returns at once.
+__device__ __forceinline__ bool gated_off(const unsigned* gate) { return gate && *gate == 0u; }
+
 __global__ void stats_init_kernel(GridStats* s) {
     s->sp_sum = s->sp_cnt = s->sp2_sum = s->sp2_cnt = 0;
     s->md_sum = s->md_sq = s->n_valid = 0;
@@ -124,7 +129,9 @@ constexpr int SPACING_BLOCKS = 1024;
 // integers (exact); a thread's spacings add in FP32 (they only set the cell
 // size) and go to FP64 once, for the fixed-order totals.
 __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                                int rays, zt::RayParams rp, GridStats* s, double* __restrict__ part) {
+                                int rays, zt::RayParams rp, GridStats* s, double* __restrict__ part,
+                                const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     const size_t n = (size_t)rows * cols;
     float df = 0.f;
     unsigned ci = 0u, nvi = 0u, dev = 0u;
@@ -173,7 +180,9 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
 
 // pass 2: mean spacing over pairs closer than 3x the pass-1 mean
 __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows, int cols,
-                                const GridStats* __restrict__ s, double* __restrict__ part) {
+                                const GridStats* __restrict__ s, double* __restrict__ part,
+                                const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     const size_t n = (size_t)rows * cols;
     const double m1 = s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 0.0;
     const float cut = (float)(3.0 * m1);  // the pass only sets the cell size
@@ -197,7 +206,9 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
 // Fixed-order total of the spacing passes' block partials (one block of
 // SPACING_BLOCKS threads).  pass 1 sets the mean spacing and the valid count,
 // pass 2 the trimmed mean spacing.
-__global__ void spacing_total_kernel(const double* __restrict__ part, int nblk, int pass, GridStats* s) {
+__global__ void spacing_total_kernel(const double* __restrict__ part, int nblk, int pass, GridStats* s,
+                                     const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     const int t = threadIdx.x;
     double d = t < nblk ? part[3 * t] : 0.0, c = t < nblk ? part[3 * t + 1] : 0.0;
     double nv = t < nblk ? part[3 * t + 2] : 0.0;
@@ -220,7 +231,8 @@ __global__ void spacing_total_kernel(const double* __restrict__ part, int nblk, 
 // hashed level).  The coarse level is a dense grid over the bounding box with
 // cells of COARSE_MULT finest cells, enlarged until it has at most DENSE_MAX
 // cells.  The cell sizes only affect speed, never the result.
-__global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int levels) {
+__global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int levels, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
     float cell = fixed_cell;
     if (!(cell > 0.f)) {
         double sp = s->sp2_cnt > 0 ? s->sp2_sum / s->sp2_cnt : 1.0;
@@ -315,10 +327,6 @@ __device__ __forceinline__ unsigned grid_slot(const GridStats* __restrict__ s, i
     int iz = min(max(__float2int_rd((z - s->org[2]) * ic), 0), s->dims[2] - 1);
     return ((unsigned)iz * (unsigned)s->dims[1] + (unsigned)iy) * (unsigned)s->dims[0] + (unsigned)ix;
 }
-
-// The table-build kernels take a gate: when it points to 0 the tables are not
-// needed (no query is left for the grid) and every block returns at once.
-__device__ __forceinline__ bool gated_off(const unsigned* gate) { return gate && *gate == 0u; }
 
 // Neighbouring pixels mostly share a cell, so the lanes of a warp that hit the
 // same slot add to it once (the lowest such lane).
@@ -1777,24 +1785,68 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     return ZIM_OK;
 }
 
+// Largest distance of a valid point from its pixel ray into ray_dev_bits (NaN
+// counts as unbounded): grid-stride, four pixels' loads in flight per thread,
+// one atomic per block.
+__global__ void ray_dev_max_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
+                                   int cols, zt::RayParams rp, GridStats* s) {
+    __shared__ unsigned wmax[GB / 32];
+    const size_t n = (size_t)rows * cols, stride = (size_t)gridDim.x * blockDim.x;
+    unsigned dev = 0u;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        float p[4][3];
+        bool v[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const size_t i = i0 + r * stride;
+            v[r] = i < n && mask[i];
+            p[r][0] = v[r] ? xyz[3 * i] : 0.f;
+            p[r][1] = v[r] ? xyz[3 * i + 1] : 0.f;
+            p[r][2] = v[r] ? xyz[3 * i + 2] : 0.f;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            if (!v[r]) continue;
+            const size_t i = i0 + r * stride;
+            float ax, ay, az;
+            zt::ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
+            const float d = zt::ray_dev(p[r][0], p[r][1], p[r][2], ax, ay, az);
+            dev = max(dev, __float_as_uint(d == d ? d : INFINITY));
+        }
+    }
+    dev = __reduce_max_sync(0xffffffffu, dev);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = dev;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int j = 1; j < GB / 32; j++) dev = max(dev, wmax[j]);
+        if (dev) atomicMax(&s->ray_dev_bits, dev);
+    }
+}
+
 // The grid's statistics (spacing, bounding box, cell sizes; with pixel rays
 // also the largest distance of a point from its ray, ray_dev_bits).
+// init = false: the stats were zeroed already (and may hold counts); gate as
+// for the build kernels.
 zim_status grid_stats(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols, float fixed_cell,
-                      float factor, const RayParams* rays, GridScratch& G, cudaStream_t st) {
+                      float factor, const RayParams* rays, GridScratch& G, cudaStream_t st, bool init = true,
+                      const unsigned* gate = nullptr) {
     size_t n = (size_t)rows * cols;
     unsigned nblk = (unsigned)((n + GB - 1) / GB);
-    stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
+    if (init) {
+        stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
+        ctx->launches += 1;
+    }
     const unsigned sblk = nblk < (unsigned)SPACING_BLOCKS ? nblk : (unsigned)SPACING_BLOCKS;
     spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, rays ? 1 : 0, rays ? *rays : RayParams{}, G.stats,
-                                         G.part);
-    spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats);
+                                         G.part, gate);
+    spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats, gate);
     if (!(fixed_cell > 0.f)) {  // the trimmed spacing sets the cell
-        spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part);
-        spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats);
+        spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part, gate);
+        spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats, gate);
         ctx->launches += 2;
     }
-    cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels);
-    ctx->launches += 4;
+    cell_kernel<<<1, 1, 0, st>>>(G.stats, fixed_cell, factor, G.levels, gate);
+    ctx->launches += 3;
     ZIM_LAUNCH_CHECK(ctx);
     return ZIM_OK;
 }
@@ -1909,8 +1961,18 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     if (s) return s;
     const float rad = (float)(3.0 * sigma);
     const RayParams rpw = zt::ray_params(rays);
-    s = grid_stats(ctx, xyz, mask, rows, cols, rad, 1.0f, rays.valid ? &rpw : nullptr, G, st);
-    if (s) return s;
+    if (rays.valid) {
+        // the window pass needs only the largest ray distance; the grid's
+        // statistics wait for the window pass's verdict
+        stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
+        const unsigned dblk = (unsigned)std::min<size_t>((n + 4 * GB - 1) / (4 * GB),
+                                                         (size_t)8 * (ctx->sm_count > 0 ? ctx->sm_count : 152));
+        ray_dev_max_kernel<<<dblk, GB, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats);
+        ctx->launches += 2;
+    } else {
+        s = grid_stats(ctx, xyz, mask, rows, cols, rad, 1.0f, nullptr, G, st);
+        if (s) return s;
+    }
     Level g{G.tab[0], G.pts[0], G.tsize[0] - 1};
     const float inv2s2 = (float)(1.0 / (2.0 * sigma * sigma));
     float* pending = nullptr;
@@ -1921,8 +1983,12 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);
         ctx->launches += 1;
     }
-    // the grid only for the queries the window pass left (built, then skipped
-    // on the device when there are none)
+    // the grid only for the queries the window pass left (launched, and
+    // skipped on the device when there are none)
+    if (pending) {
+        s = grid_stats(ctx, xyz, mask, rows, cols, rad, 1.0f, nullptr, G, st, false, &G.stats->n_pending);
+        if (s) return s;
+    }
     s = grid_tables(ctx, xyz, mask, n, false, G, st, 0, pending ? &G.stats->n_pending : nullptr);
     if (s) return s;
     metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
