@@ -132,30 +132,32 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
                                 int rays, zt::RayParams rp, GridStats* s, double* __restrict__ part,
                                 const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
-    const size_t n = (size_t)rows * cols;
     float df = 0.f;
     unsigned ci = 0u, nvi = 0u, dev = 0u;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (!mask[i]) continue;
-        nvi++;
-        const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-        for (int a = 0; a < 3; a++) {
-            mn[a] = min(mn[a], fbits(p[a]));
-            mx[a] = max(mx[a], fbits(p[a]));
+    // blocks over rows, threads over a row's pixels: no index division
+    for (int y = blockIdx.x; y < rows; y += gridDim.x)
+        for (int x = threadIdx.x; x < cols; x += blockDim.x) {
+            const size_t i = (size_t)y * cols + x;
+            if (!mask[i]) continue;
+            nvi++;
+            const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+            for (int a = 0; a < 3; a++) {
+                mn[a] = min(mn[a], fbits(p[a]));
+                mx[a] = max(mx[a], fbits(p[a]));
+            }
+            if (rays) {
+                float ax, ay, az;
+                zt::ray_dir(rp, x, y, ax, ay, az);
+                const float d = zt::ray_dev(p[0], p[1], p[2], ax, ay, az);
+                dev = max(dev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
+            }
+            if (x + 1 < cols && mask[i + 1]) {
+                float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
+                df += sqrtf(dx * dx + dy * dy + dz * dz);
+                ci++;
+            }
         }
-        if (rays) {
-            float ax, ay, az;
-            zt::ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
-            const float d = zt::ray_dev(p[0], p[1], p[2], ax, ay, az);
-            dev = max(dev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
-        }
-        if ((i % cols) + 1 < (size_t)cols && mask[i + 1]) {
-            float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
-            df += sqrtf(dx * dx + dy * dy + dz * dz);
-            ci++;
-        }
-    }
     double d = block_reduce((double)df, Add(), 0.0);
     double c = block_reduce((double)ci, Add(), 0.0);
     double nv = block_reduce((double)nvi, Add(), 0.0);
@@ -183,17 +185,19 @@ __global__ void spacing2_kernel(const float* __restrict__ xyz, const uint8_t* __
                                 const GridStats* __restrict__ s, double* __restrict__ part,
                                 const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
-    const size_t n = (size_t)rows * cols;
     const double m1 = s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 0.0;
     const float cut = (float)(3.0 * m1);  // the pass only sets the cell size
     float df = 0.f;
     unsigned ci = 0u;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        if (!(mask[i] && (i % cols) + 1 < (size_t)cols && mask[i + 1])) continue;
-        float dx = xyz[3 * i + 3] - xyz[3 * i], dy = xyz[3 * i + 4] - xyz[3 * i + 1], dz = xyz[3 * i + 5] - xyz[3 * i + 2];
-        float v = sqrtf(dx * dx + dy * dy + dz * dz);
-        if (v <= cut) { df += v; ci++; }
-    }
+    for (int y = blockIdx.x; y < rows; y += gridDim.x)
+        for (int x = threadIdx.x; x + 1 < cols; x += blockDim.x) {
+            const size_t i = (size_t)y * cols + x;
+            if (!(mask[i] && mask[i + 1])) continue;
+            float dx = xyz[3 * i + 3] - xyz[3 * i], dy = xyz[3 * i + 4] - xyz[3 * i + 1],
+                  dz = xyz[3 * i + 5] - xyz[3 * i + 2];
+            float v = sqrtf(dx * dx + dy * dy + dz * dz);
+            if (v <= cut) { df += v; ci++; }
+        }
     double d = block_reduce((double)df, Add(), 0.0);
     double c = block_reduce((double)ci, Add(), 0.0);
     if (threadIdx.x == 0) {
@@ -1786,34 +1790,21 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
 }
 
 // Largest distance of a valid point from its pixel ray into ray_dev_bits (NaN
-// counts as unbounded): grid-stride, four pixels' loads in flight per thread,
-// one atomic per block.
+// counts as unbounded): blocks over rows, threads over a row's pixels, one
+// atomic per block.
 __global__ void ray_dev_max_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
                                    int cols, zt::RayParams rp, GridStats* s) {
     __shared__ unsigned wmax[GB / 32];
-    const size_t n = (size_t)rows * cols, stride = (size_t)gridDim.x * blockDim.x;
     unsigned dev = 0u;
-    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
-        float p[4][3];
-        bool v[4];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const size_t i = i0 + r * stride;
-            v[r] = i < n && mask[i];
-            p[r][0] = v[r] ? xyz[3 * i] : 0.f;
-            p[r][1] = v[r] ? xyz[3 * i + 1] : 0.f;
-            p[r][2] = v[r] ? xyz[3 * i + 2] : 0.f;
-        }
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            if (!v[r]) continue;
-            const size_t i = i0 + r * stride;
+    for (int y = blockIdx.x; y < rows; y += gridDim.x)
+        for (int x = threadIdx.x; x < cols; x += blockDim.x) {
+            const size_t i = (size_t)y * cols + x;
+            if (!mask[i]) continue;
             float ax, ay, az;
-            zt::ray_dir(rp, (int)(i % cols), (int)(i / cols), ax, ay, az);
-            const float d = zt::ray_dev(p[r][0], p[r][1], p[r][2], ax, ay, az);
+            zt::ray_dir(rp, x, y, ax, ay, az);
+            const float d = zt::ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
             dev = max(dev, __float_as_uint(d == d ? d : INFINITY));
         }
-    }
     dev = __reduce_max_sync(0xffffffffu, dev);
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = dev;
     __syncthreads();
@@ -1965,8 +1956,7 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         // the window pass needs only the largest ray distance; the grid's
         // statistics wait for the window pass's verdict
         stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
-        const unsigned dblk = (unsigned)std::min<size_t>((n + 4 * GB - 1) / (4 * GB),
-                                                         (size_t)8 * (ctx->sm_count > 0 ? ctx->sm_count : 152));
+        const unsigned dblk = (unsigned)std::min(rows, 8 * (ctx->sm_count > 0 ? ctx->sm_count : 152));
         ray_dev_max_kernel<<<dblk, GB, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats);
         ctx->launches += 2;
     } else {
