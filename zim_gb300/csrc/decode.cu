@@ -67,7 +67,9 @@ __device__ __forceinline__ bool mbar_wait0(unsigned bar, unsigned polls) {
     return false;
 }
 
-template <typename T>
+// NPS / NS: frequency count and frames per frequency fixed at compile time
+// (0: from p), so the sample loops unroll with constant table offsets.
+template <typename T, int NPS, int NS>
 __global__ void __launch_bounds__(zt::DX* zt::DY) decode_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                      const T* __restrict__ frames, DecodeParams p,
                                                                      int nfr, int32_t* __restrict__ order,
@@ -112,12 +114,16 @@ __global__ void __launch_bounds__(zt::DX* zt::DY) decode_tma_kernel(const __grid
         const int hy = h / zt::DHX, hx = h - hy * zt::DHX;
         const int gy = min(max(gy0 + hy, 0), p.rows - 1), gx = min(max(gx0 + hx, 0), p.cols - 1);
         const T* bp = box + (gy - oy) * BW + (gx - ox);
+        const int n_ps = NPS ? NPS : p.n_ps;
 #pragma unroll
-        for (int i = 0; i < zt::DEC_MAX_PS; i++) {
-            if (i >= p.n_ps) break;
-            const int f0 = p.fbase[i];
+        for (int i = 0; i < (NPS ? NPS : zt::DEC_MAX_PS); i++) {
+            if (i >= n_ps) break;
+            const int f0 = NS ? i * NS : p.fbase[i];  // frequencies' frames are consecutive
+            const int N = NS ? NS : p.shift[i];
             float sv = 0.f, cv = 0.f, mv = 0.f;
-            for (int k = 0; k < p.shift[i]; k++) {
+#pragma unroll
+            for (int k = 0; k < (NS ? NS : 32); k++) {  // 3..32 steps
+                if (k >= N) break;
                 const float v = (float)bp[(f0 + k) * plane];
                 sv = fmaf(-p.sinv[f0 + k], v, sv);
                 cv = fmaf(p.cosv[f0 + k], v, cv);
@@ -129,7 +135,7 @@ __global__ void __launch_bounds__(zt::DX* zt::DY) decode_tma_kernel(const __grid
         }
     }
     __syncthreads();
-    zt::decode_finish<T>(frames, p, bx, by, tid, sm, order, residual, mod_out, valid_out);
+    zt::decode_finish<T, NPS, NS>(frames, p, bx, by, tid, sm, order, residual, mod_out, valid_out);
 }
 
 // cuTensorMapEncodeTiled from the driver, looked up once (no link to libcuda)
@@ -181,8 +187,17 @@ bool launch_decode_tma(zim_ctx* ctx, const void* frames, const DecodeParams& p, 
     int nfr = 0;
     if (!decode_tensor_map<T>(frames, p, &m, &nfr)) return false;
     const size_t dsm = (size_t)tma_bw<T>() * zt::DHY * nfr * sizeof(T);
-    decode_tma_kernel<T><<<grd, blk, dsm, st>>>(m, (const T*)frames, p, nfr, order, residual, mod, valid,
-                                                ctx->d_error);
+    bool four = true;  // every frequency 4-step (the common configurations)
+    for (int i = 0; i < p.n_ps; i++) four = four && p.shift[i] == 4;
+    if (four && p.n_ps == 3)
+        decode_tma_kernel<T, 3, 4><<<grd, blk, dsm, st>>>(m, (const T*)frames, p, nfr, order, residual, mod, valid,
+                                                          ctx->d_error);
+    else if (four && p.n_ps == 1)
+        decode_tma_kernel<T, 1, 4><<<grd, blk, dsm, st>>>(m, (const T*)frames, p, nfr, order, residual, mod, valid,
+                                                          ctx->d_error);
+    else
+        decode_tma_kernel<T, 0, 0><<<grd, blk, dsm, st>>>(m, (const T*)frames, p, nfr, order, residual, mod, valid,
+                                                          ctx->d_error);
     return true;
 }
 

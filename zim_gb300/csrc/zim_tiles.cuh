@@ -206,8 +206,10 @@ __device__ __forceinline__ void decode_stage_sums(const T* __restrict__ frames, 
 // per-pixel sums, staged over the tile's 1-pixel halo in shared memory (by
 // decode_stage_sums or the caller, before this is called; not with HDR).
 // Ends with every thread past its last shared read, so the caller may start
-// the next tile at once.
-template <typename T>
+// the next tile at once.  NPS / NS: the frequency count and the frames per
+// frequency when known at compile time (0: taken from p); the arithmetic is
+// the same either way.
+template <typename T, int NPS = 0, int NS = 0>
 __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, const DecodeParams& p, int bx, int by,
                                               int tid, DecodeSmem& sm, int32_t* __restrict__ order,
                                               float* __restrict__ residual, float* __restrict__ mod_out,
@@ -220,8 +222,11 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
     float mod0 = 0.f;
     bool ok = true;
     const bool inside = x < p.cols && y < p.rows;
-    for (int i = 0; i < p.n_ps; i++) {
-        const int N = p.shift[i];
+    const int n_ps = NPS ? NPS : p.n_ps;
+#pragma unroll
+    for (int i = 0; i < (NPS ? NPS : DEC_MAX_PS); i++) {
+        if (i >= n_ps) break;
+        const int N = NS ? NS : p.shift[i];
         const T* fb = frames + (size_t)p.fbase[i] * npx;
         const float* sv = p.sinv + p.fbase[i];
         const float* cv = p.cosv + p.fbase[i];
@@ -302,13 +307,13 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
             const float wr[4] = {wrap0, wrap1, wrap2, wrap3};
 #pragma unroll
             for (int i = 1; i < 4; i++) {
-                if (i < p.n_ps) {
+                if (i < n_ps) {
                     float a = fmaf(p.fratio[i], wr[i - 1] + ZIM_PI_F, -(wr[i] + ZIM_PI_F)) * ZIM_INV_TWO_PI_F;
                     k = p.iratio[i] * k + (int)roundf(a);
                     r = wr[i];
                 }
             }
-            if (p.n_ps == 1) r = wrap0;
+            if (n_ps == 1) r = wrap0;
         } else {
             const int N = p.shift[0];
             int sum_raw = 0;
