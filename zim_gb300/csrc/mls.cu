@@ -336,12 +336,16 @@ inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * 
 // Every neighbour is a staged pixel, so the bound takes the largest distance of
 // a staged point from its own ray (points smoothed across a depth edge lie far
 // off their rays, but only near the edge).
+// HW: the half-window at compile time (0: the hw argument), which makes the
+// tile width and every neighbour offset constants.
+template <int HW>
 __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restrict__ src,
-                                                          const uint8_t* __restrict__ mask, int rows, int cols, int hw,
+                                                          const uint8_t* __restrict__ mask, int rows, int cols, int hw_arg,
                                                           float inv_2s2, int order, float r2c, int rays,
                                                           zt::RayParams rp, float* __restrict__ dst) {
     extern __shared__ float4 mls_sp[];
     __shared__ unsigned warp_dev[MX * MY / 32];
+    const int hw = HW ? HW : hw_arg;
     const int TW = MX + 2 * hw, TH = MY + 2 * hw;
     const int gx0 = blockIdx.x * MX - hw, gy0 = blockIdx.y * MY - hw;
     const int tid = threadIdx.y * MX + threadIdx.x;
@@ -431,7 +435,8 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const size_t smem = mls_smem_bytes(window);
     const bool use_smem = smem <= 96 * 1024;
     if (use_smem)
-        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(mls_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(window == 7 ? mls_smem_kernel<7> : mls_smem_kernel<0>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int use_rays = use_smem && rays.valid;
     const zt::RayParams rp = zt::ray_params(rays);
     // ping-pong so that the last pass lands in `out`
@@ -440,8 +445,8 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
         if (use_smem)
-            mls_smem_kernel<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp,
-                                                    dst);
+            (window == 7 ? mls_smem_kernel<7> : mls_smem_kernel<0>)<<<grd, blk, smem, st>>>(
+                in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp, dst);
         else
             mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;
