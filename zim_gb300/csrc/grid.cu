@@ -56,7 +56,7 @@ constexpr int TILE_DILATE = 2;        // cells added around a tile's box
 constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
 constexpr int TILE_MAX_CAND = 1536;   // gathered points per tile (a surface tile gathers ~800)
 constexpr int COARSE_MULT = 16;       // coarse level cell = 16 x finest
-constexpr long long DENSE_MAX = 1 << 21;  // cells of the dense coarse level
+constexpr long long DENSE_MAX = 1 << 18;  // cells of the dense coarse level (caps its scans and sweeps)
 
 struct GridStats {
     double sp_sum, sp_cnt;    // spacing pass 1
