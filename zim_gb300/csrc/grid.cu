@@ -508,11 +508,12 @@ constexpr int SV_CAP = 128;  // survivors per warp query (k + 1 <= 64 of them ke
 //    exact.  The warp does this one query at a time, lanes over candidates.
 // Queries the box cannot settle search the finest-level cells that hold the
 // ball of radius sqrt(tau0) (up to FINE_RINGS rings).  Unresolved queries are
-// appended to the deferred list with md = -1.
+// appended to the deferred list with md = -1.  (Clouds with pixel rays skip
+// this phase: the window passes take every query.)
 __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __restrict__ xyz,
                                                               const uint8_t* __restrict__ mask, int rows, int cols,
                                                               int k, Level g, GridStats* s, float* __restrict__ md_out,
-                                                              unsigned* __restrict__ deferred, int unresolved_only) {
+                                                              unsigned* __restrict__ deferred) {
     extern __shared__ float4 tile_smem[];
     float4* cand = tile_smem;                  // TILE_MAX_CAND
     __shared__ int s_off[TILE_MAX_CELLS + 1];  // candidate offset of each box cell
@@ -527,9 +528,8 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
     const int x = x0 + (tid % TILE_X), y = y0 + (tid / TILE_X);
     const bool in = x < cols && y < rows;
     const size_t i = in ? (size_t)y * cols + x : 0;
-    // after the window pass only the queries it left (md = -2) are searched here
-    const bool active = in && mask[i] && s->n_valid > k && (!unresolved_only || md_out[i] == -2.f);
-    if (in && !active && !unresolved_only) md_out[i] = 0.f;
+    const bool active = in && mask[i] && s->n_valid > k;
+    if (in && !active) md_out[i] = 0.f;
     if (!__syncthreads_or(active)) return;  // the whole CTA leaves together
     const float ic = s->inv_cell[0], cell = s->cell[0];
     float qx = 0.f, qy = 0.f, qz = 0.f;
@@ -792,7 +792,8 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
 // averaged across a depth edge lie far off their rays, but only near it), so
 // the spiral stops at the radius that local bound gives and the cloud-wide
 // maximum only has to clear the window's edge.  Queries the bounds do not
-// certify are left to the grid search (md = -2).
+// certify go to the deferred list (md = -1) for the second window pass and
+// the grid searches.
 
 using zt::RayParams;
 using zt::ray_dir;
@@ -1912,8 +1913,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         const size_t tsm = (size_t)TILE_MAX_CAND * sizeof(float4);
         // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-        sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred,
-                                                        0);
+        sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
         ctx->launches += 1;
     }
     if (window) {
