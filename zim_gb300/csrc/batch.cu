@@ -273,6 +273,7 @@ struct zim_batch {
     cudaGraphExec_t exec = nullptr;
     // host layout of the intermediates (for resubmission with another tuning)
     std::vector<PairDev> host_pairs;
+    std::vector<char> tma;  // per pair: decoded by the bulk-copy kernel, not the queue
     size_t items_off = 0;
 };
 
@@ -309,10 +310,11 @@ void build_items(const zim_batch* b, const zim_batch_tuning& t, std::vector<int4
         const zim_batch_pair& p = b->pairs[pi];
         const zim_rect_state& C = b->calibs[p.calib];
         const int trows = (p.rows + zt::DY - 1) / zt::DY;
+        const bool tma = (size_t)pi < b->tma.size() && b->tma[pi];
         for (int cam = 0; cam < 2; cam++)
             for (int r = 0; r < trows; r += t.decode_rows) {
                 const int4 it = make_int4(pi, cam, r, std::min(t.decode_rows, trows - r));
-                items[Q_DECODE].push_back(it);
+                if (!tma) items[Q_DECODE].push_back(it);
                 if (p.decode.post_smooth) items[Q_SMOOTH].push_back(it);  // modes 1 and 2
             }
         for (int r = 0; r < C.rect_h; r += t.match_rows)
@@ -345,6 +347,19 @@ zim_status capture(zim_batch* b) {
     ZIM_CUDA_TRY(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(b->d_counters, 0, NQ * sizeof(unsigned), s);
     const Queues& q = b->q;
+    // pairs the bulk-copy decode takes (its own launch per camera; the same
+    // arithmetic as the queue's tiles)
+    for (size_t pi = 0; pi < b->tma.size(); pi++)
+        if (b->tma[pi]) {
+            const PairDev& D = b->host_pairs[pi];
+            for (int c = 0; c < 2; c++)
+                if (!zim_decode_tma_launch(ctx, D.frames[c], D.sample_type, D.dp, D.order[c], D.res[c], s)) {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(s, &g);
+                    if (g) cudaGraphDestroy(g);
+                    return zim_fail(ctx, ZIM_ERR_CUDA, "batch decode copy path unavailable");
+                }
+        }
     if (q.n[Q_DECODE])
         batch_decode_kernel<<<std::min(b->grid[Q_DECODE], q.n[Q_DECODE]), BT, 0, s>>>(
             b->d_pairs, q.items[Q_DECODE], q.n[Q_DECODE], b->d_counters + Q_DECODE);
@@ -593,6 +608,12 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "batch memory plan overflow");
     b->items_off = (size_t)(cur - (char*)b->d_mem);
     ZIM_CUDA_TRY(ctx, cudaMemcpy(b->d_pairs, b->host_pairs.data(), sizeof(PairDev) * n_pairs, cudaMemcpyHostToDevice));
+    b->tma.assign(n_pairs, 0);
+    for (int i = 0; i < n_pairs; i++) {
+        const PairDev& D = b->host_pairs[i];
+        b->tma[i] = zim_decode_tma_applies(D.frames[0], D.sample_type, D.dp) &&
+                    zim_decode_tma_applies(D.frames[1], D.sample_type, D.dp);
+    }
     return requeue(b);
 }
 

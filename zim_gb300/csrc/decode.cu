@@ -238,6 +238,23 @@ __global__ void phase_f64_kernel(const int32_t* __restrict__ order, const float*
 
 }  // namespace
 
+bool zim_decode_tma_applies(const void* frames, int sample_type, const zt::DecodeParams& p) {
+    CUtensorMap m;
+    int nfr = 0;
+    return sample_type == ZIM_SAMPLE_U8 ? decode_tensor_map<uint8_t>(frames, p, &m, &nfr)
+                                        : decode_tensor_map<uint16_t>(frames, p, &m, &nfr);
+}
+
+bool zim_decode_tma_launch(zim_ctx* ctx, const void* frames, int sample_type, const zt::DecodeParams& p,
+                           int32_t* order, float* residual, cudaStream_t st) {
+    dim3 blk(zt::DX, zt::DY), grd((p.cols + zt::DX - 1) / zt::DX, (p.rows + zt::DY - 1) / zt::DY);
+    const bool ok = sample_type == ZIM_SAMPLE_U8
+                        ? launch_decode_tma<uint8_t>(ctx, frames, p, grd, blk, order, residual, nullptr, nullptr, st)
+                        : launch_decode_tma<uint16_t>(ctx, frames, p, grd, blk, order, residual, nullptr, nullptr, st);
+    if (ok) ctx->launches += 1;
+    return ok;
+}
+
 zim_status zim_decode_launch(zim_ctx* ctx, const zim_decode_config* cfg, const void* frames, int sample_type, int rows,
                              int cols, int32_t* order, float* residual, float* mod, uint8_t* valid, cudaStream_t st) {
     DecodeParams p;

@@ -81,6 +81,14 @@ inline cudaStream_t zim_stream(void* s) { return reinterpret_cast<cudaStream_t>(
 
 // ---- internal launchers (no argument validation; callers validate) ----
 struct zim_decode_params;  // decode.cu
+namespace zt {
+struct DecodeParams;
+}
+// The bulk-tensor-copy decode: whether it applies to these frames (HDR, row
+// pitch, frame count), and its launch (false, and nothing launched, when not).
+bool zim_decode_tma_applies(const void* frames, int sample_type, const zt::DecodeParams& p);
+bool zim_decode_tma_launch(zim_ctx* ctx, const void* frames, int sample_type, const zt::DecodeParams& p,
+                           int32_t* order, float* residual, cudaStream_t st);
 zim_status zim_decode_launch(zim_ctx* ctx, const zim_decode_config* cfg, const void* frames,
                              int sample_type, int rows, int cols, int32_t* order, float* residual,
                              float* mod, uint8_t* valid, cudaStream_t st);
