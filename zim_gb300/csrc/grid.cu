@@ -831,13 +831,17 @@ __device__ __forceinline__ int win_upto(float r2) { return r2 < (float)WR2MAX ? 
 // Per-thread max-heap of the K1 smallest squared distances seen so far, in
 // column tid of a [K1][TILE_T] shared array (conflict-free): the root is the
 // current K1-th smallest, and a nearer point replaces it with one sift-down.
+template <int KC>  // the heap size at compile time (0: K1)
 struct WinHeap {
     float* L;
-    int K1;
+    int K1_;
+    __device__ __forceinline__ int size() const { return KC ? KC : K1_; }
     __device__ __forceinline__ float& at(int j) { return L[j * TILE_T]; }
     // places v at j, moving larger children up
     __device__ __forceinline__ void sift(int j, float v) {
-        for (;;) {
+        const int K1 = size();
+#pragma unroll
+        for (int lev = 0; lev < 6; lev++) {  // a heap of at most 64 entries is 6 levels deep
             int c = 2 * j + 1;
             if (c >= K1) break;
             float cv = at(c);
@@ -855,7 +859,7 @@ struct WinHeap {
         at(j) = v;
     }
     __device__ __forceinline__ void build() {
-        for (int j = K1 / 2 - 1; j >= 0; j--) sift(j, at(j));
+        for (int j = size() / 2 - 1; j >= 0; j--) sift(j, at(j));
     }
 };
 
@@ -866,6 +870,8 @@ __device__ __forceinline__ void defer_query(GridStats* s, unsigned* deferred, fl
     deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
 }
 
+// K1T: k + 1 at compile time (0: from k)
+template <int K1T>
 __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restrict__ xyz,
                                                             const uint8_t* __restrict__ mask, int rows, int cols,
                                                             int k, RayParams rp, GridStats* __restrict__ s,
@@ -908,10 +914,10 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     }
     const int wc = (ty + WR) * WW + tx + WR;
     const float4 q = W[wc];
-    const int K1 = k + 1;
+    const int K1 = K1T ? K1T : k + 1;
     // the query and its first k valid window pixels in spiral order fill the
     // heap; its root (their largest distance) is the first bound
-    WinHeap heap{Ls + tid, K1};
+    WinHeap<K1T> heap{Ls + tid, K1};
     heap.at(0) = 0.f;
     int cnt = 1, o = 0;
     for (; o < WN && cnt < K1; o++) {
@@ -972,7 +978,11 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const int e = root_exponent(kth);
     const float sc = root_scale(e);
     unsigned sum = 0;
-    for (int j = 0; j < K1; j++) sum += root_fixed(heap.at(j), sc);
+#pragma unroll
+    for (int j = 0; j < (K1T ? K1T : 64); j++) {
+        if (j >= K1) break;
+        sum += root_fixed(heap.at(j), sc);
+    }
     md_out[i] = fixed_mean(sum, e, k);
 }
 
@@ -1905,8 +1915,10 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     if (window) {
         const RayParams rp = rpw;
         const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
-        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        sor_window_kernel<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred);
+        // k = 30 (the pipeline's) with a compile-time heap size
+        auto kern = mean_k == 30 ? sor_window_kernel<31> : sor_window_kernel<0>;
+        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+        kern<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred);
         ctx->launches += 1;
     } else {
         // without pixel rays every query starts on the finest grid level
