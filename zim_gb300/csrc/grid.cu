@@ -1915,8 +1915,8 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     if (window) {
         const RayParams rp = rpw;
         const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
-        // k = 30 (the pipeline's) with a compile-time heap size
-        auto kern = mean_k == 30 ? sor_window_kernel<31> : sor_window_kernel<0>;
+        // k = 30 and 50 (the configurations') with a compile-time heap size
+        auto kern = mean_k == 30 ? sor_window_kernel<31> : mean_k == 50 ? sor_window_kernel<51> : sor_window_kernel<0>;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
         kern<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred);
         ctx->launches += 1;
