@@ -1638,7 +1638,9 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
     for (int t = tid; t < GW * GH; t += TILE_T) {
         const int wx = x0 - WRG + t % GW, wy = y0 - WRG + t / GW;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        // invalid and off-image pixels are NaN: their distance test fails
+        const float nan = __int_as_float(0x7fc00000);
+        float4 v = make_float4(nan, nan, nan, 0.f);
         if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
             const size_t j = (size_t)wy * cols + wx;
             if (mask[j]) v = make_float4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 1.f);
@@ -1679,10 +1681,9 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     static_assert(GW == WW && WRG == WR, "the window table's tile");
     for (int o = 0; o < lim; o++) {
         const float4 p = W[wc + win_off(o)];
-        if (p.w == 0.f) continue;
         const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
         const float d2 = sqdist(ex, ey, ez);
-        if (d2 > r2) continue;
+        if (!(d2 <= r2)) continue;  // also every invalid pixel (NaN)
         const float w = __expf(-d2 * inv2s2);
         sx = fmaf(w, ex, sx); sy = fmaf(w, ey, sy); sz = fmaf(w, ez, sz);
         sw += w;
