@@ -886,7 +886,10 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     unsigned tdev = 0u;  // largest dev of this thread's staged points (float bits, >= 0)
     for (int t = tid; t < WW * WH; t += TILE_T) {
         const int wx = x0 - WR + t % WW, wy = y0 - WR + t / WW;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        // invalid and off-image pixels: NaN coordinates (their squared distance
+        // never passes a comparison), w = 0
+        const float nan = __int_as_float(0x7fc00000);
+        float4 v = make_float4(nan, nan, nan, 0.f);
         if (wx >= 0 && wx < cols && wy >= 0 && wy < rows) {
             const size_t j = (size_t)wy * cols + wx;
             if (mask[j]) {
@@ -956,9 +959,8 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     int lim = win_upto(stop_r2(thr));
     for (; o < lim; o++) {
         const float4 p = W[wc + win_off(o)];
-        if (p.w == 0.f) continue;
         const float d2 = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
-        if (d2 < thr) {
+        if (d2 < thr) {  // false for an invalid pixel (NaN)
             heap.sift(0, d2);
             thr = heap.at(0);
             lim = win_upto(stop_r2(thr));
