@@ -597,30 +597,11 @@ inline RayParams ray_params(const zim_ray_model& r) {
     return p;
 }
 
-// pixel offsets of the window ordered by length, then row, then column
+// half-size and offset count of the window-pass windows (the offsets
+// themselves, ordered by length, then row, then column, are a compile-time
+// table beside the kernels)
 constexpr int SPIRAL_R = 7;
 constexpr int SPIRAL_N = (2 * SPIRAL_R + 1) * (2 * SPIRAL_R + 1) - 1;
-__constant__ signed char c_spiral7[SPIRAL_N][2] = {
-    {0, -1}, {-1, 0}, {1, 0}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0}, {2, 0}, {0, 2},
-    {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
-    {0, -3}, {-3, 0}, {3, 0}, {0, 3}, {-1, -3}, {1, -3}, {-3, -1}, {3, -1}, {-3, 1}, {3, 1}, {-1, 3}, {1, 3},
-    {-2, -3}, {2, -3}, {-3, -2}, {3, -2}, {-3, 2}, {3, 2}, {-2, 3}, {2, 3}, {0, -4}, {-4, 0}, {4, 0}, {0, 4},
-    {-1, -4}, {1, -4}, {-4, -1}, {4, -1}, {-4, 1}, {4, 1}, {-1, 4}, {1, 4}, {-3, -3}, {3, -3}, {-3, 3}, {3, 3},
-    {-2, -4}, {2, -4}, {-4, -2}, {4, -2}, {-4, 2}, {4, 2}, {-2, 4}, {2, 4}, {0, -5}, {-3, -4}, {3, -4}, {-4, -3},
-    {4, -3}, {-5, 0}, {5, 0}, {-4, 3}, {4, 3}, {-3, 4}, {3, 4}, {0, 5}, {-1, -5}, {1, -5}, {-5, -1}, {5, -1},
-    {-5, 1}, {5, 1}, {-1, 5}, {1, 5}, {-2, -5}, {2, -5}, {-5, -2}, {5, -2}, {-5, 2}, {5, 2}, {-2, 5}, {2, 5},
-    {-4, -4}, {4, -4}, {-4, 4}, {4, 4}, {-3, -5}, {3, -5}, {-5, -3}, {5, -3}, {-5, 3}, {5, 3}, {-3, 5}, {3, 5},
-    {0, -6}, {-6, 0}, {6, 0}, {0, 6}, {-1, -6}, {1, -6}, {-6, -1}, {6, -1}, {-6, 1}, {6, 1}, {-1, 6}, {1, 6},
-    {-2, -6}, {2, -6}, {-6, -2}, {6, -2}, {-6, 2}, {6, 2}, {-2, 6}, {2, 6}, {-4, -5}, {4, -5}, {-5, -4}, {5, -4},
-    {-5, 4}, {5, 4}, {-4, 5}, {4, 5}, {-3, -6}, {3, -6}, {-6, -3}, {6, -3}, {-6, 3}, {6, 3}, {-3, 6}, {3, 6},
-    {0, -7}, {-7, 0}, {7, 0}, {0, 7}, {-1, -7}, {1, -7}, {-5, -5}, {5, -5}, {-7, -1}, {7, -1}, {-7, 1}, {7, 1},
-    {-5, 5}, {5, 5}, {-1, 7}, {1, 7}, {-4, -6}, {4, -6}, {-6, -4}, {6, -4}, {-6, 4}, {6, 4}, {-4, 6}, {4, 6},
-    {-2, -7}, {2, -7}, {-7, -2}, {7, -2}, {-7, 2}, {7, 2}, {-2, 7}, {2, 7}, {-3, -7}, {3, -7}, {-7, -3}, {7, -3},
-    {-7, 3}, {7, 3}, {-3, 7}, {3, 7}, {-5, -6}, {5, -6}, {-6, -5}, {6, -5}, {-6, 5}, {6, 5}, {-5, 6}, {5, 6},
-    {-4, -7}, {4, -7}, {-7, -4}, {7, -4}, {-7, 4}, {7, 4}, {-4, 7}, {4, 7}, {-6, -6}, {6, -6}, {-6, 6}, {6, 6},
-    {-5, -7}, {5, -7}, {-7, -5}, {7, -5}, {-7, 5}, {7, 5}, {-5, 7}, {5, 7}, {-6, -7}, {6, -7}, {-7, -6}, {7, -6},
-    {-7, 6}, {7, 6}, {-6, 7}, {6, 7}, {-7, -7}, {7, -7}, {-7, 7}, {7, 7},
-};
 
 // -------------------------------------------------- median + reprojection ----
 
