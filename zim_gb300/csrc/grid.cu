@@ -11,27 +11,34 @@
 // Build (no host synchronisation): a trimmed mean of adjacent-pixel spacing
 // sets the finest cell c on the device; the finest level (cell c) is
 // counting-sorted into a power-of-two hash table of (offset, count) pairs, the
-// coarse level (cell >= 16c) into a dense grid over the bounding box.  Exact
-// k-nearest neighbours in two phases:
-//   phase 1: one CTA per 16x8 pixel tile gathers the finest-level points of
-//            the tile's cell box (dilated by TILE_DILATE cells) into shared
-//            memory; every thread scans the same candidate list and is exact
-//            once it holds k + 1 candidates within its distance to the box
-//            boundary;
-//   phase 2: one warp per remaining point searches rings of coarse cells
+// coarse level (cell >= 16c) into a dense grid over the bounding box.
+//
+// SOR on a cloud with pixel rays (the organised cloud of the calibrated size):
+//   window pass: one thread per pixel walks its 15x15 window in a spiral with
+//            a max-heap of the k + 1 nearest, certified exact by a bound on
+//            the distance to every point seen along another pixel's ray;
+//   second window pass: one warp per uncertified point walks pixel rings out
+//            to 24 px with the same certificate;
+//   far search: one warp per remaining point searches rings of coarse cells
 //            around its own until the next ring lies beyond the (k + 1)-th
 //            distance held;
-//   phase 3: the few points still open (far-isolated outliers) take one CTA
-//            each over the coarse level's occupied cells.
-// A visited point's finest cell is re-derived from its coordinates, so hash
-// collisions never count a point twice.  Both filters are deterministic: the
-// SOR statistics are summed in a fixed order, and the Gaussian's grid path sums
-// in 64-bit fixed point (independent of bucket order).
+//   hard search: the few points still open (far-isolated outliers) take one
+//            CTA each over the coarse level's occupied cells.
+// Without pixel rays the first two passes are replaced by the tile search:
+// one CTA per 16x8 pixel tile gathers the finest-level points of the tile's
+// cell box (dilated by TILE_DILATE cells) into shared memory; every thread
+// scans the same candidate list and is exact once it holds k + 1 candidates
+// within its distance to the box boundary.  A visited point's finest cell is
+// re-derived from its coordinates, so hash collisions never count a point
+// twice.  Every path sums the same k + 1 roots in fixed point, so a query's
+// mean distance has the same bits whichever path settles it.
 //
-// Window fast paths (sor_window_kernel, mg_window_kernel): on an organised
-// cloud most queries are settled from their pixel window alone, certified
-// exact by a bound on the distance to every point seen along another pixel's
-// ray; only the queries the bound does not certify reach the grid searches.
+// The metric Gaussian: a window pass with the same ray bound; the queries it
+// cannot certify take the grid path (27 cells of side 3 sigma, 64-bit
+// fixed-point sums), whose build is skipped on the device when none are left.
+// The SOR statistics are summed in a fixed order: both filters are
+// deterministic.
+
 #include <algorithm>
 #include <cfloat>
 #include <climits>
