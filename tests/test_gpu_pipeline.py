@@ -64,7 +64,10 @@ def test_pair_matches_oracle_end_to_end(ctx, oracle_lib, name, kw):
 
 
 @pytest.mark.gpu
-def test_host_entry_equals_device_entry(ctx, oracle_lib):
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_entry_equals_device_entry(ctx, oracle_lib, pinned):
+    """Pageable outputs are copied back; a pinned cloud buffer takes the last
+    stage's writes directly.  Both equal the device entry bit for bit."""
     from zim_gb300 import api
     spec, L, R, _ = scene_data("config1", width=612, height=512)
     ctx.set_calibration(spec.rig.as_dict(), True)
@@ -73,8 +76,13 @@ def test_host_entry_equals_device_entry(ctx, oracle_lib):
                             mls_polynomial_order=2, mls_max_radius=2.0, mls_iterations=1)
     xyz, mask, disp = api.reconstruct_pair(ctx, dcfg, rcfg, torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda(),
                                            want_disp=True)
+    kw = {}
+    if pinned:
+        kw = dict(xyz=torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32).pin_memory(),
+                  mask=torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory())
     hx, hm, hd = api.reconstruct_pair_host(ctx, dcfg, rcfg, L, R,
-                                           disp=np.empty((ctx.rect_h, ctx.rect_w), np.float32))
+                                           disp=np.empty((ctx.rect_h, ctx.rect_w), np.float32), **kw)
+    hx, hm = np.asarray(hx), np.asarray(hm)
     assert np.array_equal(hm, mask.cpu().numpy())
     assert np.array_equal(hx, xyz.cpu().numpy())
     assert np.array_equal(hd, disp.cpu().numpy())

@@ -462,9 +462,23 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     PairBuffers B;
     s = carve_pair(ctx, r, rows, cols, ddisp, B);
     if (s) return s;
-    s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, dxyz, dmask, ddisp, B, st, ctx->aux_event);
+    // A pinned (page-locked) cloud buffer takes the last stage's writes
+    // directly through its device address: the copy back overlaps that
+    // stage.  (Only the last stage writes it; the mask, which later stages
+    // read, stays on the device and is copied.)
+    float* xyz_dev = nullptr;
+    {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, xyz) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+            a.devicePointer != nullptr)
+            xyz_dev = static_cast<float*>(a.devicePointer);
+        else
+            cudaGetLastError();  // pageable memory: clear the query's error, copy back below
+    }
+    s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, xyz_dev ? xyz_dev : dxyz, dmask, ddisp, B, st,
+                 ctx->aux_event);
     if (s) return s;
-    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st));
+    if (!xyz_dev) ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st));
     ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st));
     if (disp) ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(disp, ddisp, dst * 4, cudaMemcpyDeviceToHost, st));
     ZIM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
