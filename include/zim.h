@@ -351,7 +351,10 @@ ZIM_API zim_status zim_reconstruct_pair(zim_ctx* ctx, const zim_decode_config* d
 
 /* The same from HOST buffers (the reference's cv::Mat entry): uploads both frame
  * stacks, runs the pair, downloads xyz and mask (and disp if non-NULL), and
- * synchronises.  Host buffers may be pageable; pinned is faster. */
+ * synchronises.  Host buffers may be pageable; pinned is faster.  A pinned
+ * (page-locked) xyz buffer is written by the last stage through its device
+ * address instead of by a copy afterwards: it must not be read or written by
+ * the host until the call returns (as with any output). */
 ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_config* dcfg,
                                              const zim_recon_config* rcfg, const void* left_frames,
                                              const void* right_frames, int sample_type, int rows,
