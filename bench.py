@@ -237,7 +237,9 @@ def run_ours(args):
         dom = max(per_step, key=per_step.get)
         peak, src = peaks()
         npx, rpx = H * W, ctx.rect_h * ctx.rect_w
-        # algorithmic bytes per launch (measurement section)
+        # algorithmic bytes per launch: each stage's compulsory reads + writes per source pixel (npx)
+        # or rectified pixel (rpx), e.g. decode reads F u16 frames and writes an int32 fringe order
+        # and an f32 residual phase (8 B)
         alg = {"decode": npx * (F * 2 + 8), "rectify": npx * 8 + rpx * 12, "match": rpx * (12 + 12 + 4),
                "median_reproject": rpx * (4 + 13), "sor": rpx * (13 + 13), "mls": rpx * (13 + 12),
                "metric_gaussian": rpx * (13 + 12)}
