@@ -109,7 +109,12 @@ def config1_recon(api):
 
 
 def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
-    """Per-stage device time (CUDA events on the launching stream), ms per launch."""
+    """Per-stage device time (CUDA events on the launching stream), ms per launch.
+
+    The stages are called one by one from Python, so each step starts with a
+    bounded spin kernel (about 2 ms) queued ahead of the first event: the host
+    enqueues the stages while the device is still busy, and each event pair
+    brackets device work only, not the Python call between two stages."""
     import torch
     H, W = dL.shape[1:]
     st = torch.cuda.current_stream()
@@ -117,8 +122,11 @@ def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
     acc = {n: 0.0 for n in names}
     cnt = {n: 0 for n in names}
     ev = lambda: torch.cuda.Event(enable_timing=True)
+    hold = getattr(torch.cuda, "_sleep", None)
     for _ in range(steps):
         e = [ev() for _ in range(12)]
+        if hold is not None:
+            hold(4_000_000)  # clock cycles
         e[0].record(st)
         dl = api.decode(ctx, dcfg, dL, want_mod=False, want_valid=False)
         e[1].record(st)
