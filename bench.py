@@ -301,7 +301,7 @@ def cpu_band_step(spec, L, R, rect, y0, y1):
     return time.perf_counter() - t, int(mask.sum())
 
 
-def cpu_baseline(spec, L, R, band_rows=256):
+def cpu_baseline(spec, L, R, band_rows=768):
     """The CPU restatement on a bounded sample: one band of rectified rows."""
     from oracle import pipeline as P
     rect = P.Rectification(spec.rig.as_dict(), True)
