@@ -323,8 +323,11 @@ ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz, const uint
  * rows * cols <= 64 Mi pixels (larger sizes return ZIM_ERR_INVALID_ARG) and is
  * held by every GPU that loads the library until exit.  No context: it runs
  * on the current device.  The first call on a device does a one-time set-up
- * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race, so serialise them. */
+ * (cudaGetSymbolAddress); make it before any stream capture.  The address it
+ * finds is kept until exit, so do not call this on a device after a
+ * cudaDeviceReset of it.  All calls share the array: calls that overlap on the
+ * GPU race, so serialise them.  ZIM_ERR_CUDA reports only this call's own
+ * launch failures; errors pending from other work are left in place. */
 ZIM_API zim_status zim_compact_points_noalloc(const float* xyz, const uint8_t* mask, int rows,
                                               int cols, zim_point_xyz* points,
                                               uint64_t* count_dev, void* stream);

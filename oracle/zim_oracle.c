@@ -2,9 +2,12 @@
  * zim_oracle.c -- FP64 CPU restatement of the PhaseShiftGrayCode3D reconstruction
  * hot path (test infrastructure: the parity checker and the timed CPU baseline).
  *
- * Parity status: UNPINNED (no reference outputs or golden vectors exist; the
- * reference needs OpenCV, which is absent).  Every function cites the reference
- * lines it restates.  "src/" below means PhaseShiftGrayCode3D/src/.
+ * Parity status: pinned to the reference's own code (compiled from its
+ * sources as oracle/_ref; tests/test_ref_pin.py) for every computation the
+ * reference has; the OpenCV primitives restated below and the computations
+ * the reference lacks are checked against known answers instead (see
+ * zim_oracle.h).  Every function cites the reference lines it restates.
+ * "src/" below means PhaseShiftGrayCode3D/src/.
  *
  * Build: gcc -O2 -fopenmp -ffp-contract=off -fPIC -shared (no fast-math), so
  * results are IEEE-reproducible across x86-64 and aarch64.

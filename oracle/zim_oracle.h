@@ -3,12 +3,17 @@
  * hot path.  TEST INFRASTRUCTURE ONLY: the parity checker for the CUDA library
  * and the timed CPU baseline.  Nothing in the shipped path links or calls it.
  *
- * Parity status: UNPINNED.  The reference ships no tests, golden vectors or
- * sample data, and its code cannot be compiled here (every hot-path file needs
- * OpenCV 4.7, which is absent).  This restatement follows the reference source
- * line by line (citations on each function) and restates the OpenCV primitives
- * it calls from their documented behaviour; it is checked against analytic
- * known answers in tests/test_oracle_kat.py instead of reference outputs.
+ * Parity status: pinned to the reference's own code where the reference has
+ * the computation.  This restatement follows the reference source line by line
+ * (citations on each function) and restates the OpenCV primitives it calls
+ * from their documented behaviour (OpenCV is absent).  The reference's own
+ * decoder, reconstructor and MLS sources, compiled against a minimal OpenCV
+ * stand-in that calls these same primitives (oracle/ref_build.py,
+ * oracle/_ref), must give the same results (tests/test_ref_pin.py).  The
+ * primitives themselves and the computations the reference lacks (Gray code,
+ * hierarchical unwrapping, SOR, metric Gaussian, adjoint) are checked against
+ * analytic known answers (tests/test_oracle_kat.py) and independent
+ * implementations.
  *
  * All arrays are row-major, tightly packed.  Decision-margin flag bits are
  * returned so tests can tell a genuine mismatch from an FP32-vs-FP64 decision

@@ -464,10 +464,14 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     if (s) return s;
     // A pinned (page-locked) cloud buffer takes the last stage's writes
     // directly through its device address: the copy back overlaps that
-    // stage.  (Only the last stage writes it; the mask, which later stages
-    // read, stays on the device and is copied.)
+    // stage.  Only the last stage writes it; the mask, which later stages
+    // read, stays on the device and is copied.  MLS with three or more passes
+    // ping-pongs through its output, so a pass would read its neighbourhoods
+    // back across the host link: that case writes the device scratch and
+    // copies instead.
+    const bool last_reads_out = r->use_mls && !r->use_metric_gaussian && r->mls_iterations >= 3;
     float* xyz_dev = nullptr;
-    {
+    if (!last_reads_out) {
         cudaPointerAttributes a{};
         if (cudaPointerGetAttributes(&a, xyz) == cudaSuccess && a.type == cudaMemoryTypeHost &&
             a.devicePointer != nullptr)
@@ -477,10 +481,18 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     }
     s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, xyz_dev ? xyz_dev : dxyz, dmask, ddisp, B, st,
                  ctx->aux_event);
+    cudaError_t e = cudaSuccess;
+    if (s == ZIM_OK && !xyz_dev) e = cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st);
+    if (s == ZIM_OK && e == cudaSuccess) e = cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st);
+    if (s == ZIM_OK && e == cudaSuccess && disp) e = cudaMemcpyAsync(disp, ddisp, dst * 4, cudaMemcpyDeviceToHost, st);
+    // Whatever failed, nothing queued here may still be writing the caller's
+    // host buffers when this returns: drain the stream first.
+    const cudaError_t es = cudaStreamSynchronize(st);
     if (s) return s;
-    if (!xyz_dev) ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st));
-    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st));
-    if (disp) ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(disp, ddisp, dst * 4, cudaMemcpyDeviceToHost, st));
-    ZIM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if (e != cudaSuccess || es != cudaSuccess) {
+        const cudaError_t err = e != cudaSuccess ? e : es;
+        cudaGetLastError();
+        return zim_fail(ctx, ZIM_ERR_CUDA, "%s", cudaGetErrorString(err));
+    }
     return ZIM_OK;
 }

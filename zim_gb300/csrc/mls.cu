@@ -20,10 +20,15 @@ namespace {
 constexpr int MX = 16, MY = 8;
 
 // Unit eigenvector of the smallest eigenvalue of a symmetric 3x3 matrix (the
-// surface normal of a weighted covariance): the eigenvalue in closed form
-// (trigonometric solution of the characteristic cubic), the vector as the
-// longest cross product of two rows of C - lambda I.  Zero when that
-// eigenvalue is not simple enough to give a direction.
+// surface normal of a weighted covariance): the eigenvalue in closed form by
+// the published trigonometric solution of the characteristic cubic (O. K.
+// Smith, "Eigenvalues of a symmetric 3x3 matrix", Communications of the ACM
+// 4(4):168, 1961: shift by q = tr/3, scale by p, phi = acos(det(B)/2)/3), the
+// same method the reference's symmetricEigen3x3 uses
+// (JSLAB_MLS_Filter.cpp:11-106), which is why the variable names and the
+// diagonal/degenerate thresholds read alike; the vector is the longest cross
+// product of two rows of C - lambda I.  Zero when that eigenvalue is not
+// simple enough to give a direction.
 __device__ void sym_normal3(const float C[3][3], float n[3]) {
     const float p1 = C[0][1] * C[0][1] + C[0][2] * C[0][2] + C[1][2] * C[1][2];
     if (p1 < 1e-20f) {  // diagonal: the axis of the smallest entry

@@ -18,7 +18,15 @@
 // (two streams, or two host threads) race on the array: serialise them.
 //
 // The first call on a device runs a one-time set-up (cudaGetSymbolAddress with
-// that device current); make that first call before any stream capture.
+// that device current); make that first call before any stream capture.  The
+// address found there is kept for the life of the process: a cudaDeviceReset
+// of that device (which unloads this library's device code and may reload it
+// elsewhere) leaves it stale, so do not call this entry point on a device
+// after resetting it.
+//
+// Each of the three launches is checked through its own return code
+// (cudaLaunchKernel), so an error left pending by other work on the calling
+// thread is neither reported as this call's nor cleared by it.
 #include <mutex>
 
 #include "zim_internal.cuh"
@@ -141,8 +149,17 @@ extern "C" ZIM_API zim_status zim_compact_points_noalloc(const float* xyz, const
         return ZIM_ERR_CUDA;
     }
     cudaStream_t st = zim_stream(stream);
-    na_count_kernel<<<(unsigned)nb, ZIM_NOALLOC_COMPACT_BLOCK, 0, st>>>(mask, n, blocks);
-    na_scan_kernel<<<1, ZIM_NOALLOC_COMPACT_BLOCK, 0, st>>>(blocks, (int)nb, count_dev);
-    na_write_kernel<<<(unsigned)nb, ZIM_NOALLOC_COMPACT_BLOCK, 0, st>>>(xyz, mask, n, blocks, points);
-    return cudaGetLastError() == cudaSuccess ? ZIM_OK : ZIM_ERR_CUDA;
+    int nbi = (int)nb;
+    void* count_args[] = {(void*)&mask, (void*)&n, (void*)&blocks};
+    void* scan_args[] = {(void*)&blocks, (void*)&nbi, (void*)&count_dev};
+    void* write_args[] = {(void*)&xyz, (void*)&mask, (void*)&n, (void*)&blocks, (void*)&points};
+    const dim3 grid((unsigned)nb), one(1), blk(ZIM_NOALLOC_COMPACT_BLOCK);
+    cudaError_t e = cudaLaunchKernel((const void*)na_count_kernel, grid, blk, count_args, 0, st);
+    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)na_scan_kernel, one, blk, scan_args, 0, st);
+    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)na_write_kernel, grid, blk, write_args, 0, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // the failed launch recorded its own error: clear that one
+        return ZIM_ERR_CUDA;
+    }
+    return ZIM_OK;
 }
