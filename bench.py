@@ -15,7 +15,9 @@ exceed the 129 MB L2, so no flush is needed between steps.
 N > 1 runs under torchrun: independent replicas, one pair per rank per step
 (weak scaling, no collective on the data path); the time is the max over ranks.
 --impl reference times the CPU restatement of the path (oracle/, all host
-threads) on a bounded sample of the same workload: a band of rectified rows.
+threads; the CPU suite pins it to the reference's own code) on the same
+workload: each timed step is one whole pair (warm-up steps are one band of
+rows each, to warm the caches and the thread pool only).
 """
 from __future__ import annotations
 
@@ -44,6 +46,14 @@ def workload_name(W, H):
     return WORKLOAD.replace("5MP pair: 2448x2048", f"{W}x{H} pair (5 MP workload scaled)")
 
 
+def workload_config(W, H, F, rect_w, rect_h, input_bytes):
+    """The `config` object, identical for both arms (same workload, same keys)."""
+    return {"workload": workload_name(W, H), "width": W, "height": H, "rect": [rect_w, rect_h],
+            "frames_per_camera": F, "parallelism": "one pair per step per GPU (replicas)",
+            "l2": (f"inputs {input_bytes / 1e6:.0f} MB per pair > 129 MB L2 (no flush)"
+                   if input_bytes > 129e6 else "inputs smaller than L2: profiling size only")}
+
+
 def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
@@ -57,22 +67,28 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons during the timed region."""
+    """nvidia-smi clocks / throttle reasons, sampled every 20 ms from before
+    the warm-up to after the timed regions; the summary keeps the samples
+    taken inside the windows passed to mark()."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
-        self.gpu, self.rows, self.proc = gpu, [], None
+    def __init__(self, gpu: int, period_ms: int = 20):
+        self.gpu, self.rows, self.proc, self.period = gpu, [], None, period_ms
+        self.windows = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0:  # sampler running before any timing
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -81,7 +97,11 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
+
+    def mark(self, t0, t1):
+        """A timed window (perf_counter seconds)."""
+        self.windows.append((t0, t1))
 
     def __exit__(self, *a):
         if self.proc:
@@ -94,12 +114,16 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        inside = [r for t, r in self.rows if any(a <= t <= b for a, b in self.windows)]
+        rows = inside or [r for _, r in self.rows]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "in_timed_windows": bool(inside),
+                "samples_total": len(self.rows),
+                "period_ms": self.period}
 
 
 def config1_recon(api):
@@ -123,6 +147,7 @@ def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
     cnt = {n: 0 for n in names}
     ev = lambda: torch.cuda.Event(enable_timing=True)
     hold = getattr(torch.cuda, "_sleep", None)
+    stage_breakdown.hold_ran = hold is not None
     for _ in range(steps):
         e = [ev() for _ in range(12)]
         if hold is not None:
@@ -191,28 +216,6 @@ def run_ours(args):
 
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        torch.cuda.synchronize()
-        l0 = ctx.launch_count()
-        e0.record(st)
-        for _ in range(args.steps):
-            api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
-        e1.record(st)
-        torch.cuda.synchronize()
-        barrier()
-        launches = ctx.launch_count() - l0
-    ms = e0.elapsed_time(e1) / args.steps
-    pts_total = n_pts
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        p = torch.tensor([n_pts], device="cuda", dtype=torch.float64)
-        dist.all_reduce(p, op=dist.ReduceOp.SUM)
-        pts_total = int(p.item())
-    value = pts_total / (ms * 1e-3) / 1e6
-
     # end to end through the host entry: pinned frames in, xyz + mask out, copies timed
     hL = torch.from_numpy(L).pin_memory()
     hR = torch.from_numpy(R).pin_memory()
@@ -220,21 +223,42 @@ def run_ours(args):
     hm = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory()
     for _ in range(max(1, args.warmup // 2)):
         api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e0.record(st)
-    for _ in range(args.steps):
-        api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
-    e1.record(st)
-    torch.cuda.synchronize()
-    wall = (time.perf_counter() - t0) / args.steps
-    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count()
+        t0 = time.perf_counter()
+        e0.record(st)
+        for _ in range(args.steps):
+            api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
+        e1.record(st)
+        torch.cuda.synchronize()
+        clk.mark(t0, time.perf_counter())
+        barrier()
+        launches = ctx.launch_count() - l0
+        ms = e0.elapsed_time(e1) / args.steps
+
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(st)
+        for _ in range(args.steps):
+            api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
+        e1.record(st)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+        clk.mark(t0, time.perf_counter())
+        barrier()
     e2e_ms = max(e0.elapsed_time(e1) / args.steps, wall * 1e3)
+    pts_total = n_pts
     if dist:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        t = torch.tensor([ms, e2e_ms], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+        ms, e2e_ms = float(t[0].item()), float(t[1].item())
+        p = torch.tensor([n_pts], device="cuda", dtype=torch.float64)
+        dist.all_reduce(p, op=dist.ReduceOp.SUM)
+        pts_total = int(p.item())
+    value = pts_total / (ms * 1e-3) / 1e6
     e2e = pts_total / (e2e_ms * 1e-3) / 1e6
     h2d = 2 * L.nbytes
     d2h = hx.numel() * 4 + hm.numel()
@@ -263,10 +287,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (u16 samples; FP64 only for near-zero-disparity divides)",
             "data": "synthetic (seeded scene renderer, zim_gb300/synth)",
-            "config": {"workload": workload_name(W, H), "width": W, "height": H, "rect": [ctx.rect_w, ctx.rect_h],
-                       "frames_per_camera": F, "points_per_pair": n_pts, "parallelism": f"replicas x{world}",
-                       "l2": (f"inputs {2 * L.nbytes / 1e6:.0f} MB per pair > 129 MB L2 (no flush)"
-                              if 2 * L.nbytes > 129e6 else "inputs smaller than L2: profiling size only")},
+            "config": workload_config(W, H, F, ctx.rect_w, ctx.rect_h, 2 * L.nbytes),
+            "points_per_pair": n_pts, "replicas": world,
             "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms, 4)},
             "gpu_launches": int(launches),
@@ -276,6 +298,7 @@ def run_ours(args):
                          "decode_kernel": {"achieved": round(dec_achieved, 1),
                                            "frac": round(dec_achieved / peak, 4)}},
             "stages": stages,
+            "stages_hold": bool(getattr(stage_breakdown, "hold_ran", False)),
             "clocks": clk.summary(),
         }
         if cpu:
@@ -301,16 +324,31 @@ def cpu_band_step(spec, L, R, rect, y0, y1):
     return time.perf_counter() - t, int(mask.sum())
 
 
-def cpu_baseline(spec, L, R, band_rows=768):
-    """The CPU restatement on a bounded sample: one band of rectified rows."""
+def cpu_pair_step(spec, L, R, rect):
+    """The whole pair on the CPU restatement (every stage, SOR statistics over
+    the whole cloud): seconds and points."""
+    from oracle import pipeline as P
+    t = time.perf_counter()
+    xyz, mask = P.run_pair(spec.decode_kwargs(), spec.pha_f, L, R, rect, P.CONFIG1_FILTERS)
+    return time.perf_counter() - t, int(mask.sum())
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
+
+
+def cpu_baseline(spec, L, R):
+    """The CPU restatement on one whole pair of the same workload (all host threads)."""
     from oracle import pipeline as P
     rect = P.Rectification(spec.rig.as_dict(), True)
-    y0 = rect.h // 2 - band_rows // 2
-    cpu_band_step(spec, L, R, rect, y0, y0 + 16)  # warm caches / OpenMP pool
-    dt, n = cpu_band_step(spec, L, R, rect, y0, y0 + band_rows)
-    return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"rectified rows [{y0},{y0 + band_rows}) of the same pair ({band_rows}/{rect.h} rows), "
-                      f"whole path incl. filters, {dt:.2f} s"}
+    cpu_band_step(spec, L, R, rect, rect.h // 2, rect.h // 2 + 16)  # warm caches / OpenMP pool
+    dt, n = cpu_pair_step(spec, L, R, rect)
+    return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+            "sample": f"one whole pair of the same workload ({n} points), every stage incl. SOR/MLS/Gaussian, "
+                      f"{dt:.2f} s; the restatement is pinned to the reference's own code by the CPU tests"}
 
 
 DIFF_WORKLOAD = ("planar target at 8 seeded poses (tilt +-30 deg, depth 600-1200 mm), 2448x2048 x2 cams, "
@@ -546,32 +584,39 @@ def run_batch(api, local, steps, warmup, n_pairs=64):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the path (oracle/, all host
+    threads), which the CPU suite pins to the reference's own code; each timed
+    step is one whole pair of the same workload.  Warm-up steps are one band of
+    rows each (they warm the caches and the thread pool; they are not timed)."""
     rank, local, world = env_rank()
     if rank != 0:
         return None
     from oracle import pipeline as P
     from zim_gb300 import synth
-    spec = synth.config1(seed=1)
+    spec = synth.config1(seed=1, width=args.width, height=args.height)
     L, R = spec.render(0), spec.render(1)
+    F, H, W = L.shape
     rect = P.Rectification(spec.rig.as_dict(), True)
-    band = 128
-    rows = list(range(0, rect.h - band, band))
+    band = 64
     for i in range(args.warmup):
-        y0 = rows[(i * 7) % len(rows)]
+        y0 = (rect.h // 2 + 97 * i) % max(1, rect.h - band)
         cpu_band_step(spec, L, R, rect, y0, y0 + band)
     tot_t, tot_n = 0.0, 0
-    for i in range(args.steps):
-        y0 = rows[(i * 5 + 3) % len(rows)]
-        dt, n = cpu_band_step(spec, L, R, rect, y0, y0 + band)
+    for _ in range(args.steps):
+        dt, n = cpu_pair_step(spec, L, R, rect)
         tot_t += dt
         tot_n += n
     value = tot_n / tot_t / 1e6
+    cores = cpu_threads()
     res = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(tot_t / args.steps * 1e3, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene renderer)",
-           "config": {"workload": WORKLOAD, "parallelism": "host threads"}, "impl": "reference",
-           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                            "sample": f"each step: {band} rectified rows of the 5 MP pair, whole path incl. filters"},
+           "config": workload_config(W, H, F, rect.w, rect.h, 2 * L.nbytes), "impl": "reference",
+           "points_per_pair": tot_n // max(1, args.steps),
+           "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": "each timed step: one whole pair, every stage incl. SOR/MLS/Gaussian "
+                                      "(warm-up steps: one 64-row band each); the restatement is pinned to the "
+                                      "reference's own code by the CPU tests"},
            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(res))
     return res

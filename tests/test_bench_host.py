@@ -1,13 +1,13 @@
 """Host logic of bench.py that needs no GPU: the clock record summary, the
-workload name and the peak lookup."""
+workload name and config, and the peak lookup."""
 import json
 
 import bench
 
 
-def _row(sm, mx, hw="Not Active", hwt="Not Active", swt="Not Active", pc="Not Active"):
-    # index, clocks.sm, clocks.max.sm, power.draw, reasons.active, hw, hw_thermal, sw_thermal, sw_power_cap
-    return ["0", str(sm), str(mx), "900.0", "0x0", hw, hwt, swt, pc]
+def _row(sm, mx, hw="Not Active", hwt="Not Active", swt="Not Active", pc="Not Active", t=1.0):
+    # (time, [index, clocks.sm, clocks.max.sm, power.draw, reasons.active, hw, hw_thermal, sw_thermal, sw_power_cap])
+    return (t, ["0", str(sm), str(mx), "900.0", "0x0", hw, hwt, swt, pc])
 
 
 def test_clock_summary_median_max_and_no_reasons():
@@ -49,3 +49,19 @@ def test_peaks_reads_measured_file_or_falls_back(tmp_path, monkeypatch):
     assert bench.peaks() == (6800.0, "fallback")
     (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6786.9}))
     assert bench.peaks() == (6786.9, "measured")
+
+
+def test_clock_summary_keeps_the_timed_windows():
+    c = bench.ClockSampler(0)
+    c.rows = [_row(1000, 2070, t=0.5), _row(2070, 2070, t=1.5, pc="Active"), _row(2055, 2070, t=1.6),
+              _row(900, 2070, t=3.0, hwt="Active")]
+    c.mark(1.0, 2.0)
+    s = c.summary()
+    assert s["samples"] == 2 and s["samples_total"] == 4
+    assert s["sm_mhz"] == 2062.5 and s["reasons"] == ["sw_power_cap"]
+
+
+def test_both_arms_share_one_config():
+    a = bench.workload_config(2448, 2048, 12, 2501, 2092, 2 * 12 * 2448 * 2048 * 2)
+    b = bench.workload_config(2448, 2048, 12, 2501, 2092, 240648192)
+    assert a == b and a["workload"] == bench.WORKLOAD and "> 129 MB L2" in a["l2"]

@@ -137,3 +137,56 @@ def test_median_reproject_parity(ctx, oracle_lib, name, kw, rectified):
     print(name, rectified, "reproject max rel err", rel.max(), "points", int(both.sum()))
     assert rel.max() <= 1e-5
     assert (gx[gm == 0] == 0).all()
+
+
+def _rows_case(rows=64, cols=512, pha_f=16, seed=11):
+    """Rectified phase rows that exercise both matching paths: rising spans
+    (binary search), noisy spans that fall back to the scan, foreign orders
+    inside spans, and plateaus of equal phase (ties)."""
+    rng = np.random.default_rng(seed)
+    c = np.arange(cols, dtype=np.float64)
+    rph = np.zeros((rows, cols)); lph = np.zeros((rows, cols))
+    for i in range(rows):
+        off = rng.uniform(0.0, 1.0)
+        r = off + 0.2 * c
+        kind = i % 4
+        if kind == 1:
+            r = r + rng.uniform(-0.15, 0.15, cols)
+        elif kind == 3:
+            r = np.floor(r / 0.4) * 0.4 + off  # pairs of equal values
+        disp = rng.uniform(5.0, 40.0)
+        lph[i] = off + 0.2 * (c - disp) + rng.normal(0, 0.01, cols)
+        rph[i] = r
+    rk = np.clip(np.floor(rph / TWO_PI).astype(np.int32) + 1, 0, pha_f)
+    lk = np.clip(np.floor(lph / TWO_PI).astype(np.int32) + 1, 0, pha_f)
+    for i in range(2, rows, 4):  # foreign orders inside the spans
+        j = rng.integers(0, cols, 12)
+        rk[i, j] = rng.integers(1, pha_f + 1, 12)
+    return lph, lk, rph, rk, pha_f
+
+
+TWO_PI = 2 * math.pi
+
+
+@pytest.mark.gpu
+def test_match_fast_path_and_scan_agree_with_oracle(ctx, oracle_lib):
+    from zim_gb300 import api
+    lph, lk, rph, rk, pha_f = _rows_case()
+
+    def split(ph, k):
+        base = np.floor(ph / TWO_PI + 0.5).astype(np.int32)
+        res = (ph - TWO_PI * base).astype(np.float32)
+        f64 = TWO_PI * base.astype(np.float64) + res.astype(np.float64)
+        return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (base, res, k.astype(np.int32))], f64
+
+    L, lf = split(lph, lk)
+    R, rf = split(rph, rk)
+    disp, best = api.match(ctx, L, R, pha_f, 1.0)
+    od, ob, near = oracle_lib.stereo_match(lf, rf, lk, rk, pha_f, 1.0, eps=EPS)
+    gb, gd = best.cpu().numpy(), disp.cpu().numpy()
+    ok = near == 0
+    assert np.array_equal(gb[ok], ob[ok])
+    m = ok & (ob >= 0)
+    assert np.abs(gd[m].astype(np.float64) - od[m]).max() <= 2e-4
+    for kind in range(4):  # every row kind matches something
+        assert (ob[kind::4] >= 0).mean() > 0.3, kind

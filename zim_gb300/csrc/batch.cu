@@ -145,11 +145,13 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
         const PairDev& P = pairs[w.x];
         const int cols = P.rw, pha_f = P.pha_f;
         int* s_hi = s_lo + (pha_f + 1);
+        int* s_bad = s_hi + (pha_f + 1);
         for (int row = w.y; row < w.y + w.z; row++) {
             const size_t ro = (size_t)row * cols;
             for (int k = tid; k <= pha_f; k += BT) {
                 s_lo[k] = INT_MAX;
                 s_hi[k] = -1;
+                s_bad[k] = 0;
             }
             for (int j = tid; j < cols; j += BT) {
                 int32_t b, o;
@@ -167,6 +169,8 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
             __syncthreads();
             zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, tid, BT);
             __syncthreads();
+            zt::match_spans_check(s_ord, s_base, s_res, cols, pha_f, s_hi, s_bad, tid, BT);
+            __syncthreads();
             for (int j = tid; j < cols; j += BT) {
                 int32_t bL, kL;
                 float rL;
@@ -178,8 +182,8 @@ __global__ void __launch_bounds__(BT) batch_match_kernel(const PairDev* __restri
                                       __ldg(P.map[0][1] + ro + j), P.post_smooth, bL, rL, kL);
                 float d;
                 int best;
-                zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, cols, pha_f, P.grad_threshold, d,
-                                best);
+                zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, s_bad, cols, pha_f, P.grad_threshold,
+                                d, best);
                 P.disp_raw[ro + j] = d;
             }
             __syncthreads();
@@ -522,7 +526,7 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     if (tuning) b->tuning = *tuning;
     b->max_cols = max_cols;
     b->max_pha_f = max_pha;
-    b->match_smem = (size_t)max_cols * 12 + (size_t)(max_pha + 1) * 8;
+    b->match_smem = (size_t)max_cols * 12 + (size_t)(max_pha + 1) * 12;
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(batch_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)b->match_smem));
     b->ror_smem = b->use_ror ? zt::ror_smem_bytes(rcfg->radius_window_size / 2) : 0;

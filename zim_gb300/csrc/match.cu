@@ -7,9 +7,11 @@
 //
 // One CTA per rectified row.  The right row (order, phase base, residual) is
 // staged in shared memory; the per-order column span [lo, hi] is built with
-// shared-memory atomics; each left pixel of order k in [1, pha_f] scans the
-// span for right pixels of order k and keeps the first column of minimum
-// |phase_R - phase_L| (strict <, so the smallest column wins ties), rejects
+// shared-memory atomics and checked for a strictly rising phase; each left
+// pixel of order k in [1, pha_f] finds the first column of minimum
+// |phase_R - phase_L| among the right pixels of order k (strict <, so the
+// smallest column wins ties) -- by binary search on a checked span, by a scan
+// of the span otherwise, the same column either way -- rejects
 // min >= grad_threshold and columns < 2 or >= cols - 1, then refines with the
 // parabola through the costs of columns best-1, best, best+1.
 #include <climits>
@@ -43,12 +45,14 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(MatchWin w, int ph
     float* s_res = reinterpret_cast<float*>(s_base + cols);
     int* s_lo = reinterpret_cast<int*>(s_res + cols);
     int* s_hi = s_lo + (pha_f + 1);
+    int* s_bad = s_hi + (pha_f + 1);
 
     const int row = blockIdx.x;
     const size_t ro = (size_t)row * w.stride;
     for (int k = threadIdx.x; k <= pha_f; k += blockDim.x) {
         s_lo[k] = INT_MAX;
         s_hi[k] = -1;
+        s_bad[k] = 0;
     }
     for (int j = threadIdx.x; j < cols; j += blockDim.x) {
         s_ord[j] = w.r_order[ro + j];
@@ -58,13 +62,15 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(MatchWin w, int ph
     __syncthreads();
     zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, threadIdx.x, blockDim.x);
     __syncthreads();
+    zt::match_spans_check(s_ord, s_base, s_res, cols, pha_f, s_hi, s_bad, threadIdx.x, blockDim.x);
+    __syncthreads();
     const size_t oo = (size_t)row * w.out_stride;
     for (int j = threadIdx.x; j < w.l_cols; j += blockDim.x) {
         float d = 0.f;
         int best = -1;
         if (!w.l_mask || w.l_mask[ro + j])
             zt::match_pixel(j, w.l_order[ro + j], w.l_base[ro + j], w.l_res[ro + j], s_ord, s_base, s_res, s_lo,
-                            s_hi, cols, pha_f, grad_threshold, d, best, w.dx_off);
+                            s_hi, s_bad, cols, pha_f, grad_threshold, d, best, w.dx_off);
         w.disp[oo + j] = d;
         if (w.best_col) w.best_col[oo + j] = best;
     }
@@ -72,7 +78,7 @@ __global__ void __launch_bounds__(MATCH_THREADS) match_kernel(MatchWin w, int ph
 
 zim_status launch_match(zim_ctx* ctx, const MatchWin& w, int rows, int pha_f, double grad_threshold,
                         cudaStream_t st) {
-    size_t smem = (size_t)w.r_cols * 12 + (size_t)(pha_f + 1) * 8;
+    size_t smem = (size_t)w.r_cols * 12 + (size_t)(pha_f + 1) * 12;
     // the attribute is per device and per function: set it on every call
     ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     match_kernel<<<rows, MATCH_THREADS, smem, st>>>(w, pha_f, (float)grad_threshold);

@@ -512,16 +512,31 @@ __device__ __forceinline__ float phase_diff(int bR, float rR, int bL, float rL) 
     return fmaf((float)(bR - bL), ZIM_TWO_PI_F, rR - rL);
 }
 
+// Monotone spans.  Within a right row the rectified phase of one fringe order
+// normally rises column by column.  When the order's span [lo, hi] holds only
+// pixels of that order and every step to the next column rises by more than
+// MATCH_MONO_MARGIN (verified per row and order by match_spans_check), the
+// float differences d(c) = phase_R(c) - phase_L computed by phase_diff are
+// strictly increasing in c for any left pixel whose phase lies within 1024
+// cycles of the span (the rounding of each d is below half the margin), so
+// |d| falls, then rises, and its first minimum is at the sign change of d: a
+// binary search finds the same column as the reference's scan over every
+// candidate (ties keep the earlier column, as the scan's strict < does).
+// Spans that fail the check are scanned in full.
+constexpr float MATCH_MONO_MARGIN = 2e-3f;
+
 // One left pixel against a right row staged in shared memory (s_ord, s_base,
-// s_res; cols columns) with the per-order column spans [s_lo, s_hi]: the first
+// s_res; cols columns) with the per-order column spans [s_lo, s_hi] and the
+// spans' failed-check flags s_bad (null: always the full scan): the first
 // column of minimum |phase_R - phase_L| among right pixels of the same order
 // (strict <), rejected if min >= grad_threshold or the column is < 2 or
 // >= cols - 1, then the reference's three-point sub-pixel refinement.
 // dx_off is (left window x) - (right window x) for the ROI path
 // (startCalculate_v2_roi, V2.cpp:719-778: global left x - global right x - delta).
 __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, const int* s_ord, const int* s_base,
-                                            const float* s_res, const int* s_lo, const int* s_hi, int cols, int pha_f,
-                                            float grad_threshold, float& d, int& best, int dx_off = 0) {
+                                            const float* s_res, const int* s_lo, const int* s_hi, const int* s_bad,
+                                            int cols, int pha_f, float grad_threshold, float& d, int& best,
+                                            int dx_off = 0) {
     d = 0.f;
     best = -1;
     if (k < 1 || k > pha_f) return;
@@ -529,12 +544,34 @@ __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, cons
     if (lo > hi) return;
     float min_cost = 1e9f;
     int bj = -1;
-    for (int c = lo; c <= hi; c++) {
-        if (s_ord[c] != k) continue;
-        float diff = fabsf(phase_diff(s_base[c], s_res[c], bL, rL));
-        if (diff < min_cost) {
-            min_cost = diff;
-            bj = c;
+    if (s_bad && !s_bad[k] && abs(s_base[lo] - bL) < 1024 && abs(s_base[hi] - bL) < 1024) {
+        // first column with d >= 0 (hi + 1 if none)
+        int a = lo, b = hi + 1;
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            if (phase_diff(s_base[m], s_res[m], bL, rL) < 0.f) a = m + 1;
+            else b = m;
+        }
+        if (a > hi) {
+            bj = hi;
+            min_cost = fabsf(phase_diff(s_base[hi], s_res[hi], bL, rL));
+        } else if (a == lo) {
+            bj = lo;
+            min_cost = fabsf(phase_diff(s_base[lo], s_res[lo], bL, rL));
+        } else {
+            const float dn = fabsf(phase_diff(s_base[a - 1], s_res[a - 1], bL, rL));
+            const float dp = fabsf(phase_diff(s_base[a], s_res[a], bL, rL));
+            bj = dp < dn ? a : a - 1;
+            min_cost = dp < dn ? dp : dn;
+        }
+    } else {
+        for (int c = lo; c <= hi; c++) {
+            if (s_ord[c] != k) continue;
+            float diff = fabsf(phase_diff(s_base[c], s_res[c], bL, rL));
+            if (diff < min_cost) {
+                min_cost = diff;
+                bj = c;
+            }
         }
     }
     if (bj >= 0 && min_cost < grad_threshold && bj >= 2 && bj < cols - 1) {
@@ -549,8 +586,9 @@ __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, cons
     }
 }
 
-// Per-order column spans of a staged right row (shared atomics).  Callers sync
-// before and after.
+// Per-order column spans of a staged right row (shared atomics).  Callers
+// initialise s_lo = INT_MAX, s_hi = -1, s_bad = 0 and sync before, and sync
+// after, then run match_spans_check (and sync again).
 __device__ __forceinline__ void match_spans(const int* s_ord, int cols, int pha_f, int* s_lo, int* s_hi, int tid,
                                             int nthreads) {
     for (int j = tid; j < cols; j += nthreads) {
@@ -559,6 +597,20 @@ __device__ __forceinline__ void match_spans(const int* s_ord, int cols, int pha_
             atomicMin(&s_lo[k], j);
             atomicMax(&s_hi[k], j);
         }
+    }
+}
+
+// Marks in s_bad every order whose span holds a pixel of another order or a
+// step that does not rise by MATCH_MONO_MARGIN (see match_pixel).  A foreign
+// run inside a span always follows a pixel of the span's order, so checking
+// each pixel against its right neighbour finds it.
+__device__ __forceinline__ void match_spans_check(const int* s_ord, const int* s_base, const float* s_res, int cols,
+                                                  int pha_f, const int* s_hi, int* s_bad, int tid, int nthreads) {
+    for (int j = tid; j + 1 < cols; j += nthreads) {
+        const int k = s_ord[j];
+        if (k < 0 || k > pha_f || j >= s_hi[k]) continue;
+        if (s_ord[j + 1] != k || !(phase_diff(s_base[j + 1], s_res[j + 1], s_base[j], s_res[j]) > MATCH_MONO_MARGIN))
+            s_bad[k] = 1;
     }
 }
 
