@@ -394,7 +394,8 @@ def cpu_diff_baseline(spec, ctx, pose, theta):
     order = [o.cpu().numpy() for o in pose.order]
     res = [r.cpu().numpy().astype(np.float64) for r in pose.residual]
     t = time.perf_counter()
-    o = O.diff_eval(geom, theta, order[0], res[0], order[1], res[1], pose.best.cpu().numpy(), pose.plane)
+    o = O.diff_eval(geom, theta, order[0], res[0], order[1], res[1], pose.best.cpu().numpy(), pose.plane,
+                    want_grad_abs=True)
     dt = time.perf_counter() - t
     return o, dt
 
@@ -442,6 +443,14 @@ def run_diff(api, local, steps, warmup, want_cpu=True):
         out["grad_err_vs_fp64"] = {"normwise_rel": float(np.linalg.norm(g - go) / np.linalg.norm(go)),
                                    "worst_component_rel": float(np.max(np.abs(g - go) / np.abs(go))),
                                    "loss_rel": float(abs(one["loss"] - o["loss"]) / o["loss"])}
+        # per component: the error against the FP64 oracle, and the floor FP32
+        # per-point terms put under it -- the unit roundoff 2^-24 times the
+        # cancellation factor sum|term| / |sum term| of that component
+        from zim_gb300 import diff as D
+        canc = o["grad_abs"] / np.maximum(np.abs(go), 1e-300)
+        out["grad_components"] = {
+            D.PARAM_NAMES[k]: {"rel_err": float(abs(g[k] - go[k]) / abs(go[k])), "cancellation": float(canc[k]),
+                               "fp32_floor": float(canc[k] * 2.0 ** -24)} for k in range(len(go))}
         out["cpu_baseline"] = {"value": round(o["n_points"] / dt / 1e6, 4), "unit": "Mpoints/s (forward+adjoint)",
                                "cores": 1, "kind": "port", "sample": "pose 0 of 8, FP64 oracle, one thread",
                                "seconds": round(dt, 3)}

@@ -403,6 +403,8 @@ typedef struct zim_batch_tuning {
  * bound to ctx's device. */
 ZIM_API zim_status zim_batch_create(zim_ctx* ctx, const zim_stereo_calib* calibs, int n_calibs,
                                     int use_full_left_rectification, zim_batch** out);
+/* Destroys a batch; it reads nothing of its context, so it may run after
+ * zim_destroy of that context (as a garbage-collected caller may order them). */
 ZIM_API void zim_batch_destroy(zim_batch* batch);
 ZIM_API zim_status zim_batch_rect_size(const zim_batch* batch, int calib, int* rect_w, int* rect_h);
 /* Validates the pairs, allocates the intermediates, builds the work queues

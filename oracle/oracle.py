@@ -358,7 +358,8 @@ def diff_geom(ir, dist, Q, baseline0, rect_w, rect_h, src_w, src_h):
 
 
 def diff_eval(geom, theta, order_l, res_l, order_r, res_r, best, plane, zmin=0.0, zmax=1e4, loss_weight=1.0,
-              want_grad=True, want_points=False, want_phase_grad=False, cells=None, cells_mode=0):
+              want_grad=True, want_points=False, want_phase_grad=False, cells=None, cells_mode=0,
+              want_grad_abs=False):
     """FP64 loss of one view and (optionally) its analytic gradient, J^T J,
     points and phase gradients.  cells: int32 array of rect_h*rect_w*8 for
     cells_mode 1 (record) / 2 (reuse the recorded bilinear cells).  Returns a dict."""
@@ -374,13 +375,14 @@ def diff_eval(geom, theta, order_l, res_l, order_r, res_r, best, plane, zmin=0.0
     mask = np.zeros((geom.rect_h, geom.rect_w), np.uint8) if want_points else None
     gl = np.zeros(ol.shape) if want_phase_grad else None
     gr = np.zeros(ol.shape) if want_phase_grad else None
+    ga = np.zeros(16) if want_grad_abs else None
     nul = C.c_void_p()
     lib().zo_diff_eval(C.byref(geom), _p(th), _p(ol), _p(rl), _p(orr), _p(rr), _p(bc), _p(pl), C.c_double(zmin),
                        C.c_double(zmax), C.c_double(loss_weight), C.byref(loss), C.byref(npts),
                        _p(grad) if want_grad else nul, _p(jtj) if want_grad else nul,
                        _p(xyz) if want_points else nul, _p(mask) if want_points else nul,
                        _p(gl) if want_phase_grad else nul, _p(gr) if want_phase_grad else nul,
-                       _p(cells) if cells is not None else nul, C.c_int(cells_mode))
+                       _p(cells) if cells is not None else nul, C.c_int(cells_mode), _p(ga) if want_grad_abs else nul)
     out = {"loss": loss.value, "n_points": npts.value}
     if want_grad:
         out["grad"], out["jtj"] = grad, jtj.reshape(16, 16)
@@ -388,6 +390,8 @@ def diff_eval(geom, theta, order_l, res_l, order_r, res_r, best, plane, zmin=0.0
         out["xyz"], out["mask"] = xyz, mask
     if want_phase_grad:
         out["grad_phase"] = (gl, gr)
+    if want_grad_abs:
+        out["grad_abs"] = ga
     return out
 
 

@@ -175,12 +175,15 @@ typedef struct {
  * (zim_diff_params order), J^T J of the distances, the points / mask and the
  * phase gradients (accumulated, +=).  cells (rect_w*rect_h*8 ints, may be
  * NULL): cells_mode 1 records each sample's bilinear cell, 2 reuses recorded
- * cells, so finite differences see one smooth patch per sample. */
+ * cells, so finite differences see one smooth patch per sample.  gabs (may be
+ * NULL) receives, per parameter, the sum over points of |that point's term of
+ * the gradient|: gabs[k] / |grad[k]| is the cancellation factor that scales
+ * the rounding of the per-point terms into the error of component k. */
 void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* order_l, const double* res_l,
                   const int32_t* order_r, const double* res_r, const int32_t* best, const double plane[4],
                   double zmin, double zmax, double loss_weight, double* loss, double* npts, double grad[16],
                   double jtj[256], double* xyz, uint8_t* mask, double* gphase_l, double* gphase_r, int32_t* cells,
-                  int cells_mode);
+                  int cells_mode, double gabs[16]);
 
 #ifdef __cplusplus
 }

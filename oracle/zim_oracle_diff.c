@@ -113,7 +113,7 @@ void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* 
                   const int32_t* order_r, const double* res_r, const int32_t* best, const double plane[4],
                   double zmin, double zmax, double loss_weight, double* loss, double* npts, double grad[16],
                   double jtj[256], double* xyz, uint8_t* mask, double* gphase_l, double* gphase_r, int32_t* cells,
-                  int cells_mode) {
+                  int cells_mode, double gabs[16]) {
     cam_t cam[2];
     for (int c = 0; c < 2; c++) {
         if (c == 0) {
@@ -142,7 +142,7 @@ void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* 
     double Tx0 = -1.0 / Q[14], dcx = Q[15] * Tx0;
     double Tx = Tx0 * theta[12] / G->baseline0, dTx = Tx0 / G->baseline0;
     double q32 = -1.0 / Tx, q33 = dcx / Tx, dq32 = dTx / (Tx * Tx), dq33 = -dcx * dTx / (Tx * Tx);
-    double L = 0, cnt = 0, g[16] = {0}, H[256] = {0};
+    double L = 0, cnt = 0, g[16] = {0}, H[256] = {0}, ga[16] = {0};
     const int rw = G->rect_w, rh = G->rect_h, sw = G->src_w, sh = G->src_h;
     for (int i = 0; i < rh; i++)
         for (int j = 0; j < rw; j++) {
@@ -196,7 +196,10 @@ void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* 
                 for (int k = 0; k < 3; k++)
                     Jw[13 + k] += wR[m] * (sR[m].gu * sR[m].ju[6 + k] + sR[m].gv * sR[m].jv[6 + k]);
             }
-            for (int k = 0; k < 16; k++) g[k] += s_up * Jw[k];
+            for (int k = 0; k < 16; k++) {
+                g[k] += s_up * Jw[k];
+                ga[k] += fabs(s_up * Jw[k]);
+            }
             for (int a = 0; a < 16; a++)
                 for (int q = 0; q < 16; q++) H[a * 16 + q] += (s_r * Jw[a]) * (s_r * Jw[q]);
             scatter(gphase_l, sw, &sL, s_up * wL);
@@ -206,4 +209,5 @@ void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* 
     *npts = cnt;
     if (grad) memcpy(grad, g, sizeof g);
     if (jtj) memcpy(jtj, H, sizeof H);
+    if (gabs) memcpy(gabs, ga, sizeof ga);
 }

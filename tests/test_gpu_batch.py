@@ -121,3 +121,21 @@ def test_batch_rejects_bad_submissions(setup):
             b.submit(bad, api.recon_config())
     with pytest.raises(ZimError):
         b.run()  # nothing submitted successfully
+
+
+def test_batch_destroyed_after_its_context_leaves_no_error(setup):
+    """A garbage collector may destroy a context before a batch made on it:
+    the batch's destruction must not read the context, nor leave an error
+    behind for the thread's next call (a launch check would report it)."""
+    from zim_gb300 import api
+    from zim_gb300.batch import Batch
+    _, scenes, calib_of, calibs = setup
+    ctx = api.Context(0)
+    b = Batch(ctx, calibs[:1])
+    ctx.close()
+    b.close()
+    spec, L, _, _ = scenes[0]
+    c2 = api.Context(0)
+    c2.set_calibration(spec.rig.as_dict(), True)
+    d = api.decode(c2, api.decode_config(**spec.decode_kwargs()), torch.from_numpy(L).cuda())
+    assert int(d["valid"].sum().item()) > 0

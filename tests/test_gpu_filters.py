@@ -78,12 +78,16 @@ def test_ror_parity(ctx, oracle_lib):
 @pytest.mark.gpu
 # The test scene is 612 px wide (1.5 mm pixel spacing, 4x the 5 MP scene's), so
 # the 5 MP settings (radius 2 mm, sigma 2/sqrt(2)) are scaled by 4 here.
-@pytest.mark.parametrize("order,window,sigma,radius,iters", [(2, 7, 5.656854, 8.0, 1), (1, 5, 2.4, 0.0, 2),
-                                                               (0, 4, 2.0, 0.0, 1)])
-def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters):
+# flag_max: the flagged fraction measured on this cloud by the oracle alone
+# (2.50 %, 0.26 %, 0.22 %) plus a margin.
+@pytest.mark.parametrize("order,window,sigma,radius,iters,flag_max", [(2, 7, 5.656854, 8.0, 1, 0.030),
+                                                                        (1, 5, 2.4, 0.0, 2, 0.004),
+                                                                        (0, 4, 2.0, 0.0, 1, 0.0035)])
+def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters, flag_max):
     """Points the oracle flags (a neighbour within 1e-6 of the cut-off, or a
     frame / normal-equation conditioning at which FP32 rounding alone moves the
-    result by more than 1e-5 mm) are counted; all others must agree."""
+    result by more than 1e-5 mm) are counted and bounded by flag_max; all
+    others must agree."""
     from zim_gb300 import api
     xyz, mask = cloud(ctx, oracle_lib)
     out = api.filter_mls(ctx, xyz, mask, window, sigma, order, radius, iters)
@@ -98,7 +102,7 @@ def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters):
     print("  flagged:", int((m & (near > 0)).sum()), "of", int(m.sum()), " beyond tolerance:", int(bad.sum()),
           " all-points max/rms err mm:", float(allerr.max()), float(np.sqrt((allerr ** 2).mean())))
     assert bad.sum() == 0
-    assert (m & (near > 0)).sum() <= 0.05 * m.sum()
+    assert (m & (near > 0)).sum() <= flag_max * m.sum()
     assert np.array_equal(g[~m], xyz.cpu().numpy()[~m])
 
 

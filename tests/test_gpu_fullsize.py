@@ -93,3 +93,65 @@ def test_fullsize_host_entry(ctx, oracle_lib, full):
     xyz, mask, _ = api.reconstruct_pair(ctx, dcfg, rcfg, torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda())
     hx, hm, _ = api.reconstruct_pair_host(ctx, dcfg, rcfg, L, R)
     assert np.array_equal(hm, mask.cpu().numpy()) and np.array_equal(hx, xyz.cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_fullsize_filters_parity(ctx, oracle_lib, full):
+    """The filters of the timed 5 MP configuration, point by point against
+    the oracle on the whole cloud: SOR (k = 30, std-mul 1) on the GPU's
+    reprojected cloud, MLS (half-window 7, sigma 2/sqrt(2), order 2, cut-off
+    2 mm) on the SOR output, the metric Gaussian (sigma 0.5 mm) on the MLS
+    output.  Masks identical except decisions the oracle flags within 1e-5 of
+    their threshold; points within 1e-5 mm + 2 float ulps except flagged ones,
+    whose counts are bounded by what the oracle alone measures on this cloud
+    (SOR 1 decision, MLS 3365 points = 0.085 %, Gaussian 470) plus a margin.
+    The stages composed here give the same bits as the timed whole-pair call."""
+    from zim_gb300 import api
+    spec, L, R, _ = full
+    ctx.set_calibration(spec.rig.as_dict(), True)
+    cfg = api.decode_config(**spec.decode_kwargs())
+    rects = []
+    for cam, fr in enumerate((L, R)):
+        d = api.decode(ctx, cfg, torch.from_numpy(fr).cuda())
+        rects.append(api.rectify(ctx, cam, d["order"], d["residual"], True))
+    disp, _ = api.match(ctx, rects[0], rects[1], spec.pha_f, 1.0, want_best=False)
+    _, xyz, mask = api.median_reproject(ctx, api.recon_config(), disp)
+    x0, m0 = xyz.cpu().numpy(), mask.cpu().numpy()
+
+    # SOR
+    m2, _ = api.filter_sor(ctx, xyz, mask, 30, 1.0)
+    om2, _, _, snear = oracle_lib.sor(x0, m0, 30, 1.0, eps=EPS)
+    g2 = m2.cpu().numpy()
+    mis = g2 != om2
+    print("5MP SOR: valid", int(m0.sum()), "kept", int(om2.sum()), "mismatch", int(mis.sum()), "near", int(snear.sum()))
+    assert (mis & (snear == 0)).sum() == 0 and snear.sum() <= 20
+
+    # MLS on the SOR output (removed points read as zero, as in the pipeline)
+    x2 = xyz * m2.unsqueeze(-1).to(xyz.dtype)
+    w, sig, order, rad = 7, 2.0 / math.sqrt(2.0), 2, 2.0
+    x3 = api.filter_mls(ctx, x2, m2, w, sig, order, rad, 1)
+    ox3, mnear = oracle_lib.mls(x2.cpu().numpy(), g2, w, sig, order, rad, 1, eps=EPS)
+    g3 = x3.cpu().numpy()
+    v = g2 > 0
+    sel = v & (mnear == 0)
+    big = np.abs(ox3[sel]).max(axis=-1, keepdims=True).astype(np.float32)
+    err = np.abs(g3[sel].astype(np.float64) - ox3[sel])
+    print("5MP MLS: points", int(v.sum()), "flagged", int((v & ~sel).sum()), "max err mm", float(err.max()))
+    assert (err <= 1e-5 + 2 * np.spacing(big)).all()
+    assert (v & ~sel).sum() <= 0.0012 * v.sum()
+
+    # metric Gaussian on the MLS output
+    x4 = api.filter_metric_gaussian(ctx, x3, m2, 0.5)
+    ox4, gnear = oracle_lib.metric_gaussian(g3, g2, 0.5, eps=EPS)
+    g4 = x4.cpu().numpy()
+    sel = v & (gnear == 0)
+    big = np.abs(ox4[sel]).max(axis=-1, keepdims=True).astype(np.float32)
+    err = np.abs(g4[sel].astype(np.float64) - ox4[sel])
+    print("5MP metric Gaussian: flagged", int((v & ~sel).sum()), "max err mm", float(err.max()))
+    assert (err <= 1e-5 + 2 * np.spacing(big)).all()
+    assert (v & ~sel).sum() <= 2000
+
+    # the timed call composes exactly these stages
+    px, pm, _ = api.reconstruct_pair(ctx, cfg, config1_recon(api), torch.from_numpy(L).cuda(),
+                                     torch.from_numpy(R).cuda())
+    assert torch.equal(pm, m2) and torch.equal(px, x4)

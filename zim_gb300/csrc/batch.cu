@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(BT) batch_ror_kernel(const PairDev* __restrict
 
 struct zim_batch {
     zim_ctx* ctx = nullptr;
+    int device = 0;  // the context's device, kept so that destruction never reads the context
     std::vector<zim_rect_state> calibs;
     std::vector<zim_batch_pair> pairs;
     zim_recon_config rcfg{};
@@ -447,6 +448,7 @@ extern "C" ZIM_API zim_status zim_batch_create(zim_ctx* ctx, const zim_stereo_ca
     *out = nullptr;
     zim_batch* b = new zim_batch;
     b->ctx = ctx;
+    b->device = ctx->device;
     for (int i = 0; i < n_calibs; i++) {
         zim_rect_state st;
         zim_status s = zim_rect_build(ctx, &calibs[i], use_full_left, st);
@@ -465,14 +467,19 @@ extern "C" ZIM_API zim_status zim_batch_create(zim_ctx* ctx, const zim_stereo_ca
     return ZIM_OK;
 }
 
+// Destruction reads nothing of the batch's context, which a garbage-collected
+// host language may already have destroyed (the reverse order of creation is
+// not guaranteed there).  It cannot report errors, so it clears those its own
+// calls leave behind rather than let a later call of the thread report them.
 extern "C" ZIM_API void zim_batch_destroy(zim_batch* b) {
     if (!b) return;
-    cudaSetDevice(b->ctx->device);
+    cudaSetDevice(b->device);
     cudaDeviceSynchronize();
     release_submission(b);
     for (zim_rect_state& st : b->calibs) zim_rect_free(st);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
+    cudaGetLastError();
 }
 
 extern "C" ZIM_API zim_status zim_batch_rect_size(const zim_batch* b, int calib, int* rw, int* rh) {

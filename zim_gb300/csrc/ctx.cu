@@ -170,6 +170,7 @@ extern "C" ZIM_API void zim_destroy(zim_ctx* ctx) {
     if (ctx->aux_event) cudaEventDestroy(ctx->aux_event);
     if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     delete ctx;
+    cudaGetLastError();  // destruction cannot report: do not leave its errors to the thread's next call
 }
 
 extern "C" ZIM_API const char* zim_last_error(const zim_ctx* ctx) {

@@ -180,36 +180,27 @@ __device__ __forceinline__ void fit_accumulate(Visit& visit, float kw, float r2c
         for (int b = 0; b < a; b++) A[a][b] = A[b][a];
 }
 
-// MLS of one valid point.  visit(fn) calls fn(dx, dy, dz) with the offset from
-// the query point of every valid neighbour of its window (in a fixed order);
-// the distance test against the cut-off is made here.
-template <typename Visit>
-__device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, Visit visit, float& ox, float& oy,
-                                          float& oz, bool& moved) {
-    moved = false;
-    const float kw = -1.44269504088896341f * inv_2s2;  // -log2(e) / (2 s^2)
-    // 1. weighted centroid and covariance in one sweep, from the moments about
-    // the query point (offsets of at most the cut-off radius, so the FP32
-    // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
-    // ~1e-7 rad, far below the 1e-5 mm the points are held to)
-    float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
-    float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f;
-    int nv = 0;
-    visit([&](float dx, float dy, float dz) {
-        float d2 = dx * dx + dy * dy + dz * dz;
-        if (!(d2 <= r2c)) return;
-        float w = mls_weight(d2, kw);
-        cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
-        const float wx = w * dx, wy = w * dy;
-        m00 = fmaf(wx, dx, m00); m01 = fmaf(wx, dy, m01); m02 = fmaf(wx, dz, m02);
-        m11 = fmaf(wy, dy, m11); m12 = fmaf(wy, dz, m12); m22 = fmaf(w * dz, dz, m22);
-        ws += w;
-        nv++;
-    });
-    if (nv < 3 || ws < 1e-12f) return;
+// The state of one query after the first sweep: centroid (relative to the
+// query point), unit normal and orthonormal tangent frame, and the polynomial
+// order the fit uses.
+struct MlsFrame {
+    float cx, cy, cz;
+    float nx, ny, nz, t1x, t1y, t1z, t2x, t2y, t2z;
+    int cur;
+};
+
+// From the first sweep's weighted sums about the query point (weight sum ws,
+// in-radius count nv, sum w d, sum w d d^T): the centroid, the weighted
+// covariance about it, its smallest eigenvector (the normal) and the tangent
+// frame.  False when the point keeps its position (fewer than 3 neighbours or
+// no weight).  Order selection follows the CPU reference: order drops to 0
+// with fewer than {3, 5, 8}[order] neighbours.
+__device__ __forceinline__ bool mls_frame(float ws, int nv, float cx, float cy, float cz, float m00, float m01,
+                                          float m02, float m11, float m12, float m22, int order, MlsFrame& F) {
+    if (nv < 3 || ws < 1e-12f) return false;
     const float iw = 1.0f / ws;
     cx *= iw; cy *= iw; cz *= iw;
-    // 2. weighted covariance about the centroid: sum w d d^T - ws c c^T
+    // weighted covariance about the centroid: sum w d d^T - ws c c^T
     float C[3][3];
     C[0][0] = fmaf(-ws * cx, cx, m00); C[0][1] = fmaf(-ws * cx, cy, m01); C[0][2] = fmaf(-ws * cx, cz, m02);
     C[1][1] = fmaf(-ws * cy, cy, m11); C[1][2] = fmaf(-ws * cy, cz, m12); C[2][2] = fmaf(-ws * cz, cz, m22);
@@ -241,64 +232,118 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
             nx = ny = nz = 0.f;
         }
     }
+    F.cx = cx; F.cy = cy; F.cz = cz;
+    F.nx = nx; F.ny = ny; F.nz = nz;
+    F.t1x = t1x; F.t1y = t1y; F.t1z = t1z; F.t2x = t2x; F.t2y = t2y; F.t2z = t2z;
     const int min_nb = order == 2 ? 8 : (order == 1 ? 5 : 3);
-    int cur = nv >= min_nb ? order : 0;
-    // query point relative to the centroid: e0 = p - c = -c_rel
-    const float ex0 = -cx, ey0 = -cy, ez0 = -cz;
+    F.cur = nv >= min_nb ? order : 0;
+    return true;
+}
+
+// Singular-pivot thresholds of the Cholesky solve (the reference's 1e-12) for
+// a basis scaled by is = 1 / cut-off radius: the pivot of a degree-d row
+// scales by is^(2d).
+__device__ __forceinline__ void mls_thresholds(float is, float (&thr)[6]) {
+    const float s2 = is * is, s4 = s2 * s2;
+    thr[0] = 1e-12f; thr[1] = thr[2] = 1e-12f * s2; thr[3] = thr[4] = thr[5] = 1e-12f * s4;
+}
+
+// Solves the order-N normal equations (N = 6 falls back to order 1 on their
+// leading block, as the reference's 2 -> 1 fallback does) and projects the
+// query point onto the fitted surface (onto the tangent plane when no fit is
+// solved).  cur: the frame's order, lowered to 1 by the fallback.  (ox, oy,
+// oz) is the moved point relative to the query point.
+template <int N>
+__device__ __forceinline__ void mls_solve_project(const MlsFrame& F, int cur, const float (&A)[N][N],
+                                                  const float (&bv)[N], float is, float& ox, float& oy, float& oz) {
+    float thr[6];
+    mls_thresholds(is, thr);
     bool solved = false;
     float co[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
-    // radius): the fitted surface is the same, the normal equations are O(1).
-    const float is = rsqrtf(r2c);
-    float thr[6];
-    {
-        const float s2 = is * is, s4 = s2 * s2;  // pivot of degree-d row scales by h^(-2d)
-        thr[0] = 1e-12f; thr[1] = thr[2] = 1e-12f * s2; thr[3] = thr[4] = thr[5] = 1e-12f * s4;
-    }
-    if (cur == 2) {
-        float A[6][6], bv[6], x6[6];
-        fit_accumulate<6>(visit, kw, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
-        solved = cholesky_fixed<6>(A, bv, x6, thr);
+    if (cur == 2 && N == 6) {
+        float x6[N];
+        solved = cholesky_fixed<N>(A, bv, x6, thr);
         if (solved) {
 #pragma unroll
-            for (int a = 0; a < 6; a++) co[a] = x6[a];
-        } else {
-            // order 1 on the leading block of the same normal equations
-            float A3[3][3], b3[3], x3[3];
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                b3[a] = bv[a];
-#pragma unroll
-                for (int b = 0; b < 3; b++) A3[a][b] = A[a][b];
-            }
-            solved = cholesky_fixed<3>(A3, b3, x3, thr);
-            if (solved) {
-                cur = 1;
-#pragma unroll
-                for (int a = 0; a < 3; a++) co[a] = x3[a];
-            }
+            for (int a = 0; a < N; a++) co[a] = x6[a];
         }
-    } else if (cur == 1) {
-        float A[3][3], bv[3], x3[3];
-        fit_accumulate<3>(visit, kw, r2c, is, cx, cy, cz, t1x, t1y, t1z, t2x, t2y, t2z, nx, ny, nz, A, bv);
-        solved = cholesky_fixed<3>(A, bv, x3, thr);
-        if (solved)
+    }
+    if (cur >= 1 && !solved) {
+        // order 1 on the leading 3 x 3 block of the same normal equations
+        float A3[3][3], b3[3], x3[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            b3[a] = bv[a];
+#pragma unroll
+            for (int b = 0; b < 3; b++) A3[a][b] = A[a][b];
+        }
+        solved = cholesky_fixed<3>(A3, b3, x3, thr);
+        if (solved) {
+            cur = 1;
 #pragma unroll
             for (int a = 0; a < 3; a++) co[a] = x3[a];
+        }
     }
+    // query point relative to the centroid: e0 = p - c = -c_rel
+    const float ex0 = -F.cx, ey0 = -F.cy, ez0 = -F.cz;
     if (!solved) {
-        float dot = ex0 * nx + ey0 * ny + ez0 * nz;
-        ox = -dot * nx; oy = -dot * ny; oz = -dot * nz;
+        float dot = ex0 * F.nx + ey0 * F.ny + ez0 * F.nz;
+        ox = -dot * F.nx; oy = -dot * F.ny; oz = -dot * F.nz;
     } else {
-        float u0 = ex0 * t1x + ey0 * t1y + ez0 * t1z;
-        float v0 = ex0 * t2x + ey0 * t2y + ez0 * t2z;
+        float u0 = ex0 * F.t1x + ey0 * F.t1y + ez0 * F.t1z;
+        float v0 = ex0 * F.t2x + ey0 * F.t2y + ez0 * F.t2z;
         float us = u0 * is, vs = v0 * is;
         float ff = co[0] + co[1] * us + co[2] * vs;
         if (cur == 2) ff += co[3] * us * us + co[4] * us * vs + co[5] * vs * vs;
         // out = c + u0 t1 + v0 t2 + f n = p + (c_rel + u0 t1 + v0 t2 + f n)
-        ox = cx + u0 * t1x + v0 * t2x + ff * nx;
-        oy = cy + u0 * t1y + v0 * t2y + ff * ny;
-        oz = cz + u0 * t1z + v0 * t2z + ff * nz;
+        ox = F.cx + u0 * F.t1x + v0 * F.t2x + ff * F.nx;
+        oy = F.cy + u0 * F.t1y + v0 * F.t2y + ff * F.ny;
+        oz = F.cz + u0 * F.t1z + v0 * F.t2z + ff * F.nz;
+    }
+}
+
+// MLS of one valid point.  visit(fn) calls fn(dx, dy, dz) with the offset from
+// the query point of every valid neighbour of its window (in a fixed order);
+// the distance test against the cut-off is made here.
+template <typename Visit>
+__device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, Visit visit, float& ox, float& oy,
+                                          float& oz, bool& moved) {
+    moved = false;
+    const float kw = -1.44269504088896341f * inv_2s2;  // -log2(e) / (2 s^2)
+    // 1. weighted centroid and covariance in one sweep, from the moments about
+    // the query point (offsets of at most the cut-off radius, so the FP32
+    // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
+    // ~1e-7 rad, far below the 1e-5 mm the points are held to)
+    float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
+    float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f;
+    int nv = 0;
+    visit([&](float dx, float dy, float dz) {
+        float d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 <= r2c)) return;
+        float w = mls_weight(d2, kw);
+        cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
+        const float wx = w * dx, wy = w * dy;
+        m00 = fmaf(wx, dx, m00); m01 = fmaf(wx, dy, m01); m02 = fmaf(wx, dz, m02);
+        m11 = fmaf(wy, dy, m11); m12 = fmaf(wy, dz, m12); m22 = fmaf(w * dz, dz, m22);
+        ws += w;
+        nv++;
+    });
+    MlsFrame F;
+    if (!mls_frame(ws, nv, cx, cy, cz, m00, m01, m02, m11, m12, m22, order, F)) return;
+    // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
+    // radius): the fitted surface is the same, the normal equations are O(1).
+    const float is = rsqrtf(r2c);
+    if (F.cur == 2) {
+        float A[6][6], bv[6];
+        fit_accumulate<6>(visit, kw, r2c, is, F.cx, F.cy, F.cz, F.t1x, F.t1y, F.t1z, F.t2x, F.t2y, F.t2z, F.nx, F.ny,
+                          F.nz, A, bv);
+        mls_solve_project<6>(F, 2, A, bv, is, ox, oy, oz);
+    } else {
+        float A[3][3] = {}, bv[3] = {};
+        if (F.cur == 1)
+            fit_accumulate<3>(visit, kw, r2c, is, F.cx, F.cy, F.cz, F.t1x, F.t1y, F.t1z, F.t2x, F.t2y, F.t2z, F.nx,
+                              F.ny, F.nz, A, bv);
+        mls_solve_project<3>(F, F.cur, A, bv, is, ox, oy, oz);
     }
     moved = true;
 }
@@ -333,6 +378,8 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
 // The tile and its hw halo staged in shared memory as float4, NaN for invalid
 // and off-image pixels (their distance test fails).
 inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * hw) * sizeof(float4); }
+// The same for the two-row tiles of mls_pair_kernel (MX x 2 MY pixels).
+inline size_t mls_pair_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (2 * MY + 2 * hw) * sizeof(float4); }
 
 // With pixel rays (rays != 0) each row of the window is cut to the disk beyond
 // which the ray bound puts every point outside the cut-off: the pixels left out
@@ -425,6 +472,249 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     dst[3 * o + 2] = moved ? pz + oz : pz;
 }
 
+// ---- two queries per thread in packed FP32x2 ----
+//
+// Blackwell issues a pair of FP32 adds, multiplies or fused multiply-adds as
+// one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn: each lane rounded as
+// the scalar operation).  A thread takes the queries of rows y and y + 1 of
+// one column; every neighbour of the two windows is loaded once, and the
+// offsets, distances and weighted sums of both queries advance together in
+// the two lanes of each packed operation.  Only the weights (one ex2 each),
+// the per-query frame, solve and projection are scalar.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
+// Visits the union of the two queries' windows (row offsets -hw .. hw + 1
+// from the upper query), each row cut to the wider of the two queries' ray
+// disks; fn(q, row_a, row_b) gets the staged neighbour and whether the row
+// lies in each query's own window.  A neighbour inside the union but outside
+// a query's disk fails that query's distance test, so each query sees exactly
+// the in-radius neighbours of its window, in window order.
+template <typename Fn>
+__device__ __forceinline__ void pair_visit(const float4* sp, int cc, int TW, int hw, float wr2, Fn&& fn) {
+    for (int i = -hw; i <= hw + 1; i++) {
+        const int m = min(abs(i), abs(i - 1));
+        const float rem = wr2 - (float)(m * m);
+        if (rem < 0.f) continue;
+        const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
+        const bool row_a = i <= hw, row_b = i > -hw;
+        for (int j = -w; j <= w; j++) fn(sp[cc + i * TW + j], row_a, row_b);
+    }
+}
+
+// Offsets of neighbour q from the two queries, their squared lengths and
+// in-radius weights; a lane whose test fails gets weight 0 and zero offsets
+// (so a NaN or far neighbour adds exact zeros to that lane's sums).  ok_a /
+// ok_b come in as "the lane may take it" and leave as "the lane took it".
+// False when neither lane takes the neighbour.
+__device__ __forceinline__ bool pair_offsets(const float4& q, bool& ok_a, bool& ok_b, float2 npx, float2 npy,
+                                             float2 npz, float r2c, float2 kw2, float2& dx, float2& dy, float2& dz,
+                                             float2& w) {
+    dx = add2(dup2(q.x), npx);
+    dy = add2(dup2(q.y), npy);
+    dz = add2(dup2(q.z), npz);
+    const float2 d2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+    ok_a = ok_a && d2.x <= r2c;
+    ok_b = ok_b && d2.y <= r2c;
+    if (!(ok_a || ok_b)) return false;
+    const float2 t = mul2(d2, kw2);
+    float ea, eb;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ea) : "f"(t.x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(eb) : "f"(t.y));
+    w = make_float2(ok_a ? ea : 0.f, ok_b ? eb : 0.f);
+    if (!(ok_a && ok_b)) {
+        if (!ok_a) { dx.x = 0.f; dy.x = 0.f; dz.x = 0.f; }
+        if (!ok_b) { dx.y = 0.f; dy.y = 0.f; dz.y = 0.f; }
+    }
+    return true;
+}
+
+template <int HW>
+__global__ void __launch_bounds__(MX* MY) mls_pair_kernel(const float* __restrict__ src,
+                                                          const uint8_t* __restrict__ mask, int rows, int cols,
+                                                          int hw_arg, float inv_2s2, int order, float r2c, int rays,
+                                                          zt::RayParams rp, float* __restrict__ dst) {
+    extern __shared__ float4 mls_sp[];
+    __shared__ unsigned warp_dev[MX * MY / 32];
+    const int hw = HW ? HW : hw_arg;
+    const int TW = MX + 2 * hw, TH = 2 * MY + 2 * hw;
+    const int gx0 = blockIdx.x * MX - hw, gy0 = blockIdx.y * (2 * MY) - hw;
+    const int tid = threadIdx.y * MX + threadIdx.x;
+    unsigned tdev = 0u;  // largest ray distance of this thread's staged points (float bits, >= 0)
+    for (int t = tid; t < TW * TH; t += MX * MY) {
+        const int ty = t / TW, tx = t - ty * TW;
+        const int gx = gx0 + tx, gy = gy0 + ty;
+        float4 v = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+        if (gx >= 0 && gy >= 0 && gx < cols && gy < rows) {
+            const size_t q = (size_t)gy * cols + gx;
+            if (__ldg(mask + q)) {
+                v = make_float4(__ldg(src + 3 * q), __ldg(src + 3 * q + 1), __ldg(src + 3 * q + 2), 1.f);
+                if (rays) {
+                    float ax, ay, az;
+                    zt::ray_dir(rp, gx, gy, ax, ay, az);
+                    const float d = zt::ray_dev(v.x, v.y, v.z, ax, ay, az);
+                    tdev = max(tdev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
+                }
+            }
+        }
+        mls_sp[t] = v;
+    }
+    tdev = __reduce_max_sync(0xffffffffu, tdev);
+    if ((tid & 31) == 0) warp_dev[tid >> 5] = tdev;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < MX * MY / 32; j++) tdev = max(tdev, warp_dev[j]);
+    const int x = blockIdx.x * MX + threadIdx.x, y0 = blockIdx.y * (2 * MY) + 2 * threadIdx.y;
+    const bool in_a = x < cols && y0 < rows, in_b = x < cols && y0 + 1 < rows;
+    const int cc = (2 * threadIdx.y + hw) * TW + threadIdx.x + hw;  // upper query's tile index
+    const float4 ca = mls_sp[cc], cb = mls_sp[cc + TW];
+    const bool va = in_a && ca.w != 0.f, vb = in_b && cb.w != 0.f;
+    float wr2 = INFINITY;  // squared pixel radius of the warp's disk
+    if (rays) {
+        float rs2 = 0.f;
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            const float4 c = l ? cb : ca;
+            if (!(l ? vb : va)) continue;
+            float ax, ay, az;
+            zt::ray_dir(rp, x, y0 + l, ax, ay, az);
+            const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
+            const float qn = sqrtf(fmaf(c.x, c.x, fmaf(c.y, c.y, c.z * c.z)));
+            const float C = qn * rp.f / an;
+            const float sd = sqrtf(r2c) + zt::ray_dev(c.x, c.y, c.z, ax, ay, az) + __uint_as_float(tdev) + 1e-5f * qn;
+            float r2 = INFINITY;
+            if (C > sd) {
+                const float r = sd * an / (C - sd);
+                r2 = r * r;
+            }
+            rs2 = fmaxf(rs2, r2);
+        }
+        wr2 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(rs2)));
+    }
+    if (!in_a) return;
+    float oa0 = ca.x, oa1 = ca.y, oa2 = ca.z, ob0 = cb.x, ob1 = cb.y, ob2 = cb.z;  // outputs: unmoved by default
+    if (va || vb) {
+        const float kw = -1.44269504088896341f * inv_2s2;  // -log2(e) / (2 s^2)
+        const float2 kw2 = dup2(kw);
+        // a lane without a query gets a finite stand-in; all its tests fail
+        const float2 npx = make_float2(va ? -ca.x : 0.f, vb ? -cb.x : 0.f);
+        const float2 npy = make_float2(va ? -ca.y : 0.f, vb ? -cb.y : 0.f);
+        const float2 npz = make_float2(va ? -ca.z : 0.f, vb ? -cb.z : 0.f);
+        // 1. weighted centroid and covariance sums about each query point
+        float2 cx = dup2(0.f), cy = dup2(0.f), cz = dup2(0.f), ws = dup2(0.f);
+        float2 m00 = dup2(0.f), m01 = dup2(0.f), m02 = dup2(0.f), m11 = dup2(0.f), m12 = dup2(0.f), m22 = dup2(0.f);
+        int nva = 0, nvb = 0;
+        pair_visit(mls_sp, cc, TW, hw, wr2, [&](const float4& q, bool row_a, bool row_b) {
+            float2 dx, dy, dz, w;
+            bool ta = row_a && va, tb = row_b && vb;
+            if (!pair_offsets(q, ta, tb, npx, npy, npz, r2c, kw2, dx, dy, dz, w)) return;
+            cx = fma2(w, dx, cx); cy = fma2(w, dy, cy); cz = fma2(w, dz, cz);
+            const float2 wx = mul2(w, dx), wy = mul2(w, dy);
+            m00 = fma2(wx, dx, m00); m01 = fma2(wx, dy, m01); m02 = fma2(wx, dz, m02);
+            m11 = fma2(wy, dy, m11); m12 = fma2(wy, dz, m12); m22 = fma2(mul2(w, dz), dz, m22);
+            ws = add2(ws, w);
+            nva += ta;
+            nvb += tb;
+        });
+        MlsFrame Fa{}, Fb{};
+        const bool fa = va && mls_frame(ws.x, nva, cx.x, cy.x, cz.x, m00.x, m01.x, m02.x, m11.x, m12.x, m22.x, order, Fa);
+        const bool fb = vb && mls_frame(ws.y, nvb, cx.y, cy.y, cz.y, m00.y, m01.y, m02.y, m11.y, m12.y, m22.y, order, Fb);
+        const float is = rsqrtf(r2c);
+        const int fit_a = fa ? Fa.cur : 0, fit_b = fb ? Fb.cur : 0;
+        float da0 = 0.f, da1 = 0.f, da2 = 0.f, db0 = 0.f, db1 = 0.f, db2 = 0.f;
+        if (order >= 1 && (fit_a >= 1 || fit_b >= 1)) {
+            // 2. the polynomial fit's moments in each query's tangent frame
+            // (u = (d - c) . t1 is as one FMA chain on d; likewise v, f)
+            const float2 ax = make_float2(Fa.t1x * is, Fb.t1x * is), ay = make_float2(Fa.t1y * is, Fb.t1y * is),
+                         az = make_float2(Fa.t1z * is, Fb.t1z * is);
+            const float2 bx = make_float2(Fa.t2x * is, Fb.t2x * is), by = make_float2(Fa.t2y * is, Fb.t2y * is),
+                         bz = make_float2(Fa.t2z * is, Fb.t2z * is);
+            const float2 nx = make_float2(Fa.nx, Fb.nx), ny = make_float2(Fa.ny, Fb.ny), nz = make_float2(Fa.nz, Fb.nz);
+            const float2 nuc = make_float2(-fmaf(Fa.cx, ax.x, fmaf(Fa.cy, ay.x, Fa.cz * az.x)),
+                                           -fmaf(Fb.cx, ax.y, fmaf(Fb.cy, ay.y, Fb.cz * az.y)));
+            const float2 nvc = make_float2(-fmaf(Fa.cx, bx.x, fmaf(Fa.cy, by.x, Fa.cz * bz.x)),
+                                           -fmaf(Fb.cx, bx.y, fmaf(Fb.cy, by.y, Fb.cz * bz.y)));
+            const float2 nfc = make_float2(-fmaf(Fa.cx, nx.x, fmaf(Fa.cy, ny.x, Fa.cz * nz.x)),
+                                           -fmaf(Fb.cx, nx.y, fmaf(Fb.cy, ny.y, Fb.cz * nz.y)));
+            const bool six = order == 2;
+            float2 M00 = dup2(0.f), M10 = dup2(0.f), M01 = dup2(0.f), M20 = dup2(0.f), M11 = dup2(0.f),
+                   M02 = dup2(0.f);
+            float2 M30 = dup2(0.f), M21 = dup2(0.f), M12 = dup2(0.f), M03 = dup2(0.f), M40 = dup2(0.f),
+                   M31 = dup2(0.f), M22 = dup2(0.f), M13 = dup2(0.f), M04 = dup2(0.f);
+            float2 B0 = dup2(0.f), B1 = dup2(0.f), B2 = dup2(0.f), B3 = dup2(0.f), B4 = dup2(0.f), B5 = dup2(0.f);
+            const bool ua = va && fit_a >= 1, ub = vb && fit_b >= 1;
+            pair_visit(mls_sp, cc, TW, hw, wr2, [&](const float4& q, bool row_a, bool row_b) {
+                float2 dx, dy, dz, w;
+                bool ta = row_a && ua, tb = row_b && ub;
+                if (!pair_offsets(q, ta, tb, npx, npy, npz, r2c, kw2, dx, dy, dz, w)) return;
+                const float2 u = fma2(dx, ax, fma2(dy, ay, fma2(dz, az, nuc)));
+                const float2 v = fma2(dx, bx, fma2(dy, by, fma2(dz, bz, nvc)));
+                const float2 f = fma2(dx, nx, fma2(dy, ny, fma2(dz, nz, nfc)));
+                const float2 wu = mul2(w, u), wv = mul2(w, v), wf = mul2(w, f);
+                M00 = add2(M00, w); M10 = add2(M10, wu); M01 = add2(M01, wv);
+                M20 = fma2(wu, u, M20); M11 = fma2(wu, v, M11); M02 = fma2(wv, v, M02);
+                B0 = add2(B0, wf); B1 = fma2(wf, u, B1); B2 = fma2(wf, v, B2);
+                if (six) {
+                    const float2 uu = mul2(u, u), uv = mul2(u, v), vv = mul2(v, v);
+                    M30 = fma2(wu, uu, M30); M21 = fma2(wu, uv, M21); M12 = fma2(wu, vv, M12); M03 = fma2(wv, vv, M03);
+                    const float2 wuu = mul2(wu, u), wvv = mul2(wv, v);
+                    M40 = fma2(wuu, uu, M40); M31 = fma2(wuu, uv, M31); M22 = fma2(wuu, vv, M22);
+                    M13 = fma2(wvv, uv, M13); M04 = fma2(wvv, vv, M04);
+                    B3 = fma2(wf, uu, B3); B4 = fma2(wf, uv, B4); B5 = fma2(wf, vv, B5);
+                }
+            });
+            auto fit_lane = [&](const MlsFrame& F, int cur, bool hi, float& o0, float& o1, float& o2) {
+                auto pick = [hi](float2 a) { return hi ? a.y : a.x; };
+                if (six) {
+                    float A[6][6], bv[6];
+                    A[0][0] = pick(M00); A[0][1] = pick(M10); A[0][2] = pick(M01);
+                    A[1][1] = pick(M20); A[1][2] = pick(M11); A[2][2] = pick(M02);
+                    A[0][3] = pick(M20); A[0][4] = pick(M11); A[0][5] = pick(M02);
+                    A[1][3] = pick(M30); A[1][4] = pick(M21); A[1][5] = pick(M12);
+                    A[2][3] = pick(M21); A[2][4] = pick(M12); A[2][5] = pick(M03);
+                    A[3][3] = pick(M40); A[3][4] = pick(M31); A[3][5] = pick(M22);
+                    A[4][4] = pick(M22); A[4][5] = pick(M13); A[5][5] = pick(M04);
+                    bv[0] = pick(B0); bv[1] = pick(B1); bv[2] = pick(B2);
+                    bv[3] = pick(B3); bv[4] = pick(B4); bv[5] = pick(B5);
+#pragma unroll
+                    for (int a = 0; a < 6; a++)
+#pragma unroll
+                        for (int b = 0; b < a; b++) A[a][b] = A[b][a];
+                    mls_solve_project<6>(F, cur, A, bv, is, o0, o1, o2);
+                } else {
+                    float A[3][3], bv[3];
+                    A[0][0] = pick(M00); A[0][1] = pick(M10); A[0][2] = pick(M01);
+                    A[1][1] = pick(M20); A[1][2] = pick(M11); A[2][2] = pick(M02);
+                    A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
+                    bv[0] = pick(B0); bv[1] = pick(B1); bv[2] = pick(B2);
+                    mls_solve_project<3>(F, cur, A, bv, is, o0, o1, o2);
+                }
+            };
+            if (fa && fit_a >= 1) fit_lane(Fa, fit_a, false, da0, da1, da2);
+            if (fb && fit_b >= 1) fit_lane(Fb, fit_b, true, db0, db1, db2);
+        }
+        // order 0 (or a query whose order dropped to 0): the tangent-plane projection
+        {
+            float A[3][3] = {}, bv[3] = {};
+            if (fa && fit_a < 1) mls_solve_project<3>(Fa, 0, A, bv, is, da0, da1, da2);
+            if (fb && fit_b < 1) mls_solve_project<3>(Fb, 0, A, bv, is, db0, db1, db2);
+        }
+        if (fa) { oa0 += da0; oa1 += da1; oa2 += da2; }
+        if (fb) { ob0 += db0; ob1 += db1; ob2 += db2; }
+    }
+    const size_t o = (size_t)y0 * cols + x;
+    // invalid pixels pass their input through (the staged value is NaN there)
+    if (!va) { oa0 = src[3 * o]; oa1 = src[3 * o + 1]; oa2 = src[3 * o + 2]; }
+    dst[3 * o] = oa0; dst[3 * o + 1] = oa1; dst[3 * o + 2] = oa2;
+    if (in_b) {
+        const size_t o1 = o + cols;
+        if (!vb) { ob0 = src[3 * o1]; ob1 = src[3 * o1 + 1]; ob2 = src[3 * o1 + 2]; }
+        dst[3 * o1] = ob0; dst[3 * o1 + 1] = ob1; dst[3 * o1 + 2] = ob2;
+    }
+}
+
 }  // namespace
 
 size_t zim_mls_scratch_bytes(size_t n_points) { return zim_align256(n_points * 12); }
@@ -437,11 +727,11 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const int ord = order < 0 ? 0 : (order > 2 ? 2 : order);
     const int n_iter = iterations < 1 ? 1 : iterations;
     dim3 blk(MX, MY), grd((cols + MX - 1) / MX, (rows + MY - 1) / MY);
-    const size_t smem = mls_smem_bytes(window);
+    dim3 grd2((cols + MX - 1) / MX, (rows + 2 * MY - 1) / (2 * MY));
+    const size_t smem = mls_pair_smem_bytes(window);
     const bool use_smem = smem <= 96 * 1024;
-    if (use_smem)
-        ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(window == 7 ? mls_smem_kernel<7> : mls_smem_kernel<0>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = window == 7 ? mls_pair_kernel<7> : mls_pair_kernel<0>;
+    if (use_smem) ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int use_rays = use_smem && rays.valid;
     const zt::RayParams rp = zt::ray_params(rays);
     // ping-pong so that the last pass lands in `out`
@@ -450,8 +740,7 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
         if (use_smem)
-            (window == 7 ? mls_smem_kernel<7> : mls_smem_kernel<0>)<<<grd, blk, smem, st>>>(
-                in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp, dst);
+            kern<<<grd2, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp, dst);
         else
             mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;
