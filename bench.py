@@ -142,7 +142,7 @@ def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
     import torch
     H, W = dL.shape[1:]
     st = torch.cuda.current_stream()
-    names = ["decode", "rectify", "match", "median_reproject", "sor", "mls", "metric_gaussian"]
+    names = ["decode", "rectify_match", "median_reproject", "sor", "mls", "metric_gaussian"]
     acc = {n: 0.0 for n in names}
     cnt = {n: 0 for n in names}
     ev = lambda: torch.cuda.Event(enable_timing=True)
@@ -157,10 +157,8 @@ def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
         e[1].record(st)
         dr = api.decode(ctx, dcfg, dR, want_mod=False, want_valid=False)
         e[2].record(st)
-        rl = api.rectify(ctx, 0, dl["order"], dl["residual"], True)
-        rr = api.rectify(ctx, 1, dr["order"], dr["residual"], True)
+        disp = api.rectify_match(ctx, (dl["order"], dl["residual"]), (dr["order"], dr["residual"]), spec.pha_f)
         e[3].record(st)
-        disp, _ = api.match(ctx, rl, rr, spec.pha_f, 1.0, want_best=False)
         e[4].record(st)
         _, xyz, mask = api.median_reproject(ctx, rcfg, disp)
         e[5].record(st)
@@ -172,8 +170,7 @@ def stage_breakdown(api, ctx, dcfg, rcfg, spec, dL, dR, steps):
         e[8].record(st)
         torch.cuda.synchronize()
         acc["decode"] += e[0].elapsed_time(e[1]) + e[1].elapsed_time(e[2]); cnt["decode"] += 2
-        acc["rectify"] += e[2].elapsed_time(e[3]); cnt["rectify"] += 2
-        acc["match"] += e[3].elapsed_time(e[4]); cnt["match"] += 1
+        acc["rectify_match"] += e[2].elapsed_time(e[4]); cnt["rectify_match"] += 1
         acc["median_reproject"] += e[4].elapsed_time(e[5]); cnt["median_reproject"] += 1
         acc["sor"] += e[5].elapsed_time(e[6]); cnt["sor"] += 1
         acc["mls"] += e[6].elapsed_time(e[7]); cnt["mls"] += 1
@@ -272,7 +269,9 @@ def run_ours(args):
         # algorithmic bytes per launch: each stage's compulsory reads + writes per source pixel (npx)
         # or rectified pixel (rpx), e.g. decode reads F u16 frames and writes an int32 fringe order
         # and an f32 residual phase (8 B)
-        alg = {"decode": npx * (F * 2 + 8), "rectify": npx * 8 + rpx * 12, "match": rpx * (12 + 12 + 4),
+        # rectify_match: both cameras' decoded maps read (8 B per source pixel each; the post-smooth's
+        # taps are an intermediate) and the raw disparity written (4 B per rectified pixel)
+        alg = {"decode": npx * (F * 2 + 8), "rectify_match": 2 * npx * 8 + rpx * 4,
                "median_reproject": rpx * (4 + 13), "sor": rpx * (13 + 13), "mls": rpx * (13 + 12),
                "metric_gaussian": rpx * (13 + 12)}
         stages = {n: {"ms_per_step": round(per_step[n], 4), "ms_per_launch": round(per_launch[n], 4),
@@ -308,7 +307,7 @@ def run_ours(args):
         if not args.no_diff:
             result["diff"] = run_diff(api, local, steps=5, warmup=3,
                                       want_cpu=world == 1 and not args.no_cpu_baseline)
-        if args.refine:
+        if not args.no_refine:
             result["refine"] = run_refine(api, local, args.refine_poses, args.refine_iters)
         print(json.dumps(result))
     if dist:
@@ -397,6 +396,14 @@ def cpu_diff_baseline(spec, ctx, pose, theta):
     o = O.diff_eval(geom, theta, order[0], res[0], order[1], res[1], pose.best.cpu().numpy(), pose.plane,
                     want_grad_abs=True)
     dt = time.perf_counter() - t
+    # the same gradient with only the sample positions rounded to FP32: the
+    # floor FP32 positions put under an FP32 implementation
+    O.diff_round_positions(True)
+    try:
+        o["grad_fp32_positions"] = O.diff_eval(geom, theta, order[0], res[0], order[1], res[1],
+                                               pose.best.cpu().numpy(), pose.plane)["grad"]
+    finally:
+        O.diff_round_positions(False)
     return o, dt
 
 
@@ -443,22 +450,30 @@ def run_diff(api, local, steps, warmup, want_cpu=True):
         out["grad_err_vs_fp64"] = {"normwise_rel": float(np.linalg.norm(g - go) / np.linalg.norm(go)),
                                    "worst_component_rel": float(np.max(np.abs(g - go) / np.abs(go))),
                                    "loss_rel": float(abs(one["loss"] - o["loss"]) / o["loss"])}
-        # per component: the error against the FP64 oracle, and the floor FP32
-        # per-point terms put under it -- the unit roundoff 2^-24 times the
-        # cancellation factor sum|term| / |sum term| of that component
+        # per component: the error against the FP64 oracle, the cancellation
+        # factor sum|term| / |sum term|, and the floor of FP32 sample
+        # positions (the FP64 oracle's own change when only its positions are
+        # rounded to FP32)
         from zim_gb300 import diff as D
         canc = o["grad_abs"] / np.maximum(np.abs(go), 1e-300)
+        gp = o["grad_fp32_positions"]
         out["grad_components"] = {
             D.PARAM_NAMES[k]: {"rel_err": float(abs(g[k] - go[k]) / abs(go[k])), "cancellation": float(canc[k]),
-                               "fp32_floor": float(canc[k] * 2.0 ** -24)} for k in range(len(go))}
+                               "fp32_position_floor": float(abs(gp[k] - go[k]) / abs(go[k]))}
+            for k in range(len(go))}
+        out["grad_err_vs_fp64"]["fp32_position_floor_normwise"] = float(np.linalg.norm(gp - go) /
+                                                                         np.linalg.norm(go))
         out["cpu_baseline"] = {"value": round(o["n_points"] / dt / 1e6, 4), "unit": "Mpoints/s (forward+adjoint)",
                                "cores": 1, "kind": "port", "sample": "pose 0 of 8, FP64 oracle, one thread",
                                "seconds": round(dt, 3)}
     return out
 
 
-def run_refine(api, local, n_poses=32, iterations=200):
-    """Config 4: calibration refinement from a perturbed calibration."""
+def run_refine(api, local, n_poses=8, iterations=60):
+    """Config 4 (scaled: n_poses of its 32 planar-target poses, `iterations`
+    of its 200 Levenberg-Marquardt steps; --refine-poses 32 --refine-iters 200
+    runs it in full): calibration refinement from the perturbed calibration,
+    with every parameter's final error against the true calibration."""
     import numpy as np
     import torch
     from zim_gb300 import calib_refine as CR, diff, synth
@@ -488,7 +503,9 @@ def run_refine(api, local, n_poses=32, iterations=200):
     names = diff.PARAM_NAMES
     err0 = th0 - theta_true
     err1 = th - theta_true
-    return {"poses": n_poses, "iterations": iterations, "seconds": round(log.seconds, 3),
+    return {"workload": f"{n_poses} of config 4's 32 planar-target poses at 2448x2048, {iterations} of its 200 "
+                        "Levenberg-Marquardt iterations, from baseline +0.5%, cx0 +3 px, k1_0 +0.02",
+            "poses": n_poses, "iterations": iterations, "seconds": round(log.seconds, 3),
             "iterations_per_s": round(iterations / log.seconds, 3), "prepare_s": round(prep_s, 1),
             "start_error": {names[k]: float(err0[k]) for k in (2, 4, 12)},
             "final_error": {n: float(e) for n, e in zip(names, err1)},
@@ -496,9 +513,9 @@ def run_refine(api, local, n_poses=32, iterations=200):
 
 
 BATCH_WORKLOAD = ("64 seeded stereo pairs, sizes drawn from {640x480, 1280x1024, 2448x2048, 4096x3000}, each "
-                  "4-step + 5-bit Gray + complementary (config-0 scene/rig, u8) or 3-frequency heterodyne "
-                  "121/110/120 x 4 steps (config-1 scene/rig, u8); decode+rectify+match+median+reproject+pixel "
-                  "Gaussian+radius outlier filter (reference defaults); 8 distinct calibrations")
+                  "4-step + 5-bit Gray + complementary (config-0 scene/rig, u8) or three-frequency 1/8/64 x 4 steps "
+                  "(config-1 scene/rig, 12-bit u16); decode+rectify+match+median+reproject+pixel Gaussian+radius "
+                  "outlier filter (reference defaults); 8 distinct calibrations")
 
 
 def run_batch(api, local, steps, warmup, n_pairs=64):
@@ -640,9 +657,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diff", action="store_true", help="skip the forward/adjoint leg (8 planar poses)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (64 mixed pairs)")
-    ap.add_argument("--refine", action="store_true", help="also run calibration refinement (32 poses)")
-    ap.add_argument("--refine-poses", type=int, default=32)
-    ap.add_argument("--refine-iters", type=int, default=200)
+    ap.add_argument("--no-refine", action="store_true", help="skip the calibration-refinement leg")
+    ap.add_argument("--refine", action="store_true", help="(the refinement leg runs by default)")
+    ap.add_argument("--refine-poses", type=int, default=8)
+    ap.add_argument("--refine-iters", type=int, default=60)
     ap.add_argument("--width", type=int, default=2448, help="camera width (default: the 5 MP workload)")
     ap.add_argument("--height", type=int, default=2048)
     args = ap.parse_args()

@@ -309,6 +309,19 @@ ZIM_API zim_status zim_filter_metric_gaussian(zim_ctx* ctx, const float* xyz, co
                                               int rows, int cols, double sigma, float* out,
                                               void* stream);
 
+/* setData + stereoMatch in one step (JSLAB_PhaseEpipolarReconstructor_V2.cpp:
+ * 368-395 then :933-1006; the order zim_reconstruct_pair runs them in): the
+ * optional post-smooth of both cameras' decoded maps (source size rows x cols,
+ * as zim_rectify's post_smooth), then one launch that rectifies each right row
+ * into on-chip memory and each left pixel in registers and matches them.
+ * disp (rect_h x rect_w) is the raw disparity of zim_match; the rectified
+ * maps are never written.  Equal to zim_rectify of both cameras followed by
+ * zim_match, bit for bit. */
+ZIM_API zim_status zim_rectify_match(zim_ctx* ctx, const int32_t* l_order, const float* l_res,
+                                     const int32_t* r_order, const float* r_res, int rows, int cols,
+                                     int post_smooth, int pha_f, double grad_threshold, float* disp,
+                                     void* stream);
+
 /* Compacts valid points into PCL PointXYZ layout; *count_dev (device) gets the
  * number written.  Row-major order is preserved. */
 ZIM_API zim_status zim_compact_points(zim_ctx* ctx, const float* xyz, const uint8_t* mask,

@@ -395,6 +395,11 @@ def diff_eval(geom, theta, order_l, res_l, order_r, res_r, best, plane, zmin=0.0
     return out
 
 
+def diff_round_positions(on: bool):
+    """zo_diff_round_positions: round diff_eval's sample positions to FP32."""
+    lib().zo_diff_round_positions(C.c_int(int(bool(on))))
+
+
 def _setup_prototypes():
     L = lib()
     L.zo_decode.restype = C.c_int

@@ -184,6 +184,10 @@ void zo_diff_eval(const zo_diff_geom* G, const double theta[16], const int32_t* 
                   double zmin, double zmax, double loss_weight, double* loss, double* npts, double grad[16],
                   double jtj[256], double* xyz, uint8_t* mask, double* gphase_l, double* gphase_r, int32_t* cells,
                   int cells_mode, double gabs[16]);
+/* on != 0: zo_diff_eval rounds each sample position (u, v) to FP32 before
+ * the bilinear lookup (everything else FP64), to measure the floor FP32
+ * positions put under the gradient; 0 restores exact positions. */
+void zo_diff_round_positions(int on);
 
 #ifdef __cplusplus
 }

@@ -43,6 +43,13 @@ typedef struct {
     double ju[9], jv[9];
 } samp_t;
 
+/* When set, each sample position (u, v) is rounded to FP32 before the
+ * bilinear lookup, everything else staying FP64: the gradient's change under
+ * this one rounding is the floor that FP32 sample positions put under an FP32
+ * implementation (zo_diff_round_positions). */
+static int g_round_positions = 0;
+void zo_diff_round_positions(int on) { g_round_positions = on; }
+
 static int sample(const cam_t* c, double col, double row, const int32_t* ord, const double* res, int sw, int sh,
                   samp_t* s, int32_t* cell, int cells_mode) {
     double X0 = c->ir[0] * col + c->ir[1] * row + c->ir[2];
@@ -54,6 +61,10 @@ static int sample(const cam_t* c, double col, double row, const int32_t* ord, co
     double xd = x * sd + 2.0 * c->p1 * x * y + c->p2 * (r2 + 2.0 * x * x);
     double yd = y * sd + c->p1 * (r2 + 2.0 * y * y) + 2.0 * c->p2 * x * y;
     double u = c->fx * xd + c->cx, v = c->fy * yd + c->cy;
+    if (g_round_positions) {
+        u = (double)(float)u;
+        v = (double)(float)v;
+    }
     s->ok = 0;
     int x0, y0;
     if (cells_mode == 2) {

@@ -200,3 +200,25 @@ def test_match_fast_path_and_scan_agree_with_oracle(ctx, oracle_lib):
     assert np.abs(gd[rr, cc][well].astype(np.float64) - od[rr, cc][well]).max() <= 2e-4
     for kind in range(4):  # every row kind matches something
         assert (ob[kind::4] >= 0).mean() > 0.3, kind
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,kw", SMALL_SCENES)
+def test_rectify_match_equals_rectify_then_match(ctx, oracle_lib, name, kw):
+    """zim_rectify_match (the whole-pair path's fused setData + stereoMatch)
+    gives the disparity of zim_rectify on both cameras then zim_match, bit for
+    bit, with and without the post-smooth."""
+    from zim_gb300 import api
+    spec, L, R, _ = scene_data(name, **kw)
+    setup(ctx, oracle_lib, spec)
+    cfg = api.decode_config(**spec.decode_kwargs())
+    dl = api.decode(ctx, cfg, torch.from_numpy(L).cuda())
+    dr = api.decode(ctx, cfg, torch.from_numpy(R).cuda())
+    for smooth in (True, False):
+        rl = api.rectify(ctx, 0, dl["order"], dl["residual"], smooth)
+        rr = api.rectify(ctx, 1, dr["order"], dr["residual"], smooth)
+        disp, _ = api.match(ctx, rl, rr, spec.pha_f, 1.0, want_best=False)
+        fused = api.rectify_match(ctx, (dl["order"], dl["residual"]), (dr["order"], dr["residual"]), spec.pha_f,
+                                  post_smooth=smooth)
+        assert torch.equal(disp, fused), smooth
+        assert (fused != 0).float().mean().item() > 0.3

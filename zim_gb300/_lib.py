@@ -129,6 +129,7 @@ PROTOTYPES = {
     "zim_pack_ply": (I, [V, V, V, V, I, I, I, V, V, V]),
     "zim_rectify": (I, [V, I, V, V, I, I, I, V, V, V, V]),
     "zim_match": (I, [V, V, V, V, V, V, V, I, I, I, D, V, V, V]),
+    "zim_rectify_match": (I, [V, V, V, V, V, I, I, I, I, D, V, V]),
     "zim_median_reproject": (I, [V, V, V, I, I, V, V, V, V]),
     "zim_filter_px_gaussian": (I, [V, V, V, I, I, V, V, V]),
     "zim_filter_ror": (I, [V, V, V, I, I, Fl, I, I, V, V, V]),

@@ -239,6 +239,19 @@ def match(ctx: Context, left, right, pha_f, grad_threshold=1.0, want_best=True):
     return disp, best
 
 
+def rectify_match(ctx: Context, left, right, pha_f, post_smooth=True, grad_threshold=1.0, hdr=False):
+    """setData + stereoMatch fused (zim_rectify_match): left/right are the
+    decoded (order, residual) of each camera; returns the raw disparity."""
+    lo, lr = left
+    ro, rr = right
+    H, W = lo.shape
+    disp = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.float32, device=lo.device)
+    mode = (2 if post_smooth else 3) if hdr else (1 if post_smooth else 0)
+    ctx.check(_lib.load().zim_rectify_match(ctx.h, _p(lo), _p(lr), _p(ro), _p(rr), H, W, mode, int(pha_f),
+                                            float(grad_threshold), _p(disp), _stream()))
+    return disp
+
+
 def median_reproject(ctx: Context, rcfg, disp):
     H, W = disp.shape
     dout = torch.empty_like(disp)

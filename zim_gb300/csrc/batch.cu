@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(BT) batch_reproject_kernel(const PairDev* __re
         if (it >= n_items) break;
         const int4 w = items[it];  // pair, first tile row, tile rows
         const PairDev& P = pairs[w.x];
-        const int tiles_x = (P.rw + zt::RX - 1) / zt::RX;
+        const int tiles_x = (P.rw + zt::MTX - 1) / zt::MTX;
         for (int ty = w.y; ty < w.y + w.z; ty++)
             for (int tx = 0; tx < tiles_x; tx++)
                 zt::median_reproject_tile(P.disp_raw, P.rh, P.rw, P.rp, tx, ty, tid, sm, P.disp_out, P.x_rep, P.m_rep);

@@ -500,6 +500,18 @@ zim_status zim_rectify_launch(zim_ctx* ctx, int cam, const int32_t* order, const
     return ZIM_OK;
 }
 
+// The post-smooth alone (post_smooth 1 or 2; nothing to do otherwise), for
+// the fused rectify + match of the whole-pair path.
+zim_status zim_smooth_launch(zim_ctx* ctx, const int32_t* order, const float* residual, int rows, int cols,
+                             int post_smooth, int32_t* smooth_k16, float* smooth_r, cudaStream_t st) {
+    if (post_smooth != 1 && post_smooth != 2) return ZIM_OK;
+    dim3 blk(32, 8), sgrd((cols + 31) / 32, (rows + 7) / 8);
+    smooth_kernel<<<sgrd, blk, 0, st>>>(order, residual, rows, cols, post_smooth == 2 ? 1 : 0, smooth_k16, smooth_r);
+    ctx->launches += 1;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
+
 extern "C" ZIM_API zim_status zim_rectify(zim_ctx* ctx, int cam, const int32_t* order, const float* residual, int rows,
                                           int cols, int post_smooth, int32_t* rbase, float* rres, int32_t* rorder,
                                           void* stream) {

@@ -231,9 +231,6 @@ namespace {
 struct PairBuffers {
     int32_t* order[2];
     float* res[2];
-    int32_t* rbase[2];
-    float* rres[2];
-    int32_t* rorder[2];
     int32_t* sk[2];  // post-smoothed taps (16 x cycles, residual)
     float* sr[2];
     float* disp_raw;
@@ -248,7 +245,6 @@ size_t pair_scratch_bytes(const zim_ctx* ctx, const zim_recon_config* r, int row
     size_t src = (size_t)rows * cols, dst = (size_t)ctx->rect_h * ctx->rect_w;
     size_t b = 0;
     b += 2 * (zim_align256(src * 4) * 4);
-    b += 2 * (zim_align256(dst * 4) * 3);
     b += zim_align256(dst * 4);
     if (need_disp) b += zim_align256(dst * 4);
     b += 2 * (zim_align256(dst * 12) + zim_align256(dst));
@@ -288,19 +284,24 @@ static zim_status run_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_r
                            cudaEvent_t right_ready = nullptr) {
     zim_status s;
     const void* frames[2] = {lf, rf};
+    const int post = d->enable_hdr ? (d->post_smooth ? 2 : 3) : (d->post_smooth ? 1 : 0);
     for (int c = 0; c < 2; c++) {
         if (c == 1 && right_ready) ZIM_CUDA_TRY(ctx, cudaStreamWaitEvent(st, right_ready, 0));
         s = zim_decode_launch(ctx, d, frames[c], sample_type, rows, cols, B.order[c], B.res[c], nullptr, nullptr, st);
         if (s) return s;
-        s = zim_rectify_launch(ctx, c, B.order[c], B.res[c], rows, cols, d->enable_hdr ? (d->post_smooth ? 2 : 3) : (d->post_smooth ? 1 : 0),
-                               B.sk[c], B.sr[c], B.rbase[c], B.rres[c], B.rorder[c], st);
+        s = zim_smooth_launch(ctx, B.order[c], B.res[c], rows, cols, post, B.sk[c], B.sr[c], st);
         if (s) return s;
     }
     const int RH = ctx->rect_h, RW = ctx->rect_w;
     if (pha_f <= 0) pha_f = zim_decode_max_order(d);
-    s = zim_match_launch(ctx, B.rbase[0], B.rres[0], B.rorder[0], B.rbase[1], B.rres[1], B.rorder[1], RH, RW, pha_f,
-                         r->grad_threshold, B.disp_raw, nullptr, st);
-    if (s) return s;
+    // setData's remap fused into the matching: the rectified maps stay on chip
+    {
+        const int32_t* ord[2] = {B.order[0], B.order[1]};
+        const float* res[2] = {B.res[0], B.res[1]};
+        s = zim_rectify_match_launch(ctx, ord, res, B.sk, B.sr, rows, cols, post, pha_f, r->grad_threshold,
+                                     B.disp_raw, st);
+        if (s) return s;
+    }
 
     // Stage routing: the last writer of xyz / mask writes the caller's buffers.
     enum { ST_REPROJ, ST_PXG, ST_ROR, ST_SOR, ST_MLS, ST_MG };
@@ -396,9 +397,6 @@ static zim_status carve_pair(zim_ctx* ctx, const zim_recon_config* r, int rows, 
         B.res[c] = (float*)zim_scratch_take(ctx, src * 4);
         B.sk[c] = (int32_t*)zim_scratch_take(ctx, src * 4);
         B.sr[c] = (float*)zim_scratch_take(ctx, src * 4);
-        B.rbase[c] = (int32_t*)zim_scratch_take(ctx, dst * 4);
-        B.rres[c] = (float*)zim_scratch_take(ctx, dst * 4);
-        B.rorder[c] = (int32_t*)zim_scratch_take(ctx, dst * 4);
         B.xyz[c] = (float*)zim_scratch_take(ctx, dst * 12);
         B.mask[c] = (uint8_t*)zim_scratch_take(ctx, dst);
     }
@@ -406,7 +404,7 @@ static zim_status carve_pair(zim_ctx* ctx, const zim_recon_config* r, int rows, 
     B.disp_med = disp_out ? disp_out : (float*)zim_scratch_take(ctx, dst * 4);
     B.mls_tmp = r->use_mls ? (float*)zim_scratch_take(ctx, dst * 12) : nullptr;
     for (int c = 0; c < 2; c++)
-        if (!B.order[c] || !B.res[c] || !B.rbase[c] || !B.rres[c] || !B.rorder[c] || !B.xyz[c] || !B.mask[c])
+        if (!B.order[c] || !B.res[c] || !B.sk[c] || !B.sr[c] || !B.xyz[c] || !B.mask[c])
             return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "scratch carve failed");
     if (!B.disp_raw || !B.disp_med || (r->use_mls && !B.mls_tmp))
         return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "scratch carve failed");

@@ -120,17 +120,16 @@ __global__ void __launch_bounds__(zt::DX* zt::DY) decode_tma_kernel(const __grid
             if (i >= n_ps) break;
             const int f0 = NS ? i * NS : p.fbase[i];  // frequencies' frames are consecutive
             const int N = NS ? NS : p.shift[i];
-            float sv = 0.f, cv = 0.f, mv = 0.f;
+            float2 sc = make_float2(0.f, 0.f);
+            float mv = 0.f;
 #pragma unroll
             for (int k = 0; k < (NS ? NS : 32); k++) {  // 3..32 steps
                 if (k >= N) break;
                 const float v = (float)bp[(f0 + k) * plane];
-                sv = fmaf(-p.sinv[f0 + k], v, sv);
-                cv = fmaf(p.cosv[f0 + k], v, cv);
+                sc = zt::sc_add(sc, p.sinv[f0 + k], p.cosv[f0 + k], v);
                 mv += v;
             }
-            sm.S[i][hy][hx] = sv;
-            sm.C[i][hy][hx] = cv;
+            sm.SC[i][hy][hx] = sc;
             sm.M[i][hy][hx] = mv;
         }
     }

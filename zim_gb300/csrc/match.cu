@@ -87,7 +87,104 @@ zim_status launch_match(zim_ctx* ctx, const MatchWin& w, int rows, int pha_f, do
     return ZIM_OK;
 }
 
+// Rectification fused into matching (the plain whole-pair path): one CTA per
+// rectified row rectifies the right row straight into shared memory and each
+// left pixel in registers (the setData remap, zt::rectify_pixel[_smoothed], so
+// the results are those of rectify + match), and the rectified maps never
+// reach global memory.  post_smooth 1 / 2: sk / sr hold the post-smoothed taps
+// of each camera (smooth_kernel); 0 / 3: the remap reads order / residual.
+struct RectMatchArgs {
+    const int32_t* order[2];
+    const float* res[2];
+    const int32_t* sk[2];
+    const float* sr[2];
+    const float* map[2][2];
+    int srows, scols, rows, cols, post_smooth;
+    float* disp;
+};
+
+__device__ __forceinline__ void rect_px(const RectMatchArgs& a, int cam, size_t o, int32_t& b, float& r, int32_t& k) {
+    const float mx = __ldg(a.map[cam][0] + o), my = __ldg(a.map[cam][1] + o);
+    if (a.post_smooth == 1 || a.post_smooth == 2)
+        zt::rectify_pixel_smoothed(a.sk[cam], a.sr[cam], a.order[cam], a.srows, a.scols, mx, my, b, r, k);
+    else
+        zt::rectify_pixel(a.order[cam], a.res[cam], a.srows, a.scols, mx, my, a.post_smooth, b, r, k);
+}
+
+__global__ void __launch_bounds__(MATCH_THREADS) rectify_match_kernel(RectMatchArgs a, int pha_f,
+                                                                      float grad_threshold) {
+    extern __shared__ int4 smem_raw[];
+    const int cols = a.cols;
+    int* s_ord = reinterpret_cast<int*>(smem_raw);
+    int* s_base = s_ord + cols;
+    float* s_res = reinterpret_cast<float*>(s_base + cols);
+    int* s_lo = reinterpret_cast<int*>(s_res + cols);
+    int* s_hi = s_lo + (pha_f + 1);
+    int* s_bad = s_hi + (pha_f + 1);
+    const int row = blockIdx.x;
+    const size_t ro = (size_t)row * cols;
+    for (int k = threadIdx.x; k <= pha_f; k += blockDim.x) {
+        s_lo[k] = INT_MAX;
+        s_hi[k] = -1;
+        s_bad[k] = 0;
+    }
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        int32_t b, k;
+        float r;
+        rect_px(a, 1, ro + j, b, r, k);
+        s_ord[j] = k;
+        s_base[j] = b;
+        s_res[j] = r;
+    }
+    __syncthreads();
+    zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, threadIdx.x, blockDim.x);
+    __syncthreads();
+    zt::match_spans_check(s_ord, s_base, s_res, cols, pha_f, s_hi, s_bad, threadIdx.x, blockDim.x);
+    __syncthreads();
+    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+        int32_t bL, kL;
+        float rL;
+        rect_px(a, 0, ro + j, bL, rL, kL);
+        float d;
+        int best;
+        zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, s_bad, cols, pha_f, grad_threshold, d,
+                        best);
+        a.disp[ro + j] = d;
+    }
+}
+
 }  // namespace
+
+// The plain path's rectify + match of both cameras (see rectify_match_kernel);
+// sk / sr: per camera the post-smoothed taps (post_smooth 1 or 2), else null.
+zim_status zim_rectify_match_launch(zim_ctx* ctx, const int32_t* const order[2], const float* const res[2],
+                                    int32_t* const sk[2], float* const sr[2], int srows, int scols, int post_smooth,
+                                    int pha_f, double grad_threshold, float* disp, cudaStream_t st) {
+    RectMatchArgs a{};
+    for (int c = 0; c < 2; c++) {
+        a.order[c] = order[c];
+        a.res[c] = res[c];
+        a.sk[c] = sk[c];
+        a.sr[c] = sr[c];
+        a.map[c][0] = ctx->d_map[c][0];
+        a.map[c][1] = ctx->d_map[c][1];
+    }
+    a.srows = srows;
+    a.scols = scols;
+    a.rows = ctx->rect_h;
+    a.cols = ctx->rect_w;
+    a.post_smooth = post_smooth;
+    a.disp = disp;
+    if (a.cols > ZIM_MAX_MATCH_COLS)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "rectified width %d above %d", a.cols, ZIM_MAX_MATCH_COLS);
+    const size_t smem = (size_t)a.cols * 12 + (size_t)(pha_f + 1) * 12;
+    ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(rectify_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+    rectify_match_kernel<<<a.rows, MATCH_THREADS, smem, st>>>(a, pha_f, (float)grad_threshold);
+    ctx->launches += 1;
+    ZIM_LAUNCH_CHECK(ctx);
+    return ZIM_OK;
+}
 
 zim_status zim_match_launch(zim_ctx* ctx, const int32_t* l_base, const float* l_res, const int32_t* l_order,
                             const int32_t* r_base, const float* r_res, const int32_t* r_order, int rows, int cols,
@@ -123,4 +220,37 @@ extern "C" ZIM_API zim_status zim_match(zim_ctx* ctx, const int32_t* l_base, con
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     return zim_match_launch(ctx, l_base, l_res, l_order, r_base, r_res, r_order, rows, cols, pha_f, grad_threshold,
                             disp, best_col, zim_stream(stream));
+}
+
+extern "C" ZIM_API zim_status zim_rectify_match(zim_ctx* ctx, const int32_t* l_order, const float* l_res,
+                                                const int32_t* r_order, const float* r_res, int rows, int cols,
+                                                int post_smooth, int pha_f, double grad_threshold, float* disp,
+                                                void* stream) {
+    if (!ctx) return ZIM_ERR_INVALID_ARG;
+    if (!ctx->calibrated) return zim_fail(ctx, ZIM_ERR_NOT_CALIBRATED, "not calibrated");
+    if (!l_order || !l_res || !r_order || !r_res || !disp) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "null argument");
+    if (rows != ctx->src_h || cols != ctx->src_w)
+        return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "image size differs from calibration");
+    if (post_smooth < 0 || post_smooth > 3) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "post_smooth must be 0..3");
+    if (pha_f < 0 || pha_f > ZIM_MAX_ORDER) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pha_f out of range");
+    ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    int32_t* sk[2] = {nullptr, nullptr};
+    float* sr[2] = {nullptr, nullptr};
+    cudaStream_t st = zim_stream(stream);
+    const int32_t* ord[2] = {l_order, r_order};
+    const float* res[2] = {l_res, r_res};
+    if (post_smooth == 1 || post_smooth == 2) {
+        const size_t src = (size_t)rows * cols;
+        zim_status s = zim_scratch_reserve(ctx, 4 * zim_align256(src * 4) + 1024);
+        if (s) return s;
+        zim_scratch_reset(ctx);
+        for (int c = 0; c < 2; c++) {
+            sk[c] = (int32_t*)zim_scratch_take(ctx, src * 4);
+            sr[c] = (float*)zim_scratch_take(ctx, src * 4);
+            if (!sk[c] || !sr[c]) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "rectify scratch");
+            s = zim_smooth_launch(ctx, ord[c], res[c], rows, cols, post_smooth, sk[c], sr[c], st);
+            if (s) return s;
+        }
+    }
+    return zim_rectify_match_launch(ctx, ord, res, sk, sr, rows, cols, post_smooth, pha_f, grad_threshold, disp, st);
 }

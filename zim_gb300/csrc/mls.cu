@@ -378,8 +378,7 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
 // The tile and its hw halo staged in shared memory as float4, NaN for invalid
 // and off-image pixels (their distance test fails).
 inline size_t mls_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (MY + 2 * hw) * sizeof(float4); }
-// The same for the two-row tiles of mls_pair_kernel (MX x 2 MY pixels).
-inline size_t mls_pair_smem_bytes(int hw) { return (size_t)(MX + 2 * hw) * (2 * MY + 2 * hw) * sizeof(float4); }
+
 
 // With pixel rays (rays != 0) each row of the window is cut to the disk beyond
 // which the ray bound puts every point outside the cut-off: the pixels left out
@@ -472,249 +471,6 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     dst[3 * o + 2] = moved ? pz + oz : pz;
 }
 
-// ---- two queries per thread in packed FP32x2 ----
-//
-// Blackwell issues a pair of FP32 adds, multiplies or fused multiply-adds as
-// one instruction (__fadd2_rn, __fmul2_rn, __ffma2_rn: each lane rounded as
-// the scalar operation).  A thread takes the queries of rows y and y + 1 of
-// one column; every neighbour of the two windows is loaded once, and the
-// offsets, distances and weighted sums of both queries advance together in
-// the two lanes of each packed operation.  Only the weights (one ex2 each),
-// the per-query frame, solve and projection are scalar.
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
-
-// Visits the union of the two queries' windows (row offsets -hw .. hw + 1
-// from the upper query), each row cut to the wider of the two queries' ray
-// disks; fn(q, row_a, row_b) gets the staged neighbour and whether the row
-// lies in each query's own window.  A neighbour inside the union but outside
-// a query's disk fails that query's distance test, so each query sees exactly
-// the in-radius neighbours of its window, in window order.
-template <typename Fn>
-__device__ __forceinline__ void pair_visit(const float4* sp, int cc, int TW, int hw, float wr2, Fn&& fn) {
-    for (int i = -hw; i <= hw + 1; i++) {
-        const int m = min(abs(i), abs(i - 1));
-        const float rem = wr2 - (float)(m * m);
-        if (rem < 0.f) continue;
-        const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
-        const bool row_a = i <= hw, row_b = i > -hw;
-        for (int j = -w; j <= w; j++) fn(sp[cc + i * TW + j], row_a, row_b);
-    }
-}
-
-// Offsets of neighbour q from the two queries, their squared lengths and
-// in-radius weights; a lane whose test fails gets weight 0 and zero offsets
-// (so a NaN or far neighbour adds exact zeros to that lane's sums).  ok_a /
-// ok_b come in as "the lane may take it" and leave as "the lane took it".
-// False when neither lane takes the neighbour.
-__device__ __forceinline__ bool pair_offsets(const float4& q, bool& ok_a, bool& ok_b, float2 npx, float2 npy,
-                                             float2 npz, float r2c, float2 kw2, float2& dx, float2& dy, float2& dz,
-                                             float2& w) {
-    dx = add2(dup2(q.x), npx);
-    dy = add2(dup2(q.y), npy);
-    dz = add2(dup2(q.z), npz);
-    const float2 d2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
-    ok_a = ok_a && d2.x <= r2c;
-    ok_b = ok_b && d2.y <= r2c;
-    if (!(ok_a || ok_b)) return false;
-    const float2 t = mul2(d2, kw2);
-    float ea, eb;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ea) : "f"(t.x));
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(eb) : "f"(t.y));
-    w = make_float2(ok_a ? ea : 0.f, ok_b ? eb : 0.f);
-    if (!(ok_a && ok_b)) {
-        if (!ok_a) { dx.x = 0.f; dy.x = 0.f; dz.x = 0.f; }
-        if (!ok_b) { dx.y = 0.f; dy.y = 0.f; dz.y = 0.f; }
-    }
-    return true;
-}
-
-template <int HW>
-__global__ void __launch_bounds__(MX* MY) mls_pair_kernel(const float* __restrict__ src,
-                                                          const uint8_t* __restrict__ mask, int rows, int cols,
-                                                          int hw_arg, float inv_2s2, int order, float r2c, int rays,
-                                                          zt::RayParams rp, float* __restrict__ dst) {
-    extern __shared__ float4 mls_sp[];
-    __shared__ unsigned warp_dev[MX * MY / 32];
-    const int hw = HW ? HW : hw_arg;
-    const int TW = MX + 2 * hw, TH = 2 * MY + 2 * hw;
-    const int gx0 = blockIdx.x * MX - hw, gy0 = blockIdx.y * (2 * MY) - hw;
-    const int tid = threadIdx.y * MX + threadIdx.x;
-    unsigned tdev = 0u;  // largest ray distance of this thread's staged points (float bits, >= 0)
-    for (int t = tid; t < TW * TH; t += MX * MY) {
-        const int ty = t / TW, tx = t - ty * TW;
-        const int gx = gx0 + tx, gy = gy0 + ty;
-        float4 v = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
-        if (gx >= 0 && gy >= 0 && gx < cols && gy < rows) {
-            const size_t q = (size_t)gy * cols + gx;
-            if (__ldg(mask + q)) {
-                v = make_float4(__ldg(src + 3 * q), __ldg(src + 3 * q + 1), __ldg(src + 3 * q + 2), 1.f);
-                if (rays) {
-                    float ax, ay, az;
-                    zt::ray_dir(rp, gx, gy, ax, ay, az);
-                    const float d = zt::ray_dev(v.x, v.y, v.z, ax, ay, az);
-                    tdev = max(tdev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
-                }
-            }
-        }
-        mls_sp[t] = v;
-    }
-    tdev = __reduce_max_sync(0xffffffffu, tdev);
-    if ((tid & 31) == 0) warp_dev[tid >> 5] = tdev;
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < MX * MY / 32; j++) tdev = max(tdev, warp_dev[j]);
-    const int x = blockIdx.x * MX + threadIdx.x, y0 = blockIdx.y * (2 * MY) + 2 * threadIdx.y;
-    const bool in_a = x < cols && y0 < rows, in_b = x < cols && y0 + 1 < rows;
-    const int cc = (2 * threadIdx.y + hw) * TW + threadIdx.x + hw;  // upper query's tile index
-    const float4 ca = mls_sp[cc], cb = mls_sp[cc + TW];
-    const bool va = in_a && ca.w != 0.f, vb = in_b && cb.w != 0.f;
-    float wr2 = INFINITY;  // squared pixel radius of the warp's disk
-    if (rays) {
-        float rs2 = 0.f;
-#pragma unroll
-        for (int l = 0; l < 2; l++) {
-            const float4 c = l ? cb : ca;
-            if (!(l ? vb : va)) continue;
-            float ax, ay, az;
-            zt::ray_dir(rp, x, y0 + l, ax, ay, az);
-            const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-            const float qn = sqrtf(fmaf(c.x, c.x, fmaf(c.y, c.y, c.z * c.z)));
-            const float C = qn * rp.f / an;
-            const float sd = sqrtf(r2c) + zt::ray_dev(c.x, c.y, c.z, ax, ay, az) + __uint_as_float(tdev) + 1e-5f * qn;
-            float r2 = INFINITY;
-            if (C > sd) {
-                const float r = sd * an / (C - sd);
-                r2 = r * r;
-            }
-            rs2 = fmaxf(rs2, r2);
-        }
-        wr2 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(rs2)));
-    }
-    if (!in_a) return;
-    float oa0 = ca.x, oa1 = ca.y, oa2 = ca.z, ob0 = cb.x, ob1 = cb.y, ob2 = cb.z;  // outputs: unmoved by default
-    if (va || vb) {
-        const float kw = -1.44269504088896341f * inv_2s2;  // -log2(e) / (2 s^2)
-        const float2 kw2 = dup2(kw);
-        // a lane without a query gets a finite stand-in; all its tests fail
-        const float2 npx = make_float2(va ? -ca.x : 0.f, vb ? -cb.x : 0.f);
-        const float2 npy = make_float2(va ? -ca.y : 0.f, vb ? -cb.y : 0.f);
-        const float2 npz = make_float2(va ? -ca.z : 0.f, vb ? -cb.z : 0.f);
-        // 1. weighted centroid and covariance sums about each query point
-        float2 cx = dup2(0.f), cy = dup2(0.f), cz = dup2(0.f), ws = dup2(0.f);
-        float2 m00 = dup2(0.f), m01 = dup2(0.f), m02 = dup2(0.f), m11 = dup2(0.f), m12 = dup2(0.f), m22 = dup2(0.f);
-        int nva = 0, nvb = 0;
-        pair_visit(mls_sp, cc, TW, hw, wr2, [&](const float4& q, bool row_a, bool row_b) {
-            float2 dx, dy, dz, w;
-            bool ta = row_a && va, tb = row_b && vb;
-            if (!pair_offsets(q, ta, tb, npx, npy, npz, r2c, kw2, dx, dy, dz, w)) return;
-            cx = fma2(w, dx, cx); cy = fma2(w, dy, cy); cz = fma2(w, dz, cz);
-            const float2 wx = mul2(w, dx), wy = mul2(w, dy);
-            m00 = fma2(wx, dx, m00); m01 = fma2(wx, dy, m01); m02 = fma2(wx, dz, m02);
-            m11 = fma2(wy, dy, m11); m12 = fma2(wy, dz, m12); m22 = fma2(mul2(w, dz), dz, m22);
-            ws = add2(ws, w);
-            nva += ta;
-            nvb += tb;
-        });
-        MlsFrame Fa{}, Fb{};
-        const bool fa = va && mls_frame(ws.x, nva, cx.x, cy.x, cz.x, m00.x, m01.x, m02.x, m11.x, m12.x, m22.x, order, Fa);
-        const bool fb = vb && mls_frame(ws.y, nvb, cx.y, cy.y, cz.y, m00.y, m01.y, m02.y, m11.y, m12.y, m22.y, order, Fb);
-        const float is = rsqrtf(r2c);
-        const int fit_a = fa ? Fa.cur : 0, fit_b = fb ? Fb.cur : 0;
-        float da0 = 0.f, da1 = 0.f, da2 = 0.f, db0 = 0.f, db1 = 0.f, db2 = 0.f;
-        if (order >= 1 && (fit_a >= 1 || fit_b >= 1)) {
-            // 2. the polynomial fit's moments in each query's tangent frame
-            // (u = (d - c) . t1 is as one FMA chain on d; likewise v, f)
-            const float2 ax = make_float2(Fa.t1x * is, Fb.t1x * is), ay = make_float2(Fa.t1y * is, Fb.t1y * is),
-                         az = make_float2(Fa.t1z * is, Fb.t1z * is);
-            const float2 bx = make_float2(Fa.t2x * is, Fb.t2x * is), by = make_float2(Fa.t2y * is, Fb.t2y * is),
-                         bz = make_float2(Fa.t2z * is, Fb.t2z * is);
-            const float2 nx = make_float2(Fa.nx, Fb.nx), ny = make_float2(Fa.ny, Fb.ny), nz = make_float2(Fa.nz, Fb.nz);
-            const float2 nuc = make_float2(-fmaf(Fa.cx, ax.x, fmaf(Fa.cy, ay.x, Fa.cz * az.x)),
-                                           -fmaf(Fb.cx, ax.y, fmaf(Fb.cy, ay.y, Fb.cz * az.y)));
-            const float2 nvc = make_float2(-fmaf(Fa.cx, bx.x, fmaf(Fa.cy, by.x, Fa.cz * bz.x)),
-                                           -fmaf(Fb.cx, bx.y, fmaf(Fb.cy, by.y, Fb.cz * bz.y)));
-            const float2 nfc = make_float2(-fmaf(Fa.cx, nx.x, fmaf(Fa.cy, ny.x, Fa.cz * nz.x)),
-                                           -fmaf(Fb.cx, nx.y, fmaf(Fb.cy, ny.y, Fb.cz * nz.y)));
-            const bool six = order == 2;
-            float2 M00 = dup2(0.f), M10 = dup2(0.f), M01 = dup2(0.f), M20 = dup2(0.f), M11 = dup2(0.f),
-                   M02 = dup2(0.f);
-            float2 M30 = dup2(0.f), M21 = dup2(0.f), M12 = dup2(0.f), M03 = dup2(0.f), M40 = dup2(0.f),
-                   M31 = dup2(0.f), M22 = dup2(0.f), M13 = dup2(0.f), M04 = dup2(0.f);
-            float2 B0 = dup2(0.f), B1 = dup2(0.f), B2 = dup2(0.f), B3 = dup2(0.f), B4 = dup2(0.f), B5 = dup2(0.f);
-            const bool ua = va && fit_a >= 1, ub = vb && fit_b >= 1;
-            pair_visit(mls_sp, cc, TW, hw, wr2, [&](const float4& q, bool row_a, bool row_b) {
-                float2 dx, dy, dz, w;
-                bool ta = row_a && ua, tb = row_b && ub;
-                if (!pair_offsets(q, ta, tb, npx, npy, npz, r2c, kw2, dx, dy, dz, w)) return;
-                const float2 u = fma2(dx, ax, fma2(dy, ay, fma2(dz, az, nuc)));
-                const float2 v = fma2(dx, bx, fma2(dy, by, fma2(dz, bz, nvc)));
-                const float2 f = fma2(dx, nx, fma2(dy, ny, fma2(dz, nz, nfc)));
-                const float2 wu = mul2(w, u), wv = mul2(w, v), wf = mul2(w, f);
-                M00 = add2(M00, w); M10 = add2(M10, wu); M01 = add2(M01, wv);
-                M20 = fma2(wu, u, M20); M11 = fma2(wu, v, M11); M02 = fma2(wv, v, M02);
-                B0 = add2(B0, wf); B1 = fma2(wf, u, B1); B2 = fma2(wf, v, B2);
-                if (six) {
-                    const float2 uu = mul2(u, u), uv = mul2(u, v), vv = mul2(v, v);
-                    M30 = fma2(wu, uu, M30); M21 = fma2(wu, uv, M21); M12 = fma2(wu, vv, M12); M03 = fma2(wv, vv, M03);
-                    const float2 wuu = mul2(wu, u), wvv = mul2(wv, v);
-                    M40 = fma2(wuu, uu, M40); M31 = fma2(wuu, uv, M31); M22 = fma2(wuu, vv, M22);
-                    M13 = fma2(wvv, uv, M13); M04 = fma2(wvv, vv, M04);
-                    B3 = fma2(wf, uu, B3); B4 = fma2(wf, uv, B4); B5 = fma2(wf, vv, B5);
-                }
-            });
-            auto fit_lane = [&](const MlsFrame& F, int cur, bool hi, float& o0, float& o1, float& o2) {
-                auto pick = [hi](float2 a) { return hi ? a.y : a.x; };
-                if (six) {
-                    float A[6][6], bv[6];
-                    A[0][0] = pick(M00); A[0][1] = pick(M10); A[0][2] = pick(M01);
-                    A[1][1] = pick(M20); A[1][2] = pick(M11); A[2][2] = pick(M02);
-                    A[0][3] = pick(M20); A[0][4] = pick(M11); A[0][5] = pick(M02);
-                    A[1][3] = pick(M30); A[1][4] = pick(M21); A[1][5] = pick(M12);
-                    A[2][3] = pick(M21); A[2][4] = pick(M12); A[2][5] = pick(M03);
-                    A[3][3] = pick(M40); A[3][4] = pick(M31); A[3][5] = pick(M22);
-                    A[4][4] = pick(M22); A[4][5] = pick(M13); A[5][5] = pick(M04);
-                    bv[0] = pick(B0); bv[1] = pick(B1); bv[2] = pick(B2);
-                    bv[3] = pick(B3); bv[4] = pick(B4); bv[5] = pick(B5);
-#pragma unroll
-                    for (int a = 0; a < 6; a++)
-#pragma unroll
-                        for (int b = 0; b < a; b++) A[a][b] = A[b][a];
-                    mls_solve_project<6>(F, cur, A, bv, is, o0, o1, o2);
-                } else {
-                    float A[3][3], bv[3];
-                    A[0][0] = pick(M00); A[0][1] = pick(M10); A[0][2] = pick(M01);
-                    A[1][1] = pick(M20); A[1][2] = pick(M11); A[2][2] = pick(M02);
-                    A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
-                    bv[0] = pick(B0); bv[1] = pick(B1); bv[2] = pick(B2);
-                    mls_solve_project<3>(F, cur, A, bv, is, o0, o1, o2);
-                }
-            };
-            if (fa && fit_a >= 1) fit_lane(Fa, fit_a, false, da0, da1, da2);
-            if (fb && fit_b >= 1) fit_lane(Fb, fit_b, true, db0, db1, db2);
-        }
-        // order 0 (or a query whose order dropped to 0): the tangent-plane projection
-        {
-            float A[3][3] = {}, bv[3] = {};
-            if (fa && fit_a < 1) mls_solve_project<3>(Fa, 0, A, bv, is, da0, da1, da2);
-            if (fb && fit_b < 1) mls_solve_project<3>(Fb, 0, A, bv, is, db0, db1, db2);
-        }
-        if (fa) { oa0 += da0; oa1 += da1; oa2 += da2; }
-        if (fb) { ob0 += db0; ob1 += db1; ob2 += db2; }
-    }
-    const size_t o = (size_t)y0 * cols + x;
-    // invalid pixels pass their input through (the staged value is NaN there)
-    if (!va) { oa0 = src[3 * o]; oa1 = src[3 * o + 1]; oa2 = src[3 * o + 2]; }
-    dst[3 * o] = oa0; dst[3 * o + 1] = oa1; dst[3 * o + 2] = oa2;
-    if (in_b) {
-        const size_t o1 = o + cols;
-        if (!vb) { ob0 = src[3 * o1]; ob1 = src[3 * o1 + 1]; ob2 = src[3 * o1 + 2]; }
-        dst[3 * o1] = ob0; dst[3 * o1 + 1] = ob1; dst[3 * o1 + 2] = ob2;
-    }
-}
-
 }  // namespace
 
 size_t zim_mls_scratch_bytes(size_t n_points) { return zim_align256(n_points * 12); }
@@ -727,10 +483,9 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const int ord = order < 0 ? 0 : (order > 2 ? 2 : order);
     const int n_iter = iterations < 1 ? 1 : iterations;
     dim3 blk(MX, MY), grd((cols + MX - 1) / MX, (rows + MY - 1) / MY);
-    dim3 grd2((cols + MX - 1) / MX, (rows + 2 * MY - 1) / (2 * MY));
-    const size_t smem = mls_pair_smem_bytes(window);
+    const size_t smem = mls_smem_bytes(window);
     const bool use_smem = smem <= 96 * 1024;
-    auto kern = window == 7 ? mls_pair_kernel<7> : mls_pair_kernel<0>;
+    auto kern = window == 7 ? mls_smem_kernel<7> : mls_smem_kernel<0>;
     if (use_smem) ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int use_rays = use_smem && rays.valid;
     const zt::RayParams rp = zt::ray_params(rays);
@@ -740,7 +495,7 @@ zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         float* dst = ((n_iter - 1 - it) % 2 == 0) ? out : tmp;
         if (dst == in) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "MLS in-place not supported");
         if (use_smem)
-            kern<<<grd2, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp, dst);
+            kern<<<grd, blk, smem, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, use_rays, rp, dst);
         else
             mls_kernel<<<grd, blk, 0, st>>>(in, mask, rows, cols, window, inv_2s2, ord, r2c, dst);
         ctx->launches += 1;

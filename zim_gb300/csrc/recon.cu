@@ -149,7 +149,7 @@ zim_status zim_median_reproject_launch(zim_ctx* ctx, const zim_recon_config* cfg
     ReprojParams p;
     zt::reproj_params(ctx->Q, ctx->R1, cfg, p);
     for (int k = 0; k < 3; k++) p.poly[k] = ctx->d_poly[k];
-    dim3 blk(RX, RY), grd((cols + RX - 1) / RX, (rows + RY - 1) / RY);
+    dim3 blk(RX, RY), grd((cols + zt::MTX - 1) / zt::MTX, (rows + RY - 1) / RY);
     median_reproject_kernel<<<grd, blk, 0, st>>>(disp, rows, cols, p, disp_out, xyz, mask);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);

@@ -387,7 +387,7 @@ extern "C" ZIM_API zim_status zim_reconstruct_roi(zim_ctx* ctx, const zim_recon_
     p.oy = L.y;
     p.gstride = RW;
     p.roi_mask = roi_mask;
-    dim3 blk(zt::RX, zt::RY), grd((W + zt::RX - 1) / zt::RX, (H + zt::RY - 1) / zt::RY);
+    dim3 blk(zt::RX, zt::RY), grd((W + zt::MTX - 1) / zt::MTX, (H + zt::RY - 1) / zt::RY);
     roi_reproject_kernel<<<grd, blk, 0, st>>>(d_raw, H, W, p, d_med, xb[0], mb[0]);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);

@@ -125,6 +125,11 @@ zim_status zim_px_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint8_t*
 zim_status zim_ror_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
                           float radius, int min_neighbors, int window_size, float* out,
                           uint8_t* mask_out, cudaStream_t st);
+zim_status zim_smooth_launch(zim_ctx* ctx, const int32_t* order, const float* residual, int rows, int cols,
+                             int post_smooth, int32_t* smooth_k16, float* smooth_r, cudaStream_t st);
+zim_status zim_rectify_match_launch(zim_ctx* ctx, const int32_t* const order[2], const float* const res[2],
+                                    int32_t* const sk[2], float* const sr[2], int srows, int scols, int post_smooth,
+                                    int pha_f, double grad_threshold, float* disp, cudaStream_t st);
 zim_status zim_mls_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int rows, int cols,
                           int window, float sigma, int order, float max_radius, int iterations,
                           float* out, float* tmp, const zim_ray_model& rays, cudaStream_t st);

@@ -145,31 +145,40 @@ __device__ __forceinline__ int floor_div(int a, int b, float inv_b) {
     return q;
 }
 
-// Shared memory of one decode tile: the raw per-pixel sums of the tile + halo.
+// Shared memory of one decode tile: the raw per-pixel sums of the tile + halo,
+// the phase-shift pair (S, C) as one float2 so that both are staged, loaded
+// and blurred by paired FP32 instructions (__ffma2_rn: each lane rounded as
+// the scalar fmaf, so the sums are those of the scalar sequence).
 constexpr int DEC_MAX_PS = 4;  // phase-shift frequencies staged together
 struct DecodeSmem {
-    float S[DEC_MAX_PS][DHY][DHX + 1], C[DEC_MAX_PS][DHY][DHX + 1], M[DEC_MAX_PS][DHY][DHX + 1];
+    float2 SC[DEC_MAX_PS][DHY][DHX + 1];
+    float M[DEC_MAX_PS][DHY][DHX + 1];
 };
+
+// sc += (-sin_k, cos_k) v: the S and C sums of one sample in one paired FMA
+__device__ __forceinline__ float2 sc_add(float2 sc, float sn, float cs, float v) {
+    return __ffma2_rn(make_float2(-sn, cs), make_float2(v, v), sc);
+}
 
 // Raw sums of one halo pixel over the N frames of one frequency, four frames'
 // loads in flight at a time (the same accumulation order as one at a time).
 template <typename T>
 __device__ __forceinline__ void frame_sums(const T* __restrict__ src, size_t npx, int N, const float* sv,
-                                           const float* cv, float& s, float& c, float& m) {
-    s = 0.f; c = 0.f; m = 0.f;
+                                           const float* cv, float2& sc, float& m) {
+    sc = make_float2(0.f, 0.f);
+    m = 0.f;
     int k = 0;
     for (; k + 4 <= N; k += 4) {
         const float v0 = (float)__ldg(src + (size_t)k * npx), v1 = (float)__ldg(src + (size_t)(k + 1) * npx);
         const float v2 = (float)__ldg(src + (size_t)(k + 2) * npx), v3 = (float)__ldg(src + (size_t)(k + 3) * npx);
-        s = fmaf(-sv[k], v0, s); c = fmaf(cv[k], v0, c); m += v0;
-        s = fmaf(-sv[k + 1], v1, s); c = fmaf(cv[k + 1], v1, c); m += v1;
-        s = fmaf(-sv[k + 2], v2, s); c = fmaf(cv[k + 2], v2, c); m += v2;
-        s = fmaf(-sv[k + 3], v3, s); c = fmaf(cv[k + 3], v3, c); m += v3;
+        sc = sc_add(sc, sv[k], cv[k], v0); m += v0;
+        sc = sc_add(sc, sv[k + 1], cv[k + 1], v1); m += v1;
+        sc = sc_add(sc, sv[k + 2], cv[k + 2], v2); m += v2;
+        sc = sc_add(sc, sv[k + 3], cv[k + 3], v3); m += v3;
     }
     for (; k < N; k++) {
         float v = (float)__ldg(src + (size_t)k * npx);
-        s = fmaf(-sv[k], v, s);
-        c = fmaf(cv[k], v, c);
+        sc = sc_add(sc, sv[k], cv[k], v);
         m += v;
     }
 }
@@ -189,11 +198,11 @@ __device__ __forceinline__ void decode_stage_sums(const T* __restrict__ frames, 
 #pragma unroll
         for (int i = 0; i < DEC_MAX_PS; i++) {
             if (i >= p.n_ps) break;
-            float s, c, m;
+            float2 sc;
+            float m;
             frame_sums(frames + (size_t)p.fbase[i] * npx + pix, npx, p.shift[i], p.sinv + p.fbase[i],
-                       p.cosv + p.fbase[i], s, c, m);
-            sm.S[i][hy][hx] = s;
-            sm.C[i][hy][hx] = c;
+                       p.cosv + p.fbase[i], sc, m);
+            sm.SC[i][hy][hx] = sc;
             sm.M[i][hy][hx] = m;
         }
     }
@@ -248,16 +257,17 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
             }
             continue;
         }
-        float S = 0.f, C = 0.f, M = 0.f;
+        float2 SC = make_float2(0.f, 0.f);
+        float M = 0.f;
 #pragma unroll
         for (int a = 0; a < 3; a++)
 #pragma unroll
             for (int b = 0; b < 3; b++) {
                 float w = p.w2d[a * 3 + b];
-                S = fmaf(w, sm.S[i][ty + a][tx + b], S);
-                C = fmaf(w, sm.C[i][ty + a][tx + b], C);
+                SC = __ffma2_rn(make_float2(w, w), sm.SC[i][ty + a][tx + b], SC);
                 M = fmaf(w, sm.M[i][ty + a][tx + b], M);
             }
+        const float S = SC.x, C = SC.y;
         if (ok) {
             const float wr = atan2f(S, C);
             if (i == 0) wrap0 = wr;
@@ -798,45 +808,48 @@ __device__ __forceinline__ float median25(float* a) {
     return a[7];
 }
 
+// Two horizontally adjacent 5x5 windows share 20 values.  A shared value of
+// rank r among those 20 has rank r .. r + 5 in either window, so only ranks
+// 8..13 can be a window's median (rank 13 of 25); with the 7 lower shared
+// values below them and at most 5 own values among the rest, each window's
+// median is the median (rank 6) of those 6 and its own 5-value column.
+// mid6_of_20: forgetful selection on a[0..19] leaving ranks 8..13 in a[4..9]
+// (each dropped min has rank <= 7, each dropped max rank >= 14).
+__device__ __forceinline__ void mid6_of_20(float* a) {
+    minmax_ends<14>(a);            // live a[1..12], unseen a[14..19]
+    a[13] = a[14]; minmax_ends<13>(a + 1);  // live a[2..12]
+    a[1] = a[15];  minmax_ends<12>(a + 1);  // live a[2..11]
+    a[12] = a[16]; minmax_ends<11>(a + 2);  // live a[3..11]
+    a[2] = a[17];  minmax_ends<10>(a + 2);  // live a[3..10]
+    a[11] = a[18]; minmax_ends<9>(a + 3);   // live a[4..10]
+    a[3] = a[19];  minmax_ends<8>(a + 3);   // live a[4..9]
+    // ranks 8..13 of the 20 in a[4..9]
+}
+
+// Median (rank 6) of 11 values by forgetful selection.
+__device__ __forceinline__ float median11(float* a) {
+    minmax_ends<7>(a);            // live a[1..5], unseen a[7..10]
+    a[6] = a[7];  minmax_ends<6>(a + 1);  // live a[2..5]
+    a[1] = a[8];  minmax_ends<5>(a + 1);  // live a[2..4]
+    a[5] = a[9];  minmax_ends<4>(a + 2);  // live a[3..4]
+    a[2] = a[10]; minmax_ends<3>(a + 2);  // live a[3]
+    return a[3];
+}
+
+// Median tiles are MTX x RY pixels for RX x RY threads: each thread takes two
+// adjacent pixels (2 tx, 2 tx + 1) of a row.
+constexpr int MTX = 2 * RX;
+
 struct MedianSmem {
-    float tile[RY + 4][RX + 5];
+    __align__(8) float tile[RY + 4][MTX + 4];
 };
 
-// 5x5 median (replicate border) + Q reprojection of tile (bx, by) with the
-// RX * RY threads of a block.  Ends past the last shared read.
-__device__ __forceinline__ void median_reproject_tile(const float* __restrict__ disp, int rows, int cols,
-                                                      const ReprojParams& p, int bx, int by, int tid, MedianSmem& sm,
-                                                      float* __restrict__ disp_out, float* __restrict__ xyz,
-                                                      uint8_t* __restrict__ mask) {
-    const int tx = tid % RX, ty = tid / RX;
-    const int x = bx * RX + tx, y = by * RY + ty;
-    float d = 0.f;
-    if (p.use_median) {
-        const int gx0 = bx * RX - 2, gy0 = by * RY - 2;
-        for (int h = tid; h < (RX + 4) * (RY + 4); h += RX * RY) {
-            int hy = h / (RX + 4), hx = h - hy * (RX + 4);
-            int gy = min(max(gy0 + hy, 0), rows - 1), gx = min(max(gx0 + hx, 0), cols - 1);
-            sm.tile[hy][hx] = __ldg(disp + (size_t)gy * cols + gx);
-        }
-        __syncthreads();
-        float a[25];
-#pragma unroll
-        for (int dy = 0; dy < 5; dy++)
-#pragma unroll
-            for (int dx = 0; dx < 5; dx++) a[dy * 5 + dx] = sm.tile[ty + dy][tx + dx];
-        __syncthreads();
-        d = median25(a);
-    } else if (x < cols && y < rows) {
-        d = disp[(size_t)y * cols + x];
-    }
-    if (x >= cols || y >= rows) return;
-    const size_t o = (size_t)y * cols + x;
-    if (disp_out) disp_out[o] = d;
-    float ox = 0.f, oy = 0.f, oz = 0.f;
-    uint8_t m = 0;
-    // rectified-frame pixel (ROI tiles are offset) and its index in the maps
-    const int gx = x + p.ox, gy = y + p.oy;
-    const size_t go = p.gstride ? (size_t)gy * p.gstride + gx : o;
+// Q (or polynomial-map) reprojection of one pixel's disparity; (gx, gy) its
+// rectified-frame pixel, go its index in the maps.
+__device__ __forceinline__ void reproject_pixel(const ReprojParams& p, int gx, int gy, size_t go, float d, float& ox,
+                                                float& oy, float& oz, uint8_t& m) {
+    ox = oy = oz = 0.f;
+    m = 0;
     // the reference gates |d| < 1e-5 on the disparity widened to double
     const bool has_d = fabs((double)d) >= 1e-5 && (!p.roi_mask || p.roi_mask[go]);
     if (p.model == 1) {
@@ -876,10 +889,69 @@ __device__ __forceinline__ void median_reproject_tile(const float* __restrict__ 
             }
         }
     }
-    xyz[3 * o] = ox;
-    xyz[3 * o + 1] = oy;
-    xyz[3 * o + 2] = oz;
-    mask[o] = m;
+}
+
+// 5x5 median (replicate border) + Q reprojection of median tile (bx, by)
+// (MTX x RY pixels) with the RX * RY threads of a block.  Ends past the last
+// shared read.
+__device__ __forceinline__ void median_reproject_tile(const float* __restrict__ disp, int rows, int cols,
+                                                      const ReprojParams& p, int bx, int by, int tid, MedianSmem& sm,
+                                                      float* __restrict__ disp_out, float* __restrict__ xyz,
+                                                      uint8_t* __restrict__ mask) {
+    const int tx = tid % RX, ty = tid / RX;
+    const int x = bx * MTX + 2 * tx, y = by * RY + ty;  // the thread's pixels: x and x + 1
+    float d0 = 0.f, d1 = 0.f;
+    if (p.use_median) {
+        const int gx0 = bx * MTX - 2, gy0 = by * RY - 2;
+        for (int h = tid; h < (MTX + 4) * (RY + 4); h += RX * RY) {
+            int hy = h / (MTX + 4), hx = h - hy * (MTX + 4);
+            int gy = min(max(gy0 + hy, 0), rows - 1), gx = min(max(gx0 + hx, 0), cols - 1);
+            sm.tile[hy][hx] = __ldg(disp + (size_t)gy * cols + gx);
+        }
+        __syncthreads();
+        // columns x - 2 .. x + 3 of five rows as float2 pairs: c0 only in
+        // pixel x's window, c5 only in pixel x + 1's, c1..c4 in both
+        float sh[20], own0[5], own1[5];
+#pragma unroll
+        for (int dy = 0; dy < 5; dy++) {
+            const float2* r2 = reinterpret_cast<const float2*>(&sm.tile[ty + dy][2 * tx]);
+            const float2 a = r2[0], b = r2[1], c = r2[2];
+            own0[dy] = a.x;
+            sh[4 * dy] = a.y; sh[4 * dy + 1] = b.x; sh[4 * dy + 2] = b.y; sh[4 * dy + 3] = c.x;
+            own1[dy] = c.y;
+        }
+        __syncthreads();
+        mid6_of_20(sh);
+        float m0[11], m1[11];
+#pragma unroll
+        for (int q = 0; q < 6; q++) m0[q] = m1[q] = sh[4 + q];
+#pragma unroll
+        for (int q = 0; q < 5; q++) { m0[6 + q] = own0[q]; m1[6 + q] = own1[q]; }
+        d0 = median11(m0);
+        d1 = median11(m1);
+    } else if (y < rows) {
+        if (x < cols) d0 = disp[(size_t)y * cols + x];
+        if (x + 1 < cols) d1 = disp[(size_t)y * cols + x + 1];
+    }
+    if (y >= rows) return;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const int xx = x + l;
+        if (xx >= cols) break;
+        const float d = l ? d1 : d0;
+        const size_t o = (size_t)y * cols + xx;
+        if (disp_out) disp_out[o] = d;
+        // rectified-frame pixel (ROI tiles are offset) and its index in the maps
+        const int gx = xx + p.ox, gy = y + p.oy;
+        const size_t go = p.gstride ? (size_t)gy * p.gstride + gx : o;
+        float ox, oy, oz;
+        uint8_t m;
+        reproject_pixel(p, gx, gy, go, d, ox, oy, oz, m);
+        xyz[3 * o] = ox;
+        xyz[3 * o + 1] = oy;
+        xyz[3 * o + 2] = oz;
+        mask[o] = m;
+    }
 }
 
 // ------------------------------------------------- pixel-window filters ----

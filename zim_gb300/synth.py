@@ -247,25 +247,20 @@ CONFIG2_SIZES = ((640, 480), (1280, 1024), (2448, 2048), (4096, 3000))
 def config2(seed: int = 7, n_pairs: int = 64, sizes=CONFIG2_SIZES):
     """The mixed batch: n_pairs stereo pairs, each with a size drawn from
     `sizes` and an encoding drawn from {4-step + 5-bit Gray + complementary bit
-    (the config-0 scene and rig, scaled to the size), 3-frequency heterodyne
-    121/110/120 x 4 steps (the config-1 scene and rig, scaled)}.  Pairs of the
-    same size and encoding share a calibration.  Returns (specs, calib_keys)."""
+    (the config-0 scene and rig, scaled to the size, 8-bit), three-frequency
+    1/8/64 x 4 steps in 12-bit u16 (the config-1 encoding, scene and rig,
+    scaled, with a pair-specific seed)}.  Pairs of the same size and encoding
+    share a calibration.  Returns (specs, calib_keys)."""
     rng = np.random.default_rng(seed)
     specs, keys = [], []
     for i in range(n_pairs):
         w, h = sizes[int(rng.integers(len(sizes)))]
         gray = bool(rng.integers(2))
         sd = int(seed * 1000 + i)
-        if gray:
-            s = config0(sd, w, h)
-        else:
-            s = ref_heterodyne(sd, w, h, steps=4)
-            # config-1 scene with a pair-specific seed
-            r2 = np.random.default_rng(sd)
-            s.bumps, s.boxes = _bumps_boxes(r2)
+        s = config0(sd, w, h) if gray else config1(sd, w, h)
         s.name = f"config2_{i}"
         specs.append(s)
-        keys.append(("gray" if gray else "het", w, h))
+        keys.append(("gray" if gray else "freq3", w, h))
     return specs, keys
 
 
