@@ -58,6 +58,12 @@ def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+# DRAM bytes per launch (read + write) of a stage's kernel on the 5 MP
+# workload, from one ncu capture each (profiles/*_5mp_dram.md): the
+# roofline's `traffic` for that kernel when it dominates the step.
+MEASURED_TRAFFIC = {("mls", 2448, 2048): (68127488 + 26212864, "profiles/mls_smem_kernel_5mp_dram.md")}
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -293,7 +299,9 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "peak_source": src, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": None,
+                         "traffic": MEASURED_TRAFFIC.get((dom, W, H), (None, None))[0],
+                         "traffic_source": MEASURED_TRAFFIC.get((dom, W, H), (None, None))[1],
+                         "algorithmic_bytes": alg[dom],
                          "decode_kernel": {"achieved": round(dec_achieved, 1),
                                            "frac": round(dec_achieved / peak, 4)}},
             "stages": stages,

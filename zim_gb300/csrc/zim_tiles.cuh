@@ -598,14 +598,18 @@ __device__ __forceinline__ void match_pixel(int j, int k, int bL, float rL, cons
 
 // Per-order column spans of a staged right row (shared atomics).  Callers
 // initialise s_lo = INT_MAX, s_hi = -1, s_bad = 0 and sync before, and sync
-// after, then run match_spans_check (and sync again).
+// after, then run match_spans_check (and sync again).  A span's first column
+// is the first column of one of its order's runs and its last the last of
+// one, so only run starts update s_lo and only run ends s_hi: about two
+// atomics per run instead of one per pixel (a warp's lanes nearly always
+// share an order, and same-address atomics serialise).
 __device__ __forceinline__ void match_spans(const int* s_ord, int cols, int pha_f, int* s_lo, int* s_hi, int tid,
                                             int nthreads) {
     for (int j = tid; j < cols; j += nthreads) {
         int k = s_ord[j];
         if (k >= 0 && k <= pha_f) {
-            atomicMin(&s_lo[k], j);
-            atomicMax(&s_hi[k], j);
+            if (j == 0 || s_ord[j - 1] != k) atomicMin(&s_lo[k], j);
+            if (j == cols - 1 || s_ord[j + 1] != k) atomicMax(&s_hi[k], j);
         }
     }
 }
