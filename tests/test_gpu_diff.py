@@ -117,10 +117,12 @@ def test_backward_matches_oracle(gctx, cases, pert):
         print("  %-8s gpu % .9e  fp64 % .9e  rel %.2e" % (PARAMS[k], g[k], go[k], rel[k]))
     nrm = np.linalg.norm(g - go) / np.linalg.norm(go)
     print("backward: gradient rel err: norm-wise %.2e, worst component %.2e" % (nrm, rel.max()))
-    # FP32 per-point terms, FP64 sums: components that cancel to a small total
-    # (e.g. fy, whose phase slope is near zero for vertical fringes) keep less
-    assert nrm < 1e-5
-    assert rel.max() < 1e-3
+    # FP32 per-point terms, FP64 sums: measured 3.3e-6 norm-wise and 2.5e-4 on
+    # the worst component (fy1, whose phase slope is near zero for vertical
+    # fringes); FP32 sample positions alone move the FP64 gradient by as much
+    # (test_oracle_diff.py).  Bounds: about twice the measured values.
+    assert nrm < 6e-6
+    assert rel.max() < 5e-4
     H, Ho = r["jtj"], o["jtj"]
     assert np.linalg.norm(H - Ho) / np.linalg.norm(Ho) < 1e-4
     for cam in (0, 1):
@@ -128,7 +130,7 @@ def test_backward_matches_oracle(gctx, cases, pert):
         gpo = o["grad_phase"][cam]
         e = np.linalg.norm(gp - gpo) / np.linalg.norm(gpo)
         print("  phase gradient cam %d: rel L2 err %.2e" % (cam, e))
-        assert e < 5e-3
+        assert e < 5e-5  # measured 1.6e-5, 1.7e-5
 
 
 def test_gpu_gradient_against_finite_differences(gctx, cases, pert):
@@ -158,8 +160,8 @@ def test_gpu_gradient_against_finite_differences(gctx, cases, pert):
     rel = np.abs(r["grad"] - fd) / np.abs(fd)
     nrm = np.linalg.norm(r["grad"] - fd) / np.linalg.norm(fd)
     print("GPU gradient vs FP64 central differences: norm-wise %.2e, worst component %.2e" % (nrm, rel.max()))
-    assert nrm < 1e-5
-    assert rel.max() < 1e-3
+    assert nrm < 6e-6  # measured 3.3e-6
+    assert rel.max() < 5e-4  # measured 2.5e-4
 
 
 def test_batched_views_sum(gctx, cases):
