@@ -81,6 +81,8 @@ def test_ror_parity(ctx, oracle_lib):
 # flag_max: the flagged fraction measured on this cloud by the oracle alone
 # (2.50 %, 0.26 %, 0.22 %) plus a margin.
 @pytest.mark.parametrize("order,window,sigma,radius,iters,flag_max", [(2, 7, 5.656854, 8.0, 1, 0.030),
+                                                                        (1, 7, 5.656854, 8.0, 1, 0.030),
+                                                                        (0, 7, 5.656854, 8.0, 2, 0.030),
                                                                         (1, 5, 2.4, 0.0, 2, 0.004),
                                                                         (0, 4, 2.0, 0.0, 1, 0.0035)])
 def test_mls_parity(ctx, oracle_lib, order, window, sigma, radius, iters, flag_max):

@@ -116,69 +116,12 @@ __device__ __forceinline__ bool cholesky_fixed(const float (&A)[N][N], const flo
 
 // Gaussian weight exp(-d2 / (2 s^2)) = 2^(d2 * kw) with kw = -log2(e) / (2 s^2):
 // one multiply and the hardware base-2 exponential (PTX ex2.approx).
-__device__ __forceinline__ float mls_weight(float d2, float kw) {
+__device__ __forceinline__ float mls_weight_arg(float a) {
     float w;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(d2 * kw));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(a));
     return w;
 }
-
-// Normal equations of the order-N polynomial fit (N = 3: 1, u, v; N = 6: also
-// u^2, uv, v^2) in tangent coordinates u, v (scaled by is) and height f about
-// the centroid c.  Entry (a, b) is the weighted moment of u^i v^j whose
-// exponents are those of basis terms a and b added: the 15 moments with
-// i + j <= 4 (6 for N = 3) and the right-hand side's 6 (3) are accumulated,
-// then the symmetric matrix is filled.
-template <int N, typename Visit>
-__device__ __forceinline__ void fit_accumulate(Visit& visit, float kw, float r2c, float is, float cx, float cy,
-                                               float cz, float t1x, float t1y, float t1z, float t2x, float t2y,
-                                               float t2z, float nx, float ny, float nz, float (&A)[N][N],
-                                               float (&bv)[N]) {
-    // u = (d - c) . t1 is as one FMA chain on d (likewise v, f)
-    const float ax = t1x * is, ay = t1y * is, az = t1z * is;
-    const float bx = t2x * is, by = t2y * is, bz = t2z * is;
-    const float uc = fmaf(cx, ax, fmaf(cy, ay, cz * az));
-    const float vc = fmaf(cx, bx, fmaf(cy, by, cz * bz));
-    const float fc = fmaf(cx, nx, fmaf(cy, ny, cz * nz));
-    float m00 = 0.f, m10 = 0.f, m01 = 0.f, m20 = 0.f, m11 = 0.f, m02 = 0.f;
-    float m30 = 0.f, m21 = 0.f, m12 = 0.f, m03 = 0.f, m40 = 0.f, m31 = 0.f, m22 = 0.f, m13 = 0.f, m04 = 0.f;
-    float b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f, b4 = 0.f, b5 = 0.f;
-    visit([&](float dx, float dy, float dz) {
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        if (!(d2 <= r2c)) return;
-        const float w = mls_weight(d2, kw);
-        const float u = fmaf(dx, ax, fmaf(dy, ay, fmaf(dz, az, -uc)));
-        const float v = fmaf(dx, bx, fmaf(dy, by, fmaf(dz, bz, -vc)));
-        const float f = fmaf(dx, nx, fmaf(dy, ny, fmaf(dz, nz, -fc)));
-        const float wu = w * u, wv = w * v, wf = w * f;
-        m00 += w; m10 += wu; m01 += wv;
-        m20 = fmaf(wu, u, m20); m11 = fmaf(wu, v, m11); m02 = fmaf(wv, v, m02);
-        b0 += wf; b1 = fmaf(wf, u, b1); b2 = fmaf(wf, v, b2);
-        if (N == 6) {
-            const float uu = u * u, uv = u * v, vv = v * v;
-            m30 = fmaf(wu, uu, m30); m21 = fmaf(wu, uv, m21); m12 = fmaf(wu, vv, m12); m03 = fmaf(wv, vv, m03);
-            const float wuu = wu * u, wvv = wv * v;
-            m40 = fmaf(wuu, uu, m40); m31 = fmaf(wuu, uv, m31); m22 = fmaf(wuu, vv, m22);
-            m13 = fmaf(wvv, uv, m13); m04 = fmaf(wvv, vv, m04);
-            b3 = fmaf(wf, uu, b3); b4 = fmaf(wf, uv, b4); b5 = fmaf(wf, vv, b5);
-        }
-    });
-    // basis exponents: 1 (0,0), u (1,0), v (0,1), u^2 (2,0), uv (1,1), v^2 (0,2)
-    A[0][0] = m00; A[0][1] = m10; A[0][2] = m01;
-    A[1][1] = m20; A[1][2] = m11; A[2][2] = m02;
-    bv[0] = b0; bv[1] = b1; bv[2] = b2;
-    if constexpr (N == 6) {
-        A[0][3] = m20; A[0][4] = m11; A[0][5] = m02;
-        A[1][3] = m30; A[1][4] = m21; A[1][5] = m12;
-        A[2][3] = m21; A[2][4] = m12; A[2][5] = m03;
-        A[3][3] = m40; A[3][4] = m31; A[3][5] = m22;
-        A[4][4] = m22; A[4][5] = m13; A[5][5] = m04;
-        bv[3] = b3; bv[4] = b4; bv[5] = b5;
-    }
-#pragma unroll
-    for (int a = 0; a < N; a++)
-#pragma unroll
-        for (int b = 0; b < a; b++) A[a][b] = A[b][a];
-}
+__device__ __forceinline__ float mls_weight(float d2, float kw) { return mls_weight_arg(d2 * kw); }
 
 // The state of one query after the first sweep: centroid (relative to the
 // query point), unit normal and orthonormal tangent frame, and the polynomial
@@ -196,7 +139,8 @@ struct MlsFrame {
 // no weight).  Order selection follows the CPU reference: order drops to 0
 // with fewer than {3, 5, 8}[order] neighbours.
 __device__ __forceinline__ bool mls_frame(float ws, int nv, float cx, float cy, float cz, float m00, float m01,
-                                          float m02, float m11, float m12, float m22, int order, MlsFrame& F) {
+                                          float m02, float m11, float m12, float m22, int order, MlsFrame& F,
+                                          float (*Cout)[3] = nullptr) {
     if (nv < 3 || ws < 1e-12f) return false;
     const float iw = 1.0f / ws;
     cx *= iw; cy *= iw; cz *= iw;
@@ -205,6 +149,9 @@ __device__ __forceinline__ bool mls_frame(float ws, int nv, float cx, float cy, 
     C[0][0] = fmaf(-ws * cx, cx, m00); C[0][1] = fmaf(-ws * cx, cy, m01); C[0][2] = fmaf(-ws * cx, cz, m02);
     C[1][1] = fmaf(-ws * cy, cy, m11); C[1][2] = fmaf(-ws * cy, cz, m12); C[2][2] = fmaf(-ws * cz, cz, m22);
     C[1][0] = C[0][1]; C[2][0] = C[0][2]; C[2][1] = C[1][2];
+    if (Cout)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Cout[i][j] = C[i][j];
     float nv3[3];
     sym_normal3(C, nv3);
     // Orthonormal tangent frame about the normal: the polynomial spaces of
@@ -238,6 +185,73 @@ __device__ __forceinline__ bool mls_frame(float ws, int nv, float cx, float cy, 
     const int min_nb = order == 2 ? 8 : (order == 1 ? 5 : 3);
     F.cur = nv >= min_nb ? order : 0;
     return true;
+}
+
+// Normal equations of the order-N polynomial fit (N = 3: 1, u, v; N = 6: also
+// u^2, uv, v^2) in tangent coordinates u, v (scaled by is) and height f about
+// the centroid.  Entry (a, b) is the weighted moment of u^i v^j whose exponents
+// are those of basis terms a and b added.  The moments of degree <= 2 and the
+// right-hand sides sum w f, sum w f u, sum w f v follow from the first sweep:
+// about the centroid sum w u = sum w v = sum w f = 0, and sum w (u, v, f)
+// (u, v, f)^T is the weighted covariance C expressed in the frame
+// (t1 is, t2 is, n).  So the second sweep (N = 6 only) sums just the nine
+// moments of degree 3 and 4 and sum w f (u^2, uv, v^2).
+template <int N, typename Visit>
+__device__ __forceinline__ void fit_normal_equations(Visit& visit, float kw, float r2c, float is, float ws,
+                                                     const float (&C)[3][3], const MlsFrame& F, float (&A)[N][N],
+                                                     float (&bv)[N]) {
+    float Ct1[3], Ct2[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        Ct1[a] = fmaf(C[a][0], F.t1x, fmaf(C[a][1], F.t1y, C[a][2] * F.t1z));
+        Ct2[a] = fmaf(C[a][0], F.t2x, fmaf(C[a][1], F.t2y, C[a][2] * F.t2z));
+    }
+    const float is2 = is * is;
+    const float m20 = is2 * fmaf(F.t1x, Ct1[0], fmaf(F.t1y, Ct1[1], F.t1z * Ct1[2]));
+    const float m11 = is2 * fmaf(F.t1x, Ct2[0], fmaf(F.t1y, Ct2[1], F.t1z * Ct2[2]));
+    const float m02 = is2 * fmaf(F.t2x, Ct2[0], fmaf(F.t2y, Ct2[1], F.t2z * Ct2[2]));
+    A[0][0] = ws; A[0][1] = 0.f; A[0][2] = 0.f;
+    A[1][1] = m20; A[1][2] = m11; A[2][2] = m02;
+    bv[0] = 0.f;
+    bv[1] = is * fmaf(F.nx, Ct1[0], fmaf(F.ny, Ct1[1], F.nz * Ct1[2]));
+    bv[2] = is * fmaf(F.nx, Ct2[0], fmaf(F.ny, Ct2[1], F.nz * Ct2[2]));
+    if constexpr (N == 6) {
+        // u = (d - c) . t1 is as one FMA chain on d (likewise v, f)
+        const float ax = F.t1x * is, ay = F.t1y * is, az = F.t1z * is;
+        const float bx = F.t2x * is, by = F.t2y * is, bz = F.t2z * is;
+        const float nx = F.nx, ny = F.ny, nz = F.nz;
+        const float uc = fmaf(F.cx, ax, fmaf(F.cy, ay, F.cz * az));
+        const float vc = fmaf(F.cx, bx, fmaf(F.cy, by, F.cz * bz));
+        const float fc = fmaf(F.cx, nx, fmaf(F.cy, ny, F.cz * nz));
+        float m30 = 0.f, m21 = 0.f, m12 = 0.f, m03 = 0.f, m40 = 0.f, m31 = 0.f, m22 = 0.f, m13 = 0.f, m04 = 0.f;
+        float b3 = 0.f, b4 = 0.f, b5 = 0.f;
+        visit([&](float dx, float dy, float dz) {
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 <= r2c)) return;
+            const float w = mls_weight(d2, kw);
+            const float u = fmaf(dx, ax, fmaf(dy, ay, fmaf(dz, az, -uc)));
+            const float v = fmaf(dx, bx, fmaf(dy, by, fmaf(dz, bz, -vc)));
+            const float f = fmaf(dx, nx, fmaf(dy, ny, fmaf(dz, nz, -fc)));
+            const float wu = w * u, wv = w * v, wf = w * f;
+            const float uu = u * u, uv = u * v, vv = v * v;
+            m30 = fmaf(wu, uu, m30); m21 = fmaf(wu, uv, m21); m12 = fmaf(wu, vv, m12); m03 = fmaf(wv, vv, m03);
+            const float wuu = wu * u, wvv = wv * v;
+            m40 = fmaf(wuu, uu, m40); m31 = fmaf(wuu, uv, m31); m22 = fmaf(wuu, vv, m22);
+            m13 = fmaf(wvv, uv, m13); m04 = fmaf(wvv, vv, m04);
+            b3 = fmaf(wf, uu, b3); b4 = fmaf(wf, uv, b4); b5 = fmaf(wf, vv, b5);
+        });
+        // basis exponents: 1 (0,0), u (1,0), v (0,1), u^2 (2,0), uv (1,1), v^2 (0,2)
+        A[0][3] = m20; A[0][4] = m11; A[0][5] = m02;
+        A[1][3] = m30; A[1][4] = m21; A[1][5] = m12;
+        A[2][3] = m21; A[2][4] = m12; A[2][5] = m03;
+        A[3][3] = m40; A[3][4] = m31; A[3][5] = m22;
+        A[4][4] = m22; A[4][5] = m13; A[5][5] = m04;
+        bv[3] = b3; bv[4] = b4; bv[5] = b5;
+    }
+#pragma unroll
+    for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int b = 0; b < a; b++) A[a][b] = A[b][a];
 }
 
 // Singular-pivot thresholds of the Cholesky solve (the reference's 1e-12) for
@@ -329,20 +343,18 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
         nv++;
     });
     MlsFrame F;
-    if (!mls_frame(ws, nv, cx, cy, cz, m00, m01, m02, m11, m12, m22, order, F)) return;
+    float C[3][3];
+    if (!mls_frame(ws, nv, cx, cy, cz, m00, m01, m02, m11, m12, m22, order, F, C)) return;
     // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
     // radius): the fitted surface is the same, the normal equations are O(1).
     const float is = rsqrtf(r2c);
     if (F.cur == 2) {
         float A[6][6], bv[6];
-        fit_accumulate<6>(visit, kw, r2c, is, F.cx, F.cy, F.cz, F.t1x, F.t1y, F.t1z, F.t2x, F.t2y, F.t2z, F.nx, F.ny,
-                          F.nz, A, bv);
+        fit_normal_equations<6>(visit, kw, r2c, is, ws, C, F, A, bv);
         mls_solve_project<6>(F, 2, A, bv, is, ox, oy, oz);
     } else {
-        float A[3][3] = {}, bv[3] = {};
-        if (F.cur == 1)
-            fit_accumulate<3>(visit, kw, r2c, is, F.cx, F.cy, F.cz, F.t1x, F.t1y, F.t1z, F.t2x, F.t2y, F.t2z, F.nx,
-                              F.ny, F.nz, A, bv);
+        float A[3][3], bv[3];
+        fit_normal_equations<3>(visit, kw, r2c, is, ws, C, F, A, bv);
         mls_solve_project<3>(F, F.cur, A, bv, is, ox, oy, oz);
     }
     moved = true;
@@ -453,18 +465,43 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     bool moved = false;
     if (c.w != 0.f) {
         // invalid and off-image neighbours are NaN and fail the distance test
-        auto visit = [&](auto&& fn) {
-            for (int i = -hw; i <= hw; i++) {
-                const float rem = wr2 - (float)(i * i);
-                if (rem < 0.f) continue;
-                const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
-                for (int j = -w; j <= w; j++) {
-                    const float4 q = mls_sp[cc + i * TW + j];
-                    fn(q.x - px, q.y - py, q.z - pz);
-                }
+        if constexpr (HW >= 1 && HW <= 7) {
+            // half-width of window rows +-i, found once for both sweeps
+            // (warp-uniform; 15 = row skipped)
+            unsigned wpack = 0u;
+#pragma unroll
+            for (int ai = 0; ai <= HW; ai++) {
+                const float rem = wr2 - (float)(ai * ai);
+                const unsigned code =
+                    rem < 0.f ? 15u : (rem < (float)(HW * HW) ? (unsigned)(int)sqrtf(rem) : (unsigned)HW);
+                wpack |= code << (4 * ai);
             }
-        };
-        mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
+            auto visit = [&](auto&& fn) {
+#pragma unroll 1
+                for (int i = -HW; i <= HW; i++) {
+                    const int w = (int)((wpack >> (4 * (i < 0 ? -i : i))) & 15u);
+                    if (w == 15) continue;
+                    for (int j = -w; j <= w; j++) {
+                        const float4 q = mls_sp[cc + i * TW + j];
+                        fn(q.x - px, q.y - py, q.z - pz);
+                    }
+                }
+            };
+            mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
+        } else {
+            auto visit = [&](auto&& fn) {
+                for (int i = -hw; i <= hw; i++) {
+                    const float rem = wr2 - (float)(i * i);
+                    if (rem < 0.f) continue;
+                    const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
+                    for (int j = -w; j <= w; j++) {
+                        const float4 q = mls_sp[cc + i * TW + j];
+                        fn(q.x - px, q.y - py, q.z - pz);
+                    }
+                }
+            };
+            mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
+        }
     }
     dst[3 * o] = moved ? px + ox : px;
     dst[3 * o + 1] = moved ? py + oy : py;
