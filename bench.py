@@ -200,53 +200,79 @@ def run_ours(args):
     spec = synth.config1(seed=1 + rank, width=args.width, height=args.height)
     L, R = spec.render(0), spec.render(1)
     F, H, W = L.shape
-    ctx = api.Context(local)
-    ctx.set_calibration(spec.rig.as_dict(), True)
+    # `inflight` pairs in flight: one context (scratch) and one stream each,
+    # pairs assigned round-robin; the timed region spans all of them
+    nf = max(1, args.inflight)
+    ctxs = [api.Context(local) for _ in range(nf)]
+    for c in ctxs:
+        c.set_calibration(spec.rig.as_dict(), True)
+    ctx = ctxs[0]
     dcfg = api.decode_config(**spec.decode_kwargs())
     rcfg = config1_recon(api)
     dL, dR = torch.from_numpy(L).cuda(), torch.from_numpy(R).cuda()
-    xyz = torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32, device="cuda")
-    mask = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device="cuda")
-    out = (xyz, mask, None)
-    for _ in range(args.warmup):
-        api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
+    outs = [(torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32, device="cuda"),
+             torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8, device="cuda"), None) for _ in range(nf)]
+    streams = [torch.cuda.Stream() for _ in range(nf)]
+    st = torch.cuda.current_stream()
+    for i in range(args.warmup):
+        with torch.cuda.stream(streams[i % nf]):
+            api.reconstruct_pair(ctxs[i % nf], dcfg, rcfg, dL, dR, out=outs[i % nf])
     torch.cuda.synchronize()
-    n_pts = int(mask.sum().item())
+    n_pts = int(outs[0][1].sum().item())
 
     def barrier():
         if dist:
             dist.barrier()
 
-    st = torch.cuda.current_stream()
+    def fork(ev):
+        ev.record(st)
+        for s in streams:
+            s.wait_event(ev)
+
+    def join():
+        for s in streams:
+            ev = torch.cuda.Event()
+            ev.record(s)
+            st.wait_event(ev)
+
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # end to end through the host entry: pinned frames in, xyz + mask out, copies timed
     hL = torch.from_numpy(L).pin_memory()
     hR = torch.from_numpy(R).pin_memory()
-    hx = torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32).pin_memory()
-    hm = torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory()
-    for _ in range(max(1, args.warmup // 2)):
-        api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
+    houts = [(torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32).pin_memory(),
+              torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory()) for _ in range(nf)]
+    hx, hm = houts[0]
+
+    def host_pairs(steps):
+        for i in range(steps):
+            api.reconstruct_pair_host(ctxs[i % nf], dcfg, rcfg, hL, hR, xyz=houts[i % nf][0], mask=houts[i % nf][1],
+                                      stream=streams[i % nf], asynchronous=True)
+
+    host_pairs(max(nf, args.warmup // 2))
+    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         barrier()
         torch.cuda.synchronize()
-        l0 = ctx.launch_count()
+        l0 = sum(c.launch_count() for c in ctxs)
         t0 = time.perf_counter()
-        e0.record(st)
-        for _ in range(args.steps):
-            api.reconstruct_pair(ctx, dcfg, rcfg, dL, dR, out=out)
+        fork(e0)
+        for i in range(args.steps):
+            with torch.cuda.stream(streams[i % nf]):
+                api.reconstruct_pair(ctxs[i % nf], dcfg, rcfg, dL, dR, out=outs[i % nf])
+        join()
         e1.record(st)
         torch.cuda.synchronize()
         clk.mark(t0, time.perf_counter())
         barrier()
-        launches = ctx.launch_count() - l0
+        launches = sum(c.launch_count() for c in ctxs) - l0
         ms = e0.elapsed_time(e1) / args.steps
 
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        e0.record(st)
-        for _ in range(args.steps):
-            api.reconstruct_pair_host(ctx, dcfg, rcfg, hL, hR, xyz=hx, mask=hm)
+        fork(e0)
+        host_pairs(args.steps)
+        join()
         e1.record(st)
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) / args.steps
@@ -293,7 +319,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32 (u16 samples; FP64 only for near-zero-disparity divides)",
             "data": "synthetic (seeded scene renderer, zim_gb300/synth)",
             "config": workload_config(W, H, F, ctx.rect_w, ctx.rect_h, 2 * L.nbytes),
-            "points_per_pair": n_pts, "replicas": world,
+            "points_per_pair": n_pts, "replicas": world, "pairs_in_flight": nf,
             "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms, 4)},
             "gpu_launches": int(launches),
@@ -663,6 +689,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--inflight", type=int, default=3,
+                    help="pairs in flight: one context and one stream each, round-robin (1: one stream)")
     ap.add_argument("--no-diff", action="store_true", help="skip the forward/adjoint leg (8 planar poses)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (64 mixed pairs)")
     ap.add_argument("--no-refine", action="store_true", help="skip the calibration-refinement leg")

@@ -377,6 +377,25 @@ ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_conf
                                              int cols, int pha_f, float* xyz, uint8_t* mask,
                                              float* disp, void* stream);
 
+/* The same without the final synchronisation: the uploads, the pair and the
+ * downloads are queued on `stream` (the right frames on the context's second
+ * copy queue) and the call returns; the outputs are complete, and the frame
+ * buffers free for reuse, once `stream` has drained (cudaStreamSynchronize or
+ * an event recorded after the call).  With page-locked frames and outputs the
+ * copies overlap other work on the GPU, so a caller that keeps two pairs in
+ * flight -- one context and one stream each, alternating -- hides the
+ * transfers of one pair behind the kernels of the other.  Calls on one context
+ * reuse its scratch: give them the same stream (or order them yourself), and
+ * keep one context per pair in flight.  On an error after work was queued the
+ * call drains the stream before returning.  The reference's entry
+ * (startCalculate, JSLAB_PhaseEpipolarReconstructor_V2.cpp:397-480) is
+ * synchronous; this is its pipelined form. */
+ZIM_API zim_status zim_reconstruct_pair_host_async(zim_ctx* ctx, const zim_decode_config* dcfg,
+                                                   const zim_recon_config* rcfg, const void* left_frames,
+                                                   const void* right_frames, int sample_type, int rows,
+                                                   int cols, int pha_f, float* xyz, uint8_t* mask,
+                                                   float* disp, void* stream);
+
 /* ---- batched path: many stereo pairs of uneven size and encoding ----
  * No counterpart in the reference (it reconstructs one pair per call through
  * JSLAB_PhaseEpipolarReconstructor_V2 / JSLAB_ReconstructPipeline_GPU).  One

@@ -89,6 +89,41 @@ def test_host_entry_equals_device_entry(ctx, oracle_lib, pinned):
 
 
 @pytest.mark.gpu
+def test_async_host_entry_two_pairs_in_flight(ctx, oracle_lib):
+    """Two contexts on two streams, the asynchronous host entry alternating
+    between them over four pairs of two different scenes (each context sees
+    both scenes, so its scratch is reused while the other context's pair is in
+    flight): every output equals the synchronous entry's, bit for bit."""
+    from zim_gb300 import api
+    spec, L1, R1, _ = scene_data("config1", width=612, height=512)
+    _, L2, R2, _ = scene_data("config1", seed=5, width=612, height=512)
+    rig = spec.rig.as_dict()
+    dcfg = api.decode_config(**spec.decode_kwargs())
+    rcfg = api.recon_config(use_px_gaussian=0, use_ror=0, use_sor=1, sor_mean_k=30, use_mls=1, mls_window_size=7,
+                            mls_spatial_sigma=1.4142135, mls_polynomial_order=2, mls_max_radius=2.0,
+                            mls_iterations=1, use_metric_gaussian=1, metric_gaussian_sigma=0.5)
+    ctx.set_calibration(rig, True)
+    want = [api.reconstruct_pair_host(ctx, dcfg, rcfg, L, R)[:2] for (L, R) in ((L1, R1), (L2, R2))]
+    ctxs = [api.Context(0), api.Context(0)]
+    for c in ctxs:
+        c.set_calibration(rig, True)
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    frames = [(torch.from_numpy(L).pin_memory(), torch.from_numpy(R).pin_memory()) for (L, R) in ((L1, R1), (L2, R2))]
+    outs = [(torch.empty((ctx.rect_h, ctx.rect_w, 3), dtype=torch.float32).pin_memory(),
+             torch.empty((ctx.rect_h, ctx.rect_w), dtype=torch.uint8).pin_memory()) for _ in range(4)]
+    for i in range(4):
+        hl, hr = frames[(i // 2) % 2] if i % 2 == 0 else frames[(i // 2 + 1) % 2]
+        api.reconstruct_pair_host(ctxs[i % 2], dcfg, rcfg, hl, hr, xyz=outs[i][0], mask=outs[i][1],
+                                  stream=streams[i % 2], asynchronous=True)
+    for s in streams:
+        s.synchronize()
+    for i in range(4):
+        k = (i // 2) % 2 if i % 2 == 0 else (i // 2 + 1) % 2
+        assert np.array_equal(outs[i][1].numpy(), want[k][1]), i
+        assert np.array_equal(outs[i][0].numpy(), want[k][0]), i
+
+
+@pytest.mark.gpu
 def test_reference_classes_match_c_abi(ctx, oracle_lib):
     from zim_gb300 import api
     spec, L, R, _ = scene_data("ref_heterodyne", width=612, height=512)

@@ -141,6 +141,7 @@ PROTOTYPES = {
     "zim_compact_points_noalloc": (I, [V, V, I, I, V, V, V]),
     "zim_reconstruct_pair": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
     "zim_reconstruct_pair_host": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
+    "zim_reconstruct_pair_host_async": (I, [V, V, V, V, V, I, I, I, I, V, V, V, V]),
     "zim_batch_create": (I, [V, V, I, I, V]),
     "zim_batch_destroy": (None, [V]),
     "zim_batch_rect_size": (I, [V, I, V, V]),

@@ -487,8 +487,12 @@ def reconstruct_pair(ctx, dcfg, rcfg, left, right, pha_f=0, out=None, want_disp=
 
 
 def reconstruct_pair_host(ctx, dcfg, rcfg, left: np.ndarray, right: np.ndarray, pha_f=0, xyz=None, mask=None,
-                          disp=None):
-    """The same from host arrays (numpy or pinned CPU tensors); synchronous."""
+                          disp=None, stream=None, asynchronous=False):
+    """The same from host arrays (numpy or pinned CPU tensors); synchronous.
+    asynchronous=True queues the copies and the pair on `stream` (a
+    torch.cuda.Stream; default the current stream) and returns at once
+    (zim_reconstruct_pair_host_async): the outputs are ready, and the inputs
+    free, once that stream has drained.  Pass page-locked buffers."""
     F, H, W = left.shape
     st = SAMPLE_U8 if left.dtype in (np.uint8, torch.uint8) else SAMPLE_U16
     if xyz is None:
@@ -503,8 +507,10 @@ def reconstruct_pair_host(ctx, dcfg, rcfg, left: np.ndarray, right: np.ndarray, 
             return C.c_void_p(a.data_ptr())
         return a.ctypes.data_as(C.c_void_p)
 
-    ctx.check(_lib.load().zim_reconstruct_pair_host(ctx.h, C.byref(dcfg), C.byref(rcfg), hp(left), hp(right), st, H,
-                                                    W, int(pha_f), hp(xyz), hp(mask), hp(disp), _stream()))
+    fn = _lib.load().zim_reconstruct_pair_host_async if asynchronous else _lib.load().zim_reconstruct_pair_host
+    sp = C.c_void_p(stream.cuda_stream) if stream is not None else _stream()
+    ctx.check(fn(ctx.h, C.byref(dcfg), C.byref(rcfg), hp(left), hp(right), st, H, W, int(pha_f), hp(xyz), hp(mask),
+                 hp(disp), sp))
     return xyz, mask, disp
 
 

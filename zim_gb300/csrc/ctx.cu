@@ -427,11 +427,14 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair(zim_ctx* ctx, const zim_decod
     return run_pair(ctx, d, r, lf, rf, sample_type, rows, cols, pha_f, xyz, mask, disp, B, zim_stream(stream));
 }
 
-extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_config* d,
-                                                        const zim_recon_config* r, const void* lf,
-                                                        const void* rf, int sample_type, int rows, int cols,
-                                                        int pha_f, float* xyz, uint8_t* mask, float* disp,
-                                                        void* stream) {
+// Body of the host entries: uploads both frame stacks, runs the pair and
+// queues the downloads on `stream`.  sync: drains the stream before returning.
+// Without sync the call returns once everything is queued; on an error after
+// work was queued it drains the stream all the same, so that nothing it queued
+// still writes the caller's host buffers once it has returned.
+static zim_status host_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_recon_config* r, const void* lf,
+                            const void* rf, int sample_type, int rows, int cols, int pha_f, float* xyz,
+                            uint8_t* mask, float* disp, void* stream, bool sync) {
     zim_status s = check_pair_args(ctx, d, r, lf, rf, sample_type, rows, cols, xyz, mask);
     if (s) return s;
     ZIM_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -450,17 +453,17 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     uint8_t* dmask = (uint8_t*)zim_scratch_take(ctx, dst);
     float* ddisp = (float*)zim_scratch_take(ctx, dst * 4);
     if (!dl || !dr || !dxyz || !dmask || !ddisp) return zim_fail(ctx, ZIM_ERR_OUT_OF_MEMORY, "scratch carve failed");
-    cudaStream_t st = zim_stream(stream);
-    // the right frames travel on the second queue while the left camera decodes
-    // (the second queue starts after everything already on st)
-    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(dl, lf, fbytes, cudaMemcpyHostToDevice, st));
-    ZIM_CUDA_TRY(ctx, cudaEventRecord(ctx->aux_event, st));
-    ZIM_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_event, 0));
-    ZIM_CUDA_TRY(ctx, cudaMemcpyAsync(dr, rf, fbytes, cudaMemcpyHostToDevice, ctx->aux_stream));
-    ZIM_CUDA_TRY(ctx, cudaEventRecord(ctx->aux_event, ctx->aux_stream));
     PairBuffers B;
     s = carve_pair(ctx, r, rows, cols, ddisp, B);
     if (s) return s;
+    cudaStream_t st = zim_stream(stream);
+    // the right frames travel on the second queue while the left camera decodes
+    // (the second queue starts after everything already on st)
+    cudaError_t e = cudaMemcpyAsync(dl, lf, fbytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->aux_event, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_event, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dr, rf, fbytes, cudaMemcpyHostToDevice, ctx->aux_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->aux_event, ctx->aux_stream);
     // A pinned (page-locked) cloud buffer takes the last stage's writes
     // directly through its device address: the copy back overlaps that
     // stage.  Only the last stage writes it; the mask, which later stages
@@ -470,7 +473,7 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
     // copies instead.
     const bool last_reads_out = r->use_mls && !r->use_metric_gaussian && r->mls_iterations >= 3;
     float* xyz_dev = nullptr;
-    if (!last_reads_out) {
+    if (e == cudaSuccess && !last_reads_out) {
         cudaPointerAttributes a{};
         if (cudaPointerGetAttributes(&a, xyz) == cudaSuccess && a.type == cudaMemoryTypeHost &&
             a.devicePointer != nullptr)
@@ -478,15 +481,20 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
         else
             cudaGetLastError();  // pageable memory: clear the query's error, copy back below
     }
-    s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, xyz_dev ? xyz_dev : dxyz, dmask, ddisp, B, st,
-                 ctx->aux_event);
-    cudaError_t e = cudaSuccess;
-    if (s == ZIM_OK && !xyz_dev) e = cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st);
-    if (s == ZIM_OK && e == cudaSuccess) e = cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st);
-    if (s == ZIM_OK && e == cudaSuccess && disp) e = cudaMemcpyAsync(disp, ddisp, dst * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        s = run_pair(ctx, d, r, dl, dr, sample_type, rows, cols, pha_f, xyz_dev ? xyz_dev : dxyz, dmask, ddisp, B,
+                     st, ctx->aux_event);
+    if (e == cudaSuccess && s == ZIM_OK && !xyz_dev) e = cudaMemcpyAsync(xyz, dxyz, dst * 12, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && s == ZIM_OK) e = cudaMemcpyAsync(mask, dmask, dst, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && s == ZIM_OK && disp) e = cudaMemcpyAsync(disp, ddisp, dst * 4, cudaMemcpyDeviceToHost, st);
+    const bool failed = s != ZIM_OK || e != cudaSuccess;
     // Whatever failed, nothing queued here may still be writing the caller's
     // host buffers when this returns: drain the stream first.
-    const cudaError_t es = cudaStreamSynchronize(st);
+    cudaError_t es = cudaSuccess;
+    if (sync || failed) {
+        es = cudaStreamSynchronize(st);
+        if (failed) cudaStreamSynchronize(ctx->aux_stream);
+    }
     if (s) return s;
     if (e != cudaSuccess || es != cudaSuccess) {
         const cudaError_t err = e != cudaSuccess ? e : es;
@@ -494,4 +502,20 @@ extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_
         return zim_fail(ctx, ZIM_ERR_CUDA, "%s", cudaGetErrorString(err));
     }
     return ZIM_OK;
+}
+
+extern "C" ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_config* d,
+                                                        const zim_recon_config* r, const void* lf,
+                                                        const void* rf, int sample_type, int rows, int cols,
+                                                        int pha_f, float* xyz, uint8_t* mask, float* disp,
+                                                        void* stream) {
+    return host_pair(ctx, d, r, lf, rf, sample_type, rows, cols, pha_f, xyz, mask, disp, stream, true);
+}
+
+extern "C" ZIM_API zim_status zim_reconstruct_pair_host_async(zim_ctx* ctx, const zim_decode_config* d,
+                                                              const zim_recon_config* r, const void* lf,
+                                                              const void* rf, int sample_type, int rows, int cols,
+                                                              int pha_f, float* xyz, uint8_t* mask, float* disp,
+                                                              void* stream) {
+    return host_pair(ctx, d, r, lf, rf, sample_type, rows, cols, pha_f, xyz, mask, disp, stream, false);
 }
