@@ -26,9 +26,14 @@ Compiled, from PhaseShiftGrayCode3D/src/ of the reference:
     oracle/ref_mls_f64.cpp, which includes it with its `float` arithmetic
     widened to double (the oracle's FP64 MLS is pinned to that build; the
     FP32 one bounds the reference's own rounding).
-The reference's CUDA files are not built: this is the CPU checker.  Needs g++
-with OpenMP; the reference tree exists only where it was mounted, so this
-build runs there (never on a machine without it).
+Also built, as a second witness on the GPU (build_cubins): the reference's
+three CUDA files JSLAB_PhaseShiftDecoder_V2_GPU.cu, JSLAB_PhaseEpipolarReconstructor_V2_GPU.cu
+and JSLAB_MLS_Filter.cu, device code only (nvcc -cubin for sm_103a), into
+oracle/_ref/*.cubin, with the entry names ptxas reports written to
+oracle/_ref/ref_cubins.json.  A cubin holds GPU code only, so it runs on any
+host of the GPU; oracle/ref_cuda.py loads it through the CUDA driver API.
+Needs g++ with OpenMP and nvcc; the reference tree exists only where it was
+mounted, so this build runs there (never on a machine without it).
 """
 from __future__ import annotations
 
@@ -143,12 +148,63 @@ def build(ref: Path | None = None, force: bool = False) -> Path:
     return LIB_PATH
 
 
+CUDA_FILES = ["JSLAB_PhaseShiftDecoder_V2_GPU.cu", "JSLAB_PhaseEpipolarReconstructor_V2_GPU.cu",
+              "JSLAB_MLS_Filter.cu"]
+CUBIN_JSON = OUT_DIR / "ref_cubins.json"
+NVCC_FLAGS = ["-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w",
+              "-D__declspec(x)=", "-Xptxas", "-v"]
+
+
+def build_cubins(ref: Path | None = None, force: bool = False) -> Path:
+    """Compiles the reference's CUDA files into cubins (device code only) and
+    returns the index file mapping each cubin to its kernels' entry names."""
+    import json
+    src = ref_src(ref)
+    if not all((src / f).exists() for f in CUDA_FILES):
+        if CUBIN_JSON.exists():
+            return CUBIN_JSON
+        raise FileNotFoundError(f"reference CUDA sources not found under {src}")
+    OUT_DIR.mkdir(exist_ok=True)
+    h = hashlib.sha256()
+    for f in CUDA_FILES:
+        h.update((src / f).read_bytes())
+    for p in sorted((HERE / "cvshim").rglob("*")) + [Path(__file__)]:
+        if p.is_file():
+            h.update(p.read_bytes())
+    stamp = OUT_DIR / "cubins.sha"
+    dig = h.hexdigest()
+    if not force and CUBIN_JSON.exists() and stamp.exists() and stamp.read_text() == dig:
+        return CUBIN_JSON
+    nvcc = os.environ.get("NVCC") or "nvcc"
+    inc = ["-I", str(HERE / "cvshim"), "-I", str(HERE / "cvshim" / "opencv2"), "-I", str(src)]
+    index = {}
+    procs = []
+    for f in CUDA_FILES:
+        out = OUT_DIR / (Path(f).stem + ".cubin")
+        cmd = [nvcc, *NVCC_FLAGS, *inc, str(src / f), "-o", str(out)]
+        procs.append((f, out, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE)))
+    for f, out, p in procs:
+        o, e = p.communicate()
+        if p.returncode:
+            raise RuntimeError(f"cubin build of {f} failed:\n" + e.decode(errors="replace")[-4000:])
+        # ptxas -v names every entry it compiles: "Compiling entry function '<mangled>'"
+        names = []
+        for line in (o + e).decode(errors="replace").splitlines():
+            if "Compiling entry function '" in line:
+                names.append(line.split("'")[1])
+        index[out.name] = sorted(set(names))
+    CUBIN_JSON.write_text(json.dumps(index, indent=1))
+    stamp.write_text(dig)
+    return CUBIN_JSON
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", type=Path, default=None)
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args()
     print(build(a.ref, a.force))
+    print(build_cubins(a.ref, a.force))
 
 
 if __name__ == "__main__":
