@@ -43,6 +43,7 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <utility>
 
 #include "zim_tiles.cuh"
 
@@ -341,15 +342,25 @@ __device__ __forceinline__ unsigned grid_slot(const GridStats* __restrict__ s, i
 
 // Neighbouring pixels mostly share a cell, so the lanes of a warp that hit the
 // same slot add to it once (the lowest such lane).
+// The table kernels stride over the points with a grid sized to the GPU, not
+// to the cloud: a gated-off launch then costs a few waves of empty blocks.
 __global__ void hash_count_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
                                   const GridStats* __restrict__ s, int level, unsigned tmask,
                                   unsigned* __restrict__ counts, const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool v = i < n && mask[i];
-    const unsigned h = v ? grid_slot(s, level, tmask, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) : 0xffffffffu;
-    const unsigned grp = __match_any_sync(0xffffffffu, h);
-    if (v && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[h], (unsigned)__popc(grp));
+    for (size_t b = (size_t)blockIdx.x * blockDim.x; b < n; b += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = b + threadIdx.x;
+        const bool v = i < n && mask[i];
+        const unsigned h = v ? grid_slot(s, level, tmask, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]) : 0xffffffffu;
+        const unsigned grp = __match_any_sync(0xffffffffu, h);
+        if (v && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counts[h], (unsigned)__popc(grp));
+    }
+}
+
+__global__ void zero_kernel(unsigned* __restrict__ p, size_t n, const unsigned* __restrict__ gate) {
+    if (gated_off(gate)) return;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = 0u;
 }
 
 __device__ __forceinline__ unsigned block_scan_incl(unsigned v, unsigned* ws) {
@@ -378,11 +389,15 @@ __global__ void scan_blocks_kernel(const unsigned* __restrict__ counts, uint2* _
                                    unsigned* __restrict__ block_tot, const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
     __shared__ unsigned ws[32];
-    size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
-    unsigned v = i < n ? counts[i] : 0u;
-    unsigned incl = block_scan_incl(v, ws);
-    if (i < n) tab[i] = make_uint2(incl - v, v);
-    if (threadIdx.x == SCAN_B - 1) block_tot[blockIdx.x] = incl;
+    const size_t nb = (n + SCAN_B - 1) / SCAN_B;
+    for (size_t b = blockIdx.x; b < nb; b += gridDim.x) {
+        const size_t i = b * SCAN_B + threadIdx.x;
+        const unsigned v = i < n ? counts[i] : 0u;
+        const unsigned incl = block_scan_incl(v, ws);
+        if (i < n) tab[i] = make_uint2(incl - v, v);
+        if (threadIdx.x == SCAN_B - 1) block_tot[b] = incl;
+        __syncthreads();  // ws is reused by the next chunk
+    }
 }
 
 __global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb, const unsigned* __restrict__ gate) {
@@ -406,8 +421,11 @@ __global__ void scan_totals_kernel(unsigned* __restrict__ tot, int nb, const uns
 __global__ void scan_add_kernel(uint2* __restrict__ tab, size_t n, const unsigned* __restrict__ tot,
                                 const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
-    size_t i = (size_t)blockIdx.x * SCAN_B + threadIdx.x;
-    if (i < n) tab[i].x += tot[blockIdx.x];
+    const size_t nb = (n + SCAN_B - 1) / SCAN_B;
+    for (size_t b = blockIdx.x; b < nb; b += gridDim.x) {
+        const size_t i = b * SCAN_B + threadIdx.x;
+        if (i < n) tab[i].x += tot[b];
+    }
 }
 
 __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
@@ -415,23 +433,26 @@ __global__ void hash_scatter_kernel(const float* __restrict__ xyz, const uint8_t
                                     const uint2* __restrict__ tab, unsigned* __restrict__ fill,
                                     float4* __restrict__ pts, const unsigned* __restrict__ gate) {
     if (gated_off(gate)) return;
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool v = i < n && mask[i];
-    float x = 0.f, y = 0.f, z = 0.f;
-    unsigned h = 0xffffffffu;
-    if (v) {
-        x = xyz[3 * i]; y = xyz[3 * i + 1]; z = xyz[3 * i + 2];
-        h = grid_slot(s, level, tmask, x, y, z);
+    for (size_t b = (size_t)blockIdx.x * blockDim.x; b < n; b += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = b + threadIdx.x;
+        const bool v = i < n && mask[i];
+        float x = 0.f, y = 0.f, z = 0.f;
+        unsigned h = 0xffffffffu;
+        if (v) {
+            x = xyz[3 * i]; y = xyz[3 * i + 1]; z = xyz[3 * i + 2];
+            h = grid_slot(s, level, tmask, x, y, z);
+        }
+        // one atomic per slot and warp; lanes take consecutive places in lane order
+        const unsigned grp = __match_any_sync(0xffffffffu, h);
+        const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+        unsigned base = 0;
+        if (v && lane == leader) base = atomicAdd(&fill[h], (unsigned)__popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (v) {
+            const unsigned pos = tab[h].x + base + (unsigned)__popc(grp & ((1u << lane) - 1u));
+            pts[pos] = make_float4(x, y, z, __int_as_float((int)i));
+        }
     }
-    // one atomic per slot and warp; lanes take consecutive places in lane order
-    const unsigned grp = __match_any_sync(0xffffffffu, h);
-    const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
-    unsigned base = 0;
-    if (v && lane == leader) base = atomicAdd(&fill[h], (unsigned)__popc(grp));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (!v) return;
-    const unsigned pos = tab[h].x + base + (unsigned)__popc(grp & ((1u << lane) - 1u));
-    pts[pos] = make_float4(x, y, z, __int_as_float((int)i));
 }
 
 // Sorts each bucket by pixel index, so bucket contents no longer depend on the
@@ -830,6 +851,13 @@ struct WinSpiral {
     }
 };
 __constant__ WinSpiral c_win = WinSpiral();
+constexpr WinSpiral k_win{};  // the same table at compile time
+// tile offset of spiral entry O as a compile-time constant
+template <int O>
+__device__ __forceinline__ int win_off_c() {
+    constexpr int v = (int)(short)(k_win.ent[O] & 0xffff);
+    return v;
+}
 __device__ __forceinline__ int win_off(int o) { return (int)(short)(c_win.ent[o] & 0xffff); }
 __device__ __forceinline__ int win_len2(int o) { return c_win.ent[o] >> 16; }
 // offsets whose squared length is at most r2 (r2 >= 0 or +inf)
@@ -875,6 +903,15 @@ struct WinHeap {
 __device__ __forceinline__ void defer_query(GridStats* s, unsigned* deferred, float* md_out, size_t i) {
     md_out[i] = -1.f;
     deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
+}
+
+// The heap's first K1T - 1 distances (heap slots K1T - 2 down to 0) from the
+// first K1T - 1 spiral offsets, invalid pixels as +inf.
+template <int K1T, int... O>
+__device__ __forceinline__ void fill_first(WinHeap<K1T>& heap, const float4* W, int wc, float4 q,
+                                           std::integer_sequence<int, O...>) {
+    auto d2 = [&](const float4 p) { return p.w == 0.f ? INFINITY : sqdist(p.x - q.x, p.y - q.y, p.z - q.z); };
+    ((heap.at(K1T - 2 - O) = d2(W[wc + win_off_c<O>()])), ...);
 }
 
 // K1T: k + 1 at compile time (0: from k)
@@ -926,18 +963,33 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float4 q = W[wc];
     const int K1 = K1T ? K1T : k + 1;
     // the query and its first k valid window pixels in spiral order fill the
-    // heap; its root (their largest distance) is the first bound
+    // heap; its root (their largest distance) is the first bound.  They fill
+    // it from the last slot backwards: the spiral meets pixels roughly by
+    // increasing distance, so the array is close to descending -- close to a
+    // max-heap already -- and the build sifts little.  (Only the multiset of
+    // the heap's values matters: the root is its maximum, a replacement drops
+    // the maximum, and the mean distance is an order-free fixed-point sum.)
     WinHeap<K1T> heap{Ls + tid, K1};
-    heap.at(0) = 0.f;
-    int cnt = 1, o = 0;
-    for (; o < WN && cnt < K1; o++) {
-        const float4 p = W[wc + win_off(o)];
-        if (p.w == 0.f) continue;
-        heap.at(cnt++) = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
-    }
-    if (cnt < K1) {
-        defer_query(s, deferred, md_out, i);
-        return;
+    heap.at(K1 - 1) = 0.f;
+    int o = 0;
+    if constexpr (K1T > 0) {
+        // k known at compile time: the first k spiral offsets fill the heap
+        // straight from constant tile offsets, an invalid pixel as +inf (the
+        // largest value: the first valid distance to come replaces it, and a
+        // heap still holding one at the end means fewer than k + 1 points)
+        fill_first<K1T>(heap, W, wc, q, std::make_integer_sequence<int, K1T - 1>{});
+        o = K1T - 1;
+    } else {
+        int cnt = 1;
+        for (; o < WN && cnt < K1; o++) {
+            const float4 p = W[wc + win_off(o)];
+            if (p.w == 0.f) continue;
+            heap.at(K1 - 1 - cnt++) = sqdist(p.x - q.x, p.y - q.y, p.z - q.z);
+        }
+        if (cnt < K1) {
+            defer_query(s, deferred, md_out, i);
+            return;
+        }
     }
     heap.build();
     float thr = heap.at(0);
@@ -972,6 +1024,10 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
             thr = heap.at(0);
             lim = win_upto(stop_r2(thr));
         }
+    }
+    if (!(thr < INFINITY)) {  // fewer than k + 1 points in the whole window
+        defer_query(s, deferred, md_out, i);
+        return;
     }
     // every window offset not visited is at least as long as offset o
     const float rbreak = o < WN ? fminf(sqrtf((float)win_len2(o)), (float)(WR + 1)) : (float)(WR + 1);
@@ -1631,9 +1687,10 @@ __global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t
 // side 3 sigma around p; buckets are index-sorted, so the FP32 sums are
 // deterministic.
 // Metric Gaussian by the window fast path: the points within r of a query,
-// summed in spiral order over its window up to the pixel distance beyond which
-// the ray bound puts every point farther than r (see sor_window_kernel); the
-// others are marked -2 in `pending` for metric_gaussian_kernel.
+// summed row by row over the disk of its window out to the pixel distance
+// beyond which the ray bound puts every point farther than r (see
+// sor_window_kernel); the others are marked -2 in `pending` for
+// metric_gaussian_kernel.
 constexpr int WRG = WR;
 constexpr int GW = TILE_X + 2 * WRG, GH = TILE_Y + 2 * WRG;
 
@@ -1641,6 +1698,7 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
                                                            const uint8_t* __restrict__ mask, int rows, int cols,
                                                            float r, float inv2s2, RayParams rp,
                                                            GridStats* __restrict__ s,
+                                                           const unsigned* __restrict__ tile_dev,
                                                            float* __restrict__ pending, float* __restrict__ out) {
     __shared__ float4 W[GW * GH];
     const int tid = threadIdx.x;
@@ -1674,28 +1732,52 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
     const float qn = sqrtf(fmaf(q.x, q.x, fmaf(q.y, q.y, q.z * q.z)));
     const float C = qn * rp.f / an;
-    const float dev = ray_dev(q.x, q.y, q.z, ax, ay, az) + __uint_as_float(s->ray_dev_bits) + 1e-5f * qn;
-    // pixels farther than rs from the query hold no point within r
+    // the window's pixels are the 3 x 3 tiles around this one (halo 7 < 8):
+    // their points lie within the largest of those tiles' ray distances;
+    // pixels outside the window within the largest of all
+    unsigned td = 0u;
+    for (int by = max(0, (int)blockIdx.y - 1); by <= min((int)gridDim.y - 1, (int)blockIdx.y + 1); by++)
+        for (int bx = max(0, (int)blockIdx.x - 1); bx <= min((int)gridDim.x - 1, (int)blockIdx.x + 1); bx++)
+            td = max(td, tile_dev[(size_t)by * gridDim.x + bx]);
+    const float dev_q = ray_dev(q.x, q.y, q.z, ax, ay, az) + 1e-5f * qn;
+    const float dev = dev_q + __uint_as_float(td);
+    const float dev_out = dev_q + __uint_as_float(s->ray_dev_bits);
+    // window pixels farther than rs from the query hold no point within r,
+    // and neither does any pixel outside the window (at least WRG + 1 away)
     const float sd = r + dev;
     const float rs = C > sd ? sd * an / (C - sd) : INFINITY;
-    if (!(rs < (float)(WRG + 1))) {
+    const float ro = (float)(WRG + 1);
+    if (!(rs < ro) || !(C * ro / (an + ro) - dev_out > r)) {
         pending[i] = -2.f;
         atomicAdd(&s->n_pending, 1u);  // the grid gets built
         return;
     }
     const float r2 = r * r;
     const int wc = (ty + WRG) * GW + tx + WRG;
-    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 1.f;  // the query itself: weight 1, offset 0
-    const int lim = win_upto(rs * rs);
-    static_assert(GW == WW && WRG == WR, "the window table's tile");
-    for (int o = 0; o < lim; o++) {
-        const float4 p = W[wc + win_off(o)];
-        const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
-        const float d2 = sqdist(ex, ey, ez);
-        if (!(d2 <= r2)) continue;  // also every invalid pixel (NaN)
-        const float w = __expf(-d2 * inv2s2);
-        sx = fmaf(w, ex, sx); sy = fmaf(w, ey, sy); sz = fmaf(w, ez, sz);
-        sw += w;
+    // The disk of pixels within rs, row by row (the query itself included:
+    // offset 0, weight exactly 1); w = 2^(d2 kq), kq = -log2(e) / (2 s^2)
+    const float kq = -1.44269504088896341f * inv2s2;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+    const int R2 = (int)(rs * rs);  // offsets with dx^2 + dy^2 <= R2 (< (WRG + 1)^2)
+#pragma unroll 1
+    for (int dy = -WRG; dy <= WRG; dy++) {
+        const int rem = R2 - dy * dy;
+        if (rem < 0) continue;
+        // exact floor of the root: a root of a non-square below 64 lies at
+        // least 0.06 from an integer, far beyond the float error
+        const int w = min((int)sqrtf((float)rem), WRG);
+        const float4* row = W + wc + dy * GW;
+#pragma unroll 2
+        for (int dx = -w; dx <= w; dx++) {
+            const float4 p = row[dx];
+            const float ex = p.x - q.x, ey = p.y - q.y, ez = p.z - q.z;
+            const float d2 = sqdist(ex, ey, ez);
+            if (!(d2 <= r2)) continue;  // also every invalid pixel (NaN)
+            float wt;
+            asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(wt) : "f"(d2 * kq));
+            sx = fmaf(wt, ex, sx); sy = fmaf(wt, ey, sy); sz = fmaf(wt, ez, sz);
+            sw += wt;
+        }
     }
     const float iw = 1.0f / sw;
     out[3 * i] = q.x + sx * iw;
@@ -1704,12 +1786,10 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     pending[i] = 0.f;
 }
 
-__global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
-                                       float r2, float inv2s2, Level g, const GridStats* __restrict__ s,
-                                       const float* __restrict__ pending, float* __restrict__ out) {
-    if (pending && s->n_pending == 0u) return;  // the window pass settled every query
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void metric_gaussian_point(const float* __restrict__ xyz, const uint8_t* __restrict__ mask,
+                                                      size_t i, float r2, float inv2s2, const Level& g,
+                                                      const GridStats* __restrict__ s,
+                                                      const float* __restrict__ pending, float* __restrict__ out) {
     if (pending && pending[i] != -2.f) return;  // settled by the window pass
     const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
     if (!mask[i]) {
@@ -1739,6 +1819,16 @@ __global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint
     out[3 * i] = (float)((double)qx + (double)sx * k);
     out[3 * i + 1] = (float)((double)qy + (double)sy * k);
     out[3 * i + 2] = (float)((double)qz + (double)sz * k);
+}
+
+// Grid-stride over the points (a grid sized to the GPU: when the window pass
+// left nothing, the launch costs a few waves of blocks that return at once).
+__global__ void metric_gaussian_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, size_t n,
+                                       float r2, float inv2s2, Level g, const GridStats* __restrict__ s,
+                                       const float* __restrict__ pending, float* __restrict__ out) {
+    if (pending && s->n_pending == 0u) return;  // the window pass settled every query
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        metric_gaussian_point(xyz, mask, i, r2, inv2s2, g, s, pending, out);
 }
 
 unsigned table_size(size_t want) {
@@ -1810,27 +1900,31 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
     return ZIM_OK;
 }
 
-// Largest distance of a valid point from its pixel ray into ray_dev_bits (NaN
-// counts as unbounded): blocks over rows, threads over a row's pixels, one
-// atomic per block.
-__global__ void ray_dev_max_kernel(const float* __restrict__ xyz, const uint8_t* __restrict__ mask, int rows,
-                                   int cols, zt::RayParams rp, GridStats* s) {
-    __shared__ unsigned wmax[GB / 32];
+// Per 16x8 pixel tile (the window passes' tiles) the largest distance of a
+// valid point from its pixel ray (float bits; NaN counts as unbounded), and the
+// largest of all into ray_dev_bits.
+__global__ void __launch_bounds__(TILE_T) tile_ray_dev_kernel(const float* __restrict__ xyz,
+                                                              const uint8_t* __restrict__ mask, int rows, int cols,
+                                                              zt::RayParams rp, GridStats* s,
+                                                              unsigned* __restrict__ tile_dev) {
+    __shared__ unsigned wmax[TILE_T / 32];
+    const int x = blockIdx.x * TILE_X + (int)threadIdx.x % TILE_X, y = blockIdx.y * TILE_Y + (int)threadIdx.x / TILE_X;
     unsigned dev = 0u;
-    for (int y = blockIdx.x; y < rows; y += gridDim.x)
-        for (int x = threadIdx.x; x < cols; x += blockDim.x) {
-            const size_t i = (size_t)y * cols + x;
-            if (!mask[i]) continue;
+    if (x < cols && y < rows) {
+        const size_t i = (size_t)y * cols + x;
+        if (mask[i]) {
             float ax, ay, az;
             zt::ray_dir(rp, x, y, ax, ay, az);
             const float d = zt::ray_dev(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ax, ay, az);
-            dev = max(dev, __float_as_uint(d == d ? d : INFINITY));
+            dev = __float_as_uint(d == d ? d : INFINITY);
         }
+    }
     dev = __reduce_max_sync(0xffffffffu, dev);
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = dev;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int j = 1; j < GB / 32; j++) dev = max(dev, wmax[j]);
+        for (int j = 1; j < TILE_T / 32; j++) dev = max(dev, wmax[j]);
+        tile_dev[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = dev;
         if (dev) atomicMax(&s->ray_dev_bits, dev);
     }
 }
@@ -1867,18 +1961,22 @@ zim_status grid_stats(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
 // slot); gate as for the table kernels (null: always built).
 zim_status grid_tables(zim_ctx* ctx, const float* xyz, const uint8_t* mask, size_t n, bool sort_buckets,
                        GridScratch& G, cudaStream_t st, int first_level = 0, const unsigned* gate = nullptr) {
-    const unsigned nblk = (unsigned)((n + GB - 1) / GB);
+    // grids sized to the GPU (the kernels stride): 8 blocks of 256 per SM,
+    // 2 of the scans' 1024
+    const unsigned sms = (unsigned)(ctx->sm_count > 0 ? ctx->sm_count : 152);
+    const unsigned nblk = (unsigned)std::min<size_t>((n + GB - 1) / GB, 8 * sms);
     for (int l = first_level; l < G.levels; l++) {
         const unsigned T = G.tsize[l], nb = (T + SCAN_B - 1) / SCAN_B;
-        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
+        const unsigned tblk = std::min((T + GB - 1) / GB, 8 * sms), sblk = std::min(nb, 2 * sms);
+        zero_kernel<<<tblk, GB, 0, st>>>(G.counts, T, gate);
         hash_count_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.counts, gate);
-        scan_blocks_kernel<<<nb, SCAN_B, 0, st>>>(G.counts, G.tab[l], T, G.tot, gate);
+        scan_blocks_kernel<<<sblk, SCAN_B, 0, st>>>(G.counts, G.tab[l], T, G.tot, gate);
         scan_totals_kernel<<<1, SCAN_B, 0, st>>>(G.tot, (int)nb, gate);
-        scan_add_kernel<<<nb, SCAN_B, 0, st>>>(G.tab[l], T, G.tot, gate);
-        ZIM_CUDA_TRY(ctx, cudaMemsetAsync(G.counts, 0, (size_t)T * 4, st));
+        scan_add_kernel<<<sblk, SCAN_B, 0, st>>>(G.tab[l], T, G.tot, gate);
+        zero_kernel<<<tblk, GB, 0, st>>>(G.counts, T, gate);
         hash_scatter_kernel<<<nblk, GB, 0, st>>>(xyz, mask, n, G.stats, l, T - 1, G.tab[l], G.counts, G.pts[l],
                                                   gate);
-        ctx->launches += 5;
+        ctx->launches += 7;
         if (sort_buckets) {
             bucket_sort_kernel<<<(T + GB - 1) / GB, GB, 0, st>>>(G.tab[l], T, G.pts[l]);
             ctx->launches += 1;
@@ -1978,8 +2076,9 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         // the window pass needs only the largest ray distance; the grid's
         // statistics wait for the window pass's verdict
         stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
-        const unsigned dblk = (unsigned)std::min(rows, 8 * (ctx->sm_count > 0 ? ctx->sm_count : 152));
-        ray_dev_max_kernel<<<dblk, GB, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats);
+        dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
+        tile_ray_dev_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats,
+                                                      reinterpret_cast<unsigned*>(G.bound));
         ctx->launches += 2;
     } else {
         s = grid_stats(ctx, xyz, mask, rows, cols, rad, 1.0f, nullptr, G, st);
@@ -1992,7 +2091,9 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         const RayParams rp = rpw;
         dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
         pending = G.md;
-        mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats, pending, out);
+        // G.bound holds the per-tile ray distances (one word per tile)
+        mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats,
+                                                   reinterpret_cast<const unsigned*>(G.bound), pending, out);
         ctx->launches += 1;
     }
     // the grid only for the queries the window pass left (launched, and
@@ -2003,7 +2104,8 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     }
     s = grid_tables(ctx, xyz, mask, n, false, G, st, 0, pending ? &G.stats->n_pending : nullptr);
     if (s) return s;
-    metric_gaussian_kernel<<<(unsigned)((n + GB - 1) / GB), GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
+    const unsigned mblk = (unsigned)std::min<size_t>((n + GB - 1) / GB, 8 * (ctx->sm_count > 0 ? ctx->sm_count : 152));
+    metric_gaussian_kernel<<<mblk, GB, 0, st>>>(xyz, mask, n, rad * rad, inv2s2, g, G.stats,
                                                                         pending, out);
     ctx->launches += 1;
     ZIM_LAUNCH_CHECK(ctx);
