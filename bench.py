@@ -61,7 +61,27 @@ def env_rank():
 # DRAM bytes per launch (read + write) of a stage's kernel on the 5 MP
 # workload, from one ncu capture each (profiles/*_5mp_dram.md): the
 # roofline's `traffic` for that kernel when it dominates the step.
-MEASURED_TRAFFIC = {("mls", 2448, 2048): (68127488 + 26212864, "profiles/mls_smem_kernel_5mp_dram.md")}
+MEASURED_TRAFFIC = {("mls", 2448, 2048): (68065792 + 25864448, "profiles/mls_smem_kernel_5mp.md")}
+# Warp instructions per launch and the FMA pipe's busy fraction of a stage's
+# kernel on the 5 MP workload, from one ncu capture (profiles/*_5mp.md): the
+# issue-slot side of the roofline for kernels bound by instruction issue.
+MEASURED_ISSUE = {("mls", 2448, 2048): (1205751882, 0.5683, "profiles/mls_smem_kernel_5mp.md")}
+
+
+def issue_roofline(stage, W, H, ms_per_launch, sm_mhz):
+    """Achieved warp instructions per second against the issue peak (one warp
+    instruction per scheduler per cycle: 4 x SMs x SM clock), or None."""
+    m = MEASURED_ISSUE.get((stage, W, H))
+    if not m:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    inst, fma, src = m
+    ach = inst / (ms_per_launch * 1e-3) / 1e9
+    pk = 4 * sms * sm_mhz * 1e6 / 1e9
+    return {"warp_inst_per_launch": inst, "achieved_ginst_s": round(ach, 1), "peak_ginst_s": round(pk, 1),
+            "frac": round(ach / pk, 4), "fma_pipe_frac": fma, "source": src,
+            "note": "peak: one warp instruction per scheduler per cycle at the median SM clock of the timed region"}
 
 
 def peaks():
@@ -334,6 +354,9 @@ def run_ours(args):
             "stages_hold": bool(getattr(stage_breakdown, "hold_ran", False)),
             "clocks": clk.summary(),
         }
+        iss = issue_roofline(dom, W, H, per_launch[dom], result["clocks"].get("sm_mhz") or 2070.0)
+        if iss:
+            result["roofline"]["issue"] = iss
         if cpu:
             result["cpu_baseline"] = cpu
         if not args.no_batch:

@@ -386,8 +386,11 @@ ZIM_API zim_status zim_reconstruct_pair_host(zim_ctx* ctx, const zim_decode_conf
  * flight -- one context and one stream each, alternating -- hides the
  * transfers of one pair behind the kernels of the other.  Calls on one context
  * reuse its scratch: give them the same stream (or order them yourself), and
- * keep one context per pair in flight.  On an error after work was queued the
- * call drains the stream before returning.  The reference's entry
+ * keep one context per pair in flight.  The cloud is always written to device
+ * scratch and copied back (a pinned xyz buffer is not written directly, as the
+ * synchronous entry does: a kernel stalled on writes across the host link
+ * would hold SMs the other pairs in flight need).  On an error after work was
+ * queued the call drains the stream before returning.  The reference's entry
  * (startCalculate, JSLAB_PhaseEpipolarReconstructor_V2.cpp:397-480) is
  * synchronous; this is its pipelined form. */
 ZIM_API zim_status zim_reconstruct_pair_host_async(zim_ctx* ctx, const zim_decode_config* dcfg,

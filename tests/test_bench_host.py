@@ -65,3 +65,15 @@ def test_both_arms_share_one_config():
     a = bench.workload_config(2448, 2048, 12, 2501, 2092, 2 * 12 * 2448 * 2048 * 2)
     b = bench.workload_config(2448, 2048, 12, 2501, 2092, 240648192)
     assert a == b and a["workload"] == bench.WORKLOAD and "> 129 MB L2" in a["l2"]
+
+
+def test_measured_figures_name_committed_profiles():
+    """Every ncu figure the bench line quotes names a summary under profiles/
+    that exists, and the instruction figure is a plausible warp count."""
+    import bench
+    for table in (bench.MEASURED_TRAFFIC, bench.MEASURED_ISSUE):
+        for key, val in table.items():
+            src = val[-1]
+            assert (bench.ROOT / src).is_file(), (key, src)
+    for (_, W, H), (inst, fma, _) in bench.MEASURED_ISSUE.items():
+        assert inst > W * H / 32 and 0.0 < fma < 1.0

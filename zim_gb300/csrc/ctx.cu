@@ -464,16 +464,19 @@ static zim_status host_pair(zim_ctx* ctx, const zim_decode_config* d, const zim_
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_event, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dr, rf, fbytes, cudaMemcpyHostToDevice, ctx->aux_stream);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->aux_event, ctx->aux_stream);
-    // A pinned (page-locked) cloud buffer takes the last stage's writes
-    // directly through its device address: the copy back overlaps that
-    // stage.  Only the last stage writes it; the mask, which later stages
-    // read, stays on the device and is copied.  MLS with three or more passes
-    // ping-pongs through its output, so a pass would read its neighbourhoods
-    // back across the host link: that case writes the device scratch and
-    // copies instead.
+    // Synchronous calls: a pinned (page-locked) cloud buffer takes the last
+    // stage's writes directly through its device address, so the copy back
+    // overlaps that stage.  Only the last stage writes it; the mask, which
+    // later stages read, stays on the device and is copied.  MLS with three
+    // or more passes ping-pongs through its output, so a pass would read its
+    // neighbourhoods back across the host link: that case writes the device
+    // scratch and copies instead.  Asynchronous calls always copy: with other
+    // pairs' kernels waiting for the SMs, a kernel that stalls on writes across
+    // the host link costs more than a copy engine moving the cloud (5 MP,
+    // three pairs in flight: 1327 -> 1427 Mpoints/s end to end).
     const bool last_reads_out = r->use_mls && !r->use_metric_gaussian && r->mls_iterations >= 3;
     float* xyz_dev = nullptr;
-    if (e == cudaSuccess && !last_reads_out) {
+    if (e == cudaSuccess && !last_reads_out && sync) {
         cudaPointerAttributes a{};
         if (cudaPointerGetAttributes(&a, xyz) == cudaSuccess && a.type == cudaMemoryTypeHost &&
             a.devicePointer != nullptr)
