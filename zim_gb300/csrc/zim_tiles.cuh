@@ -209,6 +209,22 @@ __device__ __forceinline__ void decode_stage_sums(const T* __restrict__ frames, 
     __syncthreads();
 }
 
+// The validity test on the normalised modulation nm = (2 |S, C| / N) / (M / N)
+// (0 when M <= 1e-3 N): nm < thr fails the pixel.  For M > 0 that is
+// 4 (S^2 + C^2) < (thr M)^2 with thr > 0, which needs neither the square root
+// nor the division; they are computed only where nm is written out
+// (want_value: frequency 0 with a modulation map).  The two forms decide
+// differently only where nm lies within float rounding of thr.
+__device__ __forceinline__ bool modulation_ok(float S, float C, float M, int N, float thr, bool want_value,
+                                              float& value) {
+    const float q = fmaf(S, S, C * C);
+    const bool has_m = M > 1e-3f * (float)N;
+    if (want_value) value = has_m ? 2.0f * sqrtf(q) / M : 0.f;
+    if (!(thr > 0.f)) return true;
+    const float tm = thr * M;
+    return has_m && !(4.0f * q < tm * tm);
+}
+
 // Decodes tile (bx, by) of DX x DY pixels with the DX * DY threads of a block
 // (tid = ty * DX + tx).  The pre-blur is linear, so the blurred sums
 // S = -sum sin_k I_k, C = sum cos_k I_k, sum I_k are the 3x3 blur of the raw
@@ -250,10 +266,7 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
                 else if (i == 1) wrap1 = wr;
                 else if (i == 2) wrap2 = wr;
                 else wrap3 = wr;
-                // (2 |S, C| / N) / (M / N), one division
-                float nm = M > 1e-3f * (float)N ? 2.0f * sqrtf(fmaf(S, S, C * C)) / M : 0.f;
-                if (i == 0) mod0 = nm;
-                if (nm < p.thr) ok = false;
+                if (!modulation_ok(S, C, M, N, p.thr, i == 0 && mod_out, mod0)) ok = false;
             }
             continue;
         }
@@ -274,10 +287,7 @@ __device__ __forceinline__ void decode_finish(const T* __restrict__ frames, cons
             else if (i == 1) wrap1 = wr;
             else if (i == 2) wrap2 = wr;
             else wrap3 = wr;
-            // normalised modulation (2 |S, C| / N) / (M / N), one division
-            float nm = M > 1e-3f * (float)N ? 2.0f * sqrtf(fmaf(S, S, C * C)) / M : 0.f;
-            if (i == 0) mod0 = nm;
-            if (nm < p.thr) ok = false;
+            if (!modulation_ok(S, C, M, N, p.thr, i == 0 && mod_out, mod0)) ok = false;
         }
     }
     // every thread is past its last shared read before the block's next tile
