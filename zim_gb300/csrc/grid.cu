@@ -928,6 +928,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
     __shared__ unsigned warp_dev[TILE_T / 32];
     unsigned tdev = 0u;  // largest dev of this thread's staged points (float bits, >= 0)
+#pragma unroll
     for (int t = tid; t < WW * WH; t += TILE_T) {
         const int wx = x0 - WR + t % WW, wy = y0 - WR + t / WW;
         // invalid and off-image pixels: NaN coordinates (their squared distance
@@ -1703,6 +1704,7 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
     __shared__ float4 W[GW * GH];
     const int tid = threadIdx.x;
     const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+#pragma unroll
     for (int t = tid; t < GW * GH; t += TILE_T) {
         const int wx = x0 - WRG + t % GW, wy = y0 - WRG + t / GW;
         // invalid and off-image pixels are NaN: their distance test fails
