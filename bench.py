@@ -326,6 +326,14 @@ def run_ours(args):
         alg = {"decode": npx * (F * 2 + 8), "rectify_match": 2 * npx * 8 + rpx * 4,
                "median_reproject": rpx * (4 + 13), "sor": rpx * (13 + 13), "mls": rpx * (13 + 12),
                "metric_gaussian": rpx * (13 + 12)}
+        # decode + rectify + match + median + reprojection against the HBM roofline:
+        # the pair's compulsory bytes (both frame stacks in, cloud + mask out)
+        # over the stages' summed one-stream times
+        pix_ms = per_step["decode"] + per_step["rectify_match"] + per_step["median_reproject"]
+        pix_bytes = 2 * npx * F * 2 + rpx * 13
+        pixel_stages = {"ms_per_pair": round(pix_ms, 4), "compulsory_bytes": pix_bytes,
+                        "achieved_gbs": round(pix_bytes / (pix_ms * 1e-3) / 1e9, 1),
+                        "frac": round(pix_bytes / (pix_ms * 1e-3) / 1e9 / peaks()[0], 4)}
         stages = {n: {"ms_per_step": round(per_step[n], 4), "ms_per_launch": round(per_launch[n], 4),
                       "gbs": round(alg[n] / (per_launch[n] * 1e-3) / 1e9, 1)} for n in per_step}
         achieved = alg[dom] / (per_launch[dom] * 1e-3) / 1e9
@@ -340,6 +348,8 @@ def run_ours(args):
             "data": "synthetic (seeded scene renderer, zim_gb300/synth)",
             "config": workload_config(W, H, F, ctx.rect_w, ctx.rect_h, 2 * L.nbytes),
             "points_per_pair": n_pts, "replicas": world, "pairs_in_flight": nf,
+            "pixel_pairs_per_s": round(world * npx / (ms * 1e-3), 1),
+            "pixel_stages": pixel_stages,
             "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms, 4)},
             "gpu_launches": int(launches),
@@ -708,7 +718,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
