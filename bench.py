@@ -580,9 +580,10 @@ def run_refine(api, local, n_poses=8, iterations=60):
 
 
 BATCH_WORKLOAD = ("64 seeded stereo pairs, sizes drawn from {640x480, 1280x1024, 2448x2048, 4096x3000}, each "
-                  "4-step + 5-bit Gray + complementary (config-0 scene/rig, u8) or three-frequency 1/8/64 x 4 steps "
-                  "(config-1 scene/rig, 12-bit u16); decode+rectify+match+median+reproject+pixel Gaussian+radius "
-                  "outlier filter (reference defaults); 8 distinct calibrations")
+                  "4-step + 5-bit Gray + complementary (config-0 scene/rig, u8; then SOR k=50) or three-frequency "
+                  "1/8/64 x 4 steps (config-1 scene/rig, 12-bit u16; then SOR k=30 + MLS r2mm o2 + Gaussian 0.5mm); "
+                  "decode+rectify+match+median+reproject+filters; 8 distinct calibrations; plain = the whole-pair "
+                  "path pair after pair on one stream")
 
 
 def run_batch(api, local, steps, warmup, n_pairs=64):
@@ -604,7 +605,13 @@ def run_batch(api, local, steps, warmup, n_pairs=64):
             uniq.append(k)
     cidx = [uniq.index(k) for k in keys]
     rigs = [specs[keys.index(k)].rig.as_dict() for k in uniq]
-    rcfg = api.recon_config()
+    # per pair the pipeline of its kind: config 0's SOR (k = 50) after the
+    # 4-step + Gray pairs, config 1's SOR (k = 30) + MLS + metric Gaussian
+    # after the 1/8/64 pairs; no pixel-window filters (neither config has them)
+    rcfg = api.recon_config(use_px_gaussian=0, use_ror=0)
+    gray_cfg = api.recon_config(use_px_gaussian=0, use_ror=0, use_sor=1, sor_mean_k=50, sor_std_mul=1.0)
+    freq_cfg = config1_recon(api)
+    pcfg = [gray_cfg if k[0] == "gray" else freq_cfg for k in keys]
     dcfgs = [api.decode_config(**s.decode_kwargs()) for s in specs]
     st = torch.cuda.current_stream()
     ev = lambda: torch.cuda.Event(enable_timing=True)
@@ -623,7 +630,7 @@ def run_batch(api, local, steps, warmup, n_pairs=64):
 
     def plain_pass():
         for i in range(n_pairs):
-            api.reconstruct_pair(ctxs[cidx[i]], dcfgs[i], rcfg, dev[i][0], dev[i][1], out=outs[i])
+            api.reconstruct_pair(ctxs[cidx[i]], dcfgs[i], pcfg[i], dev[i][0], dev[i][1], out=outs[i])
 
     for _ in range(warmup):
         plain_pass()
@@ -640,7 +647,7 @@ def run_batch(api, local, steps, warmup, n_pairs=64):
     # batched path
     ctx = api.Context(local)
     b = Batch(ctx, rigs)
-    pairs = [BatchPair(dcfgs[i], dev[i][0], dev[i][1], calib=cidx[i]) for i in range(n_pairs)]
+    pairs = [BatchPair(dcfgs[i], dev[i][0], dev[i][1], calib=cidx[i], filters=pcfg[i]) for i in range(n_pairs)]
     b.submit(pairs, rcfg)
     tuning, tune_ms = b.autotune()
     for _ in range(warmup):

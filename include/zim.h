@@ -404,15 +404,18 @@ ZIM_API zim_status zim_reconstruct_pair_host_async(zim_ctx* ctx, const zim_decod
  * JSLAB_PhaseEpipolarReconstructor_V2 / JSLAB_ReconstructPipeline_GPU).  One
  * submission holds any number of pairs, each with its own decode config,
  * sample type and one of the batch's calibrations.  Per pair it computes what
- * zim_reconstruct_pair computes (bit-identical), for the pixel-domain stages:
- * decode, rectify, match, 5x5 median, reprojection, 3x3 Gaussian and radius
- * outlier filter.  The grid filters (SOR, MLS, metric Gaussian) work on whole
- * clouds and run per pair afterwards (zim_filter_*).
- * Execution: one persistent kernel per stage drains a device work queue of
- * (pair, row band) items over all pairs (decode; rectify fused into match;
- * median + reprojection; each pixel filter); the launch sequence is captured
- * once as a CUDA graph and zim_batch_run replays it.  Band heights and
- * persistent CTAs per SM are tunables, chosen by zim_batch_autotune. */
+ * zim_reconstruct_pair computes (bit-identical): decode, rectify, match, 5x5
+ * median, reprojection, 3x3 Gaussian and radius outlier filter, then the grid
+ * filters (SOR -> MLS -> metric Gaussian) that the pair's filter config turns
+ * on (zim_batch_pair.filters, or the submission's config).
+ * Execution: one persistent kernel per pixel-domain stage drains a device work
+ * queue of (pair, row band) items over all pairs (decode; rectify fused into
+ * match; median + reprojection; each pixel filter); then the pairs' grid
+ * filters run on a few lanes (streams, each with its own scratch) side by
+ * side, the pairs taken round-robin, so one pair's latency-bound searches
+ * overlap another's kernels.  The whole sequence is captured once as a CUDA
+ * graph and zim_batch_run replays it.  Band heights and persistent CTAs per SM
+ * are tunables, chosen by zim_batch_autotune. */
 typedef struct zim_batch zim_batch;
 
 typedef struct zim_batch_pair {
@@ -425,6 +428,12 @@ typedef struct zim_batch_pair {
     float* xyz;              /* device outputs, rect_h*rect_w of the calibration */
     uint8_t* mask;
     float* disp;             /* optional: the (median-filtered) disparity */
+    /* optional: the grid filters of this pair (use_sor, use_mls,
+     * use_metric_gaussian and their parameters are read from it); NULL: those
+     * of the submission's config.  The pixel-domain stages, the reprojection
+     * frame (use_rectified_coords) and its rays come from the submission's
+     * config for every pair. */
+    const zim_recon_config* filters;
 } zim_batch_pair;
 
 typedef struct zim_batch_tuning {

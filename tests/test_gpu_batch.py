@@ -81,6 +81,47 @@ def test_batch_matches_plain_path(setup, filters):
         assert mask.sum() > 1000
 
 
+def test_batch_grid_filters_match_plain_path(setup):
+    """Per-pair grid filters (SOR; SOR + MLS + metric Gaussian; MLS of order
+    1 + metric Gaussian; and the submission's own SOR for a pair without a
+    filter config) run on the lanes after the batched pixel stages: every
+    output equals the whole-pair path's with the pair's full config."""
+    from zim_gb300 import api
+    from zim_gb300.batch import Batch
+    ctx, scenes, calib_of, calibs = setup
+    base = dict(use_ror=0)  # pixel Gaussian on: the pixel stages end in it
+    sub = api.recon_config(**base, use_sor=1, sor_mean_k=30, sor_std_mul=1.0)
+    per_pair = [api.recon_config(**base, use_sor=1, sor_mean_k=50, sor_std_mul=1.0),
+                api.recon_config(**base, use_sor=1, sor_mean_k=30, sor_std_mul=1.0, use_mls=1, mls_window_size=7,
+                                 mls_spatial_sigma=5.656854, mls_polynomial_order=2, mls_max_radius=8.0,
+                                 mls_iterations=1, use_metric_gaussian=1, metric_gaussian_sigma=2.0),
+                api.recon_config(**base, use_mls=1, mls_window_size=5, mls_spatial_sigma=2.4, mls_polynomial_order=1,
+                                 mls_max_radius=0.0, mls_iterations=3, use_metric_gaussian=1,
+                                 metric_gaussian_sigma=1.5),
+                None]
+    b = Batch(ctx, calibs)
+    pairs = _batch_pairs(scenes, calib_of)
+    for p, f in zip(pairs, per_pair):
+        p.filters = f
+    b.submit(pairs, sub)
+    b.run()
+    torch.cuda.synchronize()
+    cache = {}
+    for (spec, L, R, _), p, f in zip(scenes, pairs, per_pair):
+        xyz, mask, _ = _plain(cache, spec, L, R, f if f is not None else sub)
+        assert np.array_equal(p.mask.cpu().numpy(), mask)
+        assert np.array_equal(p.xyz.cpu().numpy(), xyz)
+        assert mask.sum() > 1000
+    # replays are repeatable
+    ref = [(p.xyz.clone(), p.mask.clone()) for p in pairs]
+    for p in pairs:
+        p.xyz.zero_()
+    b.run()
+    torch.cuda.synchronize()
+    for (x, m), p in zip(ref, pairs):
+        assert torch.equal(p.xyz, x) and torch.equal(p.mask, m)
+
+
 def test_batch_tunings_and_autotune_agree(setup):
     from zim_gb300 import api
     from zim_gb300.batch import Batch
@@ -113,8 +154,8 @@ def test_batch_rejects_bad_submissions(setup):
     b = Batch(ctx, calibs)
     pairs = _batch_pairs(scenes[:1], calib_of[:1])
     with pytest.raises(ZimError) as e:
-        b.submit(pairs, api.recon_config(use_sor=1))
-    assert e.value.status == 2  # UNSUPPORTED: grid filters run per cloud
+        b.submit(pairs, api.recon_config(use_sor=1, sor_mean_k=64))
+    assert e.value.status == 1  # INVALID_ARG: k + 1 above 64
     bad = _batch_pairs(scenes[1:2], [0])  # 612x512 frames against the 640x480 calibration
     if calibs[0]["width"] != 612:
         with pytest.raises(ZimError):

@@ -70,7 +70,7 @@ class PointXYZ(C.Structure):
 class BatchPair(C.Structure):
     _fields_ = [("decode", DecodeConfig), ("sample_type", C.c_int), ("rows", C.c_int), ("cols", C.c_int),
                 ("calib", C.c_int), ("pha_f", C.c_int), ("frames", C.c_void_p * 2), ("xyz", C.c_void_p),
-                ("mask", C.c_void_p), ("disp", C.c_void_p)]
+                ("mask", C.c_void_p), ("disp", C.c_void_p), ("filters", C.c_void_p)]
 
 
 class BatchTuning(C.Structure):

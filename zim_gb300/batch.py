@@ -7,7 +7,9 @@
 
 Each pair gets ``xyz`` (rect_h, rect_w, 3) and ``mask`` outputs (allocated by
 ``submit`` unless given), equal bit for bit to what ``reconstruct_pair``
-returns for it with the same config.
+returns for it with the same config.  A pair's ``filters`` (a recon_config)
+chooses its grid filters (SOR, MLS, metric Gaussian); without it the
+submission's config does.
 """
 from __future__ import annotations
 
@@ -31,6 +33,7 @@ class BatchPair:
     xyz: Optional[torch.Tensor] = None
     mask: Optional[torch.Tensor] = None
     disp: Optional[torch.Tensor] = None
+    filters: Optional[object] = None  # a recon_config whose grid filters apply to this pair
 
 
 class Batch:
@@ -80,6 +83,7 @@ class Batch:
             s.xyz = _p(p.xyz).value
             s.mask = _p(p.mask).value
             s.disp = _p(p.disp).value if p.disp is not None else None
+            s.filters = C.cast(C.pointer(p.filters), C.c_void_p).value if p.filters is not None else None
         t = None
         if tuning is not None:
             t = _lib.BatchTuning(**tuning)

@@ -14,10 +14,15 @@
 //            is rectified in registers, so no rectified phase reaches HBM
 //   stage 3  median + reprojection, stage 4 pixel Gaussian, stage 5 radius
 //            outlier filter: item = (pair, band of 8-row tile rows)
+//   stage 6  the grid filters (SOR -> MLS -> metric Gaussian) of the pairs
+//            that turn them on: whole-cloud searches, run per pair on a few
+//            lanes (a stream and a scratch context each, pairs round-robin),
+//            so one pair's latency-bound passes overlap another's kernels
 // A persistent CTA takes items from its stage's queue (one atomic per item)
 // until the queue is empty, so small and large pairs share the GPU and no
 // per-pair launch or tail is paid.  Items are ordered largest pair first.
-// Stage order is kept by kernel boundaries (no inter-CTA waits).
+// Stage order is kept by kernel boundaries (no inter-CTA waits) and, for the
+// lanes, by graph edges from the last pixel stage and back to the stream.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -280,6 +285,24 @@ struct zim_batch {
     std::vector<PairDev> host_pairs;
     std::vector<char> tma;  // per pair: decoded by the bulk-copy kernel, not the queue
     size_t items_off = 0;
+    // grid filters: per pair the resolved config and its buffers (x_in / m_in:
+    // the pixel stages' output; x1, x2: intermediate clouds; mls_tmp: MLS
+    // ping-pong for three or more passes)
+    struct GridRoute {
+        bool on = false;
+        const float* x_in = nullptr;
+        const uint8_t* m_in = nullptr;
+        float *x1 = nullptr, *x2 = nullptr, *mls_tmp = nullptr;
+    };
+    std::vector<zim_recon_config> filt;
+    std::vector<GridRoute> groute;
+    static constexpr int MAX_LANES = 3;
+    int n_lanes = 0;
+    zim_ctx* lane_ctx[MAX_LANES] = {};
+    cudaStream_t lane_stream[MAX_LANES] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[MAX_LANES] = {};
+    unsigned long long lane_launches = 0;  // grid-filter kernels per graph replay
 };
 
 namespace {
@@ -334,6 +357,77 @@ void build_items(const zim_batch* b, const zim_batch_tuning& t, std::vector<int4
     }
 }
 
+// One pair's grid filters on a lane: SOR -> MLS -> metric Gaussian as the
+// whole-pair path chains them (the same launch functions, the same inputs),
+// the last writer of xyz / mask writing the pair's outputs.
+zim_status lane_filters(zim_batch* b, int pi, zim_ctx* lctx, cudaStream_t st) {
+    const zim_batch_pair& p = b->pairs[pi];
+    const zim_recon_config& r = b->filt[pi];
+    const zim_batch::GridRoute& g = b->groute[pi];
+    const zim_rect_state& C = b->calibs[p.calib];
+    const int RH = C.rect_h, RW = C.rect_w;
+    const zim_ray_model rays = zim_rays_from(C.Q, C.R1, b->rcfg.use_rectified_coords != 0, 0, 0);
+    const int last = r.use_metric_gaussian ? 2 : (r.use_mls ? 1 : 0);
+    const float* cx = g.x_in;
+    const uint8_t* cm = g.m_in;
+    zim_scratch_reset(lctx);
+    if (r.use_sor) {
+        float* ox = last == 0 ? p.xyz : g.x1;
+        zim_status s = zim_sor_launch(lctx, cx, cm, RH, RW, r.sor_mean_k, r.sor_std_mul, ox, p.mask, nullptr, rays, st);
+        if (s) return s;
+        zim_scratch_reset(lctx);
+        cx = ox;
+        cm = p.mask;
+    }
+    if (r.use_mls) {
+        float* ox = last == 1 ? p.xyz : (cx == g.x1 ? g.x2 : g.x1);
+        zim_status s = zim_mls_launch(lctx, cx, cm, RH, RW, r.mls_window_size, r.mls_spatial_sigma,
+                                      r.mls_polynomial_order, r.mls_max_radius, r.mls_iterations, ox, g.mls_tmp, rays,
+                                      st);
+        if (s) return s;
+        cx = ox;
+    }
+    if (r.use_metric_gaussian) {
+        zim_status s = zim_metric_gaussian_launch(lctx, cx, cm, RH, RW, r.metric_gaussian_sigma, p.xyz, rays, st);
+        if (s) return s;
+        zim_scratch_reset(lctx);
+    }
+    return ZIM_OK;
+}
+
+// Lanes for the grid filters: n contexts on the batch's device (scratch
+// reserved for the largest filtered cloud), a stream and a join event each.
+zim_status setup_lanes(zim_batch* b, int n, size_t scratch) {
+    zim_ctx* ctx = b->ctx;
+    for (int l = 0; l < n; l++) {
+        if (!b->lane_ctx[l]) {
+            zim_status s = zim_create(ctx->device, &b->lane_ctx[l]);
+            if (s) return zim_fail(ctx, s, "lane context creation failed");
+            ZIM_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&b->lane_stream[l], cudaStreamNonBlocking));
+            ZIM_CUDA_TRY(ctx, cudaEventCreateWithFlags(&b->join_ev[l], cudaEventDisableTiming));
+        }
+        zim_status s = zim_scratch_reserve(b->lane_ctx[l], scratch);
+        if (s) return zim_fail(ctx, s, "lane scratch: %s", zim_last_error(b->lane_ctx[l]));
+    }
+    if (!b->fork_ev) ZIM_CUDA_TRY(ctx, cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    b->n_lanes = n;
+    return ZIM_OK;
+}
+
+void free_lanes(zim_batch* b) {
+    for (int l = 0; l < zim_batch::MAX_LANES; l++) {
+        if (b->lane_ctx[l]) zim_destroy(b->lane_ctx[l]);
+        if (b->lane_stream[l]) cudaStreamDestroy(b->lane_stream[l]);
+        if (b->join_ev[l]) cudaEventDestroy(b->join_ev[l]);
+        b->lane_ctx[l] = nullptr;
+        b->lane_stream[l] = nullptr;
+        b->join_ev[l] = nullptr;
+    }
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    b->fork_ev = nullptr;
+    b->n_lanes = 0;
+}
+
 zim_status capture(zim_batch* b) {
     zim_ctx* ctx = b->ctx;
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -384,10 +478,40 @@ zim_status capture(zim_batch* b) {
         batch_ror_kernel<<<std::min(b->grid[Q_ROR], q.n[Q_ROR]), BT, b->ror_smem, s>>>(
             b->d_pairs, q.items[Q_ROR], q.n[Q_ROR], b->d_counters + Q_ROR);
     cudaError_t le = cudaGetLastError();
+    // the grid filters: the lanes fork from the capture after the pixel stages
+    // (pairs round-robin) and join back before its end
+    zim_status fs = ZIM_OK;
+    b->lane_launches = 0;
+    if (le == cudaSuccess && b->n_lanes > 0) {
+        unsigned long long l0 = 0;
+        for (int l = 0; l < b->n_lanes; l++) l0 += b->lane_ctx[l]->launches;
+        le = cudaEventRecord(b->fork_ev, s);
+        for (int l = 0; le == cudaSuccess && l < b->n_lanes; l++) le = cudaStreamWaitEvent(b->lane_stream[l], b->fork_ev, 0);
+        int lane = 0;
+        for (size_t pi = 0; le == cudaSuccess && fs == ZIM_OK && pi < b->groute.size(); pi++)
+            if (b->groute[pi].on) {
+                fs = lane_filters(b, (int)pi, b->lane_ctx[lane], b->lane_stream[lane]);
+                lane = (lane + 1) % b->n_lanes;
+            }
+        for (int l = 0; le == cudaSuccess && l < b->n_lanes; l++) {
+            le = cudaEventRecord(b->join_ev[l], b->lane_stream[l]);
+            if (le == cudaSuccess) le = cudaStreamWaitEvent(s, b->join_ev[l], 0);
+        }
+        unsigned long long l1 = 0;
+        for (int l = 0; l < b->n_lanes; l++) l1 += b->lane_ctx[l]->launches;
+        b->lane_launches = l1 - l0;
+    }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s, &g);
-    if (le != cudaSuccess || e != cudaSuccess) {
+    if (le != cudaSuccess || e != cudaSuccess || fs != ZIM_OK) {
         if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (fs != ZIM_OK) {
+            const zim_ctx* lc = nullptr;
+            for (int l = 0; l < b->n_lanes; l++)
+                if (b->lane_ctx[l] && !b->lane_ctx[l]->last_error.empty()) lc = b->lane_ctx[l];
+            return zim_fail(ctx, fs, "batch grid filters: %s", lc ? lc->last_error.c_str() : "failed");
+        }
         return zim_fail(ctx, ZIM_ERR_CUDA, "batch graph capture failed: %s",
                         cudaGetErrorString(le != cudaSuccess ? le : e));
     }
@@ -476,6 +600,7 @@ extern "C" ZIM_API void zim_batch_destroy(zim_batch* b) {
     cudaSetDevice(b->device);
     cudaDeviceSynchronize();
     release_submission(b);
+    free_lanes(b);
     for (zim_rect_state& st : b->calibs) zim_rect_free(st);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
@@ -496,9 +621,6 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     if (!pairs || n_pairs < 1 || !rcfg) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad argument");
     if (rcfg->reproject_model != 0)
         return zim_fail(ctx, ZIM_ERR_UNSUPPORTED, "the batch reprojects through each calibration's Q matrix");
-    if (rcfg->use_sor || rcfg->use_mls || rcfg->use_metric_gaussian)
-        return zim_fail(ctx, ZIM_ERR_UNSUPPORTED,
-                        "the batch runs the pixel-domain stages; run SOR / MLS / metric Gaussian per cloud after it");
     if (rcfg->use_ror && (rcfg->radius_window_size < 0 || rcfg->radius_window_size > ZIM_MAX_ROR_WINDOW))
         return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "radius_window_size must be in [0, %d]", ZIM_MAX_ROR_WINDOW);
     if (tuning && !tuning_ok(*tuning)) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "bad tuning");
@@ -518,6 +640,13 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         if (!p.frames[0] || !p.frames[1] || !p.xyz || !p.mask)
             return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: null frames or outputs", i);
         if (C.rect_w > ZIM_MAX_MATCH_COLS) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: rectified width", i);
+        const zim_recon_config& f = p.filters ? *p.filters : *rcfg;
+        if (f.use_sor && (f.sor_mean_k < 1 || f.sor_mean_k > 63))
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: sor_mean_k must be in [1, 63]", i);
+        if (f.use_mls && (f.mls_window_size < 0 || f.mls_window_size > 64 || !(f.mls_spatial_sigma > 0)))
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: bad MLS parameter", i);
+        if (f.use_metric_gaussian && !(f.metric_gaussian_sigma > 0))
+            return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: metric_gaussian_sigma must be positive", i);
         const int pf = p.pha_f > 0 ? p.pha_f : zim_decode_max_order(&p.decode);
         if (pf < 0 || pf > ZIM_MAX_ORDER) return zim_fail(ctx, ZIM_ERR_INVALID_ARG, "pair %d: pha_f out of range", i);
         max_cols = std::max(max_cols, C.rect_w);
@@ -528,6 +657,22 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
     release_submission(b);
     b->pairs.assign(pairs, pairs + n_pairs);
     b->rcfg = *rcfg;
+    // the grid filters of each pair (copied: the caller's configs need not outlive the call)
+    b->filt.assign(n_pairs, *rcfg);
+    b->groute.assign(n_pairs, zim_batch::GridRoute{});
+    size_t lane_scratch = 0;
+    int n_filtered = 0;
+    for (int i = 0; i < n_pairs; i++) {
+        if (b->pairs[i].filters) b->filt[i] = *b->pairs[i].filters;
+        b->pairs[i].filters = nullptr;
+        const zim_recon_config& f = b->filt[i];
+        b->groute[i].on = f.use_sor || f.use_mls || f.use_metric_gaussian;
+        if (b->groute[i].on) {
+            const zim_rect_state& C = b->calibs[b->pairs[i].calib];
+            lane_scratch = std::max(lane_scratch, zim_grid_scratch_bytes((size_t)C.rect_w * C.rect_h) + 4096);
+            n_filtered++;
+        }
+    }
     b->use_pxg = rcfg->use_px_gaussian != 0;
     b->use_ror = rcfg->use_ror != 0;
     if (tuning) b->tuning = *tuning;
@@ -550,6 +695,12 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         bytes += 2 * (zim_align256(src * 4) * (p.decode.post_smooth ? 4 : 2)) + zim_align256(dst * 4);
         bytes += 2 * (zim_align256(dst * 12) + zim_align256(dst));  // two intermediate clouds at most
     }
+    for (int i = 0; i < n_pairs; i++)
+        if (b->groute[i].on) {  // the pixel stages' cloud + mask, two filter clouds, MLS ping-pong
+            const zim_rect_state& C = b->calibs[b->pairs[i].calib];
+            const size_t dst = (size_t)C.rect_w * C.rect_h;
+            bytes += 4 * zim_align256(dst * 12) + zim_align256(dst);
+        }
     b->items_off = bytes;
     bytes += max_item_bytes(b) + 4096;
     if (cudaMalloc(&b->d_mem, bytes) != cudaSuccess) {
@@ -594,22 +745,36 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         }
         D.disp_raw = (float*)take(dst * 4);
         D.disp_out = p.disp;
-        // stage routing: the last writer of xyz / mask writes the caller's buffers
+        // stage routing: the last writer of xyz / mask writes the caller's
+        // buffers; with grid filters the pixel stages end in intermediates (the
+        // mask too when SOR rewrites it) and the filters write the outputs
+        zim_batch::GridRoute& G = b->groute[i];
+        float* out_x = p.xyz;
+        uint8_t* out_m = p.mask;
+        if (G.on) {
+            out_x = (float*)take(dst * 12);
+            if (b->filt[i].use_sor) out_m = (uint8_t*)take(dst);
+            G.x1 = (float*)take(dst * 12);
+            G.x2 = (float*)take(dst * 12);
+            G.mls_tmp = (float*)take(dst * 12);
+            G.x_in = out_x;
+            G.m_in = out_m;
+        }
         float* xbuf[2] = {(float*)take(dst * 12), (float*)take(dst * 12)};
         uint8_t* mbuf[2] = {(uint8_t*)take(dst), (uint8_t*)take(dst)};
         const bool last_rep = !b->use_pxg && !b->use_ror;
-        D.x_rep = last_rep ? p.xyz : xbuf[0];
-        D.m_rep = (!pxg_mask && !b->use_ror) ? p.mask : mbuf[0];
+        D.x_rep = last_rep ? out_x : xbuf[0];
+        D.m_rep = (!pxg_mask && !b->use_ror) ? out_m : mbuf[0];
         if (b->use_pxg) {
-            D.x_pxg = b->use_ror ? xbuf[1] : p.xyz;
-            D.m_pxg = pxg_mask ? (b->use_ror ? mbuf[1] : p.mask) : nullptr;
+            D.x_pxg = b->use_ror ? xbuf[1] : out_x;
+            D.m_pxg = pxg_mask ? (b->use_ror ? mbuf[1] : out_m) : nullptr;
             D.pxg_w00 = w00; D.pxg_w01 = w01; D.pxg_w11 = w11;
         }
         if (b->use_ror) {
             D.x_ror_in = b->use_pxg ? D.x_pxg : D.x_rep;
             D.m_ror_in = pxg_mask ? D.m_pxg : D.m_rep;
-            D.x_ror = p.xyz;
-            D.m_ror = p.mask;
+            D.x_ror = out_x;
+            D.m_ror = out_m;
             D.ror_r2 = rcfg->radius_search * rcfg->radius_search;
             D.ror_min_nb = rcfg->radius_min_neighbors;
             D.ror_hw = rcfg->radius_window_size / 2;
@@ -625,6 +790,11 @@ extern "C" ZIM_API zim_status zim_batch_submit(zim_batch* b, const zim_batch_pai
         b->tma[i] = zim_decode_tma_applies(D.frames[0], D.sample_type, D.dp) &&
                     zim_decode_tma_applies(D.frames[1], D.sample_type, D.dp);
     }
+    b->n_lanes = 0;
+    if (n_filtered) {
+        zim_status s = setup_lanes(b, std::min(n_filtered, (int)zim_batch::MAX_LANES), lane_scratch);
+        if (s) return s;
+    }
     return requeue(b);
 }
 
@@ -633,6 +803,7 @@ extern "C" ZIM_API zim_status zim_batch_run(zim_batch* b, void* stream) {
     if (!b->exec) return zim_fail(b->ctx, ZIM_ERR_INVALID_ARG, "nothing submitted");
     ZIM_CUDA_TRY(b->ctx, cudaGraphLaunch(b->exec, zim_stream(stream)));
     for (int q = 0; q < NQ; q++) b->ctx->launches += b->q.n[q] > 0 ? 1 : 0;  // kernels in the graph
+    b->ctx->launches += b->lane_launches;
     return ZIM_OK;
 }
 

@@ -212,15 +212,20 @@ static zim_status pack_ply_launch(zim_ctx* ctx, const float* xyz, const uint8_t*
 }
 
 zim_ray_model zim_rays_of(const zim_ctx* ctx, bool rectified_coords, int ox, int oy) {
+    if (!ctx->calibrated) return zim_ray_model{};
+    return zim_rays_from(ctx->Q, ctx->R1, rectified_coords, ox, oy);
+}
+
+zim_ray_model zim_rays_from(const double* Q, const double* R1, bool rectified_coords, int ox, int oy) {
     zim_ray_model r;
-    if (!ctx->calibrated || !(ctx->Q[11] != 0.0)) return r;
+    if (!(Q[11] != 0.0)) return r;
     // Q reprojects pixel (u, v) along (u + Q03, v + Q13, Q23)
-    r.cx = (float)-ctx->Q[3];
-    r.cy = (float)-ctx->Q[7];
-    r.f = (float)ctx->Q[11];
+    r.cx = (float)-Q[3];
+    r.cy = (float)-Q[7];
+    r.f = (float)Q[11];
     if (!rectified_coords)
         for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) r.R[3 * a + b] = (float)ctx->R1[3 * b + a];  // R1^T
+            for (int b = 0; b < 3; b++) r.R[3 * a + b] = (float)R1[3 * b + a];  // R1^T
     r.ox = ox;
     r.oy = oy;
     r.valid = 1;

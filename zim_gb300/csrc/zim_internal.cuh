@@ -113,6 +113,8 @@ struct zim_ray_model {
 // The rays of the context's rectified left camera (rotated by R1^T for clouds
 // in camera coordinates); invalid when the context is not calibrated.
 zim_ray_model zim_rays_of(const zim_ctx* ctx, bool rectified_coords, int ox, int oy);
+// The same from a rectification's Q and R1 (row-major 4x4, 3x3).
+zim_ray_model zim_rays_from(const double* Q, const double* R1, bool rectified_coords, int ox, int oy);
 
 // Checks that a reconstruction config can run on this context (reprojection
 // model and its maps).
