@@ -411,9 +411,9 @@ ZIM_API zim_status zim_reconstruct_pair_host_async(zim_ctx* ctx, const zim_decod
  * Execution: one persistent kernel per pixel-domain stage drains a device work
  * queue of (pair, row band) items over all pairs (decode; rectify fused into
  * match; median + reprojection; each pixel filter); then the pairs' grid
- * filters run on a few lanes (streams, each with its own scratch) side by
- * side, the pairs taken round-robin, so one pair's latency-bound searches
- * overlap another's kernels.  The whole sequence is captured once as a CUDA
+ * filters run on up to six lanes (streams, each with its own scratch) side by
+ * side, the largest pairs first, each to the least-loaded lane, so one pair's
+ * latency-bound searches overlap another's kernels.  The whole sequence is captured once as a CUDA
  * graph and zim_batch_run replays it.  Band heights and persistent CTAs per SM
  * are tunables, chosen by zim_batch_autotune. */
 typedef struct zim_batch zim_batch;

@@ -16,8 +16,9 @@
 //            outlier filter: item = (pair, band of 8-row tile rows)
 //   stage 6  the grid filters (SOR -> MLS -> metric Gaussian) of the pairs
 //            that turn them on: whole-cloud searches, run per pair on a few
-//            lanes (a stream and a scratch context each, pairs round-robin),
-//            so one pair's latency-bound passes overlap another's kernels
+//            lanes (a stream and a scratch context each; the largest pairs
+//            first, each to the least-loaded lane), so one pair's
+//            latency-bound passes overlap another's kernels
 // A persistent CTA takes items from its stage's queue (one atomic per item)
 // until the queue is empty, so small and large pairs share the GPU and no
 // per-pair launch or tail is paid.  Items are ordered largest pair first.
@@ -296,7 +297,7 @@ struct zim_batch {
     };
     std::vector<zim_recon_config> filt;
     std::vector<GridRoute> groute;
-    static constexpr int MAX_LANES = 3;
+    static constexpr int MAX_LANES = 6;
     int n_lanes = 0;
     zim_ctx* lane_ctx[MAX_LANES] = {};
     cudaStream_t lane_stream[MAX_LANES] = {};
@@ -479,7 +480,7 @@ zim_status capture(zim_batch* b) {
             b->d_pairs, q.items[Q_ROR], q.n[Q_ROR], b->d_counters + Q_ROR);
     cudaError_t le = cudaGetLastError();
     // the grid filters: the lanes fork from the capture after the pixel stages
-    // (pairs round-robin) and join back before its end
+    // and join back before its end
     zim_status fs = ZIM_OK;
     b->lane_launches = 0;
     if (le == cudaSuccess && b->n_lanes > 0) {
@@ -487,12 +488,26 @@ zim_status capture(zim_batch* b) {
         for (int l = 0; l < b->n_lanes; l++) l0 += b->lane_ctx[l]->launches;
         le = cudaEventRecord(b->fork_ev, s);
         for (int l = 0; le == cudaSuccess && l < b->n_lanes; l++) le = cudaStreamWaitEvent(b->lane_stream[l], b->fork_ev, 0);
-        int lane = 0;
-        for (size_t pi = 0; le == cudaSuccess && fs == ZIM_OK && pi < b->groute.size(); pi++)
+        // largest cost first, each pair to the lane with the least work so far
+        // (cost ~ rectified pixels, weighted by the filters the pair runs)
+        std::vector<std::pair<double, int>> order;
+        for (size_t pi = 0; pi < b->groute.size(); pi++)
             if (b->groute[pi].on) {
-                fs = lane_filters(b, (int)pi, b->lane_ctx[lane], b->lane_stream[lane]);
-                lane = (lane + 1) % b->n_lanes;
+                const zim_recon_config& f = b->filt[pi];
+                const zim_rect_state& C = b->calibs[b->pairs[pi].calib];
+                const double w = (f.use_sor ? 1.0 : 0.0) + (f.use_mls ? 1.3 * std::max(1, f.mls_iterations) : 0.0) +
+                                 (f.use_metric_gaussian ? 0.4 : 0.0);
+                order.push_back({-w * C.rect_w * (double)C.rect_h, (int)pi});
             }
+        std::sort(order.begin(), order.end());
+        double load[zim_batch::MAX_LANES] = {};
+        for (size_t k = 0; le == cudaSuccess && fs == ZIM_OK && k < order.size(); k++) {
+            int lane = 0;
+            for (int l = 1; l < b->n_lanes; l++)
+                if (load[l] < load[lane]) lane = l;
+            load[lane] -= order[k].first;
+            fs = lane_filters(b, order[k].second, b->lane_ctx[lane], b->lane_stream[lane]);
+        }
         for (int l = 0; le == cudaSuccess && l < b->n_lanes; l++) {
             le = cudaEventRecord(b->join_ev[l], b->lane_stream[l]);
             if (le == cudaSuccess) le = cudaStreamWaitEvent(s, b->join_ev[l], 0);
