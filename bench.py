@@ -729,7 +729,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--inflight", type=int, default=3,
+    ap.add_argument("--inflight", type=int, default=4,
                     help="pairs in flight: one context and one stream each, round-robin (1: one stream)")
     ap.add_argument("--no-diff", action="store_true", help="skip the forward/adjoint leg (8 planar poses)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg (64 mixed pairs)")
