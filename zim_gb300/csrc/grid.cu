@@ -9,7 +9,7 @@
 // nearest neighbours, threshold mean + std_mul * stddev, keep d <= threshold.
 //
 // Build (no host synchronisation): a trimmed mean of adjacent-pixel spacing
-// sets the finest cell c on the device; the finest level (cell c) is
+// (the plain mean on the pixel-ray path) sets the finest cell c on the device; the finest level (cell c) is
 // counting-sorted into a power-of-two hash table of (offset, count) pairs, the
 // coarse level (cell >= 16c) into a dense grid over the bounding box.
 //
@@ -239,7 +239,7 @@ __global__ void spacing_total_kernel(const double* __restrict__ part, int nblk, 
     }
 }
 
-// Finest cell = fixed_cell if > 0, else factor * trimmed mean spacing (a
+// Finest cell = fixed_cell if > 0, else factor * (trimmed) mean spacing (a
 // hashed level).  The coarse level is a dense grid over the bounding box with
 // cells of COARSE_MULT finest cells, enlarged until it has at most DENSE_MAX
 // cells.  The cell sizes only affect speed, never the result.
@@ -247,7 +247,8 @@ __global__ void cell_kernel(GridStats* s, float fixed_cell, float factor, int le
     if (gated_off(gate)) return;
     float cell = fixed_cell;
     if (!(cell > 0.f)) {
-        double sp = s->sp2_cnt > 0 ? s->sp2_sum / s->sp2_cnt : 1.0;
+        // the trimmed mean spacing (pass 2) where it ran, else pass 1's mean
+        double sp = s->sp2_cnt > 0 ? s->sp2_sum / s->sp2_cnt : (s->sp_cnt > 0 ? s->sp_sum / s->sp_cnt : 1.0);
         cell = (float)(factor * sp);
     }
     float ext = 0.f, e[3] = {0.f, 0.f, 0.f}, amax = 0.f;
@@ -1948,7 +1949,11 @@ zim_status grid_stats(zim_ctx* ctx, const float* xyz, const uint8_t* mask, int r
     spacing1_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, rays ? 1 : 0, rays ? *rays : RayParams{}, G.stats,
                                          G.part, gate);
     spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 1, G.stats, gate);
-    if (!(fixed_cell > 0.f)) {  // the trimmed spacing sets the cell
+    // the trimmed spacing sets the cell; with pixel rays the window passes
+    // settle nearly every query and the grid serves only the few deferred
+    // ones, so the plain mean of pass 1 sets it (the cell size only affects
+    // speed, never a result)
+    if (!(fixed_cell > 0.f) && !rays) {
         spacing2_kernel<<<sblk, GB, 0, st>>>(xyz, mask, rows, cols, G.stats, G.part, gate);
         spacing_total_kernel<<<1, SPACING_BLOCKS, 0, st>>>(G.part, (int)sblk, 2, G.stats, gate);
         ctx->launches += 2;
