@@ -17,8 +17,6 @@
 //   window pass: one thread per pixel walks its 15x15 window in a spiral with
 //            a max-heap of the k + 1 nearest, certified exact by a bound on
 //            the distance to every point seen along another pixel's ray;
-//   second window pass: one warp per uncertified point walks pixel rings out
-//            to 24 px with the same certificate;
 //   far search: one warp per remaining point searches rings of coarse cells
 //            around its own until the next ring lies beyond the (k + 1)-th
 //            distance held;
@@ -821,8 +819,7 @@ __global__ void __launch_bounds__(TILE_T) sor_knn_tile_kernel(const float* __res
 // averaged across a depth edge lie far off their rays, but only near it), so
 // the spiral stops at the radius that local bound gives and the cloud-wide
 // maximum only has to clear the window's edge.  Queries the bounds do not
-// certify go to the deferred list (md = -1) for the second window pass and
-// the grid searches.
+// certify go to the deferred list (md = -1) for the grid searches.
 
 using zt::RayParams;
 using zt::ray_dir;
@@ -900,7 +897,7 @@ struct WinHeap {
 };
 
 // A query the window pass cannot settle goes straight to the deferred list
-// (md = -1) for the second window pass and the grid searches.
+// (md = -1) for the grid searches.
 __device__ __forceinline__ void defer_query(GridStats* s, unsigned* deferred, float* md_out, size_t i) {
     md_out[i] = -1.f;
     deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
@@ -1053,15 +1050,7 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     md_out[i] = fixed_mean(sum, e, k);
 }
 
-// Second window pass for the deferred queries: one warp per query walks square
-// pixel rings r = 1, 2, ... (lanes over a ring's 8 r pixels) straight from the
-// cloud, keeping the squared distances within the current bound in the warp's
-// list, until the ray bound puts every farther pixel beyond the bound
-// (certified: md written, the query leaves the far search) or FAR_WR rings
-// pass (left to the far search).  The bound starts at the query's window
-// bound tau0 and tightens to the (k + 1)-th smallest whenever the list fills.
-constexpr int FAR_WR = 24;
-constexpr int FW_CAP = 256;  // list entries per warp (8 per lane)
+constexpr int FW_CAP = 256;  // far search: list entries per warp (8 per lane)
 
 // Smallest list value v with at least K entries <= v (entries: lane j holds
 // keys[r] for r < 8, 0xffffffff = empty; keys are non-negative float bits).
@@ -1077,135 +1066,6 @@ __device__ __forceinline__ unsigned warp_kth_key(const unsigned (&keys)[FW_CAP /
         else lo = mid + 1;
     }
     return lo;
-}
-
-__global__ void __launch_bounds__(P2_WARPS * 32) sor_far_window_kernel(const float* __restrict__ xyz,
-                                                                       const uint8_t* __restrict__ mask, int rows,
-                                                                       int cols, int k, RayParams rp,
-                                                                       GridStats* s, unsigned* __restrict__ deferred,
-                                                                       float* __restrict__ md_out,
-                                                                       float* __restrict__ bound) {
-    __shared__ float lst[P2_WARPS][FW_CAP];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned nd = s->n_deferred;
-    const int K1 = k + 1;
-    const float devmax = __uint_as_float(s->ray_dev_bits);
-    for (unsigned item = blockIdx.x * P2_WARPS + w; item < nd; item += gridDim.x * P2_WARPS) {
-        const unsigned i = deferred[item];
-        const int x = (int)(i % (unsigned)cols), y = (int)(i / (unsigned)cols);
-        const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
-        float ax, ay, az;
-        ray_dir(rp, x, y, ax, ay, az);
-        const float an = sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az)));
-        const float qn = sqrtf(fmaf(qx, qx, fmaf(qy, qy, qz * qz)));
-        const float C = qn * rp.f / an;
-        const float dev = ray_dev(qx, qy, qz, ax, ay, az) + devmax + 1e-5f * qn;
-        float thr = INFINITY;
-        if (lane == 0) lst[w][0] = 0.f;  // the query itself
-        int n = 1;                        // list entries (warp-uniform)
-        // keep only the entries <= the K1-th smallest (ties kept); the K1-th
-        // smallest of real points bounds the (k + 1)-th nearest distance
-        auto tighten = [&]() {
-            __syncwarp();
-            unsigned keys[FW_CAP / 32];
-#pragma unroll
-            for (int q = 0; q < FW_CAP / 32; q++) {
-                const int e = lane + 32 * q;
-                keys[q] = e < n ? __float_as_uint(lst[w][e]) : 0xffffffffu;
-            }
-            const unsigned kk = warp_kth_key(keys, K1);
-            thr = __uint_as_float(kk);
-            __syncwarp();
-            int m = 0;
-#pragma unroll
-            for (int q = 0; q < FW_CAP / 32; q++) {
-                const bool kp = keys[q] <= kk;
-                const unsigned bb = __ballot_sync(0xffffffffu, kp);
-                if (kp) lst[w][m + __popc(bb & ((1u << lane) - 1u))] = __uint_as_float(keys[q]);
-                m += __popc(bb);
-            }
-            n = m;
-            __syncwarp();
-        };
-        bool certified = false, overflow = false;
-        for (int r = 1; r <= FAR_WR && !certified && !overflow; r++) {
-            // every pixel of ring r and beyond is at least r pixels away
-            if (thr < INFINITY && C * (float)r / (an + (float)r) > sqrtf(thr) + dev) {
-                certified = true;
-                break;
-            }
-            for (int t0 = 0; t0 < 8 * r; t0 += 32) {
-                if (n > FW_CAP - 32) {
-                    tighten();
-                    if (n > FW_CAP - 32) {  // too many ties to hold
-                        overflow = true;
-                        break;
-                    }
-                }
-                const int t = t0 + lane;
-                float d2 = INFINITY;
-                if (t < 8 * r) {
-                    int dx, dy;
-                    const int side = t / (2 * r), o = t % (2 * r);
-                    if (side == 0) { dx = -r + o; dy = -r; }
-                    else if (side == 1) { dx = r; dy = -r + o; }
-                    else if (side == 2) { dx = r - o; dy = r; }
-                    else { dx = -r; dy = r - o; }
-                    const int px = x + dx, py = y + dy;
-                    if (px >= 0 && px < cols && py >= 0 && py < rows) {
-                        const size_t j = (size_t)py * cols + px;
-                        if (mask[j]) d2 = sqdist(xyz[3 * j] - qx, xyz[3 * j + 1] - qy, xyz[3 * j + 2] - qz);
-                    }
-                }
-                const bool keep = d2 < INFINITY && d2 <= thr;
-                const unsigned b = __ballot_sync(0xffffffffu, keep);
-                if (keep) lst[w][n + __popc(b & ((1u << lane) - 1u))] = d2;
-                n += __popc(b);
-                if (thr == INFINITY && n >= 2 * K1) tighten();
-            }
-        }
-        if (!certified && !overflow && thr < INFINITY) {
-            const float r = (float)(FAR_WR + 1);  // everything the rings did not reach
-            certified = C * r / (an + r) > sqrtf(thr) + dev;
-        }
-        if (!certified) {
-            // left to the far search, with the bound found so far
-            if (lane == 0 && thr < INFINITY) {
-                md_out[i] = MD_BOUND;
-                bound[i] = thr;
-            }
-            __syncwarp();
-            continue;
-        }
-        // the K1 smallest of the list: values below the K1-th plus its ties
-        __syncwarp();
-        unsigned keys[FW_CAP / 32];
-#pragma unroll
-        for (int q = 0; q < FW_CAP / 32; q++) {
-            const int e = lane + 32 * q;
-            keys[q] = e < n ? __float_as_uint(lst[w][e]) : 0xffffffffu;
-        }
-        const unsigned kk = warp_kth_key(keys, K1);
-        const float kth = __uint_as_float(kk);
-        const int e = root_exponent(kth);
-        const float sc = root_scale(e);
-        unsigned part = 0;
-        int below = 0;
-#pragma unroll
-        for (int q = 0; q < FW_CAP / 32; q++)
-            if (keys[q] < kk) {
-                part += root_fixed(__uint_as_float(keys[q]), sc);
-                below++;
-            }
-        part = __reduce_add_sync(0xffffffffu, part);
-        below = __reduce_add_sync(0xffffffffu, below);
-        part += (unsigned)(K1 - below) * root_fixed(kth, sc);
-        if (lane == 0) {
-            md_out[i] = fixed_mean(part, e, k);
-            deferred[item] = 0xffffffffu;  // settled: the far search skips it
-        }
-        __syncwarp();
-    }
 }
 
 // Occupied cells of the coarse (dense) level: (cell index, offset, count).
@@ -1237,9 +1097,8 @@ __device__ __forceinline__ float cell_box_d2(unsigned idx, const GridStats* __re
 // Phase 2: one warp per deferred point on the coarse (dense) level, ring by
 // ring of cells around the query's cell: ring r holds every cell at Chebyshev
 // distance r, all at least (r - 1) cells away.  The warp keeps the squared
-// distances within the bound (the second window pass's, else the (k + 1)-th
-// smallest held) in its list and stops once the next ring lies beyond the
-// bound.  Queries still open after RING_MAX rings, or whose ties overflow the
+// distances within the bound (the (k + 1)-th smallest held) in its list and
+// stops once the next ring lies beyond the bound.  Queries still open after RING_MAX rings, or whose ties overflow the
 // list, go to the hard list (md = MD_BOUND with a valid bound in the bound
 // array, or -1).  Work is handed out through an atomic counter.
 __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float* __restrict__ xyz, int k,
@@ -1261,7 +1120,6 @@ __global__ void __launch_bounds__(P2_WARPS * 32) sor_knn_far_kernel(const float*
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nd) break;
         const unsigned i = deferred[item];
-        if (i == 0xffffffffu) continue;  // settled by the second window pass
         const float qx = xyz[3 * i], qy = xyz[3 * i + 1], qz = xyz[3 * i + 2];
         // the cell mapping (x - org) * inv_cell and the cube corners org + i * cell
         // round by a few ulps of the largest coordinate
@@ -2041,12 +1899,6 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         // dynamic + static shared memory exceeds the default 48 KB (attribute is per device: set it every call)
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(sor_knn_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
         sor_knn_tile_kernel<<<tgrid, TILE_T, tsm, st>>>(xyz, mask, rows, cols, mean_k, fine, G.stats, md, G.deferred);
-        ctx->launches += 1;
-    }
-    if (window) {
-        const RayParams rp = zt::ray_params(rays);
-        sor_far_window_kernel<<<(unsigned)(8 * (ctx->sm_count > 0 ? ctx->sm_count : 152)), P2_WARPS * 32, 0, st>>>(
-            xyz, mask, rows, cols, mean_k, rp, G.stats, G.deferred, md, G.bound);
         ctx->launches += 1;
     }
     // enough warps in flight to cover the latency of the point scans
