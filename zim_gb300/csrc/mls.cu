@@ -223,30 +223,44 @@ __device__ __forceinline__ void fit_normal_equations(Visit& visit, float kw, flo
         const float uc = fmaf(F.cx, ax, fmaf(F.cy, ay, F.cz * az));
         const float vc = fmaf(F.cx, bx, fmaf(F.cy, by, F.cz * bz));
         const float fc = fmaf(F.cx, nx, fmaf(F.cy, ny, F.cz * nz));
-        float m30 = 0.f, m21 = 0.f, m12 = 0.f, m03 = 0.f, m40 = 0.f, m31 = 0.f, m22 = 0.f, m13 = 0.f, m04 = 0.f;
-        float b3 = 0.f, b4 = 0.f, b5 = 0.f;
-        visit([&](float dx, float dy, float dz) {
-            const float d2 = dx * dx + dy * dy + dz * dz;
+        // u and v as the two lanes of paired FP32 instructions (each lane
+        // rounded as the scalar instruction, so every sum below is the scalar
+        // sequence's): (u, v) = d . (t1, t2) is - (uc, vc) as one chain
+        const float2 axy = make_float2(ax, bx), ayy = make_float2(ay, by), azz = make_float2(az, bz);
+        const float2 c_uv = make_float2(-uc, -vc);
+        float2 m30_21 = make_float2(0.f, 0.f), m12_03 = m30_21, m40_31 = m30_21, m22_04 = m30_21, b3_4 = m30_21;
+        float m13 = 0.f, b5 = 0.f;
+        visit([&](float2 dxy, float dz) {
+            const float d2 = fmaf(dz, dz, fmaf(dxy.y, dxy.y, dxy.x * dxy.x));
             if (!(d2 <= r2c)) return;
             const float w = mls_weight(d2, kw);
-            const float u = fmaf(dx, ax, fmaf(dy, ay, fmaf(dz, az, -uc)));
-            const float v = fmaf(dx, bx, fmaf(dy, by, fmaf(dz, bz, -vc)));
-            const float f = fmaf(dx, nx, fmaf(dy, ny, fmaf(dz, nz, -fc)));
-            const float wu = w * u, wv = w * v, wf = w * f;
-            const float uu = u * u, uv = u * v, vv = v * v;
-            m30 = fmaf(wu, uu, m30); m21 = fmaf(wu, uv, m21); m12 = fmaf(wu, vv, m12); m03 = fmaf(wv, vv, m03);
-            const float wuu = wu * u, wvv = wv * v;
-            m40 = fmaf(wuu, uu, m40); m31 = fmaf(wuu, uv, m31); m22 = fmaf(wuu, vv, m22);
-            m13 = fmaf(wvv, uv, m13); m04 = fmaf(wvv, vv, m04);
-            b3 = fmaf(wf, uu, b3); b4 = fmaf(wf, uv, b4); b5 = fmaf(wf, vv, b5);
+            const float2 uv = __ffma2_rn(make_float2(dxy.x, dxy.x), axy,
+                                         __ffma2_rn(make_float2(dxy.y, dxy.y), ayy,
+                                                    __ffma2_rn(make_float2(dz, dz), azz, c_uv)));
+            const float f = fmaf(dxy.x, nx, fmaf(dxy.y, ny, fmaf(dz, nz, -fc)));
+            const float2 wuv = __fmul2_rn(make_float2(w, w), uv);                // (w u, w v)
+            const float wf = w * f;
+            const float2 uu_uv = __fmul2_rn(make_float2(uv.x, uv.x), uv);        // (u u, u v)
+            const float vv = uv.y * uv.y;
+            const float2 vv2 = make_float2(vv, vv);
+            m30_21 = __ffma2_rn(make_float2(wuv.x, wuv.x), uu_uv, m30_21);        // w u (uu, uv)
+            m12_03 = __ffma2_rn(wuv, vv2, m12_03);                                // (w u, w v) vv
+            const float2 wuu_vv = __fmul2_rn(wuv, uv);                            // (w u u, w v v)
+            m40_31 = __ffma2_rn(make_float2(wuu_vv.x, wuu_vv.x), uu_uv, m40_31);  // w u u (uu, uv)
+            m22_04 = __ffma2_rn(wuu_vv, vv2, m22_04);                             // (w u u, w v v) vv
+            m13 = fmaf(wuu_vv.y, uu_uv.y, m13);                                   // w v v uv
+            b3_4 = __ffma2_rn(make_float2(wf, wf), uu_uv, b3_4);                  // w f (uu, uv)
+            b5 = fmaf(wf, vv, b5);
         });
+        const float m30 = m30_21.x, m21 = m30_21.y, m12 = m12_03.x, m03 = m12_03.y;
+        const float m40 = m40_31.x, m31 = m40_31.y, m22 = m22_04.x, m04 = m22_04.y;
         // basis exponents: 1 (0,0), u (1,0), v (0,1), u^2 (2,0), uv (1,1), v^2 (0,2)
         A[0][3] = m20; A[0][4] = m11; A[0][5] = m02;
         A[1][3] = m30; A[1][4] = m21; A[1][5] = m12;
         A[2][3] = m21; A[2][4] = m12; A[2][5] = m03;
         A[3][3] = m40; A[3][4] = m31; A[3][5] = m22;
         A[4][4] = m22; A[4][5] = m13; A[5][5] = m04;
-        bv[3] = b3; bv[4] = b4; bv[5] = b5;
+        bv[3] = b3_4.x; bv[4] = b3_4.y; bv[5] = b5;
     }
 #pragma unroll
     for (int a = 0; a < N; a++)
@@ -316,7 +330,7 @@ __device__ __forceinline__ void mls_solve_project(const MlsFrame& F, int cur, co
     }
 }
 
-// MLS of one valid point.  visit(fn) calls fn(dx, dy, dz) with the offset from
+// MLS of one valid point.  visit(fn) calls fn((dx, dy), dz) with the offset from
 // the query point of every valid neighbour of its window (in a fixed order);
 // the distance test against the cut-off is made here.
 template <typename Visit>
@@ -328,23 +342,28 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
     // the query point (offsets of at most the cut-off radius, so the FP32
     // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
     // ~1e-7 rad, far below the 1e-5 mm the points are held to)
-    float cx = 0.f, cy = 0.f, cz = 0.f, ws = 0.f;
-    float m00 = 0.f, m01 = 0.f, m02 = 0.f, m11 = 0.f, m12 = 0.f, m22 = 0.f;
+    // (x, y) pairs as the two lanes of paired FP32 instructions
+    float2 cxy = make_float2(0.f, 0.f), m00_01 = cxy, m02_12 = cxy;
+    float cz = 0.f, ws = 0.f, m11 = 0.f, m22 = 0.f;
     int nv = 0;
-    visit([&](float dx, float dy, float dz) {
-        float d2 = dx * dx + dy * dy + dz * dz;
+    visit([&](float2 dxy, float dz) {
+        const float d2 = fmaf(dz, dz, fmaf(dxy.y, dxy.y, dxy.x * dxy.x));
         if (!(d2 <= r2c)) return;
-        float w = mls_weight(d2, kw);
-        cx = fmaf(w, dx, cx); cy = fmaf(w, dy, cy); cz = fmaf(w, dz, cz);
-        const float wx = w * dx, wy = w * dy;
-        m00 = fmaf(wx, dx, m00); m01 = fmaf(wx, dy, m01); m02 = fmaf(wx, dz, m02);
-        m11 = fmaf(wy, dy, m11); m12 = fmaf(wy, dz, m12); m22 = fmaf(w * dz, dz, m22);
+        const float w = mls_weight(d2, kw);
+        const float2 wxy = __fmul2_rn(make_float2(w, w), dxy);            // (w dx, w dy)
+        const float wz = w * dz;
+        cxy = __fadd2_rn(cxy, wxy);
+        cz += wz;
+        m00_01 = __ffma2_rn(make_float2(wxy.x, wxy.x), dxy, m00_01);    // w dx (dx, dy)
+        m02_12 = __ffma2_rn(wxy, make_float2(dz, dz), m02_12);          // (w dx, w dy) dz
+        m11 = fmaf(wxy.y, dxy.y, m11);
+        m22 = fmaf(wz, dz, m22);
         ws += w;
         nv++;
     });
     MlsFrame F;
     float C[3][3];
-    if (!mls_frame(ws, nv, cx, cy, cz, m00, m01, m02, m11, m12, m22, order, F, C)) return;
+    if (!mls_frame(ws, nv, cxy.x, cxy.y, cz, m00_01.x, m00_01.y, m02_12.x, m11, m02_12.y, m22, order, F, C)) return;
     // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
     // radius): the fitted surface is the same, the normal equations are O(1).
     const float is = rsqrtf(r2c);
@@ -377,7 +396,7 @@ __global__ void __launch_bounds__(MX* MY) mls_kernel(const float* __restrict__ s
                 for (int j = c0; j < c1; j++) {
                     const size_t q = (size_t)i * cols + j;
                     if (!__ldg(mask + q)) continue;
-                    fn(__ldg(src + 3 * q) - px, __ldg(src + 3 * q + 1) - py, __ldg(src + 3 * q + 2) - pz);
+                    fn(make_float2(__ldg(src + 3 * q) - px, __ldg(src + 3 * q + 1) - py), __ldg(src + 3 * q + 2) - pz);
                 }
         };
         mls_point(inv_2s2, order, r2c, visit, ox, oy, oz, moved);
@@ -461,6 +480,7 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
     if (!inside) return;
     const size_t o = (size_t)y * cols + x;
     const float px = src[3 * o], py = src[3 * o + 1], pz = src[3 * o + 2];
+    const float2 npxy = make_float2(-px, -py);  // q - p as q + (-p): the same rounding
     float ox = 0.f, oy = 0.f, oz = 0.f;
     bool moved = false;
     if (c.w != 0.f) {
@@ -483,7 +503,7 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
                     if (w == 15) continue;
                     for (int j = -w; j <= w; j++) {
                         const float4 q = mls_sp[cc + i * TW + j];
-                        fn(q.x - px, q.y - py, q.z - pz);
+                        fn(__fadd2_rn(make_float2(q.x, q.y), npxy), q.z - pz);
                     }
                 }
             };
@@ -496,7 +516,7 @@ __global__ void __launch_bounds__(MX* MY) mls_smem_kernel(const float* __restric
                     const int w = rem < (float)(hw * hw) ? (int)sqrtf(rem) : hw;
                     for (int j = -w; j <= w; j++) {
                         const float4 q = mls_sp[cc + i * TW + j];
-                        fn(q.x - px, q.y - py, q.z - pz);
+                        fn(__fadd2_rn(make_float2(q.x, q.y), npxy), q.z - pz);
                     }
                 }
             };
