@@ -343,8 +343,8 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
     // moments lose ~1e-7 of |offset|^2 to cancellation: the frame turns by
     // ~1e-7 rad, far below the 1e-5 mm the points are held to)
     // (x, y) pairs as the two lanes of paired FP32 instructions
-    float2 cxy = make_float2(0.f, 0.f), m00_01 = cxy, m02_12 = cxy;
-    float cz = 0.f, ws = 0.f, m11 = 0.f, m22 = 0.f;
+    float2 cxy = make_float2(0.f, 0.f), m00_11 = cxy;
+    float cz = 0.f, ws = 0.f, m01 = 0.f, m02 = 0.f, m12 = 0.f, m22 = 0.f;
     int nv = 0;
     visit([&](float2 dxy, float dz) {
         const float d2 = fmaf(dz, dz, fmaf(dxy.y, dxy.y, dxy.x * dxy.x));
@@ -354,16 +354,17 @@ __device__ __forceinline__ void mls_point(float inv_2s2, int order, float r2c, V
         const float wz = w * dz;
         cxy = __fadd2_rn(cxy, wxy);
         cz += wz;
-        m00_01 = __ffma2_rn(make_float2(wxy.x, wxy.x), dxy, m00_01);    // w dx (dx, dy)
-        m02_12 = __ffma2_rn(wxy, make_float2(dz, dz), m02_12);          // (w dx, w dy) dz
-        m11 = fmaf(wxy.y, dxy.y, m11);
+        m00_11 = __ffma2_rn(wxy, dxy, m00_11);
+        m01 = fmaf(wxy.x, dxy.y, m01);
+        m02 = fmaf(wxy.x, dz, m02);
+        m12 = fmaf(wxy.y, dz, m12);
         m22 = fmaf(wz, dz, m22);
         ws += w;
         nv++;
     });
     MlsFrame F;
     float C[3][3];
-    if (!mls_frame(ws, nv, cxy.x, cxy.y, cz, m00_01.x, m00_01.y, m02_12.x, m11, m02_12.y, m22, order, F, C)) return;
+    if (!mls_frame(ws, nv, cxy.x, cxy.y, cz, m00_11.x, m01, m02, m00_11.y, m12, m22, order, F, C)) return;
     // Polynomial basis in tangent coordinates scaled by 1/h (h = cut-off
     // radius): the fitted surface is the same, the normal equations are O(1).
     const float is = rsqrtf(r2c);
