@@ -103,8 +103,8 @@ struct RectMatchArgs {
     float* disp;
 };
 
-__device__ __forceinline__ void rect_px(const RectMatchArgs& a, int cam, size_t o, int32_t& b, float& r, int32_t& k) {
-    const float mx = __ldg(a.map[cam][0] + o), my = __ldg(a.map[cam][1] + o);
+__device__ __forceinline__ void rect_px(const RectMatchArgs& a, int cam, float mx, float my, int32_t& b, float& r,
+                                        int32_t& k) {
     if (a.post_smooth == 1 || a.post_smooth == 2)
         zt::rectify_pixel_smoothed(a.sk[cam], a.sr[cam], a.order[cam], a.srows, a.scols, mx, my, b, r, k);
     else
@@ -128,23 +128,45 @@ __global__ void __launch_bounds__(MATCH_THREADS) rectify_match_kernel(RectMatchA
         s_hi[k] = -1;
         s_bad[k] = 0;
     }
-    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+    // each column's map entry is loaded one iteration ahead, so that its
+    // latency overlaps the previous column's tap gathers
+    const float* mxr = a.map[1][0] + ro;
+    const float* myr = a.map[1][1] + ro;
+    int j = threadIdx.x;
+    float mx = 0.f, my = 0.f;
+    if (j < cols) { mx = __ldg(mxr + j); my = __ldg(myr + j); }
+    for (; j < cols; j += blockDim.x) {
+        const int jn = j + blockDim.x;
+        float nx = 0.f, ny = 0.f;
+        if (jn < cols) { nx = __ldg(mxr + jn); ny = __ldg(myr + jn); }
         int32_t b, k;
         float r;
-        rect_px(a, 1, ro + j, b, r, k);
+        rect_px(a, 1, mx, my, b, r, k);
         s_ord[j] = k;
         s_base[j] = b;
         s_res[j] = r;
+        mx = nx;
+        my = ny;
     }
+    // the left row's first map entries, in flight across the barriers
+    const float* mxl = a.map[0][0] + ro;
+    const float* myl = a.map[0][1] + ro;
+    j = threadIdx.x;
+    if (j < cols) { mx = __ldg(mxl + j); my = __ldg(myl + j); }
     __syncthreads();
     zt::match_spans(s_ord, cols, pha_f, s_lo, s_hi, threadIdx.x, blockDim.x);
     __syncthreads();
     zt::match_spans_check(s_ord, s_base, s_res, cols, pha_f, s_hi, s_bad, threadIdx.x, blockDim.x);
     __syncthreads();
-    for (int j = threadIdx.x; j < cols; j += blockDim.x) {
+    for (; j < cols; j += blockDim.x) {
+        const int jn = j + blockDim.x;
+        float nx = 0.f, ny = 0.f;
+        if (jn < cols) { nx = __ldg(mxl + jn); ny = __ldg(myl + jn); }
         int32_t bL, kL;
         float rL;
-        rect_px(a, 0, ro + j, bL, rL, kL);
+        rect_px(a, 0, mx, my, bL, rL, kL);
+        mx = nx;
+        my = ny;
         float d;
         int best;
         zt::match_pixel(j, kL, bL, rL, s_ord, s_base, s_res, s_lo, s_hi, s_bad, cols, pha_f, grad_threshold, d,
