@@ -903,6 +903,15 @@ __device__ __forceinline__ void defer_query(GridStats* s, unsigned* deferred, fl
     deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
 }
 
+// The same with an upper bound on its (k + 1)-th smallest squared distance
+// (md = MD_BOUND, the bound in `bound`): the grid searches start from it.
+__device__ __forceinline__ void defer_query_bound(GridStats* s, unsigned* deferred, float* md_out, float* bound,
+                                                  size_t i, float b) {
+    bound[i] = b;
+    md_out[i] = MD_BOUND;
+    deferred[atomicAdd(&s->n_deferred, 1u)] = (unsigned)i;
+}
+
 // The heap's first K1T - 1 distances (heap slots K1T - 2 down to 0) from the
 // first K1T - 1 spiral offsets, invalid pixels as +inf.
 template <int K1T, int... O>
@@ -918,7 +927,8 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
                                                             const uint8_t* __restrict__ mask, int rows, int cols,
                                                             int k, RayParams rp, GridStats* __restrict__ s,
                                                             float* __restrict__ md_out,
-                                                            unsigned* __restrict__ deferred) {
+                                                            unsigned* __restrict__ deferred,
+                                                            float* __restrict__ bound) {
     extern __shared__ float4 win_smem[];
     float4* W = win_smem;                                      // WW x WH window, w = 1 valid
     float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1) x TILE_T heaps
@@ -1036,7 +1046,9 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     const float rk = sqrtf(kth), ro = (float)(WR + 1);
     const bool ok = C * rbreak / (an + rbreak) - dev > rk && C * ro / (an + ro) - dev_out > rk;
     if (!ok) {
-        defer_query(s, deferred, md_out, i);
+        // the heap holds k + 1 distances of cloud points (the query's own 0
+        // among them): its root bounds the (k + 1)-th smallest from above
+        defer_query_bound(s, deferred, md_out, bound, i, kth);
         return;
     }
     const int e = root_exponent(kth);
@@ -1891,7 +1903,7 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
         // k = 30 and 50 (the configurations') with a compile-time heap size
         auto kern = mean_k == 30 ? sor_window_kernel<31> : mean_k == 50 ? sor_window_kernel<51> : sor_window_kernel<0>;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        kern<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred);
+        kern<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred, G.bound);
         ctx->launches += 1;
     } else {
         // without pixel rays every query starts on the finest grid level
