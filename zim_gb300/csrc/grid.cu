@@ -58,6 +58,9 @@ constexpr int RING_MAX = 6;      // phase-2 rings of dense cells before the hard
 // is handed on in the bound array (md = -1: no bound)
 constexpr float MD_BOUND = -3.f;
 constexpr int TILE_X = 16, TILE_Y = 8, TILE_T = TILE_X * TILE_Y;
+// the window passes' tiles (SOR window, metric Gaussian window, per-tile ray
+// distances): taller tiles stage less halo per query
+constexpr int WT_X = 16, WT_Y = 16, WT_T = WT_X * WT_Y;
 constexpr int TILE_DILATE = 2;        // cells added around a tile's box
 constexpr int TILE_MAX_CELLS = 1024;  // gathered box of cells per tile
 constexpr int TILE_MAX_CAND = 1536;   // gathered points per tile (a surface tile gathers ~800)
@@ -825,7 +828,7 @@ using zt::RayParams;
 using zt::ray_dir;
 using zt::ray_dev;
 constexpr int WR = zt::SPIRAL_R;  // window half-size of the fast path
-constexpr int WW = TILE_X + 2 * WR, WH = TILE_Y + 2 * WR;
+constexpr int WW = WT_X + 2 * WR, WH = WT_Y + 2 * WR;
 constexpr int WN = zt::SPIRAL_N;
 constexpr int WR2MAX = 2 * WR * WR;
 
@@ -862,14 +865,14 @@ __device__ __forceinline__ int win_len2(int o) { return c_win.ent[o] >> 16; }
 __device__ __forceinline__ int win_upto(float r2) { return r2 < (float)WR2MAX ? c_win.upto[(int)r2] : WN; }
 
 // Per-thread max-heap of the K1 smallest squared distances seen so far, in
-// column tid of a [K1][TILE_T] shared array (conflict-free): the root is the
+// column tid of a [K1][WT_T] shared array (conflict-free): the root is the
 // current K1-th smallest, and a nearer point replaces it with one sift-down.
 template <int KC>  // the heap size at compile time (0: K1)
 struct WinHeap {
     float* L;
     int K1_;
     __device__ __forceinline__ int size() const { return KC ? KC : K1_; }
-    __device__ __forceinline__ float& at(int j) { return L[j * TILE_T]; }
+    __device__ __forceinline__ float& at(int j) { return L[j * WT_T]; }
     // places v at j, moving larger children up
     __device__ __forceinline__ void sift(int j, float v) {
         const int K1 = size();
@@ -923,7 +926,7 @@ __device__ __forceinline__ void fill_first(WinHeap<K1T>& heap, const float4* W, 
 
 // K1T: k + 1 at compile time (0: from k)
 template <int K1T>
-__global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restrict__ xyz,
+__global__ void __launch_bounds__(WT_T) sor_window_kernel(const float* __restrict__ xyz,
                                                             const uint8_t* __restrict__ mask, int rows, int cols,
                                                             int k, RayParams rp, GridStats* __restrict__ s,
                                                             float* __restrict__ md_out,
@@ -931,13 +934,13 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
                                                             float* __restrict__ bound) {
     extern __shared__ float4 win_smem[];
     float4* W = win_smem;                                      // WW x WH window, w = 1 valid
-    float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1) x TILE_T heaps
+    float* Ls = reinterpret_cast<float*>(win_smem + WW * WH);  // (k + 1) x WT_T heaps
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
-    __shared__ unsigned warp_dev[TILE_T / 32];
+    const int x0 = blockIdx.x * WT_X, y0 = blockIdx.y * WT_Y;
+    __shared__ unsigned warp_dev[WT_T / 32];
     unsigned tdev = 0u;  // largest dev of this thread's staged points (float bits, >= 0)
 #pragma unroll
-    for (int t = tid; t < WW * WH; t += TILE_T) {
+    for (int t = tid; t < WW * WH; t += WT_T) {
         const int wx = x0 - WR + t % WW, wy = y0 - WR + t / WW;
         // invalid and off-image pixels: NaN coordinates (their squared distance
         // never passes a comparison), w = 0
@@ -959,8 +962,8 @@ __global__ void __launch_bounds__(TILE_T) sor_window_kernel(const float* __restr
     if ((tid & 31) == 0) warp_dev[tid >> 5] = tdev;
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < TILE_T / 32; j++) tdev = max(tdev, warp_dev[j]);
-    const int tx = tid % TILE_X, ty = tid / TILE_X;
+    for (int j = 0; j < WT_T / 32; j++) tdev = max(tdev, warp_dev[j]);
+    const int tx = tid % WT_X, ty = tid / WT_X;
     const int x = x0 + tx, y = y0 + ty;
     if (x >= cols || y >= rows) return;  // no block-wide synchronisation below
     const size_t i = (size_t)y * cols + x;
@@ -1564,9 +1567,9 @@ __global__ void sor_classify_kernel(const float* __restrict__ xyz, const uint8_t
 // sor_window_kernel); the others are marked -2 in `pending` for
 // metric_gaussian_kernel.
 constexpr int WRG = WR;
-constexpr int GW = TILE_X + 2 * WRG, GH = TILE_Y + 2 * WRG;
+constexpr int GW = WT_X + 2 * WRG, GH = WT_Y + 2 * WRG;
 
-__global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restrict__ xyz,
+__global__ void __launch_bounds__(WT_T) mg_window_kernel(const float* __restrict__ xyz,
                                                            const uint8_t* __restrict__ mask, int rows, int cols,
                                                            float r, float inv2s2, RayParams rp,
                                                            GridStats* __restrict__ s,
@@ -1574,9 +1577,9 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
                                                            float* __restrict__ pending, float* __restrict__ out) {
     __shared__ float4 W[GW * GH];
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * TILE_X, y0 = blockIdx.y * TILE_Y;
+    const int x0 = blockIdx.x * WT_X, y0 = blockIdx.y * WT_Y;
 #pragma unroll
-    for (int t = tid; t < GW * GH; t += TILE_T) {
+    for (int t = tid; t < GW * GH; t += WT_T) {
         const int wx = x0 - WRG + t % GW, wy = y0 - WRG + t / GW;
         // invalid and off-image pixels are NaN: their distance test fails
         const float nan = __int_as_float(0x7fc00000);
@@ -1588,7 +1591,7 @@ __global__ void __launch_bounds__(TILE_T) mg_window_kernel(const float* __restri
         W[t] = v;
     }
     __syncthreads();
-    const int tx = tid % TILE_X, ty = tid / TILE_X;
+    const int tx = tid % WT_X, ty = tid / WT_X;
     const int x = x0 + tx, y = y0 + ty;
     if (x >= cols || y >= rows) return;
     const size_t i = (size_t)y * cols + x;
@@ -1776,12 +1779,12 @@ zim_status carve_grid(zim_ctx* ctx, size_t n, int levels, GridScratch& G) {
 // Per 16x8 pixel tile (the window passes' tiles) the largest distance of a
 // valid point from its pixel ray (float bits; NaN counts as unbounded), and the
 // largest of all into ray_dev_bits.
-__global__ void __launch_bounds__(TILE_T) tile_ray_dev_kernel(const float* __restrict__ xyz,
+__global__ void __launch_bounds__(WT_T) tile_ray_dev_kernel(const float* __restrict__ xyz,
                                                               const uint8_t* __restrict__ mask, int rows, int cols,
                                                               zt::RayParams rp, GridStats* s,
                                                               unsigned* __restrict__ tile_dev) {
-    __shared__ unsigned wmax[TILE_T / 32];
-    const int x = blockIdx.x * TILE_X + (int)threadIdx.x % TILE_X, y = blockIdx.y * TILE_Y + (int)threadIdx.x / TILE_X;
+    __shared__ unsigned wmax[WT_T / 32];
+    const int x = blockIdx.x * WT_X + (int)threadIdx.x % WT_X, y = blockIdx.y * WT_Y + (int)threadIdx.x / WT_X;
     unsigned dev = 0u;
     if (x < cols && y < rows) {
         const size_t i = (size_t)y * cols + x;
@@ -1796,7 +1799,7 @@ __global__ void __launch_bounds__(TILE_T) tile_ray_dev_kernel(const float* __res
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = dev;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int j = 1; j < TILE_T / 32; j++) dev = max(dev, wmax[j]);
+        for (int j = 1; j < WT_T / 32; j++) dev = max(dev, wmax[j]);
         tile_dev[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = dev;
         if (dev) atomicMax(&s->ray_dev_bits, dev);
     }
@@ -1899,11 +1902,12 @@ zim_status zim_sor_launch(zim_ctx* ctx, const float* xyz, const uint8_t* mask, i
     const int window = rays.valid ? 1 : 0;
     if (window) {
         const RayParams rp = rpw;
-        const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * TILE_T * 4;
+        const dim3 wgrid((cols + WT_X - 1) / WT_X, (rows + WT_Y - 1) / WT_Y);
+        const size_t wsm = (size_t)WW * WH * sizeof(float4) + (size_t)(mean_k + 1) * WT_T * 4;
         // k = 30 and 50 (the configurations') with a compile-time heap size
         auto kern = mean_k == 30 ? sor_window_kernel<31> : mean_k == 50 ? sor_window_kernel<51> : sor_window_kernel<0>;
         ZIM_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        kern<<<tgrid, TILE_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred, G.bound);
+        kern<<<wgrid, WT_T, wsm, st>>>(xyz, mask, rows, cols, mean_k, rp, G.stats, md, G.deferred, G.bound);
         ctx->launches += 1;
     } else {
         // without pixel rays every query starts on the finest grid level
@@ -1947,8 +1951,8 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
         // the window pass needs only the largest ray distance; the grid's
         // statistics wait for the window pass's verdict
         stats_init_kernel<<<1, 1, 0, st>>>(G.stats);
-        dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
-        tile_ray_dev_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats,
+        dim3 tgrid((cols + WT_X - 1) / WT_X, (rows + WT_Y - 1) / WT_Y);
+        tile_ray_dev_kernel<<<tgrid, WT_T, 0, st>>>(xyz, mask, rows, cols, rpw, G.stats,
                                                       reinterpret_cast<unsigned*>(G.bound));
         ctx->launches += 2;
     } else {
@@ -1960,10 +1964,10 @@ zim_status zim_metric_gaussian_launch(zim_ctx* ctx, const float* xyz, const uint
     float* pending = nullptr;
     if (rays.valid) {
         const RayParams rp = rpw;
-        dim3 tgrid((cols + TILE_X - 1) / TILE_X, (rows + TILE_Y - 1) / TILE_Y);
+        dim3 tgrid((cols + WT_X - 1) / WT_X, (rows + WT_Y - 1) / WT_Y);
         pending = G.md;
         // G.bound holds the per-tile ray distances (one word per tile)
-        mg_window_kernel<<<tgrid, TILE_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats,
+        mg_window_kernel<<<tgrid, WT_T, 0, st>>>(xyz, mask, rows, cols, rad, inv2s2, rp, G.stats,
                                                    reinterpret_cast<const unsigned*>(G.bound), pending, out);
         ctx->launches += 1;
     }

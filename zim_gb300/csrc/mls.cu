@@ -17,7 +17,7 @@
 
 namespace {
 
-constexpr int MX = 16, MY = 8;
+constexpr int MX = 16, MY = 16;
 
 // Unit eigenvector of the smallest eigenvalue of a symmetric 3x3 matrix (the
 // surface normal of a weighted covariance): the eigenvalue in closed form by
