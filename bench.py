@@ -62,13 +62,13 @@ def env_rank():
 # DRAM bytes per launch (read + write) of a stage's kernel on the 5 MP
 # workload, from one ncu capture each (profiles/*_5mp_dram.md): the
 # roofline's `traffic` for that kernel when it dominates the step.
-MEASURED_TRAFFIC = {("mls", 2448, 2048): (68182784 + 26492672, "profiles/mls_smem_kernel_5mp.md")}
+MEASURED_TRAFFIC = {("mls", 2448, 2048): (68118016 + 26156032, "profiles/mls_smem_kernel_5mp.md")}
 # Warp instructions per launch and the FMA pipe's busy fraction of a stage's
 # kernel on the 5 MP workload, from one ncu capture (profiles/*_5mp.md): the
 # issue-slot side of the roofline for kernels bound by instruction issue.
 # timed blocks of the end-to-end measurement (the median is reported)
 E2E_BLOCKS = 3
-MEASURED_ISSUE = {("mls", 2448, 2048): (1100012749, 0.6384, "profiles/mls_smem_kernel_5mp.md")}
+MEASURED_ISSUE = {("mls", 2448, 2048): (1079920613, 0.6405, "profiles/mls_smem_kernel_5mp.md")}
 
 
 def issue_roofline(stage, W, H, ms_per_launch, sm_mhz):
