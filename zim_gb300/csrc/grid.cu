@@ -144,29 +144,53 @@ __global__ void spacing1_kernel(const float* __restrict__ xyz, const uint8_t* __
     float df = 0.f;
     unsigned ci = 0u, nvi = 0u, dev = 0u;
     int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-    // blocks over rows, threads over a row's pixels: no index division
-    for (int y = blockIdx.x; y < rows; y += gridDim.x)
-        for (int x = threadIdx.x; x < cols; x += blockDim.x) {
-            const size_t i = (size_t)y * cols + x;
-            if (!mask[i]) continue;
-            nvi++;
-            const float p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-            for (int a = 0; a < 3; a++) {
-                mn[a] = min(mn[a], fbits(p[a]));
-                mx[a] = max(mx[a], fbits(p[a]));
+    // blocks over rows, threads over a row's pixels (no index division), four
+    // pixels of a thread at a time with their loads issued together (the same
+    // pixels in the same order as one at a time)
+    constexpr int U = 4;
+    for (int y = blockIdx.x; y < rows; y += gridDim.x) {
+        const size_t r0 = (size_t)y * cols;
+        for (int xb = threadIdx.x; xb < cols; xb += U * blockDim.x) {
+            bool m[U], mr[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int x = xb + u * (int)blockDim.x;
+                m[u] = x < cols && mask[r0 + x];
+                mr[u] = x + 1 < cols && mask[r0 + x + 1];
             }
-            if (rays) {
-                float ax, ay, az;
-                zt::ray_dir(rp, x, y, ax, ay, az);
-                const float d = zt::ray_dev(p[0], p[1], p[2], ax, ay, az);
-                dev = max(dev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
+            float p[U][3], q[U][3];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const size_t i = r0 + xb + u * blockDim.x;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    p[u][a] = m[u] ? xyz[3 * i + a] : 0.f;
+                    q[u][a] = m[u] && mr[u] ? xyz[3 * i + 3 + a] : 0.f;
+                }
             }
-            if (x + 1 < cols && mask[i + 1]) {
-                float dx = xyz[3 * i + 3] - p[0], dy = xyz[3 * i + 4] - p[1], dz = xyz[3 * i + 5] - p[2];
-                df += sqrtf(dx * dx + dy * dy + dz * dz);
-                ci++;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (!m[u]) continue;
+                const int x = xb + u * (int)blockDim.x;
+                nvi++;
+                for (int a = 0; a < 3; a++) {
+                    mn[a] = min(mn[a], fbits(p[u][a]));
+                    mx[a] = max(mx[a], fbits(p[u][a]));
+                }
+                if (rays) {
+                    float ax, ay, az;
+                    zt::ray_dir(rp, x, y, ax, ay, az);
+                    const float d = zt::ray_dev(p[u][0], p[u][1], p[u][2], ax, ay, az);
+                    dev = max(dev, __float_as_uint(d == d ? d : INFINITY));  // NaN counts as unbounded
+                }
+                if (mr[u]) {
+                    float dx = q[u][0] - p[u][0], dy = q[u][1] - p[u][1], dz = q[u][2] - p[u][2];
+                    df += sqrtf(dx * dx + dy * dy + dz * dz);
+                    ci++;
+                }
             }
         }
+    }
     double d = block_reduce((double)df, Add(), 0.0);
     double c = block_reduce((double)ci, Add(), 0.0);
     double nv = block_reduce((double)nvi, Add(), 0.0);
